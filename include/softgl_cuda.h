@@ -1,0 +1,240 @@
+/*
+ * softgl_cuda.h — C ABI of the GB300 (sm_103a) renderer back-end.
+ *
+ * Every entry point mirrors one method of SoftGLRender's back-end abstraction so that a C++
+ * `RendererCUDA : public SoftGL::Renderer` (or any FFI caller) can forward to it one-to-one:
+ *
+ *   SoftGL::Renderer            src/Render/Renderer.h:24-59
+ *   SoftGL::FrameBuffer         src/Render/Framebuffer.h:20-91
+ *   SoftGL::Texture/TextureDesc src/Render/Texture.h:17-105
+ *   SoftGL::VertexArray(Object) src/Render/Vertex.h:15-37
+ *   SoftGL::ShaderProgram       src/Render/ShaderProgram.h:15-58
+ *   SoftGL::UniformBlock/Sampler/ShaderResources  src/Render/Uniform.h:20-64
+ *   SoftGL::RenderStates/ClearStates              src/Render/RenderStates.h:13-99
+ *
+ * ABI rules: plain C types only; resources are opaque non-zero 32-bit handles owned by a context;
+ * every call returns an sglc_status (0 = SGLC_OK) and never aborts the process; the text of the
+ * last failure of a context is available from sglc_last_error(). All enum values are the
+ * reference's own enum values (same order), so a binding passes them through unchanged.
+ *
+ * Execution model: one context = one CUDA device + one CUDA stream. Draws are enqueued
+ * asynchronously; sglc_wait_idle() synchronises (RendererSoft::waitIdle is a no-op because its
+ * draw() is synchronous, RendererSoft.cpp:136-168). Reads of attachments synchronise implicitly.
+ */
+#ifndef SOFTGL_CUDA_H_
+#define SOFTGL_CUDA_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SGLC_API __attribute__((visibility("default")))
+#else
+#define SGLC_API
+#endif
+
+typedef int32_t sglc_status;
+typedef int32_t sglc_handle; /* 0 is the null handle */
+typedef struct sglc_context sglc_context;
+
+enum {
+  SGLC_OK = 0,
+  SGLC_ERR_INVALID_HANDLE = 1,
+  SGLC_ERR_INVALID_VALUE = 2,
+  SGLC_ERR_OUT_OF_MEMORY = 3,
+  SGLC_ERR_DEVICE = 4,       /* a CUDA runtime call failed */
+  SGLC_ERR_UNSUPPORTED = 5,  /* valid in the reference API, not implemented by this back-end */
+  SGLC_ERR_OVERFLOW = 6,     /* a device-side capacity (clip vertices, tile lists) was exceeded */
+  SGLC_ERR_NO_DEVICE = 7,
+};
+
+/* ---- enums: values equal to the reference's enums ---------------------------------------- */
+/* TextureType (Texture.h:58-61) */
+enum { SGLC_TEXTURE_2D = 0, SGLC_TEXTURE_CUBE = 1 };
+/* TextureFormat (Texture.h:63-66) */
+enum { SGLC_FORMAT_RGBA8 = 0, SGLC_FORMAT_FLOAT32 = 1 };
+/* FilterMode (Texture.h:24-31) */
+enum {
+  SGLC_FILTER_NEAREST = 0, SGLC_FILTER_LINEAR, SGLC_FILTER_NEAREST_MIPMAP_NEAREST,
+  SGLC_FILTER_LINEAR_MIPMAP_NEAREST, SGLC_FILTER_NEAREST_MIPMAP_LINEAR, SGLC_FILTER_LINEAR_MIPMAP_LINEAR
+};
+/* WrapMode (Texture.h:17-22) */
+enum { SGLC_WRAP_REPEAT = 0, SGLC_WRAP_MIRRORED_REPEAT, SGLC_WRAP_CLAMP_TO_EDGE, SGLC_WRAP_CLAMP_TO_BORDER };
+/* BorderColor (Texture.h:42-45) */
+enum { SGLC_BORDER_BLACK = 0, SGLC_BORDER_WHITE = 1 };
+/* BufferLayout (Base/Buffer.h:14-18): compile-time in the reference, per texture here */
+enum { SGLC_LAYOUT_LINEAR = 0, SGLC_LAYOUT_TILED = 1, SGLC_LAYOUT_MORTON = 2 };
+/* DepthFunction / BlendFactor / BlendFunction / PolygonMode / PrimitiveType (RenderStates.h:13-77) */
+enum {
+  SGLC_DEPTH_NEVER = 0, SGLC_DEPTH_LESS, SGLC_DEPTH_EQUAL, SGLC_DEPTH_LEQUAL,
+  SGLC_DEPTH_GREATER, SGLC_DEPTH_NOTEQUAL, SGLC_DEPTH_GEQUAL, SGLC_DEPTH_ALWAYS
+};
+enum {
+  SGLC_BLEND_ZERO = 0, SGLC_BLEND_ONE, SGLC_BLEND_SRC_COLOR, SGLC_BLEND_SRC_ALPHA, SGLC_BLEND_DST_COLOR,
+  SGLC_BLEND_DST_ALPHA, SGLC_BLEND_ONE_MINUS_SRC_COLOR, SGLC_BLEND_ONE_MINUS_SRC_ALPHA,
+  SGLC_BLEND_ONE_MINUS_DST_COLOR, SGLC_BLEND_ONE_MINUS_DST_ALPHA
+};
+enum { SGLC_FUNC_ADD = 0, SGLC_FUNC_SUBTRACT, SGLC_FUNC_REVERSE_SUBTRACT, SGLC_FUNC_MIN, SGLC_FUNC_MAX };
+enum { SGLC_POLYGON_POINT = 0, SGLC_POLYGON_LINE, SGLC_POLYGON_FILL };
+enum { SGLC_PRIMITIVE_POINT = 0, SGLC_PRIMITIVE_LINE, SGLC_PRIMITIVE_TRIANGLE };
+
+/* Shading models. 1..3 are ShadingModel (Viewer/Material.h:24-33) loaded by
+ * ViewerSoftware::loadShaders (ViewerSoftware.h:54-69); 100+ are device shaders with no
+ * reference counterpart, used by the synthetic benchmark scenes. */
+enum {
+  SGLC_SHADING_BASE_COLOR = 1,          /* Shader/Software/BasicSoft.h:62-79 */
+  SGLC_SHADING_BLINN_PHONG = 2,         /* Shader/Software/BlinnPhongSoft.h:181-325 (point light) */
+  SGLC_SHADING_PBR = 3,                 /* Shader/Software/PbrSoft.h:106-323 */
+  SGLC_SHADING_BLINN_PHONG_DIR = 100,   /* Blinn-Phong, directional light, shininess 32 */
+  SGLC_SHADING_VERTEX_COLOR = 101,      /* per-vertex RGBA colour */
+};
+
+/* TextureDesc (Texture.h:76-85) plus the storage layout (reference: compile-time macro). */
+typedef struct sglc_texture_desc {
+  int32_t width;
+  int32_t height;
+  int32_t type;        /* SGLC_TEXTURE_* */
+  int32_t format;      /* SGLC_FORMAT_* */
+  uint32_t usage;      /* TextureUsage bits (Texture.h:68-74) */
+  int32_t use_mipmaps;
+  int32_t multi_sample;
+  int32_t layout;      /* SGLC_LAYOUT_* (sampled textures; attachments are stored linearly) */
+} sglc_texture_desc;
+
+/* SamplerDesc (Texture.h:47-56) */
+typedef struct sglc_sampler_desc {
+  int32_t filter_min;
+  int32_t filter_mag;
+  int32_t wrap_s;
+  int32_t wrap_t;
+  int32_t wrap_r;
+  int32_t border_color;
+} sglc_sampler_desc;
+
+/* RenderStates (RenderStates.h:79-92) with BlendParameters (:53-73) flattened. */
+typedef struct sglc_render_states {
+  int32_t blend;
+  int32_t blend_func_rgb;
+  int32_t blend_src_rgb;
+  int32_t blend_dst_rgb;
+  int32_t blend_func_alpha;
+  int32_t blend_src_alpha;
+  int32_t blend_dst_alpha;
+  int32_t depth_test;
+  int32_t depth_mask;
+  int32_t depth_func;
+  int32_t cull_face;
+  int32_t primitive_type;
+  int32_t polygon_mode;
+  float line_width;
+} sglc_render_states;
+
+/* ClearStates (RenderStates.h:94-99) */
+typedef struct sglc_clear_states {
+  int32_t depth_flag;
+  int32_t color_flag;
+  float clear_color[4];
+  float clear_depth;
+} sglc_clear_states;
+
+/* Per-draw counters (no reference counterpart; the viewer shows only a triangle count). */
+typedef struct sglc_draw_stats {
+  int64_t vertices_in;
+  int64_t triangles_in;
+  int64_t clip_vertices;      /* vertices created by frustum clipping */
+  int64_t primitives;         /* after clipping (originals + appended fan triangles) */
+  int64_t bin_entries;        /* (tile, triangle) pairs */
+} sglc_draw_stats;
+
+/* ---- context (Renderer::create / destroy, Renderer.h:27-28) ---------------------------------- */
+SGLC_API sglc_status sglc_create(sglc_context **out, int32_t device);
+SGLC_API sglc_status sglc_destroy(sglc_context *ctx);
+SGLC_API const char *sglc_last_error(sglc_context *ctx);
+/* Release one resource handle (the shared_ptr reset of the reference). */
+SGLC_API sglc_status sglc_release(sglc_context *ctx, sglc_handle h);
+
+/* ---- framebuffer (Renderer::createFrameBuffer, Renderer.h:31; FrameBuffer, Framebuffer.h:20-91) */
+SGLC_API sglc_status sglc_create_framebuffer(sglc_context *ctx, int32_t offscreen, sglc_handle *out);
+SGLC_API sglc_status sglc_framebuffer_set_color_attachment(sglc_context *ctx, sglc_handle fb, sglc_handle tex,
+                                                           int32_t layer, int32_t level);
+SGLC_API sglc_status sglc_framebuffer_set_depth_attachment(sglc_context *ctx, sglc_handle fb, sglc_handle tex);
+SGLC_API sglc_status sglc_framebuffer_is_valid(sglc_context *ctx, sglc_handle fb, int32_t *valid);
+
+/* ---- texture (Renderer::createTexture, Renderer.h:34; Texture, Texture.h:87-105) ------------- */
+SGLC_API sglc_status sglc_create_texture(sglc_context *ctx, const sglc_texture_desc *desc, sglc_handle *out);
+SGLC_API sglc_status sglc_texture_set_sampler_desc(sglc_context *ctx, sglc_handle tex,
+                                                   const sglc_sampler_desc *sampler);
+SGLC_API sglc_status sglc_texture_init_image_data(sglc_context *ctx, sglc_handle tex);
+/* Texture::setImageData: one linear width*height image per layer (1 for 2D, 6 for cube faces in
+ * CubeMapFace order); the mip chain is generated on the device when use_mipmaps is set. */
+SGLC_API sglc_status sglc_texture_set_image_data(sglc_context *ctx, sglc_handle tex, int32_t layer_count,
+                                                 const void *const *layers, size_t bytes_per_layer);
+/* Upload one mip level of one layer (the reference fills levels by rendering into a level
+ * attachment, Environment.cpp:152-195; this uploads the same bytes directly). */
+SGLC_API sglc_status sglc_texture_set_level_data(sglc_context *ctx, sglc_handle tex, int32_t layer, int32_t level,
+                                                 const void *data, size_t bytes);
+/* Texture::dumpImage analogue: copy one level of one layer to host memory in linear order.
+ * For multi-sample textures `resolved` = 0 returns the 4 interleaved samples per pixel
+ * (RGBA8: 16 B/pixel; FLOAT32: 16 B/pixel) and 1 returns the resolved RGBA8 image. */
+SGLC_API sglc_status sglc_texture_read_image(sglc_context *ctx, sglc_handle tex, int32_t layer, int32_t level,
+                                             int32_t resolved, void *out, size_t bytes);
+
+/* ---- vertex array (Renderer::createVertexArrayObject, Renderer.h:37; VertexSoft.h:16-31) ---- */
+SGLC_API sglc_status sglc_create_vertex_array(sglc_context *ctx, const void *vertexes, size_t vertexes_len,
+                                              size_t stride, const int32_t *indices, size_t indices_len,
+                                              sglc_handle *out);
+SGLC_API sglc_status sglc_vertex_array_update(sglc_context *ctx, sglc_handle vao, const void *data, size_t len);
+
+/* ---- shader program (Renderer::createShaderProgram, Renderer.h:40; ShaderProgramSoft.h:26-70) */
+SGLC_API sglc_status sglc_create_shader_program(sglc_context *ctx, sglc_handle *out);
+SGLC_API sglc_status sglc_program_add_define(sglc_context *ctx, sglc_handle prog, const char *name);
+/* ShaderProgramSoft::SetShaders(VS, FS): selects the device vertex/fragment shader pair. */
+SGLC_API sglc_status sglc_program_set_shaders(sglc_context *ctx, sglc_handle prog, int32_t shading_model);
+
+/* ---- pipeline states (Renderer::createPipelineStates, Renderer.h:43) ------------------------- */
+SGLC_API sglc_status sglc_create_pipeline_states(sglc_context *ctx, const sglc_render_states *states,
+                                                 sglc_handle *out);
+
+/* ---- uniforms (Renderer::createUniformBlock/Sampler, Renderer.h:46-47; UniformSoft.h:15-90) -- */
+SGLC_API sglc_status sglc_create_uniform_block(sglc_context *ctx, const char *name, int32_t size, sglc_handle *out);
+SGLC_API sglc_status sglc_uniform_block_set_sub_data(sglc_context *ctx, sglc_handle ub, const void *data,
+                                                     int32_t len, int32_t offset);
+SGLC_API sglc_status sglc_uniform_block_set_data(sglc_context *ctx, sglc_handle ub, const void *data, int32_t len);
+SGLC_API sglc_status sglc_create_uniform_sampler(sglc_context *ctx, const char *name, int32_t type, int32_t format,
+                                                 sglc_handle *out);
+SGLC_API sglc_status sglc_uniform_sampler_set_texture(sglc_context *ctx, sglc_handle us, sglc_handle tex);
+/* ShaderResources (Uniform.h:60-64): two maps keyed by the caller's integer key. */
+SGLC_API sglc_status sglc_create_shader_resources(sglc_context *ctx, sglc_handle *out);
+SGLC_API sglc_status sglc_shader_resources_set_block(sglc_context *ctx, sglc_handle res, int32_t key, sglc_handle ub);
+SGLC_API sglc_status sglc_shader_resources_set_sampler(sglc_context *ctx, sglc_handle res, int32_t key,
+                                                       sglc_handle us);
+
+/* ---- pipeline (Renderer.h:50-58; RendererSoft.cpp:61-168) ------------------------------------ */
+SGLC_API sglc_status sglc_begin_render_pass(sglc_context *ctx, sglc_handle fb, const sglc_clear_states *states);
+SGLC_API sglc_status sglc_set_viewport(sglc_context *ctx, int32_t x, int32_t y, int32_t width, int32_t height);
+SGLC_API sglc_status sglc_set_vertex_array(sglc_context *ctx, sglc_handle vao);
+SGLC_API sglc_status sglc_set_shader_program(sglc_context *ctx, sglc_handle prog);
+SGLC_API sglc_status sglc_set_shader_resources(sglc_context *ctx, sglc_handle res);
+SGLC_API sglc_status sglc_set_pipeline_states(sglc_context *ctx, sglc_handle states);
+SGLC_API sglc_status sglc_draw(sglc_context *ctx);
+SGLC_API sglc_status sglc_end_render_pass(sglc_context *ctx);
+SGLC_API sglc_status sglc_wait_idle(sglc_context *ctx);
+/* RendererSoft::setEnableEarlyZ (RendererSoft.h:53). */
+SGLC_API sglc_status sglc_set_enable_early_z(sglc_context *ctx, int32_t enable);
+
+/* ---- extensions (no reference counterpart) --------------------------------------------------- */
+/* Counters of the last draw (synchronises). */
+SGLC_API sglc_status sglc_get_draw_stats(sglc_context *ctx, sglc_draw_stats *out);
+/* The CUDA stream the context enqueues on (as an opaque pointer, cudaStream_t). */
+SGLC_API sglc_status sglc_get_stream(sglc_context *ctx, void **stream);
+/* Raster tile edge in pixels (8, 16 or 32); picked by the autotuner, default 16. */
+SGLC_API sglc_status sglc_set_tile_size(sglc_context *ctx, int32_t tile);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SOFTGL_CUDA_H_ */
