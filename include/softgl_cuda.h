@@ -148,6 +148,11 @@ typedef struct sglc_draw_stats {
   int64_t clip_vertices;      /* vertices created by frustum clipping */
   int64_t primitives;         /* after clipping (originals + appended fan triangles) */
   int64_t bin_entries;        /* (tile, triangle) pairs */
+  int64_t fragments_shaded;   /* fragment-shader invocations (stats level 2) */
+  float geometry_ms;          /* device time of vertex + clip + setup (stats level >= 1) */
+  float binning_ms;           /* pair emission + sort + tile ranges, including the count read-back */
+  float raster_ms;            /* tile raster + shading + ROP + resolve */
+  int32_t kernel_launches;    /* kernels this back-end launched for the draw */
 } sglc_draw_stats;
 
 /* ---- context (Renderer::create / destroy, Renderer.h:27-28) ---------------------------------- */
@@ -229,6 +234,8 @@ SGLC_API sglc_status sglc_set_enable_early_z(sglc_context *ctx, int32_t enable);
 /* ---- extensions (no reference counterpart) --------------------------------------------------- */
 /* Counters of the last draw (synchronises). */
 SGLC_API sglc_status sglc_get_draw_stats(sglc_context *ctx, sglc_draw_stats *out);
+/* 0: no instrumentation; 1: per-stage device timings of each draw; 2: also count fragments. */
+SGLC_API sglc_status sglc_set_stats_level(sglc_context *ctx, int32_t level);
 /* The CUDA stream the context enqueues on (as an opaque pointer, cudaStream_t). */
 SGLC_API sglc_status sglc_get_stream(sglc_context *ctx, void **stream);
 /* Raster tile edge in pixels (8, 16 or 32); picked by the autotuner, default 16. */

@@ -508,6 +508,12 @@ sglc_status sglr_get_stream(sglc_context *ctx, void **stream) {
   return SGLC_OK;
 }
 
+sglc_status sglr_set_stats_level(sglc_context *ctx, int32_t level) {
+  (void) ctx;
+  (void) level;
+  return SGLC_OK;
+}
+
 sglc_status sglr_set_tile_size(sglc_context *ctx, int32_t tile) {
   (void) ctx;
   (void) tile;

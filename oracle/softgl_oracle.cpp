@@ -1645,5 +1645,6 @@ sglc_status sglo_get_stream(sglc_context *, void **stream) {
   return SGLC_OK;
 }
 sglc_status sglo_set_tile_size(sglc_context *, int32_t) { return SGLC_OK; }
+sglc_status sglo_set_stats_level(sglc_context *, int32_t) { return SGLC_OK; }
 
 }  // extern "C"

@@ -84,7 +84,9 @@ class _ClearStates(C.Structure):
 
 class _DrawStats(C.Structure):
     _fields_ = [("vertices_in", C.c_int64), ("triangles_in", C.c_int64), ("clip_vertices", C.c_int64),
-                ("primitives", C.c_int64), ("bin_entries", C.c_int64)]
+                ("primitives", C.c_int64), ("bin_entries", C.c_int64), ("fragments_shaded", C.c_int64),
+                ("geometry_ms", C.c_float), ("binning_ms", C.c_float), ("raster_ms", C.c_float),
+                ("kernel_launches", C.c_int32)]
 
 
 # ---- reference value types ---------------------------------------------------------------------
@@ -195,6 +197,7 @@ _SIGS = {
     "set_enable_early_z": [C.c_void_p, C.c_int32],
     "get_draw_stats": [C.c_void_p, C.POINTER(_DrawStats)],
     "get_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
+    "set_stats_level": [C.c_void_p, C.c_int32],
     "set_tile_size": [C.c_void_p, C.c_int32],
 }
 
@@ -481,6 +484,9 @@ class Renderer:
         s = _DrawStats()
         self._call("get_draw_stats", C.byref(s))
         return {k: getattr(s, k) for k, _ in _DrawStats._fields_}
+
+    def setStatsLevel(self, level: int) -> None:
+        self._call("set_stats_level", level)
 
     def stream(self) -> int:
         p = C.c_void_p()

@@ -1,0 +1,1067 @@
+// C ABI of include/softgl_cuda.h: resources, render-state binding and draw orchestration of the
+// sm_103a renderer. Mirrors SoftGL::RendererSoft (src/Render/Software/RendererSoft.cpp) call by
+// call: resource objects are handle-table entries backed by device memory; uniform blocks are
+// copied into the program at setShaderResources time and samplers are bound by reference
+// (ShaderProgram::bindResources, src/Render/ShaderProgram.h:27-54; UniformSoft.h:26-29,79-82);
+// draw() enqueues the geometry, binning and raster kernels on the context's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "softgl_cuda.h"
+#include "sglc_device.cuh"
+#include "sglc_kernels.h"
+
+using namespace sglc;
+
+namespace {
+
+struct UniformDescEntry {
+  const char *name;
+  int offset;
+  int samplerSlot;
+};
+
+struct ShaderInfo {
+  int model;
+  std::vector<const char *> defines;
+  std::vector<UniformDescEntry> uniforms;
+  int uniformSize;
+  int varyingsCnt;
+};
+
+// uniform / varying layouts of the reference shaders with GLM aligned types
+// (BasicSoft.h:24-42, BlinnPhongSoft.h:110-150, PbrSoft.h:29-72)
+const ShaderInfo kShaders[] = {
+    {SH_BASE, {}, {{"UniformsModel", 0, -1}, {"UniformsMaterial", 256, -1}}, 304, 0},
+    {SH_BLINN, {"ALBEDO_MAP", "NORMAL_MAP", "EMISSIVE_MAP", "AO_MAP"},
+     {{"UniformsModel", 0, -1}, {"UniformsScene", 256, -1}, {"UniformsMaterial", 320, -1}, {"u_albedoMap", 368, 0},
+      {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3}, {"u_shadowMap", 400, 4}}, 416, 32},
+    {SH_PBR, {"ALBEDO_MAP", "NORMAL_MAP", "EMISSIVE_MAP", "AO_MAP", "METALROUGHNESS_MAP"},
+     {{"UniformsModel", 0, -1}, {"UniformsScene", 256, -1}, {"UniformsMaterial", 320, -1}, {"u_albedoMap", 368, 0},
+      {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3}, {"u_metalRoughnessMap", 400, 4},
+      {"u_irradianceMap", 408, 5}, {"u_prefilterMap", 416, 6}}, 432, 28},
+    {SH_BLINN_DIR, {"ALBEDO_MAP", "NORMAL_MAP", "EMISSIVE_MAP", "AO_MAP"},
+     {{"UniformsModel", 0, -1}, {"UniformsScene", 256, -1}, {"UniformsMaterial", 320, -1}, {"u_albedoMap", 368, 0},
+      {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3}, {"u_shadowMap", 400, 4}}, 416, 32},
+    {SH_VCOLOR, {}, {{"UniformsModel", 0, -1}, {"UniformsMaterial", 256, -1}}, 304, 4},
+};
+
+const ShaderInfo *findShader(int model) {
+  for (auto &s : kShaders)
+    if (s.model == model) return &s;
+  return nullptr;
+}
+
+enum Kind { K_FB = 1, K_TEX, K_VAO, K_PROG, K_STATES, K_UB, K_US, K_RES };
+
+struct TexObj {
+  sglc_texture_desc desc{};
+  sglc_sampler_desc sampler{0, 0, 2, 2, 2, 0};
+  int layers = 1;
+  int levels = 0;
+  int samplesPerTexel = 1;
+  bool allocated = false;
+  uint32_t *dev = nullptr;
+  size_t layerStride = 0;   // elements
+  uint32_t offset[kMaxLevels] = {0};
+  int w[kMaxLevels] = {0}, h[kMaxLevels] = {0}, tilesW[kMaxLevels] = {0};
+  uint32_t *resolved = nullptr;   // multi-sample RGBA8 colour: resolved image
+  bool resolvedValid = false;
+};
+
+struct FbObj {
+  int colorTex = 0, colorLayer = 0, colorLevel = 0, depthTex = 0;
+  bool colorReady = false, depthReady = false;
+};
+
+struct VaoObj {
+  float *attr = nullptr;
+  int32_t *idx = nullptr;
+  size_t stride = 0, nv = 0, nidx = 0;
+};
+
+struct ProgObj {
+  std::vector<std::string> defineNames;
+  const ShaderInfo *shader = nullptr;
+  uint8_t defines[8] = {0};
+  uint8_t uniforms[kUniformBytes] = {0};
+  int samplers[kMaxSamplers] = {0};
+};
+
+struct UsObj {
+  std::string name;
+  int type = 0, format = 0, tex = 0;
+  int filter = 1, wrap = 2;
+  uint32_t border = 0;
+  int width = 0, height = 0;
+  bool useMipmaps = false;
+};
+
+struct Object {
+  int kind = 0;
+  FbObj fb;
+  TexObj tex;
+  VaoObj vao;
+  ProgObj prog;
+  sglc_render_states states{};
+  std::string ubName;
+  std::vector<uint8_t> ubData;
+  UsObj us;
+  std::map<int, int> resBlocks, resSamplers;
+};
+
+// grow-only device buffer
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t need) {
+    if (need <= bytes) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    size_t n = std::max(need, (size_t) 256);
+    n = n + n / 4;
+    cudaError_t e = cudaMalloc(&ptr, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  template<typename T>
+  T *as() const { return reinterpret_cast<T *>(ptr); }
+};
+
+struct PendingClear {
+  int fb = 0;
+  bool active = false;
+  int colorFlag = 0, depthFlag = 0;
+  uint32_t color = 0;
+  float depth = 1.f;
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::map<int, Object> objects;
+  int next = 1;
+  std::string err;
+  bool earlyZ = true;
+  int tile = 16;
+  Viewport vp{};
+  int fb = 0, vao = 0, prog = 0, states = 0;
+  PendingClear clear;
+  sglc_draw_stats stats{};
+  int *hostCounters = nullptr;   // pinned
+  int statsLevel = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool evPending = false;
+  unsigned long long *fragCounter = nullptr;
+  // scratch
+  DevBuf vClip, vFrag, vMask, vVary, vAttrExtra, prims, clipExtra, clipAppendOff, clipPoly, clipPolyTri, counters;
+  DevBuf tri, tileCount, pairOff, keyA, keyB, valA, valB, tileStart, tileEnd, scanScratch, sortHist, sortHistScan,
+      staging;
+  // capacity hints that survive between draws
+  int extraVertHint = 0, polyHint = 0, appendHint = 0;
+
+  Object *get(int h, int kind) {
+    auto it = objects.find(h);
+    if (it == objects.end() || it->second.kind != kind) return nullptr;
+    return &it->second;
+  }
+  sglc_status fail(sglc_status s, const std::string &msg) {
+    err = msg;
+    return s;
+  }
+};
+
+#define CTX                                    \
+  if (!ctx) return SGLC_ERR_INVALID_HANDLE;    \
+  Ctx *c = reinterpret_cast<Ctx *>(ctx)
+#define GET(var, h, kind)                                                     \
+  Object *var = c->get(h, kind);                                              \
+  if (!var) return c->fail(SGLC_ERR_INVALID_HANDLE, "invalid handle");
+#define CK(call)                                                                                    \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess)                                                                          \
+      return c->fail(e_ == cudaErrorMemoryAllocation ? SGLC_ERR_OUT_OF_MEMORY : SGLC_ERR_DEVICE,    \
+                     std::string(#call) + ": " + cudaGetErrorString(e_));                           \
+  } while (0)
+
+static inline uint32_t u8c(float f) { return (uint32_t) ((int) f) & 255u; }
+
+int addObject(Ctx *c, int kind) {
+  int h = c->next++;
+  c->objects[h].kind = kind;
+  return h;
+}
+
+int levelCount(int w, int h) { return (int) std::floor(std::log2((double) std::max(w, h))) + 1; }
+
+// storage geometry of a texture (Buffer::initLayout for the three layouts, Buffer.h:28-31,140-213)
+void planLevels(TexObj &t) {
+  bool attachment = (t.desc.usage & (4u | 8u)) != 0;   // AttachmentColor | AttachmentDepth
+  if (attachment || t.desc.multi_sample) t.desc.layout = LAYOUT_LINEAR;
+  t.samplesPerTexel = t.desc.multi_sample ? 4 : 1;
+  t.levels = (t.desc.use_mipmaps && !t.desc.multi_sample) ? std::min(levelCount(t.desc.width, t.desc.height), kMaxLevels) : 1;
+  size_t off = 0;
+  for (int l = 0; l < t.levels; l++) {
+    int w = std::max(1, t.desc.width >> l), h = std::max(1, t.desc.height >> l);
+    t.w[l] = w;
+    t.h[l] = h;
+    size_t n;
+    if (t.desc.layout == LAYOUT_TILED) {
+      t.tilesW[l] = (w + 3) / 4;
+      n = (size_t) t.tilesW[l] * 4 * ((h + 3) / 4) * 4;
+    } else if (t.desc.layout == LAYOUT_MORTON) {
+      t.tilesW[l] = (w + 31) / 32;
+      n = (size_t) t.tilesW[l] * 32 * ((h + 31) / 32) * 32;
+    } else {
+      t.tilesW[l] = 0;
+      n = (size_t) w * h;
+    }
+    t.offset[l] = (uint32_t) off;
+    off += ((n * t.samplesPerTexel) + 3) & ~(size_t) 3;
+  }
+  t.layerStride = off;
+}
+
+DevTex devTex(const TexObj &t) {
+  DevTex d{};
+  d.base = t.dev;
+  d.layerStride = (uint32_t) t.layerStride;
+  d.levels = t.allocated ? t.levels : 0;
+  d.layout = t.desc.layout;
+  for (int l = 0; l < t.levels && l < kMaxLevels; l++) {
+    d.offset[l] = t.offset[l];
+    d.w[l] = (uint16_t) t.w[l];
+    d.h[l] = (uint16_t) t.h[l];
+    d.tilesW[l] = (uint16_t) t.tilesW[l];
+  }
+  return d;
+}
+
+sglc_status allocTexture(Ctx *c, TexObj &t) {
+  if (t.allocated) return SGLC_OK;
+  planLevels(t);
+  size_t bytes = t.layerStride * t.layers * sizeof(uint32_t);
+  CK(cudaMalloc(&t.dev, bytes));
+  CK(cudaMemsetAsync(t.dev, 0, bytes, c->stream));
+  if (t.desc.multi_sample && t.desc.format == SGLC_FORMAT_RGBA8) {
+    CK(cudaMalloc(&t.resolved, (size_t) t.desc.width * t.desc.height * 4));
+    CK(cudaMemsetAsync(t.resolved, 0, (size_t) t.desc.width * t.desc.height * 4, c->stream));
+  }
+  t.allocated = true;
+  return SGLC_OK;
+}
+
+void freeTexture(TexObj &t) {
+  if (t.dev) cudaFree(t.dev);
+  if (t.resolved) cudaFree(t.resolved);
+  t.dev = nullptr;
+  t.resolved = nullptr;
+  t.allocated = false;
+}
+
+// upload one linear level into the texture's layout
+sglc_status uploadLevel(Ctx *c, TexObj &t, int layer, int level, const void *data) {
+  size_t n = (size_t) t.w[level] * t.h[level];
+  uint32_t *dst = t.dev + (size_t) layer * t.layerStride + t.offset[level];
+  if (t.desc.layout == LAYOUT_LINEAR) {
+    CK(cudaMemcpyAsync(dst, data, n * 4, cudaMemcpyHostToDevice, c->stream));
+    return SGLC_OK;
+  }
+  CK(c->staging.ensure(n * 4));
+  CK(cudaMemcpyAsync(c->staging.ptr, data, n * 4, cudaMemcpyHostToDevice, c->stream));
+  launchSwizzleIn(devTex(t), layer, level, c->staging.as<uint32_t>(), c->stream);
+  CK(cudaGetLastError());
+  // the staging buffer is reused by the next upload: keep uploads ordered on the stream and make
+  // sure the host source can be released by the caller
+  CK(cudaStreamSynchronize(c->stream));
+  return SGLC_OK;
+}
+
+// materialise a pending clear (RendererSoft::beginRenderPass, RendererSoft.cpp:61-90)
+sglc_status flushClear(Ctx *c) {
+  if (!c->clear.active) return SGLC_OK;
+  c->clear.active = false;
+  Object *f = c->get(c->clear.fb, K_FB);
+  if (!f) return SGLC_OK;
+  if (c->clear.colorFlag && f->fb.colorReady) {
+    Object *t = c->get(f->fb.colorTex, K_TEX);
+    if (t && t->tex.allocated && f->fb.colorLevel < t->tex.levels) {
+      TexObj &T = t->tex;
+      size_t n = (size_t) T.w[f->fb.colorLevel] * T.h[f->fb.colorLevel] * T.samplesPerTexel;
+      launchFill32(T.dev + (size_t) f->fb.colorLayer * T.layerStride + T.offset[f->fb.colorLevel], c->clear.color, n,
+                   c->stream);
+    }
+  }
+  if (c->clear.depthFlag && f->fb.depthReady) {
+    Object *t = c->get(f->fb.depthTex, K_TEX);
+    if (t && t->tex.allocated) {
+      TexObj &T = t->tex;
+      uint32_t bits;
+      memcpy(&bits, &c->clear.depth, 4);
+      launchFill32(T.dev, bits, (size_t) T.w[0] * T.h[0] * T.samplesPerTexel, c->stream);
+    }
+  }
+  CK(cudaGetLastError());
+  return SGLC_OK;
+}
+
+TexObj *attachmentTex(Ctx *c, int h) {
+  Object *o = c->get(h, K_TEX);
+  return o ? &o->tex : nullptr;
+}
+
+sglc_status drawImpl(Ctx *c) {
+  Object *fo = c->get(c->fb, K_FB), *vo = c->get(c->vao, K_VAO), *po = c->get(c->prog, K_PROG);
+  if (!fo || !vo || !po) return SGLC_OK;   // RendererSoft::draw is a silent no-op (RendererSoft.cpp:137-139)
+  Object *so = c->get(c->states, K_STATES);
+  if (!so) return c->fail(SGLC_ERR_INVALID_VALUE, "draw: no pipeline states bound");
+  ProgObj &prog = po->prog;
+  if (!prog.shader) return c->fail(SGLC_ERR_INVALID_VALUE, "draw: program has no shaders");
+  const sglc_render_states &rs = so->states;
+  if (rs.primitive_type != SGLC_PRIMITIVE_TRIANGLE || rs.polygon_mode != SGLC_POLYGON_FILL)
+    return c->fail(SGLC_ERR_UNSUPPORTED, "draw: only filled triangles are implemented by this back-end");
+  FbObj &fb = fo->fb;
+  TexObj *ct = fb.colorReady ? attachmentTex(c, fb.colorTex) : nullptr;
+  TexObj *dt = fb.depthReady ? attachmentTex(c, fb.depthTex) : nullptr;
+  if (ct && (!ct->allocated || fb.colorLevel >= ct->levels || ct->desc.format != SGLC_FORMAT_RGBA8)) ct = nullptr;
+  if (dt && (!dt->allocated || dt->desc.format != SGLC_FORMAT_FLOAT32)) dt = nullptr;
+  if (!ct && !dt) return SGLC_OK;
+  if (ct && dt && ct->desc.multi_sample != dt->desc.multi_sample)
+    return c->fail(SGLC_ERR_UNSUPPORTED, "draw: colour and depth attachments must have the same sample count");
+  VaoObj &vao = vo->vao;
+
+  DrawParams p;
+  memset(&p, 0, sizeof(p));
+  p.shading = prog.shader->model;
+  p.varyCnt = prog.shader->varyingsCnt;
+  p.varyStride = std::max(8, ((p.varyCnt * 4 + 31) / 32) * 8);
+  memcpy(p.def, prog.defines, 8);
+  memcpy(p.u, prog.uniforms, kUniformBytes);
+  for (int s = 0; s < kMaxSamplers; s++) {
+    Object *uo = c->get(prog.samplers[s], K_US);
+    if (!uo) continue;
+    UsObj &us = uo->us;
+    Object *to = c->get(us.tex, K_TEX);
+    if (!to || !to->tex.allocated) continue;
+    DevSampler &d = p.samp[s];
+    d.valid = 1;
+    d.filter = us.filter;
+    d.wrap = us.wrap;
+    d.border = us.border;
+    d.width = us.width;
+    d.height = us.height;
+    // only samplers whose LOD callback the FS installs (setupSamplerDerivative: albedo, normal,
+    // emissive, ao; BlinnPhongSoft.h:217-230, PbrSoft.h:138-151) use derivative-based LOD
+    d.lodFromDerivative = us.useMipmaps && s <= 3 && us.type == SGLC_TEXTURE_2D;
+    d.isFloat = us.format == SGLC_FORMAT_FLOAT32;
+    d.tex = devTex(to->tex);
+  }
+  p.depthTest = rs.depth_test;
+  p.depthMask = rs.depth_mask;
+  p.depthFunc = rs.depth_func;
+  p.blend = rs.blend;
+  p.bFuncRgb = rs.blend_func_rgb;
+  p.bSrcRgb = rs.blend_src_rgb;
+  p.bDstRgb = rs.blend_dst_rgb;
+  p.bFuncA = rs.blend_func_alpha;
+  p.bSrcA = rs.blend_src_alpha;
+  p.bDstA = rs.blend_dst_alpha;
+  p.cullFace = rs.cull_face;
+  p.earlyZ = c->earlyZ;
+  p.vp = c->vp;
+  if (ct) {
+    p.color = ct->dev + (size_t) fb.colorLayer * ct->layerStride + ct->offset[fb.colorLevel];
+    p.resolved = ct->resolved;
+    p.cw = ct->w[fb.colorLevel];
+    p.ch = ct->h[fb.colorLevel];
+    p.cms = ct->desc.multi_sample;
+  }
+  if (dt) {
+    p.depth = reinterpret_cast<float *>(dt->dev);
+    p.dw = dt->w[0];
+    p.dh = dt->h[0];
+    p.dms = dt->desc.multi_sample;
+  }
+  p.samples = ct ? (ct->desc.multi_sample ? 4 : 1) : (dt->desc.multi_sample ? 4 : 1);
+  if (c->clear.active && c->clear.fb == c->fb) {
+    p.pendingClear = 1;
+    p.clearColorFlag = c->clear.colorFlag && ct;
+    p.clearDepthFlag = c->clear.depthFlag && dt;
+    p.clearColor = c->clear.color;
+    p.clearDepth = c->clear.depth;
+    c->clear.active = false;
+  } else {
+    sglc_status s = flushClear(c);
+    if (s) return s;
+  }
+  p.attr = vao.attr;
+  p.strideF = (int) (vao.stride / 4);
+  p.nv = (int) vao.nv;
+  p.indices = vao.idx;
+  p.ntri = (int) (vao.nidx / 3);
+  p.tile = c->tile;
+  int fw = std::max(p.cw, p.dw), fh = std::max(p.ch, p.dh);
+  p.tilesX = (fw + p.tile - 1) / p.tile;
+  p.tilesY = (fh + p.tile - 1) / p.tile;
+  int numTiles = p.tilesX * p.tilesY;
+
+  for (int attempt = 0; attempt < 4; attempt++) {
+    int extraVerts = std::max(std::max(4096, p.ntri / 2), c->extraVertHint);
+    int polyCap = std::max(std::max(1024, p.ntri / 4), c->polyHint);
+    int appendCap = std::max(std::max(1024, p.ntri / 4), c->appendHint);
+    p.vCap = p.nv + extraVerts;
+    p.clipPolyCap = polyCap;
+    p.primCap = p.ntri + appendCap;
+    CK(c->vClip.ensure(sizeof(float4) * p.vCap));
+    CK(c->vFrag.ensure(sizeof(float4) * p.vCap));
+    CK(c->vMask.ensure((size_t) p.vCap));
+    CK(c->vVary.ensure(sizeof(float) * (size_t) p.vCap * p.varyStride));
+    CK(c->vAttrExtra.ensure(sizeof(float) * (size_t) extraVerts * std::max(p.strideF, 1)));
+    CK(c->prims.ensure(sizeof(int4) * (size_t) p.primCap));
+    CK(c->clipExtra.ensure(sizeof(int) * (size_t) (p.ntri + 1)));
+    CK(c->clipAppendOff.ensure(sizeof(int) * (size_t) (p.ntri + 1)));
+    CK(c->clipPoly.ensure(sizeof(int4) * 3 * (size_t) polyCap));
+    CK(c->clipPolyTri.ensure(sizeof(int) * (size_t) polyCap));
+    CK(c->counters.ensure(sizeof(int) * 8));
+    CK(c->tri.ensure(sizeof(TriSetup) * (size_t) p.primCap));
+    CK(c->tileCount.ensure(sizeof(int) * (size_t) p.primCap));
+    CK(c->pairOff.ensure(sizeof(int) * (size_t) (p.primCap + 1)));
+    CK(c->scanScratch.ensure(sizeof(int) * (size_t) scanScratchInts(std::max(p.primCap, p.ntri) + 1) * 2));
+    p.vClip = c->vClip.as<float4>();
+    p.vFrag = c->vFrag.as<float4>();
+    p.vMask = c->vMask.as<uint8_t>();
+    p.vVary = c->vVary.as<float>();
+    p.vAttrExtra = c->vAttrExtra.as<float>();
+    p.prims = c->prims.as<int4>();
+    p.clipExtra = c->clipExtra.as<int>();
+    p.clipAppendOff = c->clipAppendOff.as<int>();
+    p.clipPoly = c->clipPoly.as<int4>();
+    p.clipPolyTri = c->clipPolyTri.as<int>();
+    p.counters = c->counters.as<int>();
+    p.tri = c->tri.as<TriSetup>();
+    p.tileCount = c->tileCount.as<int>();
+    p.pairOff = c->pairOff.as<int>();
+
+    CK(cudaMemsetAsync(p.counters, 0, sizeof(int) * 8, c->stream));
+    if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[0], c->stream));
+    launchVertexAndClip(p, c->stream);
+    scanExclusive(p.clipExtra, p.clipAppendOff, nullptr, std::max(p.ntri, 1), c->scanScratch.as<int>(), c->stream);
+    launchClipAppend(p, c->stream);
+    launchSetup(p, p.primCap, c->stream);
+    scanExclusive(p.tileCount, p.pairOff, p.counters + 3, p.primCap, c->scanScratch.as<int>(), c->stream);
+    CK(cudaGetLastError());
+    if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[1], c->stream));
+    CK(cudaMemcpyAsync(c->hostCounters, p.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(c->hostCounters + 4, p.pairOff + p.primCap, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int newVerts = c->hostCounters[0], polys = c->hostCounters[1], flags = c->hostCounters[2];
+    int np = c->hostCounters[3];
+    if (flags & 16) return c->fail(SGLC_ERR_INVALID_VALUE, "draw: index out of range of the vertex array");
+    if (flags & 7) {   // clip-vertex / polygon / primitive capacity: grow and redo (nothing written yet)
+      c->extraVertHint = std::max(extraVerts * 2, newVerts + 1024);
+      c->polyHint = std::max(polyCap * 2, polys + 1024);
+      c->appendHint = std::max(appendCap * 2, p.primCap);
+      continue;
+    }
+    int nPairs = c->hostCounters[4];
+    CK(c->keyA.ensure(sizeof(uint32_t) * (size_t) std::max(nPairs, 1)));
+    CK(c->keyB.ensure(sizeof(uint32_t) * (size_t) std::max(nPairs, 1)));
+    CK(c->valA.ensure(sizeof(int) * (size_t) std::max(nPairs, 1)));
+    CK(c->valB.ensure(sizeof(int) * (size_t) std::max(nPairs, 1)));
+    CK(c->tileStart.ensure(sizeof(int) * (size_t) numTiles));
+    CK(c->tileEnd.ensure(sizeof(int) * (size_t) numTiles));
+    int sortInts = sortScratchInts(nPairs);
+    CK(c->sortHist.ensure(sizeof(int) * (size_t) sortInts));
+    CK(c->sortHistScan.ensure(sizeof(int) * (size_t) sortInts));
+    CK(c->scanScratch.ensure(sizeof(int) * (size_t) (scanScratchInts(std::max(std::max(p.primCap, p.ntri) + 1, sortInts)) * 2)));
+    p.keyA = c->keyA.as<uint32_t>();
+    p.keyB = c->keyB.as<uint32_t>();
+    p.valA = c->valA.as<int>();
+    p.valB = c->valB.as<int>();
+    p.pairCap = nPairs;
+    p.tileStart = c->tileStart.as<int>();
+    p.tileEnd = c->tileEnd.as<int>();
+    CK(cudaMemsetAsync(p.tileStart, 0, sizeof(int) * numTiles, c->stream));
+    CK(cudaMemsetAsync(p.tileEnd, 0, sizeof(int) * numTiles, c->stream));
+    launchBinEmit(p, np, c->stream);
+    int keyBits = 1;
+    while ((1 << keyBits) < numTiles) keyBits++;
+    const int *nPairsDev = p.pairOff + p.primCap;
+    sortPairs(p, nPairs, nPairsDev, keyBits, c->sortHist.as<int>(), c->sortHistScan.as<int>(),
+              c->scanScratch.as<int>(), c->stream);
+    launchTileRanges(p, nPairs, nPairsDev, c->stream);
+    if (c->statsLevel >= 2) {
+      CK(cudaMemsetAsync(c->fragCounter, 0, sizeof(unsigned long long), c->stream));
+      p.fragCounter = c->fragCounter;
+    }
+    if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[2], c->stream));
+    launchRaster(p, ct != nullptr, dt != nullptr, c->stream);
+    if (c->statsLevel >= 1) {
+      CK(cudaEventRecord(c->ev[3], c->stream));
+      c->evPending = true;
+    }
+    CK(cudaGetLastError());
+    if (ct && ct->desc.multi_sample) ct->resolvedValid = true;
+    c->stats.vertices_in = p.nv;
+    c->stats.triangles_in = p.ntri;
+    c->stats.clip_vertices = newVerts;
+    c->stats.primitives = np;
+    c->stats.bin_entries = nPairs;
+    // vertex, clip, 3 scan, append, count, setup, 3 scan | emit, sort, ranges, raster
+    int sortPasses = nPairs > 0 ? (keyBits <= 8 ? 1 : 2) : 0;
+    c->stats.kernel_launches = (p.nv > 0) + (p.ntri > 0) + 3 + 2 + 1 + 3 + (np > 0) + sortPasses * 5 +
+                               (nPairs > 0) + 1 + attempt * 10;
+    return SGLC_OK;
+  }
+  return c->fail(SGLC_ERR_OVERFLOW, "draw: clip capacity could not be satisfied");
+}
+
+}  // namespace
+
+extern "C" {
+
+sglc_status sglc_create(sglc_context **out, int32_t device) {
+  if (!out) return SGLC_ERR_INVALID_VALUE;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return SGLC_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return SGLC_ERR_INVALID_VALUE;
+  if (cudaSetDevice(device) != cudaSuccess) return SGLC_ERR_DEVICE;
+  Ctx *c = new Ctx();
+  c->device = device;
+  bool ok = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaMallocHost(&c->hostCounters, 64) == cudaSuccess &&
+            cudaMalloc(&c->fragCounter, sizeof(unsigned long long)) == cudaSuccess;
+  for (int i = 0; i < 4 && ok; i++) ok = cudaEventCreate(&c->ev[i]) == cudaSuccess;
+  if (!ok) {
+    delete c;
+    return SGLC_ERR_DEVICE;
+  }
+  *out = reinterpret_cast<sglc_context *>(c);
+  return SGLC_OK;
+}
+
+sglc_status sglc_destroy(sglc_context *ctx) {
+  CTX;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto &kv : c->objects) {
+    Object &o = kv.second;
+    if (o.kind == K_TEX) freeTexture(o.tex);
+    if (o.kind == K_VAO) {
+      cudaFree(o.vao.attr);
+      cudaFree(o.vao.idx);
+    }
+  }
+  DevBuf *bufs[] = {&c->vClip, &c->vFrag, &c->vMask, &c->vVary, &c->vAttrExtra, &c->prims, &c->clipExtra,
+                    &c->clipAppendOff, &c->clipPoly, &c->clipPolyTri, &c->counters, &c->tri, &c->tileCount,
+                    &c->pairOff, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->tileStart, &c->tileEnd,
+                    &c->scanScratch, &c->sortHist, &c->sortHistScan, &c->staging};
+  for (DevBuf *b : bufs) b->release();
+  cudaFreeHost(c->hostCounters);
+  cudaFree(c->fragCounter);
+  for (int i = 0; i < 4; i++)
+    if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return SGLC_OK;
+}
+
+const char *sglc_last_error(sglc_context *ctx) {
+  if (!ctx) return "null context";
+  return reinterpret_cast<Ctx *>(ctx)->err.c_str();
+}
+
+sglc_status sglc_release(sglc_context *ctx, sglc_handle h) {
+  CTX;
+  auto it = c->objects.find(h);
+  if (it == c->objects.end()) return c->fail(SGLC_ERR_INVALID_HANDLE, "release: unknown handle");
+  CK(cudaStreamSynchronize(c->stream));
+  if (it->second.kind == K_TEX) freeTexture(it->second.tex);
+  if (it->second.kind == K_VAO) {
+    cudaFree(it->second.vao.attr);
+    cudaFree(it->second.vao.idx);
+  }
+  c->objects.erase(it);
+  return SGLC_OK;
+}
+
+sglc_status sglc_create_framebuffer(sglc_context *ctx, int32_t, sglc_handle *out) {
+  CTX;
+  *out = addObject(c, K_FB);
+  return SGLC_OK;
+}
+
+sglc_status sglc_framebuffer_set_color_attachment(sglc_context *ctx, sglc_handle fb, sglc_handle tex, int32_t layer,
+                                                  int32_t level) {
+  CTX;
+  GET(f, fb, K_FB);
+  GET(t, tex, K_TEX);
+  sglc_status s = flushClear(c);
+  if (s) return s;
+  f->fb.colorTex = tex;
+  f->fb.colorLayer = t->tex.desc.type == SGLC_TEXTURE_CUBE ? layer : 0;
+  f->fb.colorLevel = level;
+  f->fb.colorReady = true;
+  return SGLC_OK;
+}
+
+sglc_status sglc_framebuffer_set_depth_attachment(sglc_context *ctx, sglc_handle fb, sglc_handle tex) {
+  CTX;
+  GET(f, fb, K_FB);
+  GET(t, tex, K_TEX);
+  (void) t;
+  sglc_status s = flushClear(c);
+  if (s) return s;
+  f->fb.depthTex = tex;
+  f->fb.depthReady = true;
+  return SGLC_OK;
+}
+
+sglc_status sglc_framebuffer_is_valid(sglc_context *ctx, sglc_handle fb, int32_t *valid) {
+  CTX;
+  GET(f, fb, K_FB);
+  *valid = f->fb.colorReady || f->fb.depthReady;
+  return SGLC_OK;
+}
+
+sglc_status sglc_create_texture(sglc_context *ctx, const sglc_texture_desc *d, sglc_handle *out) {
+  CTX;
+  if (!d || !out) return c->fail(SGLC_ERR_INVALID_VALUE, "createTexture: null argument");
+  if (d->format != SGLC_FORMAT_RGBA8 && d->format != SGLC_FORMAT_FLOAT32)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "createTexture: unknown format");
+  if (d->type != SGLC_TEXTURE_2D && d->type != SGLC_TEXTURE_CUBE)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "createTexture: unknown type");
+  if (d->width <= 0 || d->height <= 0 || d->width > 32768 || d->height > 32768)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "createTexture: size out of range");
+  if (d->layout < LAYOUT_LINEAR || d->layout > LAYOUT_MORTON)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "createTexture: unknown layout");
+  int h = addObject(c, K_TEX);
+  TexObj &t = c->objects[h].tex;
+  t.desc = *d;
+  t.layers = d->type == SGLC_TEXTURE_CUBE ? 6 : 1;
+  *out = h;
+  return SGLC_OK;
+}
+
+sglc_status sglc_texture_set_sampler_desc(sglc_context *ctx, sglc_handle tex, const sglc_sampler_desc *s) {
+  CTX;
+  GET(t, tex, K_TEX);
+  t->tex.sampler = *s;
+  return SGLC_OK;
+}
+
+sglc_status sglc_texture_init_image_data(sglc_context *ctx, sglc_handle tex) {
+  CTX;
+  GET(t, tex, K_TEX);
+  if (t->tex.allocated) return SGLC_OK;
+  return allocTexture(c, t->tex);
+}
+
+sglc_status sglc_texture_set_image_data(sglc_context *ctx, sglc_handle tex, int32_t layer_count,
+                                        const void *const *layers, size_t bytes_per_layer) {
+  CTX;
+  GET(t, tex, K_TEX);
+  TexObj &T = t->tex;
+  if (T.desc.multi_sample) return c->fail(SGLC_ERR_INVALID_VALUE, "setImageData: multi sample texture");
+  if (layer_count < T.layers || !layers) return c->fail(SGLC_ERR_INVALID_VALUE, "setImageData: layer count");
+  if (bytes_per_layer < (size_t) T.desc.width * T.desc.height * 4)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "setImageData: size not match");
+  sglc_status s = allocTexture(c, T);
+  if (s) return s;
+  for (int l = 0; l < T.layers; l++) {
+    s = uploadLevel(c, T, l, 0, layers[l]);
+    if (s) return s;
+    // TextureImageSoft::generateMipmap (SamplerSoft.h:89-115) on the device
+    for (int lev = 1; lev < T.levels; lev++) launchMipLevel(devTex(T), l, lev, T.desc.format == SGLC_FORMAT_FLOAT32, c->stream);
+  }
+  CK(cudaGetLastError());
+  return SGLC_OK;
+}
+
+sglc_status sglc_texture_set_level_data(sglc_context *ctx, sglc_handle tex, int32_t layer, int32_t level,
+                                        const void *data, size_t bytes) {
+  CTX;
+  GET(t, tex, K_TEX);
+  TexObj &T = t->tex;
+  sglc_status s = allocTexture(c, T);
+  if (s) return s;
+  if (layer < 0 || layer >= T.layers || level < 0 || level >= T.levels || T.desc.multi_sample)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "set_level_data: bad layer/level");
+  if (bytes < (size_t) T.w[level] * T.h[level] * 4) return c->fail(SGLC_ERR_INVALID_VALUE, "set_level_data: size");
+  return uploadLevel(c, T, layer, level, data);
+}
+
+sglc_status sglc_texture_read_image(sglc_context *ctx, sglc_handle tex, int32_t layer, int32_t level, int32_t resolved,
+                                    void *out, size_t bytes) {
+  CTX;
+  GET(t, tex, K_TEX);
+  TexObj &T = t->tex;
+  sglc_status s = flushClear(c);
+  if (s) return s;
+  if (!T.allocated) {
+    s = allocTexture(c, T);
+    if (s) return s;
+  }
+  if (layer < 0 || layer >= T.layers || level < 0 || level >= T.levels)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "read_image: bad layer/level");
+  size_t n = (size_t) T.w[level] * T.h[level];
+  if (T.desc.multi_sample && resolved) {
+    if (!T.resolved) return c->fail(SGLC_ERR_INVALID_VALUE, "read_image: no resolved image");
+    if (bytes < n * 4) return c->fail(SGLC_ERR_INVALID_VALUE, "read_image: size");
+    CK(cudaMemcpyAsync(out, T.resolved, n * 4, cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    size_t total = n * 4 * T.samplesPerTexel;
+    if (bytes < total) return c->fail(SGLC_ERR_INVALID_VALUE, "read_image: size");
+    const uint32_t *src = T.dev + (size_t) layer * T.layerStride + T.offset[level];
+    if (T.desc.layout == LAYOUT_LINEAR) {
+      CK(cudaMemcpyAsync(out, src, total, cudaMemcpyDeviceToHost, c->stream));
+    } else {
+      CK(c->staging.ensure(n * 4));
+      launchSwizzleOut(devTex(T), layer, level, c->staging.as<uint32_t>(), c->stream);
+      CK(cudaMemcpyAsync(out, c->staging.ptr, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    }
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return SGLC_OK;
+}
+
+sglc_status sglc_create_vertex_array(sglc_context *ctx, const void *vertexes, size_t vlen, size_t stride,
+                                     const int32_t *indices, size_t ilen, sglc_handle *out) {
+  CTX;
+  if (stride == 0 || stride % 4 || stride > 256) return c->fail(SGLC_ERR_INVALID_VALUE, "vertex array: stride");
+  if (!out) return c->fail(SGLC_ERR_INVALID_VALUE, "vertex array: null output");
+  size_t nv = vlen / stride;
+  if (nv > (size_t) 0x3fffffff || ilen / 4 > (size_t) 0x3fffffff)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "vertex array: too large");
+  VaoObj v;
+  v.stride = stride;
+  v.nv = nv;
+  v.nidx = ilen / 4;
+  CK(cudaMalloc(&v.attr, std::max(nv * stride, (size_t) 16)));
+  CK(cudaMalloc(&v.idx, std::max(v.nidx * 4, (size_t) 16)));
+  if (nv) CK(cudaMemcpyAsync(v.attr, vertexes, nv * stride, cudaMemcpyHostToDevice, c->stream));
+  if (v.nidx) CK(cudaMemcpyAsync(v.idx, indices, v.nidx * 4, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  int h = addObject(c, K_VAO);
+  c->objects[h].vao = v;
+  *out = h;
+  return SGLC_OK;
+}
+
+sglc_status sglc_vertex_array_update(sglc_context *ctx, sglc_handle vao, const void *data, size_t len) {
+  CTX;
+  GET(v, vao, K_VAO);
+  size_t n = std::min(len, v->vao.nv * v->vao.stride);
+  if (n) CK(cudaMemcpyAsync(v->vao.attr, data, n, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SGLC_OK;
+}
+
+sglc_status sglc_create_shader_program(sglc_context *ctx, sglc_handle *out) {
+  CTX;
+  *out = addObject(c, K_PROG);
+  return SGLC_OK;
+}
+
+sglc_status sglc_program_add_define(sglc_context *ctx, sglc_handle prog, const char *name) {
+  CTX;
+  GET(p, prog, K_PROG);
+  if (!name) return c->fail(SGLC_ERR_INVALID_VALUE, "addDefine: null name");
+  p->prog.defineNames.push_back(name);
+  return SGLC_OK;
+}
+
+sglc_status sglc_program_set_shaders(sglc_context *ctx, sglc_handle prog, int32_t model) {
+  CTX;
+  GET(p, prog, K_PROG);
+  const ShaderInfo *s = findShader(model);
+  if (!s) return c->fail(SGLC_ERR_UNSUPPORTED, "setShaders: unknown shading model");
+  ProgObj &P = p->prog;
+  P.shader = s;
+  memset(P.defines, 0, sizeof(P.defines));
+  for (auto &n : P.defineNames)
+    for (size_t i = 0; i < s->defines.size(); i++)
+      if (n == s->defines[i]) P.defines[i] = 1;
+  memset(P.uniforms, 0, sizeof(P.uniforms));
+  return SGLC_OK;
+}
+
+sglc_status sglc_create_pipeline_states(sglc_context *ctx, const sglc_render_states *s, sglc_handle *out) {
+  CTX;
+  if (!s) return c->fail(SGLC_ERR_INVALID_VALUE, "pipeline states: null");
+  if (s->depth_func < 0 || s->depth_func > 7 || s->blend_src_rgb < 0 || s->blend_src_rgb > 9 || s->blend_dst_rgb < 0 ||
+      s->blend_dst_rgb > 9 || s->blend_src_alpha < 0 || s->blend_src_alpha > 9 || s->blend_dst_alpha < 0 ||
+      s->blend_dst_alpha > 9 || s->blend_func_rgb < 0 || s->blend_func_rgb > 4 || s->blend_func_alpha < 0 ||
+      s->blend_func_alpha > 4)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "pipeline states: enum out of range");
+  int h = addObject(c, K_STATES);
+  c->objects[h].states = *s;
+  *out = h;
+  return SGLC_OK;
+}
+
+sglc_status sglc_create_uniform_block(sglc_context *ctx, const char *name, int32_t size, sglc_handle *out) {
+  CTX;
+  if (!name || size < 0) return c->fail(SGLC_ERR_INVALID_VALUE, "uniform block: bad arguments");
+  int h = addObject(c, K_UB);
+  c->objects[h].ubName = name;
+  c->objects[h].ubData.assign(size, 0);
+  *out = h;
+  return SGLC_OK;
+}
+
+sglc_status sglc_uniform_block_set_sub_data(sglc_context *ctx, sglc_handle ub, const void *data, int32_t len,
+                                            int32_t offset) {
+  CTX;
+  GET(u, ub, K_UB);
+  if (offset < 0 || len < 0 || (size_t) offset + len > u->ubData.size())
+    return c->fail(SGLC_ERR_INVALID_VALUE, "uniform block: range outside the block");
+  memcpy(u->ubData.data() + offset, data, len);
+  return SGLC_OK;
+}
+
+sglc_status sglc_uniform_block_set_data(sglc_context *ctx, sglc_handle ub, const void *data, int32_t len) {
+  return sglc_uniform_block_set_sub_data(ctx, ub, data, len, 0);
+}
+
+sglc_status sglc_create_uniform_sampler(sglc_context *ctx, const char *name, int32_t type, int32_t format,
+                                        sglc_handle *out) {
+  CTX;
+  if (!name) return c->fail(SGLC_ERR_INVALID_VALUE, "uniform sampler: null name");
+  int h = addObject(c, K_US);
+  c->objects[h].us.name = name;
+  c->objects[h].us.type = type;
+  c->objects[h].us.format = format;
+  *out = h;
+  return SGLC_OK;
+}
+
+// Sampler2DSoft / SamplerCubeSoft::setTexture (SamplerSoft.h:388-436): filter = filterMin,
+// wrap = wrapS, border from the sampler desc, size of level 0 at this moment
+sglc_status sglc_uniform_sampler_set_texture(sglc_context *ctx, sglc_handle us, sglc_handle tex) {
+  CTX;
+  GET(u, us, K_US);
+  GET(t, tex, K_TEX);
+  UsObj &S = u->us;
+  TexObj &T = t->tex;
+  S.tex = tex;
+  S.filter = T.sampler.filter_min;
+  S.wrap = T.sampler.wrap_s;
+  if (S.format == SGLC_FORMAT_FLOAT32) {
+    float b = T.sampler.border_color == SGLC_BORDER_WHITE ? 1.f : 0.f;
+    memcpy(&S.border, &b, 4);
+  } else {
+    S.border = T.sampler.border_color == SGLC_BORDER_WHITE ? 0xFFFFFFFFu : 0u;
+  }
+  S.width = T.allocated ? T.w[0] : 0;
+  S.height = T.allocated ? T.h[0] : 0;
+  S.useMipmaps = S.filter > SGLC_FILTER_LINEAR;
+  return SGLC_OK;
+}
+
+sglc_status sglc_create_shader_resources(sglc_context *ctx, sglc_handle *out) {
+  CTX;
+  *out = addObject(c, K_RES);
+  return SGLC_OK;
+}
+
+sglc_status sglc_shader_resources_set_block(sglc_context *ctx, sglc_handle res, int32_t key, sglc_handle ub) {
+  CTX;
+  GET(r, res, K_RES);
+  GET(u, ub, K_UB);
+  (void) u;
+  r->resBlocks[key] = ub;
+  return SGLC_OK;
+}
+
+sglc_status sglc_shader_resources_set_sampler(sglc_context *ctx, sglc_handle res, int32_t key, sglc_handle us) {
+  CTX;
+  GET(r, res, K_RES);
+  GET(u, us, K_US);
+  (void) u;
+  r->resSamplers[key] = us;
+  return SGLC_OK;
+}
+
+sglc_status sglc_begin_render_pass(sglc_context *ctx, sglc_handle fb, const sglc_clear_states *s) {
+  CTX;
+  GET(f, fb, K_FB);
+  if (!s) return c->fail(SGLC_ERR_INVALID_VALUE, "beginRenderPass: null clear states");
+  sglc_status st = flushClear(c);
+  if (st) return st;
+  c->fb = fb;
+  // make sure the attachments have storage (the reference allocates in initImageData)
+  if (f->fb.colorReady) {
+    Object *t = c->get(f->fb.colorTex, K_TEX);
+    if (t && !t->tex.allocated) {
+      st = allocTexture(c, t->tex);
+      if (st) return st;
+    }
+  }
+  if (f->fb.depthReady) {
+    Object *t = c->get(f->fb.depthTex, K_TEX);
+    if (t && !t->tex.allocated) {
+      st = allocTexture(c, t->tex);
+      if (st) return st;
+    }
+  }
+  PendingClear &pc = c->clear;
+  pc.fb = fb;
+  pc.colorFlag = s->color_flag;
+  pc.depthFlag = s->depth_flag;
+  pc.color = u8c(s->clear_color[0] * 255) | (u8c(s->clear_color[1] * 255) << 8) | (u8c(s->clear_color[2] * 255) << 16) |
+             (u8c(s->clear_color[3] * 255) << 24);
+  pc.depth = s->clear_depth;
+  pc.active = s->color_flag || s->depth_flag;
+  return SGLC_OK;
+}
+
+sglc_status sglc_set_viewport(sglc_context *ctx, int32_t x, int32_t y, int32_t w, int32_t h) {
+  CTX;
+  Viewport &v = c->vp;
+  v.x = (float) x;
+  v.y = (float) y;
+  v.w = (float) w;
+  v.h = (float) h;
+  float minD = 0.f, maxD = 1.f;
+  v.absMin = std::min(minD, maxD);
+  v.absMax = std::max(minD, maxD);
+  v.oX = v.x + v.w / 2.f;
+  v.oY = v.y + v.h / 2.f;
+  v.oZ = minD;
+  v.oW = 0.f;
+  v.pX = v.w / 2.f;
+  v.pY = v.h / 2.f;
+  v.pZ = maxD - minD;
+  v.pW = 1.f;
+  return SGLC_OK;
+}
+
+sglc_status sglc_set_vertex_array(sglc_context *ctx, sglc_handle vao) {
+  CTX;
+  GET(v, vao, K_VAO);
+  (void) v;
+  c->vao = vao;
+  return SGLC_OK;
+}
+
+sglc_status sglc_set_shader_program(sglc_context *ctx, sglc_handle prog) {
+  CTX;
+  GET(p, prog, K_PROG);
+  (void) p;
+  c->prog = prog;
+  return SGLC_OK;
+}
+
+sglc_status sglc_set_shader_resources(sglc_context *ctx, sglc_handle res) {
+  CTX;
+  GET(r, res, K_RES);
+  Object *po = c->get(c->prog, K_PROG);
+  if (!po || !po->prog.shader) return SGLC_OK;
+  ProgObj &P = po->prog;
+  for (auto &kv : r->resBlocks) {
+    Object *u = c->get(kv.second, K_UB);
+    if (!u) continue;
+    for (auto &d : P.shader->uniforms) {
+      if (d.samplerSlot >= 0 || u->ubName != d.name) continue;
+      size_t n = std::min(u->ubData.size(), (size_t) (P.shader->uniformSize - d.offset));
+      memcpy(P.uniforms + d.offset, u->ubData.data(), n);
+    }
+  }
+  for (auto &kv : r->resSamplers) {
+    Object *u = c->get(kv.second, K_US);
+    if (!u) continue;
+    for (auto &d : P.shader->uniforms)
+      if (d.samplerSlot >= 0 && u->us.name == d.name) P.samplers[d.samplerSlot] = kv.second;
+  }
+  return SGLC_OK;
+}
+
+sglc_status sglc_set_pipeline_states(sglc_context *ctx, sglc_handle st) {
+  CTX;
+  GET(s, st, K_STATES);
+  (void) s;
+  c->states = st;
+  return SGLC_OK;
+}
+
+sglc_status sglc_draw(sglc_context *ctx) {
+  CTX;
+  return drawImpl(c);
+}
+
+sglc_status sglc_end_render_pass(sglc_context *ctx) {
+  CTX;
+  return flushClear(c);
+}
+
+sglc_status sglc_wait_idle(sglc_context *ctx) {
+  CTX;
+  sglc_status s = flushClear(c);
+  if (s) return s;
+  CK(cudaStreamSynchronize(c->stream));
+  return SGLC_OK;
+}
+
+sglc_status sglc_set_enable_early_z(sglc_context *ctx, int32_t enable) {
+  CTX;
+  c->earlyZ = enable != 0;
+  return SGLC_OK;
+}
+
+sglc_status sglc_get_draw_stats(sglc_context *ctx, sglc_draw_stats *out) {
+  CTX;
+  CK(cudaStreamSynchronize(c->stream));
+  if (c->evPending) {
+    CK(cudaEventElapsedTime(&c->stats.geometry_ms, c->ev[0], c->ev[1]));
+    CK(cudaEventElapsedTime(&c->stats.binning_ms, c->ev[1], c->ev[2]));
+    CK(cudaEventElapsedTime(&c->stats.raster_ms, c->ev[2], c->ev[3]));
+    if (c->statsLevel >= 2) {
+      unsigned long long n = 0;
+      CK(cudaMemcpy(&n, c->fragCounter, sizeof(n), cudaMemcpyDeviceToHost));
+      c->stats.fragments_shaded = (int64_t) n;
+    }
+    c->evPending = false;
+  }
+  *out = c->stats;
+  return SGLC_OK;
+}
+
+sglc_status sglc_set_stats_level(sglc_context *ctx, int32_t level) {
+  CTX;
+  if (level < 0 || level > 2) return c->fail(SGLC_ERR_INVALID_VALUE, "stats level must be 0, 1 or 2");
+  c->statsLevel = level;
+  c->stats.fragments_shaded = 0;
+  return SGLC_OK;
+}
+
+sglc_status sglc_get_stream(sglc_context *ctx, void **stream) {
+  CTX;
+  *stream = c->stream;
+  return SGLC_OK;
+}
+
+sglc_status sglc_set_tile_size(sglc_context *ctx, int32_t tile) {
+  CTX;
+  if (tile != 16) return c->fail(SGLC_ERR_UNSUPPORTED, "set_tile_size: this build rasterises 16x16 tiles");
+  c->tile = tile;
+  return SGLC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,306 @@
+// Device-side data structures and per-fragment arithmetic of the sm_103a renderer.
+//
+// The arithmetic reproduces SoftGLRender's RendererSoft bit for bit where the reference's result
+// is integer-like (coverage, depth, clip decisions): every kernel TU is compiled with
+// --fmad=false so `a * b + c` is two rounded operations exactly as in the reference's
+// -ffp-contract=off build, and __fmaf_rn is used only where the reference itself issues FMA
+// (the AVX2 varying interpolation, RendererSoft.cpp:1134-1138). Evaluation orders follow GLM with
+// aligned SIMD types (mat4*vec4: (m0v0+m1v1)+(m2v2+m3v3); dot(vec4): DPPS (p0+p1)+(p2+p3)).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sglc {
+
+constexpr int kMaxLevels = 16;
+constexpr int kMaxSamplers = 8;
+constexpr int kUniformBytes = 448;
+constexpr int kBlock = 32;           // RendererSoft::rasterBlockSize_ (RendererSoft.h:128)
+
+enum { LAYOUT_LINEAR = 0, LAYOUT_TILED = 1, LAYOUT_MORTON = 2 };
+enum { FILTER_NEAREST = 0, FILTER_LINEAR, FILTER_NN, FILTER_LN, FILTER_NL, FILTER_LL };
+enum { WRAP_REPEAT = 0, WRAP_MIRRORED, WRAP_EDGE, WRAP_BORDER };
+enum { SH_BASE = 1, SH_BLINN = 2, SH_PBR = 3, SH_BLINN_DIR = 100, SH_VCOLOR = 101 };
+
+// one texture as seen by a sampler: all layers x levels in one allocation
+struct DevTex {
+  const uint32_t *base;     // layer 0, level 0
+  uint32_t layerStride;     // elements between layers (cube faces)
+  int levels;
+  int layout;
+  uint32_t offset[kMaxLevels];   // element offset of each level inside a layer
+  uint16_t w[kMaxLevels], h[kMaxLevels];
+  uint16_t tilesW[kMaxLevels];   // tiles per row for Tiled (4x4) / Morton (32x32) layouts
+};
+
+// Sampler2DSoft / SamplerCubeSoft state captured by setTexture (SamplerSoft.h:388-436)
+struct DevSampler {
+  int valid;
+  int filter, wrap;
+  uint32_t border;
+  int width, height;          // level-0 size captured at setTexture (used for the LOD)
+  int lodFromDerivative;      // the FS installed its LOD callback on this sampler
+  int isFloat;
+  DevTex tex;
+};
+
+struct Viewport {
+  float x, y, w, h;
+  float oX, oY, oZ, oW;       // innerO (RendererSoft.cpp:104-107)
+  float pX, pY, pZ, pW;       // innerP (RendererSoft.cpp:109-112)
+  float absMin, absMax;
+};
+
+// per-triangle setup record read (broadcast) by every lane of the raster kernel
+struct __align__(16) TriSetup {
+  float v0x, v0y;                 // vertPos[0].xy
+  float f0x, f0y, f0z;            // vertPosFlat[0] = (v2.x, v1.x, v0.x)
+  float f1x, f1y, f1z;            // vertPosFlat[1] = (v2.y, v1.y, v0.y)
+  float z0, z1, z2, w0, w1, w2;   // fragPos.z / fragPos.w per vertex
+  float bminx, bminy, bmaxx, bmaxy;
+  int bcx, bcy;                   // 32x32 block counts
+  int vid0, vid1, vid2;           // varying rows
+  int front;
+  int rx0, rx1, ry0, ry1;         // pixel rectangle the quads can touch (inclusive)
+  int pad[2];
+};
+static_assert(sizeof(TriSetup) == 128, "TriSetup is two 64-B lines");
+
+// everything a draw's kernels read; passed by value as a __grid_constant__ parameter
+struct DrawParams {
+  // shader
+  int shading;
+  int varyCnt;                    // floats interpolated (sizeof(ShaderVaryings)/4)
+  int varyStride;                 // aligned row length in floats (multiple of 8)
+  uint8_t def[8];
+  alignas(16) uint8_t u[kUniformBytes];
+  DevSampler samp[kMaxSamplers];
+  // pipeline state
+  int depthTest, depthMask, depthFunc, blend;
+  int bFuncRgb, bSrcRgb, bDstRgb, bFuncA, bSrcA, bDstA;
+  int cullFace, earlyZ;
+  Viewport vp;
+  // attachments (linear storage; multi-sample: 4 samples interleaved per pixel)
+  uint32_t *color;
+  uint32_t *resolved;
+  float *depth;
+  int cw, ch, cms;
+  int dw, dh, dms;
+  int samples;                    // raster samples
+  int pendingClear;               // the pass's clear is fused into this draw's tile init
+  uint32_t clearColor;
+  float clearDepth;
+  int clearColorFlag, clearDepthFlag;
+  // geometry
+  const float *attr;              // vertex attributes (stride floats per vertex)
+  int strideF;
+  int nv;
+  const int32_t *indices;
+  int ntri;
+  // scratch
+  float4 *vClip;                  // clip position per vertex (original + clip-generated)
+  float4 *vFrag;                  // screen position, w = 1/w_clip
+  uint8_t *vMask;
+  float *vVary;                   // varyStride floats per vertex
+  float *vAttrExtra;              // raw attributes of clip-generated vertices
+  int vCap;                       // vertex capacity (original + generated)
+  int4 *prims;                    // i0, i1, i2, flags (bit0 discard)
+  int primCap;
+  int *clipExtra;                 // per input triangle: fan triangles appended
+  int *clipAppendOff;             // exclusive scan of clipExtra (+ total at [ntri])
+  int4 *clipPoly;                 // per clipped triangle: up to 9 vertex ids (3 x int4), see kernels
+  int *clipPolyTri;
+  int clipPolyCap;
+  int *counters;                  // [0] new vertices, [1] clipped polygons, [2] overflow flags
+  TriSetup *tri;
+  int *tileCount;                 // per primitive: tiles touched
+  int *pairOff;                   // exclusive scan of tileCount (+ total)
+  uint32_t *keyA, *keyB;          // (tile) sort keys
+  int *valA, *valB;               // primitive ids
+  int pairCap;
+  int *tileStart, *tileEnd;
+  int tile;                       // tile edge in pixels (8, 16 or 32)
+  int tilesX, tilesY;
+  unsigned long long *fragCounter;   // FS invocations (instrumented runs only), else null
+};
+
+// ------------------------------------------------------------------------------------------------
+// exact helpers
+// ------------------------------------------------------------------------------------------------
+struct f3 { float x, y, z; };
+__device__ __forceinline__ f3 mk3(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ f3 operator-(float s, f3 a) { return {s - a.x, s - a.y, s - a.z}; }
+__device__ __forceinline__ f3 operator+(f3 a, float s) { return {a.x + s, a.y + s, a.z + s}; }
+__device__ __forceinline__ f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ float dot3(f3 a, f3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ float dot4(float4 a, float4 b) { return (a.x * b.x + a.y * b.y) + (a.z * b.z + a.w * b.w); }
+__device__ __forceinline__ float gmax(float x, float y) { return (x < y) ? y : x; }
+__device__ __forceinline__ float gmin(float x, float y) { return (y < x) ? y : x; }
+__device__ __forceinline__ float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+__device__ __forceinline__ f3 normalize3(f3 v) { return v * (1.0f / sqrtf(dot3(v, v))); }
+__device__ __forceinline__ f3 cross3(f3 a, f3 b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ f3 max3(f3 a, f3 b) { return {gmax(a.x, b.x), gmax(a.y, b.y), gmax(a.z, b.z)}; }
+__device__ __forceinline__ f3 pow3(f3 a, float e) { return {powf(a.x, e), powf(a.y, e), powf(a.z, e)}; }
+__device__ __forceinline__ f3 ld3(const uint8_t *p) {
+  const float *f = reinterpret_cast<const float *>(p);
+  return {f[0], f[1], f[2]};
+}
+// float -> u8 as `static_cast<uint8_t>(float)` compiles on the reference hosts (int32 then low byte)
+__device__ __forceinline__ uint32_t u8of(float f) { return (uint32_t) ((int) f) & 255u; }
+__device__ __forceinline__ uint32_t pack4(float r, float g, float b, float a) {
+  return u8of(r) | (u8of(g) << 8) | (u8of(b) << 16) | (u8of(a) << 24);
+}
+__device__ __forceinline__ float4 unpack4(uint32_t c) {
+  return make_float4((float) (c & 255u), (float) ((c >> 8) & 255u), (float) ((c >> 16) & 255u), (float) (c >> 24));
+}
+
+// column-major glm::mat4 * vec4 (type_mat4x4.inl:540-572)
+__device__ __forceinline__ float4 mul44(const float *m, float4 v) {
+  float4 r;
+  r.x = (m[0] * v.x + m[4] * v.y) + (m[8] * v.z + m[12] * v.w);
+  r.y = (m[1] * v.x + m[5] * v.y) + (m[9] * v.z + m[13] * v.w);
+  r.z = (m[2] * v.x + m[6] * v.y) + (m[10] * v.z + m[14] * v.w);
+  r.w = (m[3] * v.x + m[7] * v.y) + (m[11] * v.z + m[15] * v.w);
+  return r;
+}
+// glm::mat3(mat4) * vec3 and a padded mat3 * vec3 (type_mat3x3.inl:468-474): same column stride
+__device__ __forceinline__ f3 mul33(const float *m, f3 v) {
+  return {m[0] * v.x + m[4] * v.y + m[8] * v.z, m[1] * v.x + m[5] * v.y + m[9] * v.z,
+          m[2] * v.x + m[6] * v.y + m[10] * v.z};
+}
+
+// ------------------------------------------------------------------------------------------------
+// texture addressing (Base/Buffer.h:20-227) and sampling (SamplerSoft.h:117-373)
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t spread5(uint32_t v) {
+  return (v & 1u) | ((v & 2u) << 1) | ((v & 4u) << 2) | ((v & 8u) << 3) | ((v & 16u) << 4);
+}
+
+__device__ __forceinline__ uint32_t texIndex(const DevTex &t, int level, int x, int y) {
+  if (t.layout == LAYOUT_LINEAR) return (uint32_t) x + (uint32_t) y * t.w[level];
+  if (t.layout == LAYOUT_TILED) {
+    uint32_t tile = (uint32_t) (y >> 2) * t.tilesW[level] + (uint32_t) (x >> 2);
+    return (tile << 4) + ((uint32_t) (y & 3) << 2) + (uint32_t) (x & 3);
+  }
+  uint32_t tile = (uint32_t) (y >> 5) * t.tilesW[level] + (uint32_t) (x >> 5);
+  return (tile << 10) + (spread5((uint32_t) (x & 31)) | (spread5((uint32_t) (y & 31)) << 1));
+}
+
+__device__ __forceinline__ uint32_t texel(const DevTex &t, int face, int level, int x, int y) {
+  return __ldg(t.base + (size_t) face * t.layerStride + t.offset[level] + texIndex(t, level, x, y));
+}
+
+__device__ __forceinline__ uint32_t pixelWrap(const DevTex &t, int face, int level, int x, int y, int wrap,
+                                              uint32_t border) {
+  int w = t.w[level], h = t.h[level];
+  switch (wrap) {
+    case WRAP_REPEAT:
+      x = (x & ((w - 1) + w)) & (w - 1);   // CoordMod as the reference's macro expands
+      y = (y & ((h - 1) + h)) & (h - 1);
+      break;
+    case WRAP_MIRRORED:
+      x = (x & ((2 * w - 1) + 2 * w)) & (2 * w - 1);
+      y = (y & ((2 * h - 1) + 2 * h)) & (2 * h - 1);
+      x -= w;
+      y -= h;
+      x = x >= 0 ? x : (-1 - x);
+      y = y >= 0 ? y : (-1 - y);
+      x = w - 1 - x;
+      y = h - 1 - y;
+      break;
+    case WRAP_EDGE:
+      x = x < 0 ? 0 : (x >= w ? w - 1 : x);
+      y = y < 0 ? 0 : (y >= h ? h - 1 : y);
+      break;
+    default:
+      if (x < 0 || x >= w || y < 0 || y >= h) return border;
+  }
+  if ((unsigned) x < (unsigned) w && (unsigned) y < (unsigned) h) return texel(t, face, level, x, y);
+  return 0;
+}
+
+__device__ __forceinline__ uint32_t mixTexel(uint32_t x, uint32_t y, float a, bool isF) {
+  if (isF) {
+    float r = __uint_as_float(x) * (1.f - a) + __uint_as_float(y) * a;
+    return __float_as_uint(r);
+  }
+  float4 X = unpack4(x), Y = unpack4(y);
+  float ia = 1.f - a;
+  return pack4(X.x * ia + Y.x * a, X.y * ia + Y.y * a, X.z * ia + Y.z * a, X.w * ia + Y.w * a);
+}
+
+__device__ __forceinline__ uint32_t bilinearPx(const DevTex &t, int face, int level, float ux, float uy, int wrap,
+                                               uint32_t border, bool isF) {
+  float fx0 = ux - 0.5f, fy0 = uy - 0.5f;
+  float flx = floorf(fx0), fly = floorf(fy0);
+  int x = (int) flx, y = (int) fly;
+  uint32_t s1 = pixelWrap(t, face, level, x, y, wrap, border);
+  uint32_t s2 = pixelWrap(t, face, level, x + 1, y, wrap, border);
+  uint32_t s3 = pixelWrap(t, face, level, x, y + 1, wrap, border);
+  uint32_t s4 = pixelWrap(t, face, level, x + 1, y + 1, wrap, border);
+  float fx = fx0 - flx, fy = fy0 - fly;
+  return mixTexel(mixTexel(s1, s2, fx, isF), mixTexel(s3, s4, fx, isF), fy, isF);
+}
+
+__device__ __forceinline__ uint32_t nearestSample(const DevTex &t, int face, int level, float u, float v, int wrap,
+                                                  uint32_t border) {
+  float tx = u * (float) t.w[level], ty = v * (float) t.h[level];
+  return pixelWrap(t, face, level, (int) floorf(tx), (int) floorf(ty), wrap, border);
+}
+
+__device__ __forceinline__ uint32_t bilinearSample(const DevTex &t, int face, int level, float u, float v, int wrap,
+                                                   uint32_t border, bool isF) {
+  return bilinearPx(t, face, level, u * (float) t.w[level], v * (float) t.h[level], wrap, border, isF);
+}
+
+__device__ inline uint32_t textureImpl(const DevSampler &s, int face, float u, float v, float lod) {
+  const DevTex &t = s.tex;
+  if (t.levels <= 0) return 0;
+  bool isF = s.isFloat;
+  if (s.filter == FILTER_NEAREST) return nearestSample(t, face, 0, u, v, s.wrap, s.border);
+  if (s.filter == FILTER_LINEAR) return bilinearSample(t, face, 0, u, v, s.wrap, s.border, isF);
+  int maxLevel = t.levels - 1;
+  if (s.filter == FILTER_NN || s.filter == FILTER_LN) {
+    int level = min(max((int) ceilf(lod + 0.5f) - 1, 0), maxLevel);
+    if (s.filter == FILTER_NN) return nearestSample(t, face, level, u, v, s.wrap, s.border);
+    return bilinearSample(t, face, level, u, v, s.wrap, s.border, isF);
+  }
+  int hi = min(max((int) floorf(lod), 0), maxLevel);
+  int lo = min(max(hi + 1, 0), maxLevel);
+  bool nearest = s.filter == FILTER_NL;
+  uint32_t th = nearest ? nearestSample(t, face, hi, u, v, s.wrap, s.border)
+                        : bilinearSample(t, face, hi, u, v, s.wrap, s.border, isF);
+  if (hi == lo) return th;
+  uint32_t tl = nearest ? nearestSample(t, face, lo, u, v, s.wrap, s.border)
+                        : bilinearSample(t, face, lo, u, v, s.wrap, s.border, isF);
+  return mixTexel(th, tl, lod - floorf(lod), isF);
+}
+
+// BaseSamplerCube::convertXYZ2UV (SamplerSoft.h:311-373), if-chain order kept for ties
+__device__ __forceinline__ void cubeUV(f3 d, int *face, float *u, float *v) {
+  float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  bool px = d.x > 0, py = d.y > 0, pz = d.z > 0;
+  float m = 0.f, uc = 0.f, vc = 0.f;
+  int f = 0;
+  if (px && ax >= ay && ax >= az) { m = ax; uc = -d.z; vc = d.y; f = 0; }
+  if (!px && ax >= ay && ax >= az) { m = ax; uc = d.z; vc = d.y; f = 1; }
+  if (py && ay >= ax && ay >= az) { m = ay; uc = d.x; vc = -d.z; f = 2; }
+  if (!py && ay >= ax && ay >= az) { m = ay; uc = d.x; vc = d.z; f = 3; }
+  if (pz && az >= ax && az >= ay) { m = az; uc = d.x; vc = d.y; f = 4; }
+  if (!pz && az >= ax && az >= ay) { m = az; uc = -d.x; vc = d.y; f = 5; }
+  vc = -vc;
+  *face = f;
+  *u = 0.5f * (uc / m + 1.0f);
+  *v = 0.5f * (vc / m + 1.0f);
+}
+
+}  // namespace sglc

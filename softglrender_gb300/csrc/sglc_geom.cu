@@ -1,0 +1,578 @@
+// sm_103a geometry-side kernels of one draw (RendererSoft::draw, RendererSoft.cpp:136-164):
+//
+//   k_vertex      vertex shader + clip mask + perspective divide + viewport   (:170-190, 971-1003)
+//   k_clip        primitive assembly + Sutherland-Hodgman clipping; new vertices re-run the VS on
+//                 lerped raw attributes; fan triangles are appended after all input triangles in
+//                 input order via a scan of per-triangle counts                (:192-257, 489-559)
+//   k_setup       face culling + bounding box + block/quad anchoring + tile range (:277-299, 720-729)
+//   k_bin_*       (tile, primitive) pairs in primitive order, stably sorted by tile (LSD radix),
+//                 so every tile list is in the reference's primitive order
+//   k_scan_*      exclusive scans whose element counts live in device memory
+//   k_fill32, k_mip_level, k_swizzle_*   clears, mip chains (SamplerSoft.h:89-115), texture layouts
+//
+// The raster kernels are in sglc_raster.cuh, instantiated per shading model in sglc_raster_*.cu.
+// Every kernel is compiled with --fmad=false (see sglc_device.cuh).
+#include <cstdio>
+
+#include "sglc_device.cuh"
+#include "sglc_kernels.h"
+#include "sglc_shaders.cuh"  // VS bodies
+
+namespace sglc {
+
+enum { CNT_NEWVERT = 0, CNT_POLY = 1, CNT_FLAGS = 2 };
+enum { OVF_VERTS = 1, OVF_POLYS = 2, OVF_PRIMS = 4, OVF_PAIRS = 8, OVF_BADINDEX = 16 };
+
+__constant__ float4 kPlanes[6] = {{-1, 0, 0, 1}, {1, 0, 0, 1}, {0, -1, 0, 1}, {0, 1, 0, 1}, {0, 0, -1, 1}, {0, 0, 1, 1}};
+
+
+__device__ __forceinline__ int clipMaskOf(float4 c) {
+  int m = 0;
+  if (c.w < c.x) m |= 1;
+  if (c.w < -c.x) m |= 2;
+  if (c.w < c.y) m |= 4;
+  if (c.w < -c.y) m |= 8;
+  if (c.w < c.z) m |= 16;
+  if (c.w < -c.z) m |= 32;
+  return m;
+}
+
+// perspectiveDivideImpl + viewportTransformImpl (RendererSoft.cpp:981-992)
+__device__ __forceinline__ float4 toScreen(const DrawParams &p, float4 c) {
+  float invW = 1.f / c.w;
+  float4 f = make_float4(c.x * invW, c.y * invW, c.z * invW, c.w * invW);
+  f.w = invW;
+  f = make_float4(f.x * p.vp.pX, f.y * p.vp.pY, f.z * p.vp.pZ, f.w * p.vp.pW);
+  return make_float4(f.x + p.vp.oX, f.y + p.vp.oY, f.z + p.vp.oZ, f.w + p.vp.oW);
+}
+
+// ------------------------------------------------------------------------------------------------
+// vertex stage
+// ------------------------------------------------------------------------------------------------
+template<int SH>
+__global__ void __launch_bounds__(256) k_vertex(const __grid_constant__ DrawParams p) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.nv) return;
+  const float *a = p.attr + (size_t) i * p.strideF;
+  float *v = p.vVary + (size_t) i * p.varyStride;
+  float4 c = runVS<SH>(p, a, v);
+  p.vClip[i] = c;
+  p.vMask[i] = (uint8_t) clipMaskOf(c);
+  p.vFrag[i] = toScreen(p, c);
+}
+
+// ------------------------------------------------------------------------------------------------
+// assembly + clipping
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ const float *attrOf(const DrawParams &p, int idx) {
+  return idx < p.nv ? p.attr + (size_t) idx * p.strideF : p.vAttrExtra + (size_t) (idx - p.nv) * p.strideF;
+}
+
+template<int SH>
+__device__ int newClipVertex(const DrawParams &p, int i0, int i1, float t) {
+  int k = atomicAdd(&p.counters[CNT_NEWVERT], 1);
+  int idx = p.nv + k;
+  if (idx >= p.vCap) {
+    atomicOr(&p.counters[CNT_FLAGS], OVF_VERTS);
+    return -1;
+  }
+  const float *A0 = attrOf(p, i0), *A1 = attrOf(p, i1);
+  float *dst = p.vAttrExtra + (size_t) k * p.strideF;
+  for (int j = 0; j < p.strideF; j++) dst[j] = A0[j] * (1.f - t) + A1[j] * t;   // glm::mix
+  float *v = p.vVary + (size_t) idx * p.varyStride;
+  float4 c = runVS<SH>(p, dst, v);
+  p.vClip[idx] = c;
+  p.vMask[idx] = (uint8_t) clipMaskOf(c);
+  p.vFrag[idx] = toScreen(p, c);
+  return idx;
+}
+
+template<int SH>
+__global__ void __launch_bounds__(128) k_clip(const __grid_constant__ DrawParams p) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= p.ntri) return;
+  int i0 = p.indices[3 * t], i1 = p.indices[3 * t + 1], i2 = p.indices[3 * t + 2];
+  p.clipExtra[t] = 0;
+  if ((unsigned) i0 >= (unsigned) p.nv || (unsigned) i1 >= (unsigned) p.nv || (unsigned) i2 >= (unsigned) p.nv) {
+    atomicOr(&p.counters[CNT_FLAGS], OVF_BADINDEX);
+    p.prims[t] = make_int4(0, 0, 0, 1);
+    return;
+  }
+  int mask = p.vMask[i0] | p.vMask[i1] | p.vMask[i2];
+  if (mask == 0) {
+    p.prims[t] = make_int4(i0, i1, i2, 0);
+    return;
+  }
+  // Sutherland-Hodgman over the flagged planes (RendererSoft.cpp:489-559)
+  int in[12], out[12];
+  int nin = 3, nout;
+  in[0] = i0; in[1] = i1; in[2] = i2;
+  bool full = false;
+  for (int pl = 0; pl < 6; pl++) {
+    if (!(mask & (1 << pl))) continue;
+    if (nin < 3) {
+      full = true;
+      break;
+    }
+    nout = 0;
+    if (nin > 10) {
+      atomicOr(&p.counters[CNT_FLAGS], OVF_POLYS);
+      p.prims[t] = make_int4(0, 0, 0, 1);
+      return;
+    }
+    float4 P = kPlanes[pl];
+    int pre = in[0];
+    float dPre = dot4(P, p.vClip[pre]);
+    in[nin] = pre;
+    for (int k = 1; k <= nin; k++) {
+      int cur = in[k];
+      float d = dot4(P, p.vClip[cur]);
+      if (nout > 9) {   // a convex clip adds at most one vertex per plane; more means degenerate input
+        atomicOr(&p.counters[CNT_FLAGS], OVF_POLYS);
+        p.prims[t] = make_int4(0, 0, 0, 1);
+        return;
+      }
+      if (dPre >= 0) out[nout++] = pre;
+      if (signbit(dPre) != signbit(d)) {
+        float tt = d < 0 ? dPre / (dPre - d) : -dPre / (d - dPre);
+        int nvid = newClipVertex<SH>(p, pre, cur, tt);
+        if (nvid < 0) {
+          p.prims[t] = make_int4(0, 0, 0, 1);
+          return;
+        }
+        out[nout++] = nvid;
+      }
+      pre = cur;
+      dPre = d;
+    }
+    for (int k = 0; k < nout; k++) in[k] = out[k];
+    nin = nout;
+  }
+  if (full || nin == 0) {
+    p.prims[t] = make_int4(0, 0, 0, 1);
+    return;
+  }
+  if (nin > 11) {
+    atomicOr(&p.counters[CNT_FLAGS], OVF_POLYS);
+    p.prims[t] = make_int4(0, 0, 0, 1);
+    return;
+  }
+  p.prims[t] = make_int4(in[0], in[1], in[2], 0);
+  if (nin > 3) {
+    int slot = atomicAdd(&p.counters[CNT_POLY], 1);
+    if (slot >= p.clipPolyCap) {
+      atomicOr(&p.counters[CNT_FLAGS], OVF_POLYS);
+      return;
+    }
+    int4 *dst = p.clipPoly + (size_t) slot * 3;
+    dst[0] = make_int4(nin, in[0], in[1], in[2]);
+    dst[1] = make_int4(nin > 3 ? in[3] : 0, nin > 4 ? in[4] : 0, nin > 5 ? in[5] : 0, nin > 6 ? in[6] : 0);
+    dst[2] = make_int4(nin > 7 ? in[7] : 0, nin > 8 ? in[8] : 0, nin > 9 ? in[9] : 0, nin > 10 ? in[10] : 0);
+    p.clipPolyTri[slot] = t;
+    p.clipExtra[t] = nin - 3;
+  }
+}
+
+// number of primitives after clipping, kept on the device for the count-driven kernels
+__global__ void k_prim_count(const __grid_constant__ DrawParams p) {
+  p.counters[3] = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
+}
+
+__global__ void k_clip_append(const __grid_constant__ DrawParams p) {
+  int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = min(p.counters[CNT_POLY], p.clipPolyCap);
+  if (slot >= n) return;
+  int t = p.clipPolyTri[slot];
+  const int4 *src = p.clipPoly + (size_t) slot * 3;
+  int4 a = src[0], b = src[1], c = src[2];
+  int ids[11] = {a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
+  int nin = a.x;
+  int base = p.ntri + p.clipAppendOff[t];
+  for (int k = 3; k < nin; k++) {
+    int dst = base + k - 3;
+    if (dst >= p.primCap) {
+      atomicOr(&p.counters[CNT_FLAGS], OVF_PRIMS);
+      return;
+    }
+    p.prims[dst] = make_int4(ids[0], ids[k - 1], ids[k], 0);
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// setup: culling, bounding box, block anchoring, tile range
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }   // std::min
+__device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }   // std::max
+
+__global__ void __launch_bounds__(256) k_setup(const __grid_constant__ DrawParams p) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int np = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
+  if (i >= np) return;
+  int4 pr = p.prims[i];
+  TriSetup T;
+  int cnt = 0;
+  T.rx0 = 1;
+  T.rx1 = 0;
+  T.ry0 = 1;
+  T.ry1 = 0;
+  if (!(pr.w & 1)) {
+    float4 a = p.vFrag[pr.x], b = p.vFrag[pr.y], c = p.vFrag[pr.z];
+    // processFaceCulling (RendererSoft.cpp:287-297)
+    f3 e1 = mk3(b.x - a.x, b.y - a.y, b.z - a.z), e2 = mk3(c.x - a.x, c.y - a.y, c.z - a.z);
+    f3 n = cross3(e1, e2);
+    float area = (n.x * 0.f + n.y * 0.f) + n.z * 1.f;
+    bool front = area > 0;
+    bool discard = p.cullFace && !front;
+    // triangleBoundingBox (RendererSoft.cpp:1005-1019) then bounds.min -= 1 (:725)
+    float minX = smin(smin(a.x, b.x), c.x), minY = smin(smin(a.y, b.y), c.y);
+    float maxX = smax(smax(a.x, b.x), c.x), maxY = smax(smax(a.y, b.y), c.y);
+    minX = smax(minX - 0.5f, 0.f);
+    minY = smax(minY - 0.5f, 0.f);
+    maxX = smin(maxX + 0.5f, p.vp.w - 1.f);
+    maxY = smin(maxY + 0.5f, p.vp.h - 1.f);
+    minX -= 1.f;
+    minY -= 1.f;
+    if (!(isfinite(minX) && isfinite(minY) && isfinite(maxX) && isfinite(maxY))) discard = true;
+    if (!discard) {
+      int bcx = (int) (((maxX - minX) + (float) kBlock - 1.f) / (float) kBlock);
+      int bcy = (int) (((maxY - minY) + (float) kBlock - 1.f) / (float) kBlock);
+      T.v0x = a.x; T.v0y = a.y;
+      T.f0x = c.x; T.f0y = b.x; T.f0z = a.x;
+      T.f1x = c.y; T.f1y = b.y; T.f1z = a.y;
+      T.z0 = a.z; T.z1 = b.z; T.z2 = c.z;
+      T.w0 = a.w; T.w1 = b.w; T.w2 = c.w;
+      T.bminx = minX; T.bminy = minY; T.bmaxx = maxX; T.bmaxy = maxY;
+      T.bcx = bcx; T.bcy = bcy;
+      T.vid0 = pr.x; T.vid1 = pr.y; T.vid2 = pr.z;
+      T.front = front;
+      if (bcx > 0 && bcy > 0) {
+        int bsx0 = (int) (minX + 0.f), bsy0 = (int) (minY + 0.f);
+        int bsxL = (int) (minX + (float) ((bcx - 1) * kBlock)), bsyL = (int) (minY + (float) ((bcy - 1) * kBlock));
+        int fw = max(p.cw, p.dw), fh = max(p.ch, p.dh);
+        T.rx0 = max(bsx0 + 1, 0);
+        T.ry0 = max(bsy0 + 1, 0);
+        T.rx1 = min(min((int) floorf(maxX) + 1, bsxL + kBlock), fw - 1);
+        T.ry1 = min(min((int) floorf(maxY) + 1, bsyL + kBlock), fh - 1);
+        if (T.rx1 >= T.rx0 && T.ry1 >= T.ry0) {
+          int tx0 = T.rx0 / p.tile, tx1 = T.rx1 / p.tile, ty0 = T.ry0 / p.tile, ty1 = T.ry1 / p.tile;
+          cnt = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
+        }
+      }
+    }
+  }
+  p.tri[i] = T;
+  p.tileCount[i] = cnt;
+}
+
+__global__ void __launch_bounds__(256) k_bin_emit(const __grid_constant__ DrawParams p) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int np = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
+  if (i >= np || p.tileCount[i] == 0) return;
+  const TriSetup &T = p.tri[i];
+  int off = p.pairOff[i];
+  int tx0 = T.rx0 / p.tile, tx1 = T.rx1 / p.tile, ty0 = T.ry0 / p.tile, ty1 = T.ry1 / p.tile;
+  for (int ty = ty0; ty <= ty1; ty++)
+    for (int tx = tx0; tx <= tx1; tx++) {
+      if (off >= p.pairCap) {
+        atomicOr(&p.counters[CNT_FLAGS], OVF_PAIRS);
+        return;
+      }
+      p.keyA[off] = (uint32_t) (ty * p.tilesX + tx);
+      p.valA[off] = i;
+      off++;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// stable LSD radix sort of (tile, primitive) pairs by tile, 8-bit digits
+// ------------------------------------------------------------------------------------------------
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;                       // per thread
+constexpr int kSortTile = kSortThreads * kSortItems; // 2048 items per CTA
+
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint32_t *keys, const int *nPtr, int shift,
+                                                             int *hist, int numBlocks) {
+  __shared__ int h[256];
+  int n = *nPtr;
+  for (int d = threadIdx.x; d < 256; d += blockDim.x) h[d] = 0;
+  __syncthreads();
+  int base = blockIdx.x * kSortTile;
+  for (int k = 0; k < kSortItems; k++) {
+    int i = base + k * kSortThreads + threadIdx.x;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d * numBlocks + blockIdx.x] = h[d];
+}
+
+// Items of a CTA are split into 8 contiguous warp ranges of 256; each warp ranks its range in
+// order (match.any + popc), then warp prefixes per digit make the scatter stable.
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t *keysIn, const int *valsIn,
+                                                                uint32_t *keysOut, int *valsOut, const int *nPtr,
+                                                                int shift, const int *histOff, int numBlocks) {
+  __shared__ int wcount[8][256];
+  int n = *nPtr;
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int d = lane; d < 256; d += 32) wcount[warp][d] = 0;
+  __syncwarp();
+  int base = blockIdx.x * kSortTile + warp * (kSortTile / 8);
+  uint32_t myKey[kSortItems];
+  int myVal[kSortItems], myPos[kSortItems], myDig[kSortItems];
+  unsigned lt = (1u << lane) - 1u;
+  for (int k = 0; k < kSortItems; k++) {
+    int i = base + k * 32 + lane;
+    bool valid = i < n;
+    uint32_t key = valid ? keysIn[i] : 0u;
+    int dig = valid ? (int) ((key >> shift) & 255u) : 256;
+    unsigned peers = __match_any_sync(0xffffffffu, dig);
+    int rank = __popc(peers & lt);
+    int before = dig < 256 ? wcount[warp][dig] : 0;
+    __syncwarp();
+    if (dig < 256 && rank == 0) wcount[warp][dig] = before + __popc(peers);
+    __syncwarp();
+    myKey[k] = key;
+    myVal[k] = valid ? valsIn[i] : 0;
+    myDig[k] = dig;
+    myPos[k] = before + rank;
+  }
+  __syncthreads();
+  // exclusive prefix over warps for each digit
+  for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+    int s = 0;
+    for (int w = 0; w < 8; w++) {
+      int c = wcount[w][d];
+      wcount[w][d] = s;
+      s += c;
+    }
+  }
+  __syncthreads();
+  for (int k = 0; k < kSortItems; k++) {
+    int d = myDig[k];
+    if (d >= 256) continue;
+    int pos = histOff[d * numBlocks + blockIdx.x] + wcount[warp][d] + myPos[k];
+    keysOut[pos] = myKey[k];
+    valsOut[pos] = myVal[k];
+  }
+}
+
+__global__ void k_tile_ranges(const uint32_t *keys, const int *nPtr, int *tileStart, int *tileEnd) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = *nPtr;
+  if (i >= n) return;
+  uint32_t k = keys[i];
+  if (i == 0 || keys[i - 1] != k) tileStart[k] = i;
+  if (i == n - 1 || keys[i + 1] != k) tileEnd[k] = i + 1;
+}
+
+// ------------------------------------------------------------------------------------------------
+// exclusive scan (three phases), counts read from device memory
+// ------------------------------------------------------------------------------------------------
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int blockExclusiveScan(int v, int *total) {
+  __shared__ int warpSums[32];
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warpSums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int nw = blockDim.x >> 5;
+    int s = lane < nw ? warpSums[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < nw) warpSums[lane] = s;
+  }
+  __syncthreads();
+  int warpPrefix = warp > 0 ? warpSums[warp - 1] : 0;
+  *total = warpSums[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return warpPrefix + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_local(const int *in, int *out, const int *nPtr, int nMax,
+                                                             int *blockSums) {
+  int n = nPtr ? min(*nPtr, nMax) : nMax;
+  int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  int v[kScanItems], s = 0;
+  for (int k = 0; k < kScanItems; k++) {
+    int i = base + k;
+    v[k] = i < n ? in[i] : 0;
+    s += v[k];
+  }
+  int total;
+  int pre = blockExclusiveScan(s, &total);
+  for (int k = 0; k < kScanItems; k++) {
+    int i = base + k;
+    if (i < nMax) out[i] = pre;
+    pre += v[k];
+  }
+  if (threadIdx.x == 0) blockSums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_sums(int *blockSums, int numBlocks) {
+  // single CTA: exclusive scan of up to kScanTile block sums, in place; total at [numBlocks]
+  int base = threadIdx.x * kScanItems;
+  int v[kScanItems], s = 0;
+  for (int k = 0; k < kScanItems; k++) {
+    int i = base + k;
+    v[k] = i < numBlocks ? blockSums[i] : 0;
+    s += v[k];
+  }
+  int total;
+  int pre = blockExclusiveScan(s, &total);
+  for (int k = 0; k < kScanItems; k++) {
+    int i = base + k;
+    if (i < numBlocks) blockSums[i] = pre;
+    pre += v[k];
+  }
+  if (threadIdx.x == 0) blockSums[numBlocks] = total;
+}
+
+__global__ void k_scan_add(int *out, const int *nPtr, int nMax, const int *blockSums, int numBlocks) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = nPtr ? min(*nPtr, nMax) : nMax;
+  if (i < nMax) out[i] += blockSums[i / kScanTile];
+  if (i == 0) out[nMax] = blockSums[numBlocks];
+  (void) n;
+}
+
+// ------------------------------------------------------------------------------------------------
+// clear, mip generation
+// ------------------------------------------------------------------------------------------------
+__global__ void k_fill32(uint32_t *dst, uint32_t value, size_t n) {
+  size_t i = (size_t) blockIdx.x * blockDim.x + threadIdx.x;
+  size_t stride = (size_t) gridDim.x * blockDim.x;
+  for (; i < n; i += stride) dst[i] = value;
+}
+
+// BaseSampler::sampleBufferBilinear (SamplerSoft.h:240-252): level l from level l-1
+__global__ void k_mip_level(DevTex t, int face, int level, int isFloat) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  int w = t.w[level], h = t.h[level];
+  if (x >= w || y >= h) return;
+  float rx = (float) t.w[level - 1] / (float) w, ry = (float) t.h[level - 1] / (float) h;
+  float dx = 0.5f * rx, dy = 0.5f * ry;
+  float u = (float) x * rx + dx, v = (float) y * ry + dy;
+  uint32_t c = bilinearPx(t, face, level - 1, u, v, WRAP_EDGE, 0u, isFloat != 0);
+  uint32_t *dst = const_cast<uint32_t *>(t.base) + (size_t) face * t.layerStride + t.offset[level] + texIndex(t, level, x, y);
+  *dst = c;
+}
+
+// linear host image -> the texture's storage layout
+__global__ void k_swizzle_in(DevTex t, int face, int level, const uint32_t *src) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  int w = t.w[level], h = t.h[level];
+  if (x >= w || y >= h) return;
+  uint32_t *dst = const_cast<uint32_t *>(t.base) + (size_t) face * t.layerStride + t.offset[level] + texIndex(t, level, x, y);
+  *dst = src[(size_t) y * w + x];
+}
+
+__global__ void k_swizzle_out(DevTex t, int face, int level, uint32_t *dst) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  int w = t.w[level], h = t.h[level];
+  if (x >= w || y >= h) return;
+  dst[(size_t) y * w + x] = texel(t, face, level, x, y);
+}
+
+// ------------------------------------------------------------------------------------------------
+// host-side launchers
+// ------------------------------------------------------------------------------------------------
+static inline int cdiv(long a, long b) { return (int) ((a + b - 1) / b); }
+
+void scanExclusive(const int *in, int *out, const int *nPtr, int nMax, int *blockSums, cudaStream_t st) {
+  int nb = max(1, cdiv(nMax, kScanTile));
+  k_scan_local<<<nb, kScanThreads, 0, st>>>(in, out, nPtr, nMax, blockSums);
+  k_scan_sums<<<1, kScanThreads, 0, st>>>(blockSums, nb);
+  k_scan_add<<<max(1, cdiv(nMax, 256)), 256, 0, st>>>(out, nPtr, nMax, blockSums, nb);
+}
+
+int scanScratchInts(int nMax) { return max(1, cdiv(nMax, kScanTile)) + 1; }
+
+template<int SH>
+static void launchGeometry(const DrawParams &p, cudaStream_t st) {
+  if (p.nv > 0) k_vertex<SH><<<cdiv(p.nv, 256), 256, 0, st>>>(p);
+  if (p.ntri > 0) k_clip<SH><<<cdiv(p.ntri, 128), 128, 0, st>>>(p);
+}
+
+void launchVertexAndClip(const DrawParams &p, cudaStream_t st) {
+  switch (p.shading) {
+    case SH_BASE: launchGeometry<SH_BASE>(p, st); break;
+    case SH_BLINN: launchGeometry<SH_BLINN>(p, st); break;
+    case SH_BLINN_DIR: launchGeometry<SH_BLINN_DIR>(p, st); break;
+    case SH_PBR: launchGeometry<SH_PBR>(p, st); break;
+    case SH_VCOLOR: launchGeometry<SH_VCOLOR>(p, st); break;
+  }
+}
+
+void launchClipAppend(const DrawParams &p, cudaStream_t st) {
+  k_clip_append<<<max(1, cdiv(p.clipPolyCap, 256)), 256, 0, st>>>(p);
+  k_prim_count<<<1, 1, 0, st>>>(p);
+}
+
+void launchSetup(const DrawParams &p, int primCount, cudaStream_t st) {
+  if (primCount > 0) k_setup<<<cdiv(primCount, 256), 256, 0, st>>>(p);
+}
+
+void launchBinEmit(const DrawParams &p, int primCount, cudaStream_t st) {
+  if (primCount > 0) k_bin_emit<<<cdiv(primCount, 256), 256, 0, st>>>(p);
+}
+
+int sortScratchInts(int nPairs) { return 256 * max(1, cdiv(nPairs, kSortTile)) + 1; }
+
+// sorts (keyA,valA) by key, result back in (keyA,valA); hist needs sortScratchInts ints plus a
+// scan scratch of scanScratchInts(256 * blocks)
+void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, int *hist, int *histScan,
+               int *scanScratch, cudaStream_t st) {
+  if (nPairs <= 0) return;
+  int nb = cdiv(nPairs, kSortTile);
+  uint32_t *kin = p.keyA, *kout = p.keyB;
+  int *vin = p.valA, *vout = p.valB;
+  int passes = keyBits <= 8 ? 1 : 2;
+  for (int pass = 0; pass < passes; pass++) {
+    int shift = pass * 8;
+    k_radix_hist<<<nb, kSortThreads, 0, st>>>(kin, nPtr, shift, hist, nb);
+    scanExclusive(hist, histScan, nullptr, 256 * nb, scanScratch, st);
+    k_radix_scatter<<<nb, kSortThreads, 0, st>>>(kin, vin, kout, vout, nPtr, shift, histScan, nb);
+    uint32_t *tk = kin; kin = kout; kout = tk;
+    int *tv = vin; vin = vout; vout = tv;
+  }
+  if (passes == 1) {   // result must land in A
+    cudaMemcpyAsync(p.keyA, p.keyB, sizeof(uint32_t) * (size_t) nPairs, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(p.valA, p.valB, sizeof(int) * (size_t) nPairs, cudaMemcpyDeviceToDevice, st);
+  }
+}
+
+void launchTileRanges(const DrawParams &p, int nPairs, const int *nPtr, cudaStream_t st) {
+  if (nPairs > 0) k_tile_ranges<<<cdiv(nPairs, 256), 256, 0, st>>>(p.keyA, nPtr, p.tileStart, p.tileEnd);
+}
+
+void launchFill32(uint32_t *dst, uint32_t value, size_t n, cudaStream_t st) {
+  if (n == 0) return;
+  int grid = (int) min((size_t) 152 * 8, (n + 255) / 256);
+  k_fill32<<<grid, 256, 0, st>>>(dst, value, n);
+}
+
+void launchMipLevel(const DevTex &t, int face, int level, int isFloat, cudaStream_t st) {
+  dim3 b(16, 16), g(cdiv(t.w[level], 16), cdiv(t.h[level], 16));
+  k_mip_level<<<g, b, 0, st>>>(t, face, level, isFloat);
+}
+
+void launchSwizzleIn(const DevTex &t, int face, int level, const uint32_t *src, cudaStream_t st) {
+  dim3 b(16, 16), g(cdiv(t.w[level], 16), cdiv(t.h[level], 16));
+  k_swizzle_in<<<g, b, 0, st>>>(t, face, level, src);
+}
+
+void launchSwizzleOut(const DevTex &t, int face, int level, uint32_t *dst, cudaStream_t st) {
+  dim3 b(16, 16), g(cdiv(t.w[level], 16), cdiv(t.h[level], 16));
+  k_swizzle_out<<<g, b, 0, st>>>(t, face, level, dst);
+}
+
+}  // namespace sglc

@@ -1,0 +1,26 @@
+// Host-side launchers of the draw kernels (sglc_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sglc_device.cuh"
+
+namespace sglc {
+
+void scanExclusive(const int *in, int *out, const int *nPtr, int nMax, int *blockSums, cudaStream_t st);
+int scanScratchInts(int nMax);
+void launchVertexAndClip(const DrawParams &p, cudaStream_t st);
+void launchClipAppend(const DrawParams &p, cudaStream_t st);
+void launchSetup(const DrawParams &p, int primCount, cudaStream_t st);
+void launchBinEmit(const DrawParams &p, int primCount, cudaStream_t st);
+int sortScratchInts(int nPairs);
+void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, int *hist, int *histScan,
+               int *scanScratch, cudaStream_t st);
+void launchTileRanges(const DrawParams &p, int nPairs, const int *nPtr, cudaStream_t st);
+void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
+void launchFill32(uint32_t *dst, uint32_t value, size_t n, cudaStream_t st);
+void launchMipLevel(const DevTex &t, int face, int level, int isFloat, cudaStream_t st);
+void launchSwizzleIn(const DevTex &t, int face, int level, const uint32_t *src, cudaStream_t st);
+void launchSwizzleOut(const DevTex &t, int face, int level, uint32_t *dst, cudaStream_t st);
+
+}  // namespace sglc

@@ -1,0 +1,27 @@
+// Raster instantiations: base colour, vertex colour and depth-only passes, plus the dispatcher.
+#include "sglc_kernels.h"
+#include "sglc_raster.cuh"
+
+namespace sglc {
+
+void launchRasterBlinn(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
+void launchRasterPbr(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
+
+void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
+  int grid = p.tilesX * p.tilesY;
+  if (!hasColor) {   // depth-only pass: the fragment shader is skipped (RendererSoft.cpp:346-348)
+    if (!hasDepth) return;
+    if (p.samples == 4) k_raster<SH_BASE, 4, false, true><<<grid, 256, 0, st>>>(p);
+    else k_raster<SH_BASE, 1, false, true><<<grid, 256, 0, st>>>(p);
+    return;
+  }
+  switch (p.shading) {
+    case SH_BASE: launchRasterModel<SH_BASE>(p, hasColor, hasDepth, st); break;
+    case SH_VCOLOR: launchRasterModel<SH_VCOLOR>(p, hasColor, hasDepth, st); break;
+    case SH_BLINN:
+    case SH_BLINN_DIR: launchRasterBlinn(p, hasColor, hasDepth, st); break;
+    case SH_PBR: launchRasterPbr(p, hasColor, hasDepth, st); break;
+  }
+}
+
+}  // namespace sglc

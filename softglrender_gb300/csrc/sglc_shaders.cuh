@@ -1,0 +1,286 @@
+// Device vertex / fragment shaders: the reference's software shaders as device functions.
+//
+//   Basic        Shader/Software/BasicSoft.h:62-79
+//   Blinn-Phong  Shader/Software/BlinnPhongSoft.h:181-325 (point light, shininess 128, PCF shadow)
+//   PBR + IBL    Shader/Software/PbrSoft.h:106-323
+//   Blinn-Phong directional (shininess 32) and vertex colour: device shaders of the synthetic
+//   benchmark scenes (no reference counterpart).
+//
+// Uniform bytes use the reference's ShaderUniforms layout (GLM aligned: vec3 = 16 B):
+// UniformsModel @0 (reverseZ, model @16, MVP @80, inverse-transpose model mat3 @144,
+// shadow MVP @192); Blinn-Phong/PBR: UniformsScene @256, UniformsMaterial @320;
+// Basic/vertex colour: UniformsMaterial @256. Varyings are ShaderVaryings floats.
+#pragma once
+
+#include "sglc_device.cuh"
+
+namespace sglc {
+
+__device__ __forceinline__ const float *uMVP(const DrawParams &p) { return reinterpret_cast<const float *>(p.u + 80); }
+__device__ __forceinline__ const float *uModel(const DrawParams &p) { return reinterpret_cast<const float *>(p.u + 16); }
+__device__ __forceinline__ const float *uITModel(const DrawParams &p) { return reinterpret_cast<const float *>(p.u + 144); }
+__device__ __forceinline__ const float *uShadowMVP(const DrawParams &p) { return reinterpret_cast<const float *>(p.u + 192); }
+__device__ __forceinline__ int uI32(const DrawParams &p, int off) { return *reinterpret_cast<const int32_t *>(p.u + off); }
+__device__ __forceinline__ float uF32(const DrawParams &p, int off) { return *reinterpret_cast<const float *>(p.u + off); }
+__device__ __forceinline__ float4 uV4(const DrawParams &p, int off) { return *reinterpret_cast<const float4 *>(p.u + off); }
+
+// VS: writes clip position and the varyings of one vertex. a = raw attribute floats.
+template<int SH>
+__device__ __forceinline__ float4 runVS(const DrawParams &p, const float *a, float *v) {
+  float4 position = make_float4(a[0], a[1], a[2], 1.0f);
+  float4 pos = mul44(uMVP(p), position);
+  if (SH == SH_VCOLOR) {
+    v[0] = a[4]; v[1] = a[5]; v[2] = a[6]; v[3] = a[7];
+  } else if (SH == SH_BLINN || SH == SH_BLINN_DIR || SH == SH_PBR) {
+    const bool bp = SH != SH_PBR;
+    v[0] = a[4];
+    v[1] = a[5];
+    if (bp) {
+      float4 s = mul44(uShadowMVP(p), position);
+      v[20] = s.x; v[21] = s.y; v[22] = s.z; v[23] = s.w;
+    }
+    float4 w4 = mul44(uModel(p), position);
+    f3 world = mk3(w4.x, w4.y, w4.z);
+    f3 nvec = mul33(uModel(p), mk3(a[8], a[9], a[10]));
+    f3 lpos = ld3(p.u + 288);
+    f3 ldir = (SH == SH_BLINN_DIR) ? lpos : lpos - world;
+    f3 cdir = ld3(p.u + 272) - world;
+    v[4] = nvec.x; v[5] = nvec.y; v[6] = nvec.z;
+    v[8] = world.x; v[9] = world.y; v[10] = world.z;
+    v[12] = cdir.x; v[13] = cdir.y; v[14] = cdir.z;
+    v[16] = ldir.x; v[17] = ldir.y; v[18] = ldir.z;
+    if (p.def[1]) {   // NORMAL_MAP
+      f3 N = normalize3(mul33(uITModel(p), mk3(a[8], a[9], a[10])));
+      f3 T = normalize3(mul33(uITModel(p), mk3(a[12], a[13], a[14])));
+      f3 Tn = normalize3(T - dot3(T, N) * N);
+      const int o = bp ? 24 : 20;
+      v[o] = N.x; v[o + 1] = N.y; v[o + 2] = N.z;
+      v[o + 4] = Tn.x; v[o + 5] = Tn.y; v[o + 6] = Tn.z;
+    }
+  }
+  return pos;
+}
+
+// Interpolated varyings of one fragment, evaluated on demand from the triangle's three vertex
+// rows with the reference's AVX2 sequence: s = v0*b0; s = fma(v1,b1,s); s = fma(v2,b2,s).
+struct Vary {
+  const float *r0, *r1, *r2;
+  float b0, b1, b2;
+  __device__ __forceinline__ float operator[](int i) const {
+    float s = __ldg(r0 + i) * b0;
+    s = __fmaf_rn(__ldg(r1 + i), b1, s);
+    s = __fmaf_rn(__ldg(r2 + i), b2, s);
+    return s;
+  }
+  __device__ __forceinline__ f3 v3(int i) const { return mk3((*this)[i], (*this)[i + 1], (*this)[i + 2]); }
+};
+
+struct FragIn {
+  Vary v;
+  float dudx, dvdx, dudy, dvdy;   // texcoord differences p1-p0, p2-p0 of the quad
+};
+
+// ShaderSoft::getSampler2DLod (Render/Software/ShaderSoft.h:117-133)
+__device__ __forceinline__ float lodOf(const DevSampler &s, const FragIn &f) {
+  float tw = (float) s.width, th = (float) s.height;
+  float dxx = f.dudx * tw, dxy = f.dvdx * th;
+  float dyx = f.dudy * tw, dyy = f.dvdy * th;
+  float d = gmax(dxx * dxx + dxy * dxy, dyx * dyx + dyy * dyy);
+  return gmax(0.5f * log2f(d), 0.0f);
+}
+
+// ShaderSoft::texture for RGBA8 2D samplers: texel / 255
+__device__ __forceinline__ float4 tex2D(const DrawParams &p, int slot, float u, float v, const FragIn &f) {
+  const DevSampler &s = p.samp[slot];
+  float lod = 0.f;
+  if (s.lodFromDerivative) lod += lodOf(s, f);
+  float4 c = unpack4(textureImpl(s, 0, u, v, lod));
+  return make_float4(c.x / 255.f, c.y / 255.f, c.z / 255.f, c.w / 255.f);
+}
+
+__device__ __forceinline__ float4 texCube(const DrawParams &p, int slot, f3 d, float lod) {
+  int face;
+  float u, v;
+  cubeUV(d, &face, &u, &v);
+  float4 c = unpack4(textureImpl(p.samp[slot], face, u, v, lod));
+  return make_float4(c.x / 255.f, c.y / 255.f, c.z / 255.f, c.w / 255.f);
+}
+
+__device__ __forceinline__ f3 normalFromMap(const DrawParams &p, const FragIn &f, int nOff, int tOff) {
+  if (p.def[1]) {
+    f3 N = normalize3(f.v.v3(nOff));
+    f3 T = normalize3(f.v.v3(tOff));
+    T = normalize3(T - dot3(T, N) * N);
+    f3 B = cross3(T, N);
+    float4 t = tex2D(p, 1, f.v[0], f.v[1], f);
+    f3 tn = mk3(t.x * 2.0f - 1.0f, t.y * 2.0f - 1.0f, t.z * 2.0f - 1.0f);
+    f3 r = mk3(T.x * tn.x + B.x * tn.y + N.x * tn.z, T.y * tn.x + B.y * tn.y + N.y * tn.z,
+               T.z * tn.x + B.z * tn.y + N.z * tn.z);
+    return normalize3(r);
+  }
+  return normalize3(f.v.v3(4));
+}
+
+// BlinnPhongSoft.h:247-271 (3x3 PCF against a FLOAT32 shadow map, sampler slot 4)
+__device__ inline float shadowCalc(const DrawParams &p, const FragIn &f, f3 normal) {
+  float fx = f.v[20], fy = f.v[21], fz = f.v[22], fw = f.v[23];
+  float px = fx / fw, py = fy / fw, cur = fz / fw;
+  if (cur < 0.f || cur > 1.f) return 0.0f;
+  float bias = gmax(0.00025f * (1.0f - dot3(normal, normalize3(f.v.v3(16)))), 0.00005f);
+  const DevSampler &s = p.samp[4];
+  float ox = 1.0f / (float) s.tex.w[0], oy = 1.0f / (float) s.tex.h[0];
+  int reverseZ = uI32(p, 0);
+  float shadow = 0.0f;
+  for (int x = -1; x <= 1; ++x)
+    for (int y = -1; y <= 1; ++y) {
+      float pcf = __uint_as_float(textureImpl(s, 0, px + (float) x * ox, py + (float) y * oy, 0.f));
+      if (reverseZ) shadow += cur + bias < pcf ? 1.0f : 0.0f;
+      else shadow += cur - bias > pcf ? 1.0f : 0.0f;
+    }
+  return shadow / 9.0f;
+}
+
+template<bool DIRECTIONAL>
+__device__ inline float4 fsBlinnPhong(const DrawParams &p, const FragIn &f) {
+  const float specExp = DIRECTIONAL ? 32.f : 128.f;
+  const float rangeInv = 1.0f / 5.f;
+  float4 base = p.def[0] ? tex2D(p, 0, f.v[0], f.v[1], f) : uV4(p, 352);
+  f3 N = normalFromMap(p, f, 24, 28);
+  float ao = 1.f;
+  if (p.def[3]) ao = tex2D(p, 3, f.v[0], f.v[1], f).x;
+  f3 baseRgb = mk3(base.x, base.y, base.z);
+  f3 ambient = baseRgb * ld3(p.u + 256) * ao;
+  f3 diffuseC = mk3(0, 0, 0), specC = mk3(0, 0, 0), emis = mk3(0, 0, 0);
+  if (uI32(p, 320)) {
+    f3 ldirRaw = f.v.v3(16);
+    f3 lightColor = ld3(p.u + 304);
+    f3 L = normalize3(ldirRaw);
+    float diffuse = gmax(dot3(N, L), 0.0f);
+    if (DIRECTIONAL) {
+      diffuseC = lightColor * baseRgb * diffuse;
+    } else {
+      f3 lDir = ldirRaw * rangeInv;
+      float att = gclamp(1.0f - dot3(lDir, lDir), 0.0f, 1.0f);
+      diffuseC = lightColor * baseRgb * diffuse * att;
+    }
+    f3 C = normalize3(f.v.v3(12));
+    f3 H = normalize3(L + C);
+    float sa = gmax(dot3(N, H), 0.0f);
+    float pw = powf(sa, specExp);
+    specC = uF32(p, 336) * mk3(pw, pw, pw);
+    if (uI32(p, 328)) {
+      float shadow = 1.0f - shadowCalc(p, f, N);
+      diffuseC = diffuseC * shadow;
+      specC = specC * shadow;
+    }
+  }
+  if (p.def[2]) {
+    float4 e = tex2D(p, 2, f.v[0], f.v[1], f);
+    emis = mk3(e.x, e.y, e.z);
+  }
+  f3 c = ambient + diffuseC + specC + emis;
+  return make_float4(c.x, c.y, c.z, base.w);
+}
+
+__device__ inline float4 fsPbr(const DrawParams &p, const FragIn &f) {
+  const float PI = 3.14159265359f;
+  const float rangeInv = 1.0f / 5.f;
+  float4 arg = p.def[0] ? tex2D(p, 0, f.v[0], f.v[1], f) : uV4(p, 352);
+  f3 albedo = mk3(powf(arg.x, 2.2f), powf(arg.y, 2.2f), powf(arg.z, 2.2f));
+  float metallic = 0.0f, roughness = 1.0f;
+  if (p.def[4]) {
+    float4 mr = tex2D(p, 4, f.v[0], f.v[1], f);
+    metallic = mr.z;
+    roughness = mr.y;
+  }
+  float ao = 1.f;
+  if (p.def[3]) ao = tex2D(p, 3, f.v[0], f.v[1], f).x;
+  f3 N = normalFromMap(p, f, 20, 24);
+  f3 V = normalize3(f.v.v3(12));
+  f3 mV = -V;
+  f3 R = mV - N * dot3(N, mV) * 2.0f;
+  f3 F0 = mk3(0.04f, 0.04f, 0.04f);
+  F0 = F0 * (1.0f - metallic) + albedo * metallic;
+  f3 Lo = mk3(0, 0, 0);
+  if (uI32(p, 320)) {
+    f3 ldir = f.v.v3(16);
+    f3 L = normalize3(ldir);
+    f3 H = normalize3(V + L);
+    f3 lDir = ldir * rangeInv;
+    float att = gclamp(1.0f - dot3(lDir, lDir), 0.0f, 1.0f);
+    f3 radiance = ld3(p.u + 304) * att;
+    float a = roughness * roughness;
+    float a2 = a * a;
+    float NdotH = gmax(dot3(N, H), 0.0f);
+    float NdotH2 = NdotH * NdotH;
+    float denom = (NdotH2 * (a2 - 1.0f) + 1.0f);
+    denom = PI * denom * denom;
+    float NDF = a2 / denom;
+    float NdotV = gmax(dot3(N, V), 0.0f);
+    float NdotL = gmax(dot3(N, L), 0.0f);
+    float r1 = (roughness + 1.0f);
+    float k = (r1 * r1) / 8.0f;
+    float ggx2 = NdotV / (NdotV * (1.0f - k) + k);
+    float ggx1 = NdotL / (NdotL * (1.0f - k) + k);
+    float G = ggx1 * ggx2;
+    float ct = gmax(dot3(H, V), 0.0f);
+    float p5 = powf(gclamp(1.0f - ct, 0.0f, 1.0f), 5.0f);
+    f3 F = F0 + (1.0f - F0) * p5;
+    f3 numerator = NDF * G * F;
+    float denominator = 4.0f * gmax(dot3(N, V), 0.0f) * gmax(dot3(N, L), 0.0f) + 0.0001f;
+    f3 specular = numerator / denominator;
+    f3 kD = 1.0f - F;
+    kD = kD * (1.0f - metallic);
+    float NdL = gmax(dot3(N, L), 0.0f);
+    Lo = Lo + (kD * albedo / PI + specular) * radiance * NdL;
+  }
+  f3 ambient;
+  if (uI32(p, 324)) {
+    float NdotV = gmax(dot3(N, V), 0.0f);
+    float p5 = powf(gclamp(1.0f - NdotV, 0.0f, 1.0f), 5.0f);
+    float omr = 1.0f - roughness;
+    f3 F = F0 + (max3(mk3(omr, omr, omr), F0) - F0) * p5;
+    f3 kD = 1.0f - F;
+    kD = kD * (1.0f - metallic);
+    float4 irr = texCube(p, 5, N, 0.f);
+    f3 diffuse = mk3(irr.x, irr.y, irr.z) * albedo;
+    float4 pre = texCube(p, 6, R, roughness * 4.0f);
+    // EnvBRDFApprox (PbrSoft.h:209-223)
+    float rx = roughness * -1.f + 1.f, ry = roughness * -0.0275f + 0.0425f;
+    float rz = roughness * -0.572f + 1.04f, rw = roughness * 0.022f + -0.04f;
+    float a004 = gmin(rx * rx, exp2f(-9.28f * NdotV)) * rx + ry;
+    float ABx = -1.04f * a004 + rz;
+    float ABy = 1.04f * a004 + rw;
+    ABy *= gmax(0.f, gmin(1.f, 50.0f * F.y));
+    f3 env = F * ABx + ABy;
+    f3 specular = mk3(pre.x, pre.y, pre.z) * env;
+    ambient = (kD * diffuse + specular) * ao;
+  } else {
+    ambient = ld3(p.u + 256) * albedo * ao;
+  }
+  f3 color = ambient + Lo;
+  color = pow3(color, 1.0f / 2.2f);
+  if (p.def[2]) {
+    float4 e = tex2D(p, 2, f.v[0], f.v[1], f);
+    color = color + mk3(e.x, e.y, e.z);
+  }
+  return make_float4(color.x, color.y, color.z, arg.w);
+}
+
+template<int SH>
+__device__ __forceinline__ float4 runFS(const DrawParams &p, const FragIn &f) {
+  if (SH == SH_BASE) return uV4(p, 256 + 32);
+  if (SH == SH_VCOLOR) return make_float4(f.v[0], f.v[1], f.v[2], f.v[3]);
+  if (SH == SH_BLINN) return fsBlinnPhong<false>(p, f);
+  if (SH == SH_BLINN_DIR) return fsBlinnPhong<true>(p, f);
+  return fsPbr(p, f);
+}
+
+// does the FS read texcoord derivatives (any bound 2D sampler with a mip filter and LOD callback)
+__device__ __forceinline__ bool needsDerivatives(const DrawParams &p) {
+  for (int s = 0; s < 4; s++)
+    if (p.samp[s].valid && p.samp[s].lodFromDerivative && p.def[s]) return true;
+  return false;
+}
+
+}  // namespace sglc

@@ -453,7 +453,11 @@ class Scene:
         h = hashlib.sha256()
         for p in self.passes:
             h.update(struct.pack("<4i", p.width, p.height, p.samples, int(p.color)))
+            h.update(repr((p.clear.depthFlag, p.clear.colorFlag, tuple(p.clear.clearColor), p.clear.clearDepth)).encode())
             for d in p.draws:
+                h.update(repr((d.shading, tuple(d.defines), d.stride, d.states)).encode())
+                for t in d.textures:
+                    h.update(repr((t.name, t.desc, t.sampler)).encode())
                 h.update(np.ascontiguousarray(d.vertexes).tobytes())
                 h.update(np.ascontiguousarray(d.indices).tobytes())
                 for k in sorted(d.blocks):
