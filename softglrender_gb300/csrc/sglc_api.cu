@@ -166,8 +166,8 @@ struct Ctx {
   unsigned long long *fragCounter = nullptr;
   // scratch
   DevBuf vClip, vFrag, vMask, vVary, vAttrExtra, prims, clipExtra, clipAppendOff, clipPoly, clipPolyTri, counters;
-  DevBuf tri, tileCount, pairOff, keyA, keyB, valA, valB, tileStart, tileEnd, scanScratch, sortHist, sortHistScan,
-      staging;
+  DevBuf tri, tileCount, pairOff, keyA, keyB, valA, valB, tileStart, tileEnd, tileOrder, scanScratch, sortHist,
+      sortHistScan, staging;
   // capacity hints that survive between draws
   int extraVertHint = 0, polyHint = 0, appendHint = 0;
 
@@ -368,6 +368,8 @@ sglc_status drawImpl(Ctx *c) {
     d.isFloat = us.format == SGLC_FORMAT_FLOAT32;
     d.tex = devTex(to->tex);
   }
+  for (int s = 0; s < 4; s++)
+    if (p.samp[s].valid && p.samp[s].lodFromDerivative && p.def[s]) p.needDeriv = 1;
   p.depthTest = rs.depth_test;
   p.depthMask = rs.depth_mask;
   p.depthFunc = rs.depth_func;
@@ -378,6 +380,35 @@ sglc_status drawImpl(Ctx *c) {
   p.bFuncA = rs.blend_func_alpha;
   p.bSrcA = rs.blend_src_alpha;
   p.bDstA = rs.blend_dst_alpha;
+  // BlendFactor -> (operand, c0, c1) with factor = c0 + c1 * operand (BlendSoft.h:13-30)
+  {
+    const int facs[4] = {rs.blend_src_rgb, rs.blend_dst_rgb, rs.blend_src_alpha, rs.blend_dst_alpha};
+    for (int k = 0; k < 4; k++) {
+      int f = facs[k], op = 0;
+      float c0 = 0.f, c1 = 0.f;
+      switch (f) {
+        case SGLC_BLEND_ZERO: break;
+        case SGLC_BLEND_ONE: c0 = 1.f; break;
+        case SGLC_BLEND_SRC_COLOR: op = 0; c1 = 1.f; break;
+        case SGLC_BLEND_SRC_ALPHA: op = 1; c1 = 1.f; break;
+        case SGLC_BLEND_DST_COLOR: op = 2; c1 = 1.f; break;
+        case SGLC_BLEND_DST_ALPHA: op = 3; c1 = 1.f; break;
+        case SGLC_BLEND_ONE_MINUS_SRC_COLOR: op = 0; c0 = 1.f; c1 = -1.f; break;
+        case SGLC_BLEND_ONE_MINUS_SRC_ALPHA: op = 1; c0 = 1.f; c1 = -1.f; break;
+        case SGLC_BLEND_ONE_MINUS_DST_COLOR: op = 2; c0 = 1.f; c1 = -1.f; break;
+        case SGLC_BLEND_ONE_MINUS_DST_ALPHA: op = 3; c0 = 1.f; c1 = -1.f; break;
+      }
+      p.bfOp[k] = op;
+      p.bfC0[k] = c0;
+      p.bfC1[k] = c1;
+    }
+    const int fns[2] = {rs.blend_func_rgb, rs.blend_func_alpha};
+    for (int k = 0; k < 2; k++) {
+      p.bKs[k] = fns[k] == SGLC_FUNC_REVERSE_SUBTRACT ? -1.f : 1.f;
+      p.bKd[k] = fns[k] == SGLC_FUNC_SUBTRACT ? -1.f : 1.f;
+      p.bMinMax[k] = fns[k] == SGLC_FUNC_MIN ? 1 : (fns[k] == SGLC_FUNC_MAX ? 2 : 0);
+    }
+  }
   p.cullFace = rs.cull_face;
   p.earlyZ = c->earlyZ;
   p.vp = c->vp;
@@ -482,6 +513,7 @@ sglc_status drawImpl(Ctx *c) {
     CK(c->valB.ensure(sizeof(int) * (size_t) std::max(nPairs, 1)));
     CK(c->tileStart.ensure(sizeof(int) * (size_t) numTiles));
     CK(c->tileEnd.ensure(sizeof(int) * (size_t) numTiles));
+    CK(c->tileOrder.ensure(sizeof(int) * (size_t) numTiles));
     int sortInts = sortScratchInts(nPairs);
     CK(c->sortHist.ensure(sizeof(int) * (size_t) sortInts));
     CK(c->sortHistScan.ensure(sizeof(int) * (size_t) sortInts));
@@ -502,6 +534,8 @@ sglc_status drawImpl(Ctx *c) {
     sortPairs(p, nPairs, nPairsDev, keyBits, c->sortHist.as<int>(), c->sortHistScan.as<int>(),
               c->scanScratch.as<int>(), c->stream);
     launchTileRanges(p, nPairs, nPairsDev, c->stream);
+    launchTileOrder(p, c->tileOrder.as<int>(), c->stream);
+    p.tileOrder = c->tileOrder.as<int>();
     if (c->statsLevel >= 2) {
       CK(cudaMemsetAsync(c->fragCounter, 0, sizeof(unsigned long long), c->stream));
       p.fragCounter = c->fragCounter;
@@ -522,7 +556,7 @@ sglc_status drawImpl(Ctx *c) {
     // vertex, clip, 3 scan, append, count, setup, 3 scan | emit, sort, ranges, raster
     int sortPasses = nPairs > 0 ? (keyBits <= 8 ? 1 : 2) : 0;
     c->stats.kernel_launches = (p.nv > 0) + (p.ntri > 0) + 3 + 2 + 1 + 3 + (np > 0) + sortPasses * 5 +
-                               (nPairs > 0) + 1 + attempt * 10;
+                               (nPairs > 0) + 1 + 1 + attempt * 10;
     return SGLC_OK;
   }
   return c->fail(SGLC_ERR_OVERFLOW, "draw: clip capacity could not be satisfied");
@@ -570,7 +604,7 @@ sglc_status sglc_destroy(sglc_context *ctx) {
   }
   DevBuf *bufs[] = {&c->vClip, &c->vFrag, &c->vMask, &c->vVary, &c->vAttrExtra, &c->prims, &c->clipExtra,
                     &c->clipAppendOff, &c->clipPoly, &c->clipPolyTri, &c->counters, &c->tri, &c->tileCount,
-                    &c->pairOff, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->tileStart, &c->tileEnd,
+                    &c->pairOff, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->tileStart, &c->tileEnd, &c->tileOrder,
                     &c->scanScratch, &c->sortHist, &c->sortHistScan, &c->staging};
   for (DevBuf *b : bufs) b->release();
   cudaFreeHost(c->hostCounters);

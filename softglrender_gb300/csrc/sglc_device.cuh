@@ -79,6 +79,13 @@ struct DrawParams {
   // pipeline state
   int depthTest, depthMask, depthFunc, blend;
   int bFuncRgb, bSrcRgb, bDstRgb, bFuncA, bSrcA, bDstA;
+  // branch-free blending (calcBlendFactor / calcBlendFunc, BlendSoft.h:13-56), set by the host:
+  // factor f = c0 + c1 * x with x = {src, srcAlpha, dst, dstAlpha}[op]; result = s*ks + d*kd
+  // (ADD/SUBTRACT/REVERSE_SUBTRACT) or min/max(s, d) when minmax is 1/2
+  int bfOp[4];                    // srcRgb, dstRgb, srcAlpha, dstAlpha
+  float bfC0[4], bfC1[4];
+  float bKs[2], bKd[2];           // rgb, alpha
+  int bMinMax[2];
   int cullFace, earlyZ;
   Viewport vp;
   // attachments (linear storage; multi-sample: 4 samples interleaved per pixel)
@@ -123,6 +130,8 @@ struct DrawParams {
   int tile;                       // tile edge in pixels (8, 16 or 32)
   int tilesX, tilesY;
   unsigned long long *fragCounter;   // FS invocations (instrumented runs only), else null
+  int needDeriv;                  // the FS reads texcoord derivatives (a bound 2D sampler with a LOD callback)
+  const int *tileOrder;           // raster CTA -> tile, heaviest tile lists first (null: identity)
 };
 
 // ------------------------------------------------------------------------------------------------
@@ -199,33 +208,24 @@ __device__ __forceinline__ uint32_t texel(const DevTex &t, int face, int level, 
   return __ldg(t.base + (size_t) face * t.layerStride + t.offset[level] + texIndex(t, level, x, y));
 }
 
+__device__ __forceinline__ int wrapCoord(int x, int n, int wrap) {
+  int rep = (x & ((n - 1) + n)) & (n - 1);   // CoordMod as the reference's macro expands (SamplerSoft.h:14)
+  int m = (x & ((2 * n - 1) + 2 * n)) & (2 * n - 1);
+  m -= n;
+  m = m >= 0 ? m : (-1 - m);
+  int mir = n - 1 - m;
+  int edge = x < 0 ? 0 : (x >= n ? n - 1 : x);
+  return wrap == WRAP_REPEAT ? rep : (wrap == WRAP_MIRRORED ? mir : (wrap == WRAP_EDGE ? edge : x));
+}
+
+// BaseSampler::pixelWithWrapMode (SamplerSoft.h:170-213), selects instead of a switch
 __device__ __forceinline__ uint32_t pixelWrap(const DevTex &t, int face, int level, int x, int y, int wrap,
                                               uint32_t border) {
   int w = t.w[level], h = t.h[level];
-  switch (wrap) {
-    case WRAP_REPEAT:
-      x = (x & ((w - 1) + w)) & (w - 1);   // CoordMod as the reference's macro expands
-      y = (y & ((h - 1) + h)) & (h - 1);
-      break;
-    case WRAP_MIRRORED:
-      x = (x & ((2 * w - 1) + 2 * w)) & (2 * w - 1);
-      y = (y & ((2 * h - 1) + 2 * h)) & (2 * h - 1);
-      x -= w;
-      y -= h;
-      x = x >= 0 ? x : (-1 - x);
-      y = y >= 0 ? y : (-1 - y);
-      x = w - 1 - x;
-      y = h - 1 - y;
-      break;
-    case WRAP_EDGE:
-      x = x < 0 ? 0 : (x >= w ? w - 1 : x);
-      y = y < 0 ? 0 : (y >= h ? h - 1 : y);
-      break;
-    default:
-      if (x < 0 || x >= w || y < 0 || y >= h) return border;
-  }
-  if ((unsigned) x < (unsigned) w && (unsigned) y < (unsigned) h) return texel(t, face, level, x, y);
-  return 0;
+  int xx = wrapCoord(x, w, wrap), yy = wrapCoord(y, h, wrap);
+  bool outside = (unsigned) xx >= (unsigned) w || (unsigned) yy >= (unsigned) h;
+  if (outside) return wrap == WRAP_BORDER ? border : 0u;
+  return texel(t, face, level, xx, yy);
 }
 
 __device__ __forceinline__ uint32_t mixTexel(uint32_t x, uint32_t y, float a, bool isF) {
@@ -262,27 +262,31 @@ __device__ __forceinline__ uint32_t bilinearSample(const DevTex &t, int face, in
   return bilinearPx(t, face, level, u * (float) t.w[level], v * (float) t.h[level], wrap, border, isF);
 }
 
-__device__ inline uint32_t textureImpl(const DevSampler &s, int face, float u, float v, float lod) {
+static __device__ __noinline__ uint32_t textureImpl(const DevSampler &s, int face, float u, float v, float lod) {
   const DevTex &t = s.tex;
   if (t.levels <= 0) return 0;
-  bool isF = s.isFloat;
-  if (s.filter == FILTER_NEAREST) return nearestSample(t, face, 0, u, v, s.wrap, s.border);
-  if (s.filter == FILTER_LINEAR) return bilinearSample(t, face, 0, u, v, s.wrap, s.border, isF);
-  int maxLevel = t.levels - 1;
-  if (s.filter == FILTER_NN || s.filter == FILTER_LN) {
-    int level = min(max((int) ceilf(lod + 0.5f) - 1, 0), maxLevel);
-    if (s.filter == FILTER_NN) return nearestSample(t, face, level, u, v, s.wrap, s.border);
-    return bilinearSample(t, face, level, u, v, s.wrap, s.border, isF);
+  const bool isF = s.isFloat;
+  const int f = s.filter;
+  const bool nearest = (f & 1) == 0;        // NEAREST, NEAREST_MIPMAP_NEAREST, NEAREST_MIPMAP_LINEAR
+  const int maxLevel = t.levels - 1;
+  int hi = 0, lo = 0;
+  bool two = false;
+  float frac = 0.f;
+  if (f == FILTER_NN || f == FILTER_LN) {
+    hi = min(max((int) ceilf(lod + 0.5f) - 1, 0), maxLevel);
+  } else if (f >= FILTER_NL) {
+    float fl = floorf(lod);
+    hi = min(max((int) fl, 0), maxLevel);
+    lo = min(max(hi + 1, 0), maxLevel);
+    two = hi != lo;
+    frac = lod - fl;
   }
-  int hi = min(max((int) floorf(lod), 0), maxLevel);
-  int lo = min(max(hi + 1, 0), maxLevel);
-  bool nearest = s.filter == FILTER_NL;
   uint32_t th = nearest ? nearestSample(t, face, hi, u, v, s.wrap, s.border)
                         : bilinearSample(t, face, hi, u, v, s.wrap, s.border, isF);
-  if (hi == lo) return th;
+  if (!two) return th;
   uint32_t tl = nearest ? nearestSample(t, face, lo, u, v, s.wrap, s.border)
                         : bilinearSample(t, face, lo, u, v, s.wrap, s.border, isF);
-  return mixTexel(th, tl, lod - floorf(lod), isF);
+  return mixTexel(th, tl, frac, isF);
 }
 
 // BaseSamplerCube::convertXYZ2UV (SamplerSoft.h:311-373), if-chain order kept for ties

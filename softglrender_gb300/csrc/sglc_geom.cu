@@ -364,6 +364,34 @@ __global__ void k_tile_ranges(const uint32_t *keys, const int *nPtr, int *tileSt
   if (i == n - 1 || keys[i + 1] != k) tileEnd[k] = i + 1;
 }
 
+// Raster CTA order: tiles bucketed by log2 of their list length, longest first, so the tiles that
+// take longest start first and do not form the tail of the launch. One CTA; order within a bucket
+// is arbitrary (tiles are independent).
+__global__ void __launch_bounds__(1024) k_tile_order(const int *tileStart, const int *tileEnd, int numTiles,
+                                                     int *order) {
+  __shared__ int cnt[33], off[33];
+  if (threadIdx.x < 33) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  for (int t = threadIdx.x; t < numTiles; t += blockDim.x) {
+    int len = tileEnd[t] - tileStart[t];
+    atomicAdd(&cnt[len > 0 ? 32 - __clz(len) : 0], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int b = 32; b >= 0; b--) {
+      off[b] = s;
+      s += cnt[b];
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < numTiles; t += blockDim.x) {
+    int len = tileEnd[t] - tileStart[t];
+    int pos = atomicAdd(&off[len > 0 ? 32 - __clz(len) : 0], 1);
+    order[pos] = t;
+  }
+}
+
 // ------------------------------------------------------------------------------------------------
 // exclusive scan (three phases), counts read from device memory
 // ------------------------------------------------------------------------------------------------
@@ -552,6 +580,10 @@ void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, in
 
 void launchTileRanges(const DrawParams &p, int nPairs, const int *nPtr, cudaStream_t st) {
   if (nPairs > 0) k_tile_ranges<<<cdiv(nPairs, 256), 256, 0, st>>>(p.keyA, nPtr, p.tileStart, p.tileEnd);
+}
+
+void launchTileOrder(const DrawParams &p, int *order, cudaStream_t st) {
+  k_tile_order<<<1, 1024, 0, st>>>(p.tileStart, p.tileEnd, p.tilesX * p.tilesY, order);
 }
 
 void launchFill32(uint32_t *dst, uint32_t value, size_t n, cudaStream_t st) {

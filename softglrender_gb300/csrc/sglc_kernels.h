@@ -17,6 +17,7 @@ int sortScratchInts(int nPairs);
 void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, int *hist, int *histScan,
                int *scanScratch, cudaStream_t st);
 void launchTileRanges(const DrawParams &p, int nPairs, const int *nPtr, cudaStream_t st);
+void launchTileOrder(const DrawParams &p, int *order, cudaStream_t st);
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 void launchFill32(uint32_t *dst, uint32_t value, size_t n, cudaStream_t st);
 void launchMipLevel(const DevTex &t, int face, int level, int isFloat, cudaStream_t st);

@@ -60,6 +60,40 @@ __device__ __forceinline__ bool bary(const Tri &t, float px, float py, float &b0
   return !(b0 < 0 || b1 < 0 || b2 < 0);
 }
 
+// Same result as bary() when it returns true. Samples whose barycentrics are clearly negative are
+// rejected first with a reciprocal estimate (its error is far below the 1e-4 margin, so every
+// rejected sample is also rejected by the exact division); the rest take the exact path.
+__device__ __forceinline__ bool baryCover(const Tri &t, float px, float py, float &b0, float &b1, float &b2) {
+  float a0 = t.f0x - t.v0x, a1 = t.f0y - t.v0x, a2 = t.f0z - px;
+  float c0 = t.f1x - t.v0y, c1 = t.f1y - t.v0y, c2 = t.f1z - py;
+  float ux = a1 * c2 - a2 * c1;
+  float uy = a2 * c0 - a0 * c2;
+  float uz = a0 * c1 - a1 * c0;
+  if (fabsf(uz) < 1.19209290e-07f) return false;
+  float r = __frcp_rn(uz);
+  float ex = ux * r, ey = uy * r;
+  if (ex < -1e-4f || ey < -1e-4f || 1.f - (ex + ey) < -1e-4f) return false;
+  ux = ux / uz;
+  uy = uy / uz;
+  b0 = 1.f - (ux + uy);
+  b1 = uy;
+  b2 = ux;
+  return !(b0 < 0 || b1 < 0 || b2 < 0);
+}
+
+// Is any coverage sample of pixel (x, y) inside the triangle? (pixel.inside after InitCoverage,
+// RendererInternal.h:97-112): the same arithmetic as the per-pixel pass, so the answer is exact.
+template<int S>
+__device__ __forceinline__ bool pixelCovered(const Tri &t, int x, int y) {
+  float b0, b1, b2;
+  const float fx = (float) x, fy = (float) y;
+  if (S == 1) return baryCover(t, fx + 0.5f, fy + 0.5f, b0, b1, b2);
+  return baryCover(t, kLoc4xR[0].x + fx, kLoc4xR[0].y + fy, b0, b1, b2) ||
+         baryCover(t, kLoc4xR[1].x + fx, kLoc4xR[1].y + fy, b0, b1, b2) ||
+         baryCover(t, kLoc4xR[2].x + fx, kLoc4xR[2].y + fy, b0, b1, b2) ||
+         baryCover(t, kLoc4xR[3].x + fx, kLoc4xR[3].y + fy, b0, b1, b2);
+}
+
 // glm::dot(bc, vec4(v0, v1, v2, 0)) with DPPS order (z and w of a sample)
 __device__ __forceinline__ float interpZW(float b0, float b1, float b2, float v0, float v1, float v2) {
   return (b0 * v0 + b1 * v1) + (b2 * v2 + 0.f * 0.f);
@@ -116,45 +150,27 @@ __device__ __forceinline__ int quadCands(float bmin, float bmax, int bc, int pos
   return n;
 }
 
+// DepthTest (DepthSoft.h:13-25) as an 8-entry truth table indexed by the depth function
 __device__ __forceinline__ bool depthCmp(float a, float b, int func) {
-  switch (func) {
-    case 0: return false;
-    case 1: return a < b;
-    case 2: return fabsf(a - b) <= 1.19209290e-07f;
-    case 3: return a <= b;
-    case 4: return a > b;
-    case 5: return fabsf(a - b) > 1.19209290e-07f;
-    case 6: return a >= b;
-    case 7: return true;
-  }
-  return a < b;
+  bool lt = a < b, gt = a > b, le = a <= b, ge = a >= b, eq = fabsf(a - b) <= 1.19209290e-07f;
+  uint32_t bits = 0x80u | ((uint32_t) lt << 1) | ((uint32_t) eq << 2) | ((uint32_t) le << 3) | ((uint32_t) gt << 4) |
+                  ((uint32_t) !eq << 5) | ((uint32_t) ge << 6);
+  return (bits >> func) & 1u;
 }
 
-__device__ __forceinline__ float blendFactor(float src, float srcA, float dst, float dstA, int f) {
-  switch (f) {
-    case 0: return 0.f;
-    case 1: return 1.f;
-    case 2: return src;
-    case 3: return srcA;
-    case 4: return dst;
-    case 5: return dstA;
-    case 6: return 1.f - src;
-    case 7: return 1.f - srcA;
-    case 8: return 1.f - dst;
-    case 9: return 1.f - dstA;
-  }
-  return 0.f;
+// calcBlendFactor: one of {0, 1, x, 1 - x}, x chosen among the four blend operands
+__device__ __forceinline__ float blendFactor(const DrawParams &p, int k, float src, float srcA, float dst, float dstA) {
+  int op = p.bfOp[k];
+  float x = op == 0 ? src : (op == 1 ? srcA : (op == 2 ? dst : dstA));
+  return p.bfC0[k] + p.bfC1[k] * x;
 }
 
-__device__ __forceinline__ float blendFn(float s, float d, int fn) {
-  switch (fn) {
-    case 0: return s + d;
-    case 1: return s - d;
-    case 2: return d - s;
-    case 3: return gmin(s, d);
-    case 4: return gmax(s, d);
-  }
-  return s + d;
+// calcBlendFunc: s + d, s - d, d - s exactly as s*ks + d*kd with ks, kd = +-1; or min / max
+__device__ __forceinline__ float blendFn(const DrawParams &p, int k, float s, float d) {
+  float r = s * p.bKs[k] + d * p.bKd[k];
+  int mm = p.bMinMax[k];
+  float mn = gmin(s, d), mx = gmax(s, d);
+  return mm == 0 ? r : (mm == 1 ? mn : mx);
 }
 
 // glm::clamp(vec4, 0, 1) on the SSE path: minps(maxps(x, 0), 1)
@@ -180,14 +196,10 @@ __device__ __forceinline__ void perSample(const DrawParams &p, bool inC, bool in
       float4 q = unpack4(col);
       d = make_float4(q.x / 255.f, q.y / 255.f, q.z / 255.f, q.w / 255.f);
     }
-    float r0 = blendFn(c0 * blendFactor(c0, c3, d.x, d.w, p.bSrcRgb), d.x * blendFactor(c0, c3, d.x, d.w, p.bDstRgb),
-                       p.bFuncRgb);
-    float r1 = blendFn(c1 * blendFactor(c1, c3, d.y, d.w, p.bSrcRgb), d.y * blendFactor(c1, c3, d.y, d.w, p.bDstRgb),
-                       p.bFuncRgb);
-    float r2 = blendFn(c2 * blendFactor(c2, c3, d.z, d.w, p.bSrcRgb), d.z * blendFactor(c2, c3, d.z, d.w, p.bDstRgb),
-                       p.bFuncRgb);
-    float r3 = blendFn(c3 * blendFactor(c3, c3, d.w, d.w, p.bSrcA), d.w * blendFactor(c3, c3, d.w, d.w, p.bDstA),
-                       p.bFuncA);
+    float r0 = blendFn(p, 0, c0 * blendFactor(p, 0, c0, c3, d.x, d.w), d.x * blendFactor(p, 1, c0, c3, d.x, d.w));
+    float r1 = blendFn(p, 0, c1 * blendFactor(p, 0, c1, c3, d.y, d.w), d.y * blendFactor(p, 1, c1, c3, d.y, d.w));
+    float r2 = blendFn(p, 0, c2 * blendFactor(p, 0, c2, c3, d.z, d.w), d.z * blendFactor(p, 1, c2, c3, d.z, d.w));
+    float r3 = blendFn(p, 1, c3 * blendFactor(p, 2, c3, c3, d.w, d.w), d.w * blendFactor(p, 3, c3, c3, d.w, d.w));
     c0 = r0; c1 = r1; c2 = r2; c3 = r3;
   }
   if (inC) col = pack4(c0 * 255.f, c1 * 255.f, c2 * 255.f, c3 * 255.f);
@@ -198,110 +210,163 @@ struct Samples4 {
   float d0, d1, d2, d3;
 };
 
-// One quad of one triangle, seen from the pixel (px, py) it contains.
-template<int SH, int S, bool HAS_COLOR, bool HAS_DEPTH>
-__device__ __forceinline__ void rasterQuadPixel(const DrawParams &p, const Tri &t, int qx, int qy, int px, int py,
-                                                bool inC, bool inD, bool needDeriv, Samples4 &fb) {
+// per-warp fragment queue in shared memory (phase A appends, phase B shades, phase C applies)
+constexpr int kQueue = 64;
+struct FragQueue {
+  int tri[kQueue];
+  uint32_t meta[kQueue];   // bits 0-4 lane, 5-8 sample mask, 9 pixel is right of quad origin, 10 below
+  float b0[kQueue], b1[kQueue], b2[kQueue];
+  float4 col[kQueue];
+};
+
+__device__ __forceinline__ bool depthPass(const DrawParams &p, float z, float dep) {
+  return depthCmp(gclamp(z, p.vp.absMin, p.vp.absMax), dep, p.depthFunc);
+}
+
+// Phase B for one fragment: quad derivatives of the texture coordinates, then the FS.
+template<int SH, int S>
+__device__ __noinline__ float4 shadeFragment(const DrawParams &p, int tri, int qx, int qy, int px, int py, float sb0,
+                                             float sb1, float sb2) {
+  Tri t = loadTri(p.tri + tri);
+  const float *r0 = p.vVary + (size_t) t.vid0 * p.varyStride;
+  const float *r1 = p.vVary + (size_t) t.vid1 * p.varyStride;
+  const float *r2 = p.vVary + (size_t) t.vid2 * p.varyStride;
+  FragIn f;
+  f.v = Vary{r0, r1, r2, sb0, sb1, sb2};
+  f.dudx = f.dvdx = f.dudy = f.dvdy = 0.f;
+  if (p.needDeriv) {
+    // p0 = (qx, qy), p1 = (qx+1, qy), p2 = (qx, qy+1): varyings at each pixel's shading sample
+    // (RendererSoft.cpp:815-820; ShaderSoft.h:117-133)
+    float u[3], v[3];
+    for (int k = 0; k < 3; k++) {
+      int nx = qx + (k == 1), ny = qy + (k == 2);
+      float c0 = sb0, c1 = sb1, c2 = sb2;
+      if (nx != px || ny != py) neighbourBC<S>(t, nx, ny, c0, c1, c2);
+      Vary vk{r0, r1, r2, c0, c1, c2};
+      u[k] = vk[0];
+      v[k] = vk[1];
+    }
+    f.dudx = u[1] - u[0];
+    f.dvdx = v[1] - v[0];
+    f.dudy = u[2] - u[0];
+    f.dvdy = v[2] - v[0];
+  }
+  return runFS<SH>(p, f);
+}
+
+template<int SH, int S, bool HAS_DEPTH>
+__device__ __forceinline__ void flushQueue(const DrawParams &p, FragQueue &q, int &count, int lane, int rx0, int ry0,
+                                           bool inC, Samples4 &fb) {
+  __syncwarp();
+  // phase B: shade the queued fragments 32 at a time
+  for (int base = 0; base < count; base += 32) {
+    int e = base + lane;
+    if (e < count) {
+      uint32_t m = q.meta[e];
+      int l = m & 31;
+      int px = rx0 + (l & 7), py = ry0 + (l >> 3);
+      int qx = px - ((m >> 9) & 1), qy = py - ((m >> 10) & 1);
+      q.col[e] = shadeFragment<SH, S>(p, q.tri[e], qx, qy, px, py, q.b0[e], q.b1[e], q.b2[e]);
+    }
+  }
+  __syncwarp();
+  if (p.fragCounter && lane == 0) atomicAdd(p.fragCounter, (unsigned long long) count);
+  // phase C: each pixel applies its fragments' colour operations in queue (= primitive) order
+  for (int e = 0; e < count; e++) {
+    uint32_t m = q.meta[e];
+    if ((int) (m & 31) != lane) continue;
+    float4 color = q.col[e];
+    uint32_t mask = (m >> 5) & 15u;
+    if (mask & 1u) perSample<true, false>(p, inC, true, fb.c0, fb.d0, 0.f, color);
+    if (S == 4) {
+      if (mask & 2u) perSample<true, false>(p, inC, true, fb.c1, fb.d1, 0.f, color);
+      if (mask & 4u) perSample<true, false>(p, inC, true, fb.c2, fb.d2, 0.f, color);
+      if (mask & 8u) perSample<true, false>(p, inC, true, fb.c3, fb.d3, 0.f, color);
+    }
+  }
+  __syncwarp();
+  count = 0;
+}
+
+// Phase A for one quad of one triangle seen from pixel (px, py): coverage, shading sample, early-Z
+// and the per-sample depth test + write. Returns the mask of samples whose colour operation must
+// follow (0 = nothing to shade) and the shading sample's perspective-corrected barycentrics.
+template<int S, bool HAS_DEPTH>
+__device__ __forceinline__ uint32_t coverQuadPixel(const DrawParams &p, const Tri &t, int px, int py, bool inD,
+                                                   Samples4 &fb, float &sb0, float &sb1, float &sb2) {
   const float fx = (float) px, fy = (float) py;
-  float sb0, sb1, sb2;   // shading-sample barycentrics
+  const bool testDepth = p.depthTest && HAS_DEPTH;
+  if (S == 1) {
+    if (!baryCover(t, fx + 0.5f, fy + 0.5f, sb0, sb1, sb2)) return 0u;
+    float z = interpZW(sb0, sb1, sb2, t.z0, t.z1, t.z2);
+    correct(t, sb0, sb1, sb2);
+    // the S=1 depth-range clip has no effect: early-Z overwrites it and the per-sample path does
+    // not read it (RendererSoft.cpp:797-799 vs :846-849, :872-874)
+    if (p.earlyZ && testDepth && !(inD && depthPass(p, z, fb.d0))) return 0u;
+    if (testDepth) {
+      if (!(inD && depthPass(p, z, fb.d0))) return 0u;
+      if (p.depthMask) fb.d0 = gclamp(z, p.vp.absMin, p.vp.absMax);
+    }
+    return 1u;
+  }
+  float a0, a1, a2, b0, b1, b2, c0, c1, c2, e0, e1, e2, m0, m1, m2;
+  bool s0 = baryCover(t, kLoc4xR[0].x + fx, kLoc4xR[0].y + fy, a0, a1, a2);
+  bool s1 = baryCover(t, kLoc4xR[1].x + fx, kLoc4xR[1].y + fy, b0, b1, b2);
+  bool s2 = baryCover(t, kLoc4xR[2].x + fx, kLoc4xR[2].y + fy, c0, c1, c2);
+  bool s3 = baryCover(t, kLoc4xR[3].x + fx, kLoc4xR[3].y + fy, e0, e1, e2);
+  if (!(s0 || s1 || s2 || s3)) return 0u;
+  bool sc = baryCover(t, fx + 0.5f, fy + 0.5f, m0, m1, m2);
+  // InitShadingSample: the centre if covered, else the first covered sample
+  if (sc) { sb0 = m0; sb1 = m1; sb2 = m2; }
+  else if (s0) { sb0 = a0; sb1 = a1; sb2 = a2; }
+  else if (s1) { sb0 = b0; sb1 = b1; sb2 = b2; }
+  else if (s2) { sb0 = c0; sb1 = c1; sb2 = c2; }
+  else { sb0 = e0; sb1 = e1; sb2 = e2; }
   float z0 = 0.f, z1 = 0.f, z2 = 0.f, z3 = 0.f;
   bool i0 = false, i1 = false, i2 = false, i3 = false;
-  if (S == 1) {
-    if (!bary(t, fx + 0.5f, fy + 0.5f, sb0, sb1, sb2)) return;
-    z0 = interpZW(sb0, sb1, sb2, t.z0, t.z1, t.z2);
-    correct(t, sb0, sb1, sb2);
-    // the S=1 depth-range clip has no effect: early-Z overwrites it and the per-sample path
-    // does not read it (RendererSoft.cpp:797-799 vs :846-849, :872-874)
-    if (p.earlyZ && p.depthTest && HAS_DEPTH) {
-      float d = gclamp(z0, p.vp.absMin, p.vp.absMax);
-      if (!inD || !depthCmp(d, fb.d0, p.depthFunc)) return;
-    }
-    i0 = true;
-  } else {
-    float a0, a1, a2, b0, b1, b2, c0, c1, c2, e0, e1, e2, m0, m1, m2;
-    bool s0 = bary(t, kLoc4xR[0].x + fx, kLoc4xR[0].y + fy, a0, a1, a2);
-    bool s1 = bary(t, kLoc4xR[1].x + fx, kLoc4xR[1].y + fy, b0, b1, b2);
-    bool s2 = bary(t, kLoc4xR[2].x + fx, kLoc4xR[2].y + fy, c0, c1, c2);
-    bool s3 = bary(t, kLoc4xR[3].x + fx, kLoc4xR[3].y + fy, e0, e1, e2);
-    if (!(s0 || s1 || s2 || s3)) return;
-    bool sc = bary(t, fx + 0.5f, fy + 0.5f, m0, m1, m2);
-    // InitShadingSample: the centre if covered, else the first covered sample
-    if (sc) { sb0 = m0; sb1 = m1; sb2 = m2; }
-    else if (s0) { sb0 = a0; sb1 = a1; sb2 = a2; }
-    else if (s1) { sb0 = b0; sb1 = b1; sb2 = b2; }
-    else if (s2) { sb0 = c0; sb1 = c1; sb2 = c2; }
-    else { sb0 = e0; sb1 = e1; sb2 = e2; }
-    if (s0) { z0 = interpZW(a0, a1, a2, t.z0, t.z1, t.z2); i0 = !(z0 < p.vp.absMin || z0 > p.vp.absMax); }
-    if (s1) { z1 = interpZW(b0, b1, b2, t.z0, t.z1, t.z2); i1 = !(z1 < p.vp.absMin || z1 > p.vp.absMax); }
-    if (s2) { z2 = interpZW(c0, c1, c2, t.z0, t.z1, t.z2); i2 = !(z2 < p.vp.absMin || z2 > p.vp.absMax); }
-    if (s3) { z3 = interpZW(e0, e1, e2, t.z0, t.z1, t.z2); i3 = !(z3 < p.vp.absMin || z3 > p.vp.absMax); }
-    correct(t, sb0, sb1, sb2);
-    if (p.earlyZ && p.depthTest && HAS_DEPTH) {
-      if (i0) i0 = inD && depthCmp(gclamp(z0, p.vp.absMin, p.vp.absMax), fb.d0, p.depthFunc);
-      if (i1) i1 = inD && depthCmp(gclamp(z1, p.vp.absMin, p.vp.absMax), fb.d1, p.depthFunc);
-      if (i2) i2 = inD && depthCmp(gclamp(z2, p.vp.absMin, p.vp.absMax), fb.d2, p.depthFunc);
-      if (i3) i3 = inD && depthCmp(gclamp(z3, p.vp.absMin, p.vp.absMax), fb.d3, p.depthFunc);
-      if (!(i0 || i1 || i2 || i3)) return;
-    }
+  if (s0) { z0 = interpZW(a0, a1, a2, t.z0, t.z1, t.z2); i0 = !(z0 < p.vp.absMin || z0 > p.vp.absMax); }
+  if (s1) { z1 = interpZW(b0, b1, b2, t.z0, t.z1, t.z2); i1 = !(z1 < p.vp.absMin || z1 > p.vp.absMax); }
+  if (s2) { z2 = interpZW(c0, c1, c2, t.z0, t.z1, t.z2); i2 = !(z2 < p.vp.absMin || z2 > p.vp.absMax); }
+  if (s3) { z3 = interpZW(e0, e1, e2, t.z0, t.z1, t.z2); i3 = !(z3 < p.vp.absMin || z3 > p.vp.absMax); }
+  correct(t, sb0, sb1, sb2);
+  if (p.earlyZ && testDepth) {
+    if (i0) i0 = inD && depthPass(p, z0, fb.d0);
+    if (i1) i1 = inD && depthPass(p, z1, fb.d1);
+    if (i2) i2 = inD && depthPass(p, z2, fb.d2);
+    if (i3) i3 = inD && depthPass(p, z3, fb.d3);
+    if (!(i0 || i1 || i2 || i3)) return 0u;
   }
-  float4 color = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (HAS_COLOR) {
-    const float *r0 = p.vVary + (size_t) t.vid0 * p.varyStride;
-    const float *r1 = p.vVary + (size_t) t.vid1 * p.varyStride;
-    const float *r2 = p.vVary + (size_t) t.vid2 * p.varyStride;
-    FragIn f;
-    f.v = Vary{r0, r1, r2, sb0, sb1, sb2};
-    f.dudx = f.dvdx = f.dudy = f.dvdy = 0.f;
-    if (needDeriv) {
-      float u0, v0, u1, v1, u2, v2;
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        int nx = qx + (k == 1), ny = qy + (k == 2);
-        float c0, c1, c2;
-        if (nx == px && ny == py) {
-          c0 = sb0; c1 = sb1; c2 = sb2;
-        } else {
-          neighbourBC<S>(t, nx, ny, c0, c1, c2);
-        }
-        Vary vk{r0, r1, r2, c0, c1, c2};
-        float uu = vk[0], vv = vk[1];
-        if (k == 0) { u0 = uu; v0 = vv; }
-        else if (k == 1) { u1 = uu; v1 = vv; }
-        else { u2 = uu; v2 = vv; }
-      }
-      f.dudx = u1 - u0;
-      f.dvdx = v1 - v0;
-      f.dudy = u2 - u0;
-      f.dvdy = v2 - v0;
-    }
-    color = runFS<SH>(p, f);
-    if (p.fragCounter) atomicAdd(p.fragCounter, 1ull);
+  // per-sample depth test + write in sample order (processPerSampleOperations, :838-845)
+  if (testDepth) {
+    if (i0) { i0 = inD && depthPass(p, z0, fb.d0); if (i0 && p.depthMask) fb.d0 = gclamp(z0, p.vp.absMin, p.vp.absMax); }
+    if (i1) { i1 = inD && depthPass(p, z1, fb.d1); if (i1 && p.depthMask) fb.d1 = gclamp(z1, p.vp.absMin, p.vp.absMax); }
+    if (i2) { i2 = inD && depthPass(p, z2, fb.d2); if (i2 && p.depthMask) fb.d2 = gclamp(z2, p.vp.absMin, p.vp.absMax); }
+    if (i3) { i3 = inD && depthPass(p, z3, fb.d3); if (i3 && p.depthMask) fb.d3 = gclamp(z3, p.vp.absMin, p.vp.absMax); }
   }
-  if (i0) perSample<HAS_COLOR, HAS_DEPTH>(p, inC, inD, fb.c0, fb.d0, z0, color);
-  if (S == 4) {
-    if (i1) perSample<HAS_COLOR, HAS_DEPTH>(p, inC, inD, fb.c1, fb.d1, z1, color);
-    if (i2) perSample<HAS_COLOR, HAS_DEPTH>(p, inC, inD, fb.c2, fb.d2, z2, color);
-    if (i3) perSample<HAS_COLOR, HAS_DEPTH>(p, inC, inD, fb.c3, fb.d3, z3, color);
-  }
+  return (i0 ? 1u : 0u) | (i1 ? 2u : 0u) | (i2 ? 4u : 0u) | (i3 ? 8u : 0u);
 }
 
 template<int SH, int S, bool HAS_COLOR, bool HAS_DEPTH>
-__global__ void __launch_bounds__(256) k_raster(const __grid_constant__ DrawParams p) {
-  const int tile = blockIdx.x;
+__global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawParams p) {
+  __shared__ FragQueue queues[HAS_COLOR ? 8 : 1];
+  const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
   const int tx = tile % p.tilesX, ty = tile / p.tilesX;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
   const bool inC = HAS_COLOR && px < p.cw && py < p.ch;
   const bool inD = HAS_DEPTH && px < p.dw && py < p.dh;
+  FragQueue &q = queues[HAS_COLOR ? warp : 0];
+  int count = 0;
+  const unsigned lt = (1u << lane) - 1u;
   Samples4 fb = {0u, 0u, 0u, 0u, 0.f, 0.f, 0.f, 0.f};
   if (inC) {
     size_t pix = (size_t) py * p.cw + px;
     if (p.pendingClear && p.clearColorFlag) {
       fb.c0 = fb.c1 = fb.c2 = fb.c3 = p.clearColor;
     } else if (S == 4) {
-      uint4 q = *reinterpret_cast<const uint4 *>(p.color + pix * 4);
-      fb.c0 = q.x; fb.c1 = q.y; fb.c2 = q.z; fb.c3 = q.w;
+      uint4 v = *reinterpret_cast<const uint4 *>(p.color + pix * 4);
+      fb.c0 = v.x; fb.c1 = v.y; fb.c2 = v.z; fb.c3 = v.w;
     } else {
       fb.c0 = p.color[pix];
     }
@@ -311,58 +376,121 @@ __global__ void __launch_bounds__(256) k_raster(const __grid_constant__ DrawPara
     if (p.pendingClear && p.clearDepthFlag) {
       fb.d0 = fb.d1 = fb.d2 = fb.d3 = p.clearDepth;
     } else if (S == 4) {
-      float4 q = *reinterpret_cast<const float4 *>(p.depth + pix * 4);
-      fb.d0 = q.x; fb.d1 = q.y; fb.d2 = q.z; fb.d3 = q.w;
+      float4 v = *reinterpret_cast<const float4 *>(p.depth + pix * 4);
+      fb.d0 = v.x; fb.d1 = v.y; fb.d2 = v.z; fb.d3 = v.w;
     } else {
       fb.d0 = p.depth[pix];
     }
   }
-  const bool needDeriv = HAS_COLOR && needsDerivatives(p);
   const int start = p.tileStart[tile], end = p.tileEnd[tile];
+  // sample box offsets inside a pixel: 4x MSAA samples span [1/8, 7/8], one sample sits at 1/2
+  const float lo = S == 4 ? 0.125f : 0.5f, hi = S == 4 ? 0.875f : 0.5f;
+  const float vpExtent = fabsf(p.vp.w) + fabsf(p.vp.h) + 2.f * (float) (rx0 + ry0) + 64.f;
   for (int base = start; base < end; base += 32) {
+    // ---- pass 1 (lane = triangle of this batch): which pixels of the warp rectangle may it cover?
     int i = base + lane;
     int prim = -1;
     bool hit = false;
+    int4 r = make_int4(0, -1, 0, -1);
+    float ea[3] = {0.f, 0.f, 0.f}, eb[3] = {0.f, 0.f, 0.f}, ek[3] = {0.f, 0.f, 0.f}, et[3] = {0.f, 0.f, 0.f};
+    bool anyPix = false;
+    Tri tb;
     if (i < end) {
       prim = __ldg(p.valA + i);
-      int4 r = __ldg(reinterpret_cast<const int4 *>(&p.tri[prim].rx0));
+      const TriSetup *tp = p.tri + prim;
+      r = __ldg(reinterpret_cast<const int4 *>(&tp->rx0));
       hit = !(r.y < rx0 || r.x > rx0 + 7 || r.w < ry0 || r.z > ry0 + 3);
+      if (hit) {
+        float4 q0 = __ldg(reinterpret_cast<const float4 *>(tp));        // v0x v0y v2x v1x
+        float4 q1 = __ldg(reinterpret_cast<const float4 *>(tp) + 1);    // v0x v2y v1y v0y
+        float X[3] = {q0.x, q0.w, q0.z}, Y[3] = {q0.y, q1.z, q1.y};     // v0, v1, v2
+        float area = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
+        float mag = fabsf(X[1] - X[0]) + fabsf(Y[1] - Y[0]) + fabsf(X[2] - X[0]) + fabsf(Y[2] - Y[0]);
+        anyPix = !(fabsf(area) > 1e-3f * mag * mag + 1e-6f);   // near-degenerate: skip the edge pre-test
+        tb = loadTri(tp);
+        float o = area > 0.f ? 1.f : -1.f;
+#pragma unroll
+        for (int e = 0; e < 3; e++) {
+          // E(x, y) = a x + b y + c >= 0 inside; its maximum over a pixel's sample box is at the
+          // corner picked by the signs of a, b: E_max(px, py) = a px + b py + k
+          float sx = X[e], sy = Y[e], dx = X[(e + 1) % 3] - sx, dy = Y[(e + 1) % 3] - sy;
+          float a = -o * dy, b = o * dx, c = o * (dy * sx - dx * sy);
+          ea[e] = a;
+          eb[e] = b;
+          ek[e] = a * (a > 0.f ? hi : lo) + b * (b > 0.f ? hi : lo) + c;
+          et[e] = 1e-5f * ((fabsf(a) + fabsf(b)) * (vpExtent + fabsf(sx) + fabsf(sy)) + fabsf(c) + 1.f);
+        }
+      }
     }
-    unsigned m = __ballot_sync(0xffffffffu, hit);
-    while (m) {
-      int j = __ffs(m) - 1;
-      m &= m - 1;
-      int pr = __shfl_sync(0xffffffffu, prim, j);
-      const TriSetup *ts = p.tri + pr;
-      int4 r = __ldg(reinterpret_cast<const int4 *>(&ts->rx0));
-      if (px < r.x || px > r.y || py < r.z || py > r.w || !(inC || inD)) continue;
-      Tri t = loadTri(ts);
-      int x0 = 0, x1 = 0, y0 = 0, y1 = 0;
-      int nx = quadCands(t.bminx, t.bmaxx, t.bcx, px, x0, x1);
-      if (nx == 0) continue;
-      int ny = quadCands(t.bminy, t.bmaxy, t.bcy, py, y0, y1);
-      for (int iy = 0; iy < ny; iy++) {
-        int qy = iy ? y1 : y0;
-        for (int ix = 0; ix < nx; ix++) {
-          int qx = ix ? x1 : x0;
-          rasterQuadPixel<SH, S, HAS_COLOR, HAS_DEPTH>(p, t, qx, qy, px, py, inC, inD, needDeriv, fb);
+    unsigned cand = 0;   // this lane's pixel: candidate triangles of the batch, bit = batch index
+#pragma unroll 4
+    for (int pp = 0; pp < 32; pp++) {
+      int cx = rx0 + (pp & 7), cy = ry0 + (pp >> 3);
+      bool c = hit && cx >= r.x && cx <= r.y && cy >= r.z && cy <= r.w;
+      if (c && !anyPix) {
+        float fx = (float) cx, fy = (float) cy;
+        c = (ea[0] * fx + eb[0] * fy + ek[0] >= -et[0]) && (ea[1] * fx + eb[1] * fy + ek[1] >= -et[1]) &&
+            (ea[2] * fx + eb[2] * fy + ek[2] >= -et[2]);
+      }
+      if (c) c = pixelCovered<S>(tb, cx, cy);   // exact: some coverage sample of the pixel is inside
+      unsigned mm = __ballot_sync(0xffffffffu, c);
+      if (lane == pp) cand = mm;
+    }
+    if (!(inC || inD)) cand = 0;
+    // ---- pass 2 (lane = pixel): exact coverage and depth for each candidate, in primitive order
+    int nIter = __reduce_max_sync(0xffffffffu, __popc(cand));
+    for (int it = 0; it < nIter; it++) {
+      int j = cand ? __ffs(cand) - 1 : -1;
+      if (cand) cand &= cand - 1;
+      int pr = __shfl_sync(0xffffffffu, prim, j < 0 ? 0 : j);
+      int nx = 0, ny = 0, x0 = 0, x1 = 0, y0 = 0, y1 = 0;
+      Tri t;
+      if (j >= 0) {
+        t = loadTri(p.tri + pr);
+        nx = quadCands(t.bminx, t.bmaxx, t.bcx, px, x0, x1);
+        ny = nx ? quadCands(t.bminy, t.bmaxy, t.bcy, py, y0, y1) : 0;
+      }
+      int nq = nx * ny;
+      int nqMax = __reduce_max_sync(0xffffffffu, nq);
+      for (int k = 0; k < nqMax; k++) {
+        uint32_t mask = 0;
+        float sb0 = 0.f, sb1 = 0.f, sb2 = 0.f;
+        int qx = 0, qy = 0;
+        if (k < nq) {
+          qy = (k / nx) ? y1 : y0;
+          qx = (k % nx) ? x1 : x0;
+          mask = coverQuadPixel<S, HAS_DEPTH>(p, t, px, py, inD, fb, sb0, sb1, sb2);
+        }
+        if (HAS_COLOR) {
+          if (count + 32 > kQueue) flushQueue<SH, S, HAS_DEPTH>(p, q, count, lane, rx0, ry0, inC, fb);
+          unsigned want = __ballot_sync(0xffffffffu, mask != 0);
+          if (mask) {
+            int e = count + __popc(want & lt);
+            q.tri[e] = pr;
+            q.meta[e] = (uint32_t) lane | (mask << 5) | ((uint32_t) (px - qx) << 9) | ((uint32_t) (py - qy) << 10);
+            q.b0[e] = sb0;
+            q.b1[e] = sb1;
+            q.b2[e] = sb2;
+          }
+          count += __popc(want);
         }
       }
     }
   }
+  if (HAS_COLOR && count > 0) flushQueue<SH, S, HAS_DEPTH>(p, q, count, lane, rx0, ry0, inC, fb);
   if (inC) {
     size_t pix = (size_t) py * p.cw + px;
     if (S == 4) {
       *reinterpret_cast<uint4 *>(p.color + pix * 4) = make_uint4(fb.c0, fb.c1, fb.c2, fb.c3);
       // multiSampleResolve (RendererSoft.cpp:880-912): mean of four u8 samples, truncated
-      uint32_t r = 0;
+      uint32_t rsv = 0;
 #pragma unroll
       for (int ch = 0; ch < 4; ch++) {
-        uint32_t s = ((fb.c0 >> (8 * ch)) & 255u) + ((fb.c1 >> (8 * ch)) & 255u) + ((fb.c2 >> (8 * ch)) & 255u) +
-                     ((fb.c3 >> (8 * ch)) & 255u);
-        r |= ((s >> 2) & 255u) << (8 * ch);
+        uint32_t sum = ((fb.c0 >> (8 * ch)) & 255u) + ((fb.c1 >> (8 * ch)) & 255u) + ((fb.c2 >> (8 * ch)) & 255u) +
+                       ((fb.c3 >> (8 * ch)) & 255u);
+        rsv |= ((sum >> 2) & 255u) << (8 * ch);
       }
-      p.resolved[pix] = r;
+      p.resolved[pix] = rsv;
     } else {
       p.color[pix] = fb.c0;
     }
