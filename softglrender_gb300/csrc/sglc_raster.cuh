@@ -10,7 +10,7 @@
 //
 // RendererSoft rasterises each triangle in 32x32 blocks anchored at its own bounding box and in
 // 2x2 quads anchored at odd offsets inside each block (:727-763); the quad decides which pixels
-// share derivatives and, when blocks overlap, a pixel can be visited twice. quadCands() finds, for
+// share derivatives and, when blocks overlap, a pixel can be visited twice. quadCandsF() finds, for
 // one pixel, exactly the quads the reference visits, in the reference's order; neighbourBC()
 // recomputes the quad neighbours' shading-sample barycentrics for dFdx/dFdy.
 #pragma once
@@ -22,12 +22,28 @@ namespace sglc {
 
 __constant__ float2 kLoc4xR[4] = {{0.375f, 0.875f}, {0.875f, 0.625f}, {0.125f, 0.375f}, {0.625f, 0.125f}};
 
-struct Tri {
+// the part of a triangle's setup that coverage, depth and perspective correction read
+struct TriCov {
   float v0x, v0y, f0x, f0y, f0z, f1x, f1y, f1z;
   float z0, z1, z2, w0, w1, w2;
+};
+
+struct Tri : TriCov {
   float bminx, bminy, bmaxx, bmaxy;
   int bcx, bcy, vid0, vid1, vid2;
 };
+
+__device__ __forceinline__ TriCov loadTriCov(const TriSetup *t) {
+  const float4 *q = reinterpret_cast<const float4 *>(t);
+  float4 a = __ldg(q + 0), b = __ldg(q + 1), c = __ldg(q + 2), d = __ldg(q + 3);
+  TriCov T;
+  T.v0x = a.x; T.v0y = a.y; T.f0x = a.z; T.f0y = a.w;
+  T.f0z = b.x; T.f1x = b.y; T.f1y = b.z; T.f1z = b.w;
+  T.z0 = c.x; T.z1 = c.y; T.z2 = c.z; T.w0 = c.w;
+  T.w1 = d.x; T.w2 = d.y;
+  return T;
+}
+
 
 __device__ __forceinline__ Tri loadTri(const TriSetup *t) {
   const float4 *q = reinterpret_cast<const float4 *>(t);
@@ -45,7 +61,7 @@ __device__ __forceinline__ Tri loadTri(const TriSetup *t) {
 }
 
 // RendererSoft::barycentric, SSE lane order (RendererSoft.cpp:1025-1039, 1051-1055)
-__device__ __forceinline__ bool bary(const Tri &t, float px, float py, float &b0, float &b1, float &b2) {
+__device__ __forceinline__ bool bary(const TriCov &t, float px, float py, float &b0, float &b1, float &b2) {
   float a0 = t.f0x - t.v0x, a1 = t.f0y - t.v0x, a2 = t.f0z - px;
   float c0 = t.f1x - t.v0y, c1 = t.f1y - t.v0y, c2 = t.f1z - py;
   float ux = a1 * c2 - a2 * c1;
@@ -63,14 +79,14 @@ __device__ __forceinline__ bool bary(const Tri &t, float px, float py, float &b0
 // Same result as bary() when it returns true. Samples whose barycentrics are clearly negative are
 // rejected first with a reciprocal estimate (its error is far below the 1e-4 margin, so every
 // rejected sample is also rejected by the exact division); the rest take the exact path.
-__device__ __forceinline__ bool baryCover(const Tri &t, float px, float py, float &b0, float &b1, float &b2) {
+__device__ __forceinline__ bool baryCover(const TriCov &t, float px, float py, float &b0, float &b1, float &b2) {
   float a0 = t.f0x - t.v0x, a1 = t.f0y - t.v0x, a2 = t.f0z - px;
   float c0 = t.f1x - t.v0y, c1 = t.f1y - t.v0y, c2 = t.f1z - py;
   float ux = a1 * c2 - a2 * c1;
   float uy = a2 * c0 - a0 * c2;
   float uz = a0 * c1 - a1 * c0;
   if (fabsf(uz) < 1.19209290e-07f) return false;
-  float r = __frcp_rn(uz);
+  float r = __fdividef(1.f, uz);
   float ex = ux * r, ey = uy * r;
   if (ex < -1e-4f || ey < -1e-4f || 1.f - (ex + ey) < -1e-4f) return false;
   ux = ux / uz;
@@ -81,26 +97,13 @@ __device__ __forceinline__ bool baryCover(const Tri &t, float px, float py, floa
   return !(b0 < 0 || b1 < 0 || b2 < 0);
 }
 
-// Is any coverage sample of pixel (x, y) inside the triangle? (pixel.inside after InitCoverage,
-// RendererInternal.h:97-112): the same arithmetic as the per-pixel pass, so the answer is exact.
-template<int S>
-__device__ __forceinline__ bool pixelCovered(const Tri &t, int x, int y) {
-  float b0, b1, b2;
-  const float fx = (float) x, fy = (float) y;
-  if (S == 1) return baryCover(t, fx + 0.5f, fy + 0.5f, b0, b1, b2);
-  return baryCover(t, kLoc4xR[0].x + fx, kLoc4xR[0].y + fy, b0, b1, b2) ||
-         baryCover(t, kLoc4xR[1].x + fx, kLoc4xR[1].y + fy, b0, b1, b2) ||
-         baryCover(t, kLoc4xR[2].x + fx, kLoc4xR[2].y + fy, b0, b1, b2) ||
-         baryCover(t, kLoc4xR[3].x + fx, kLoc4xR[3].y + fy, b0, b1, b2);
-}
-
 // glm::dot(bc, vec4(v0, v1, v2, 0)) with DPPS order (z and w of a sample)
 __device__ __forceinline__ float interpZW(float b0, float b1, float b2, float v0, float v1, float v2) {
   return (b0 * v0 + b1 * v1) + (b2 * v2 + 0.f * 0.f);
 }
 
 // barycentric *= (1 / w * vertW) (RendererSoft.cpp:802)
-__device__ __forceinline__ void correct(const Tri &t, float &b0, float &b1, float &b2) {
+__device__ __forceinline__ void correct(const TriCov &t, float &b0, float &b1, float &b2) {
   float w = interpZW(b0, b1, b2, t.w0, t.w1, t.w2);
   float iw = 1.f / w;
   b0 = b0 * (iw * t.w0);
@@ -110,7 +113,7 @@ __device__ __forceinline__ void correct(const Tri &t, float &b0, float &b1, floa
 
 // shading-sample barycentrics of a quad neighbour (RendererInternal.h:97-124 + :787-804)
 template<int S>
-__device__ __forceinline__ void neighbourBC(const Tri &t, int fx, int fy, float &b0, float &b1, float &b2) {
+__device__ __forceinline__ void neighbourBC(const TriCov &t, int fx, int fy, float &b0, float &b1, float &b2) {
   const float x = (float) fx, y = (float) fy;
   float c0 = 0.f, c1 = 0.f, c2 = 0.f;
   bool cin = bary(t, x + 0.5f, y + 0.5f, c0, c1, c2);
@@ -132,7 +135,7 @@ __device__ __forceinline__ void neighbourBC(const Tri &t, int fx, int fy, float 
 }
 
 // quads of one triangle that contain coordinate `pos` along one axis, in block order (<= 2)
-__device__ __forceinline__ int quadCands(float bmin, float bmax, int bc, int pos, int &q0, int &q1) {
+__device__ __forceinline__ int quadCandsF(float bmin, float bmax, int bc, int pos, int &q0, int &q1) {
   int n = 0;
   int kEst = (int) floorf(((float) (pos - 1) - bmin) * (1.f / (float) kBlock));
 #pragma unroll
@@ -148,6 +151,15 @@ __device__ __forceinline__ int quadCands(float bmin, float bmax, int bc, int pos
     n++;
   }
   return n;
+}
+
+// quads of triangle `t` containing pixel (px, py): block bounds from the setup record
+__device__ __forceinline__ int quadsOf(const TriSetup *t, int px, int py, int &x0, int &x1, int &y0, int &y1, int &nx) {
+  const float4 *q = reinterpret_cast<const float4 *>(t);
+  float4 d = __ldg(q + 3), e = __ldg(q + 4);
+  nx = quadCandsF(d.z, e.x, __float_as_int(e.z), px, x0, x1);
+  int ny = nx ? quadCandsF(d.w, e.y, __float_as_int(e.w), py, y0, y1) : 0;
+  return nx * ny;
 }
 
 // DepthTest (DepthSoft.h:13-25) as an 8-entry truth table indexed by the depth function
@@ -255,8 +267,8 @@ __device__ __noinline__ float4 shadeFragment(const DrawParams &p, int tri, int q
 }
 
 template<int SH, int S, bool HAS_DEPTH>
-__device__ __forceinline__ void flushQueue(const DrawParams &p, FragQueue &q, int &count, int lane, int rx0, int ry0,
-                                           bool inC, Samples4 &fb) {
+__device__ __forceinline__ void flushQueue(const DrawParams &p, FragQueue &q, int &count, unsigned long long &mine,
+                                           int lane, int rx0, int ry0, bool inC, Samples4 &fb) {
   __syncwarp();
   // phase B: shade the queued fragments 32 at a time
   for (int base = 0; base < count; base += 32) {
@@ -271,12 +283,13 @@ __device__ __forceinline__ void flushQueue(const DrawParams &p, FragQueue &q, in
   }
   __syncwarp();
   if (p.fragCounter && lane == 0) atomicAdd(p.fragCounter, (unsigned long long) count);
-  // phase C: each pixel applies its fragments' colour operations in queue (= primitive) order
-  for (int e = 0; e < count; e++) {
-    uint32_t m = q.meta[e];
-    if ((int) (m & 31) != lane) continue;
+  // phase C: every pixel applies its own fragments' colour operations in queue (= primitive) order;
+  // the lanes walk their own entries concurrently
+  while (mine) {
+    int e = __ffsll(mine) - 1;
+    mine &= mine - 1;
     float4 color = q.col[e];
-    uint32_t mask = (m >> 5) & 15u;
+    uint32_t mask = (q.meta[e] >> 5) & 15u;
     if (mask & 1u) perSample<true, false>(p, inC, true, fb.c0, fb.d0, 0.f, color);
     if (S == 4) {
       if (mask & 2u) perSample<true, false>(p, inC, true, fb.c1, fb.d1, 0.f, color);
@@ -288,61 +301,78 @@ __device__ __forceinline__ void flushQueue(const DrawParams &p, FragQueue &q, in
   count = 0;
 }
 
-// Phase A for one quad of one triangle seen from pixel (px, py): coverage, shading sample, early-Z
-// and the per-sample depth test + write. Returns the mask of samples whose colour operation must
-// follow (0 = nothing to shade) and the shading sample's perspective-corrected barycentrics.
-template<int S, bool HAS_DEPTH>
-__device__ __forceinline__ uint32_t coverQuadPixel(const DrawParams &p, const Tri &t, int px, int py, bool inD,
-                                                   Samples4 &fb, float &sb0, float &sb1, float &sb2) {
+// Coverage of pixel (px, py) by one triangle: a pure function of the two (RendererSoft.cpp:776-804).
+// mask bit i = sample i covered and inside the depth range (S=1: bit 0 = centre covered; its depth
+// range clip has no effect, RendererSoft.cpp:797-799 vs :846-849, :872-874); z per sample; the
+// perspective-corrected barycentrics of the shading sample (RendererInternal.h:114-124).
+struct Cover {
+  uint32_t mask;
+  float z0, z1, z2, z3;
+  float b0, b1, b2;
+};
+
+template<int S>
+__device__ __forceinline__ Cover coverSamples(const DrawParams &p, const TriCov &t, int px, int py) {
+  Cover c;
+  c.mask = 0u;
+  c.z0 = c.z1 = c.z2 = c.z3 = 0.f;
+  c.b0 = c.b1 = c.b2 = 0.f;
   const float fx = (float) px, fy = (float) py;
-  const bool testDepth = p.depthTest && HAS_DEPTH;
   if (S == 1) {
-    if (!baryCover(t, fx + 0.5f, fy + 0.5f, sb0, sb1, sb2)) return 0u;
-    float z = interpZW(sb0, sb1, sb2, t.z0, t.z1, t.z2);
-    correct(t, sb0, sb1, sb2);
-    // the S=1 depth-range clip has no effect: early-Z overwrites it and the per-sample path does
-    // not read it (RendererSoft.cpp:797-799 vs :846-849, :872-874)
-    if (p.earlyZ && testDepth && !(inD && depthPass(p, z, fb.d0))) return 0u;
-    if (testDepth) {
-      if (!(inD && depthPass(p, z, fb.d0))) return 0u;
-      if (p.depthMask) fb.d0 = gclamp(z, p.vp.absMin, p.vp.absMax);
-    }
-    return 1u;
+    if (!baryCover(t, fx + 0.5f, fy + 0.5f, c.b0, c.b1, c.b2)) return c;
+    c.z0 = interpZW(c.b0, c.b1, c.b2, t.z0, t.z1, t.z2);
+    correct(t, c.b0, c.b1, c.b2);
+    c.mask = 1u;
+    return c;
   }
-  float a0, a1, a2, b0, b1, b2, c0, c1, c2, e0, e1, e2, m0, m1, m2;
+  float a0, a1, a2, b0, b1, b2, d0, d1, d2, e0, e1, e2, m0, m1, m2;
   bool s0 = baryCover(t, kLoc4xR[0].x + fx, kLoc4xR[0].y + fy, a0, a1, a2);
   bool s1 = baryCover(t, kLoc4xR[1].x + fx, kLoc4xR[1].y + fy, b0, b1, b2);
-  bool s2 = baryCover(t, kLoc4xR[2].x + fx, kLoc4xR[2].y + fy, c0, c1, c2);
+  bool s2 = baryCover(t, kLoc4xR[2].x + fx, kLoc4xR[2].y + fy, d0, d1, d2);
   bool s3 = baryCover(t, kLoc4xR[3].x + fx, kLoc4xR[3].y + fy, e0, e1, e2);
-  if (!(s0 || s1 || s2 || s3)) return 0u;
+  if (!(s0 || s1 || s2 || s3)) return c;
   bool sc = baryCover(t, fx + 0.5f, fy + 0.5f, m0, m1, m2);
   // InitShadingSample: the centre if covered, else the first covered sample
-  if (sc) { sb0 = m0; sb1 = m1; sb2 = m2; }
-  else if (s0) { sb0 = a0; sb1 = a1; sb2 = a2; }
-  else if (s1) { sb0 = b0; sb1 = b1; sb2 = b2; }
-  else if (s2) { sb0 = c0; sb1 = c1; sb2 = c2; }
-  else { sb0 = e0; sb1 = e1; sb2 = e2; }
-  float z0 = 0.f, z1 = 0.f, z2 = 0.f, z3 = 0.f;
-  bool i0 = false, i1 = false, i2 = false, i3 = false;
-  if (s0) { z0 = interpZW(a0, a1, a2, t.z0, t.z1, t.z2); i0 = !(z0 < p.vp.absMin || z0 > p.vp.absMax); }
-  if (s1) { z1 = interpZW(b0, b1, b2, t.z0, t.z1, t.z2); i1 = !(z1 < p.vp.absMin || z1 > p.vp.absMax); }
-  if (s2) { z2 = interpZW(c0, c1, c2, t.z0, t.z1, t.z2); i2 = !(z2 < p.vp.absMin || z2 > p.vp.absMax); }
-  if (s3) { z3 = interpZW(e0, e1, e2, t.z0, t.z1, t.z2); i3 = !(z3 < p.vp.absMin || z3 > p.vp.absMax); }
-  correct(t, sb0, sb1, sb2);
-  if (p.earlyZ && testDepth) {
-    if (i0) i0 = inD && depthPass(p, z0, fb.d0);
-    if (i1) i1 = inD && depthPass(p, z1, fb.d1);
-    if (i2) i2 = inD && depthPass(p, z2, fb.d2);
-    if (i3) i3 = inD && depthPass(p, z3, fb.d3);
+  if (sc) { c.b0 = m0; c.b1 = m1; c.b2 = m2; }
+  else if (s0) { c.b0 = a0; c.b1 = a1; c.b2 = a2; }
+  else if (s1) { c.b0 = b0; c.b1 = b1; c.b2 = b2; }
+  else if (s2) { c.b0 = d0; c.b1 = d1; c.b2 = d2; }
+  else { c.b0 = e0; c.b1 = e1; c.b2 = e2; }
+  if (s0) { c.z0 = interpZW(a0, a1, a2, t.z0, t.z1, t.z2); if (!(c.z0 < p.vp.absMin || c.z0 > p.vp.absMax)) c.mask |= 1u; }
+  if (s1) { c.z1 = interpZW(b0, b1, b2, t.z0, t.z1, t.z2); if (!(c.z1 < p.vp.absMin || c.z1 > p.vp.absMax)) c.mask |= 2u; }
+  if (s2) { c.z2 = interpZW(d0, d1, d2, t.z0, t.z1, t.z2); if (!(c.z2 < p.vp.absMin || c.z2 > p.vp.absMax)) c.mask |= 4u; }
+  if (s3) { c.z3 = interpZW(e0, e1, e2, t.z0, t.z1, t.z2); if (!(c.z3 < p.vp.absMin || c.z3 > p.vp.absMax)) c.mask |= 8u; }
+  correct(t, c.b0, c.b1, c.b2);
+  c.mask |= 16u;   // the pixel is covered (its fragment runs even if every sample is depth-clipped)
+  return c;
+}
+
+// early-Z (RendererSoft.cpp:853-878), then the per-sample depth test + write in sample order
+// (processPerSampleOperations, :838-849). Returns the samples whose colour operation follows.
+template<int S, bool HAS_DEPTH>
+__device__ __forceinline__ uint32_t depthOps(const DrawParams &p, const Cover &c, bool inD, Samples4 &fb) {
+  const bool testDepth = p.depthTest && HAS_DEPTH;
+  if (S == 1) {
+    if (!c.mask) return 0u;
+    if (!testDepth) return 1u;
+    if (!(inD && depthPass(p, c.z0, fb.d0))) return 0u;   // early-Z and the per-sample test agree
+    if (p.depthMask) fb.d0 = gclamp(c.z0, p.vp.absMin, p.vp.absMax);
+    return 1u;
+  }
+  if (!(c.mask & 16u)) return 0u;
+  bool i0 = c.mask & 1u, i1 = c.mask & 2u, i2 = c.mask & 4u, i3 = c.mask & 8u;
+  if (!testDepth) return c.mask & 15u;
+  if (p.earlyZ) {
+    if (i0) i0 = inD && depthPass(p, c.z0, fb.d0);
+    if (i1) i1 = inD && depthPass(p, c.z1, fb.d1);
+    if (i2) i2 = inD && depthPass(p, c.z2, fb.d2);
+    if (i3) i3 = inD && depthPass(p, c.z3, fb.d3);
     if (!(i0 || i1 || i2 || i3)) return 0u;
   }
-  // per-sample depth test + write in sample order (processPerSampleOperations, :838-845)
-  if (testDepth) {
-    if (i0) { i0 = inD && depthPass(p, z0, fb.d0); if (i0 && p.depthMask) fb.d0 = gclamp(z0, p.vp.absMin, p.vp.absMax); }
-    if (i1) { i1 = inD && depthPass(p, z1, fb.d1); if (i1 && p.depthMask) fb.d1 = gclamp(z1, p.vp.absMin, p.vp.absMax); }
-    if (i2) { i2 = inD && depthPass(p, z2, fb.d2); if (i2 && p.depthMask) fb.d2 = gclamp(z2, p.vp.absMin, p.vp.absMax); }
-    if (i3) { i3 = inD && depthPass(p, z3, fb.d3); if (i3 && p.depthMask) fb.d3 = gclamp(z3, p.vp.absMin, p.vp.absMax); }
-  }
+  if (i0) { i0 = inD && depthPass(p, c.z0, fb.d0); if (i0 && p.depthMask) fb.d0 = gclamp(c.z0, p.vp.absMin, p.vp.absMax); }
+  if (i1) { i1 = inD && depthPass(p, c.z1, fb.d1); if (i1 && p.depthMask) fb.d1 = gclamp(c.z1, p.vp.absMin, p.vp.absMax); }
+  if (i2) { i2 = inD && depthPass(p, c.z2, fb.d2); if (i2 && p.depthMask) fb.d2 = gclamp(c.z2, p.vp.absMin, p.vp.absMax); }
+  if (i3) { i3 = inD && depthPass(p, c.z3, fb.d3); if (i3 && p.depthMask) fb.d3 = gclamp(c.z3, p.vp.absMin, p.vp.absMax); }
   return (i0 ? 1u : 0u) | (i1 ? 2u : 0u) | (i2 ? 4u : 0u) | (i3 ? 8u : 0u);
 }
 
@@ -358,6 +388,7 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
   const bool inD = HAS_DEPTH && px < p.dw && py < p.dh;
   FragQueue &q = queues[HAS_COLOR ? warp : 0];
   int count = 0;
+  unsigned long long mine = 0ull;   // queue entries of this lane's pixel
   const unsigned lt = (1u << lane) - 1u;
   Samples4 fb = {0u, 0u, 0u, 0u, 0.f, 0.f, 0.f, 0.f};
   if (inC) {
@@ -394,7 +425,6 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
     int4 r = make_int4(0, -1, 0, -1);
     float ea[3] = {0.f, 0.f, 0.f}, eb[3] = {0.f, 0.f, 0.f}, ek[3] = {0.f, 0.f, 0.f}, et[3] = {0.f, 0.f, 0.f};
     bool anyPix = false;
-    Tri tb;
     if (i < end) {
       prim = __ldg(p.valA + i);
       const TriSetup *tp = p.tri + prim;
@@ -407,7 +437,6 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
         float area = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
         float mag = fabsf(X[1] - X[0]) + fabsf(Y[1] - Y[0]) + fabsf(X[2] - X[0]) + fabsf(Y[2] - Y[0]);
         anyPix = !(fabsf(area) > 1e-3f * mag * mag + 1e-6f);   // near-degenerate: skip the edge pre-test
-        tb = loadTri(tp);
         float o = area > 0.f ? 1.f : -1.f;
 #pragma unroll
         for (int e = 0; e < 3; e++) {
@@ -432,7 +461,6 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
         c = (ea[0] * fx + eb[0] * fy + ek[0] >= -et[0]) && (ea[1] * fx + eb[1] * fy + ek[1] >= -et[1]) &&
             (ea[2] * fx + eb[2] * fy + ek[2] >= -et[2]);
       }
-      if (c) c = pixelCovered<S>(tb, cx, cy);   // exact: some coverage sample of the pixel is inside
       unsigned mm = __ballot_sync(0xffffffffu, c);
       if (lane == pp) cand = mm;
     }
@@ -443,41 +471,42 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
       int j = cand ? __ffs(cand) - 1 : -1;
       if (cand) cand &= cand - 1;
       int pr = __shfl_sync(0xffffffffu, prim, j < 0 ? 0 : j);
-      int nx = 0, ny = 0, x0 = 0, x1 = 0, y0 = 0, y1 = 0;
-      Tri t;
+      int x0 = 0, x1 = 0, y0 = 0, y1 = 0, nx = 0, nq = 0;
+      Cover cv;
+      cv.mask = 0u;
       if (j >= 0) {
-        t = loadTri(p.tri + pr);
-        nx = quadCands(t.bminx, t.bmaxx, t.bcx, px, x0, x1);
-        ny = nx ? quadCands(t.bminy, t.bmaxy, t.bcy, py, y0, y1) : 0;
+        const TriSetup *tp = p.tri + pr;
+        nq = quadsOf(tp, px, py, x0, x1, y0, y1, nx);
+        if (nq) cv = coverSamples<S>(p, loadTriCov(tp), px, py);
+        if (!cv.mask) nq = 0;
       }
-      int nq = nx * ny;
       int nqMax = __reduce_max_sync(0xffffffffu, nq);
-      for (int k = 0; k < nqMax; k++) {
+      for (int k = 0; k < nqMax; k++) {   // a pixel can lie in two overlapping blocks' quads
         uint32_t mask = 0;
-        float sb0 = 0.f, sb1 = 0.f, sb2 = 0.f;
         int qx = 0, qy = 0;
         if (k < nq) {
           qy = (k / nx) ? y1 : y0;
           qx = (k % nx) ? x1 : x0;
-          mask = coverQuadPixel<S, HAS_DEPTH>(p, t, px, py, inD, fb, sb0, sb1, sb2);
+          mask = depthOps<S, HAS_DEPTH>(p, cv, inD, fb);
         }
         if (HAS_COLOR) {
-          if (count + 32 > kQueue) flushQueue<SH, S, HAS_DEPTH>(p, q, count, lane, rx0, ry0, inC, fb);
+          if (count + 32 > kQueue) flushQueue<SH, S, HAS_DEPTH>(p, q, count, mine, lane, rx0, ry0, inC, fb);
           unsigned want = __ballot_sync(0xffffffffu, mask != 0);
           if (mask) {
             int e = count + __popc(want & lt);
             q.tri[e] = pr;
             q.meta[e] = (uint32_t) lane | (mask << 5) | ((uint32_t) (px - qx) << 9) | ((uint32_t) (py - qy) << 10);
-            q.b0[e] = sb0;
-            q.b1[e] = sb1;
-            q.b2[e] = sb2;
+            q.b0[e] = cv.b0;
+            q.b1[e] = cv.b1;
+            q.b2[e] = cv.b2;
+            mine |= 1ull << e;
           }
           count += __popc(want);
         }
       }
     }
   }
-  if (HAS_COLOR && count > 0) flushQueue<SH, S, HAS_DEPTH>(p, q, count, lane, rx0, ry0, inC, fb);
+  if (HAS_COLOR && count > 0) flushQueue<SH, S, HAS_DEPTH>(p, q, count, mine, lane, rx0, ry0, inC, fb);
   if (inC) {
     size_t pix = (size_t) py * p.cw + px;
     if (S == 4) {
