@@ -209,16 +209,27 @@ __device__ __forceinline__ uint32_t texel(const DevTex &t, int face, int level, 
 }
 
 __device__ __forceinline__ int wrapCoord(int x, int n, int wrap) {
-  int rep = (x & ((n - 1) + n)) & (n - 1);   // CoordMod as the reference's macro expands (SamplerSoft.h:14)
-  int m = (x & ((2 * n - 1) + 2 * n)) & (2 * n - 1);
-  m -= n;
-  m = m >= 0 ? m : (-1 - m);
-  int mir = n - 1 - m;
-  int edge = x < 0 ? 0 : (x >= n ? n - 1 : x);
-  return wrap == WRAP_REPEAT ? rep : (wrap == WRAP_MIRRORED ? mir : (wrap == WRAP_EDGE ? edge : x));
+  if (wrap == WRAP_REPEAT) return (x & ((n - 1) + n)) & (n - 1);   // CoordMod as the macro expands (SamplerSoft.h:14)
+  if (wrap == WRAP_EDGE) return x < 0 ? 0 : (x >= n ? n - 1 : x);
+  if (wrap == WRAP_MIRRORED) {
+    int m = (x & ((2 * n - 1) + 2 * n)) & (2 * n - 1);
+    m -= n;
+    m = m >= 0 ? m : (-1 - m);
+    return n - 1 - m;
+  }
+  return x;   // CLAMP_TO_BORDER: range-checked by the caller
 }
 
-// BaseSampler::pixelWithWrapMode (SamplerSoft.h:170-213), selects instead of a switch
+// storage index of (x, y) in one level (Buffer::convertIndex for the three layouts)
+__device__ __forceinline__ uint32_t levelIndex(int layout, int x, int y, int w, int tilesW) {
+  if (layout == LAYOUT_LINEAR) return (uint32_t) x + (uint32_t) y * (uint32_t) w;
+  if (layout == LAYOUT_TILED)
+    return ((((uint32_t) (y >> 2) * tilesW + (uint32_t) (x >> 2))) << 4) + ((uint32_t) (y & 3) << 2) + (uint32_t) (x & 3);
+  return ((((uint32_t) (y >> 5) * tilesW + (uint32_t) (x >> 5))) << 10) +
+         (spread5((uint32_t) (x & 31)) | (spread5((uint32_t) (y & 31)) << 1));
+}
+
+// BaseSampler::pixelWithWrapMode (SamplerSoft.h:170-213)
 __device__ __forceinline__ uint32_t pixelWrap(const DevTex &t, int face, int level, int x, int y, int wrap,
                                               uint32_t border) {
   int w = t.w[level], h = t.h[level];
@@ -227,6 +238,7 @@ __device__ __forceinline__ uint32_t pixelWrap(const DevTex &t, int face, int lev
   if (outside) return wrap == WRAP_BORDER ? border : 0u;
   return texel(t, face, level, xx, yy);
 }
+
 
 __device__ __forceinline__ uint32_t mixTexel(uint32_t x, uint32_t y, float a, bool isF) {
   if (isF) {
@@ -238,15 +250,24 @@ __device__ __forceinline__ uint32_t mixTexel(uint32_t x, uint32_t y, float a, bo
   return pack4(X.x * ia + Y.x * a, X.y * ia + Y.y * a, X.z * ia + Y.z * a, X.w * ia + Y.w * a);
 }
 
+// BaseSampler::samplePixelBilinear (SamplerSoft.h:254-266): the 2x2 footprint's coordinates are
+// wrapped once per axis and the level's base, size and layout are read once
 __device__ __forceinline__ uint32_t bilinearPx(const DevTex &t, int face, int level, float ux, float uy, int wrap,
                                                uint32_t border, bool isF) {
   float fx0 = ux - 0.5f, fy0 = uy - 0.5f;
   float flx = floorf(fx0), fly = floorf(fy0);
   int x = (int) flx, y = (int) fly;
-  uint32_t s1 = pixelWrap(t, face, level, x, y, wrap, border);
-  uint32_t s2 = pixelWrap(t, face, level, x + 1, y, wrap, border);
-  uint32_t s3 = pixelWrap(t, face, level, x, y + 1, wrap, border);
-  uint32_t s4 = pixelWrap(t, face, level, x + 1, y + 1, wrap, border);
+  const int w = t.w[level], h = t.h[level], tw = t.tilesW[level], layout = t.layout;
+  const uint32_t *lv = t.base + (size_t) face * t.layerStride + t.offset[level];
+  int xa = wrapCoord(x, w, wrap), xb = wrapCoord(x + 1, w, wrap);
+  int ya = wrapCoord(y, h, wrap), yb = wrapCoord(y + 1, h, wrap);
+  bool vxa = (unsigned) xa < (unsigned) w, vxb = (unsigned) xb < (unsigned) w;
+  bool vya = (unsigned) ya < (unsigned) h, vyb = (unsigned) yb < (unsigned) h;
+  uint32_t fill = wrap == WRAP_BORDER ? border : 0u;
+  uint32_t s1 = (vxa && vya) ? __ldg(lv + levelIndex(layout, xa, ya, w, tw)) : fill;
+  uint32_t s2 = (vxb && vya) ? __ldg(lv + levelIndex(layout, xb, ya, w, tw)) : fill;
+  uint32_t s3 = (vxa && vyb) ? __ldg(lv + levelIndex(layout, xa, yb, w, tw)) : fill;
+  uint32_t s4 = (vxb && vyb) ? __ldg(lv + levelIndex(layout, xb, yb, w, tw)) : fill;
   float fx = fx0 - flx, fy = fy0 - fly;
   return mixTexel(mixTexel(s1, s2, fx, isF), mixTexel(s3, s4, fx, isF), fy, isF);
 }
