@@ -241,6 +241,45 @@ SGLC_API sglc_status sglc_get_stream(sglc_context *ctx, void **stream);
 /* Raster tile edge in pixels (8, 16 or 32); picked by the autotuner, default 16. */
 SGLC_API sglc_status sglc_set_tile_size(sglc_context *ctx, int32_t tile);
 
+/* ---- allocation-free draw ----------------------------------------------------------------- */
+/* One vertex-colour draw (position vec3 padded to 16 B + RGBA float colour, 32-B stride; the
+ * vertex-colour shading model above) into caller-owned device buffers, for callers that cannot
+ * call cudaMalloc: code whose device memory is owned by a host framework's pool, real-time
+ * render threads that must not enter the CUDA allocator, library code that must not grow the
+ * process's footprint. No counterpart in the reference. It allocates nothing: its working memory
+ * is one fixed device array of at most 24 MiB inside the library, held by every GPU that loads
+ * the library until the process exits, so there is no context to create. Limits: 65,536 vertices,
+ * 32,768 triangles, width and height <= 1024, 262,144 (tile, triangle) bin entries; larger inputs
+ * are rejected with SGLC_ERR_INVALID_VALUE and a message in `error`.
+ * The attachments are read and written in place (no clear; viewport = the whole attachment),
+ * linear, 4 interleaved samples per pixel when samples = 4. Everything is enqueued on `stream`
+ * (a cudaStream_t, 0 = default stream), which is synchronised once at the end to read the
+ * capacity flags (SGLC_ERR_OVERFLOW: the attachments' contents are then unspecified).
+ * The first call on a device looks up the array's device address; make it before any stream
+ * capture. All calls share the array: calls that overlap on the GPU (different streams or
+ * threads) race and must be serialised by the caller. */
+typedef struct sglc_noalloc_draw {
+  const void *vertexes;           /* device, vertex_count * stride bytes */
+  int32_t vertex_count;
+  int32_t stride;                 /* bytes; must be 32 */
+  const int32_t *indices;         /* device, 3 * triangle_count */
+  int32_t triangle_count;
+  const void *uniforms_model;     /* host, 256-B UniformsModel (Material.h:70-76) */
+  const void *uniforms_material;  /* host, 48-B UniformsMaterial (Material.h:78-85) */
+  int32_t width;
+  int32_t height;
+  int32_t samples;                /* 1 or 4 */
+  uint32_t *color;                /* device RGBA8, width * height * samples */
+  uint32_t *resolved;             /* device RGBA8, width * height (samples = 4 only) */
+  float *depth;                   /* device, width * height * samples */
+  sglc_render_states states;
+  int32_t early_z;
+  char *error;                    /* optional: receives a message when the call fails */
+  size_t error_len;
+} sglc_noalloc_draw;
+
+SGLC_API sglc_status sglc_draw_vertex_color_noalloc(const sglc_noalloc_draw *draw, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
