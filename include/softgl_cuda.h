@@ -241,6 +241,48 @@ SGLC_API sglc_status sglc_get_stream(sglc_context *ctx, void **stream);
 /* Raster tile edge in pixels (8, 16 or 32); picked by the autotuner, default 16. */
 SGLC_API sglc_status sglc_set_tile_size(sglc_context *ctx, int32_t tile);
 
+/* ---- neural IBL shader (no reference counterpart) ------------------------------------------- */
+/* A small MLP (12 inputs, 6-frequency encoding, 2 x 64 ReLU, 3 outputs; BF16 weights, FP32
+ * accumulation on the tensor cores) that stands in for the image-based-lighting term of the PBR
+ * shader (PbrSoft.h:296-309). It is trained on records that the plain PBR shader captures while it
+ * renders, by tensor-core forward / backward / Adam kernels, and bound to a PBR program to replace
+ * the irradiance and prefiltered-cube evaluation inside the fragment stage. Records are 16 floats:
+ * N.xyz, V.xyz, roughness, metallic, albedo texel rgb, max(dot(N, V), 0), sqrt of the IBL term
+ * rgb (before ambient occlusion), 0. Parameters are FP32 in the order W1[64][156], b1[64],
+ * W2[64][64], b2[64], W3[3][64], b3[3] (sglc_neural_param_count() floats). All calls run on the
+ * owning context's stream and synchronise before returning, except sglc_neural_capture. */
+typedef struct sglc_neural sglc_neural;
+typedef struct sglc_neural_train_params {
+  int32_t steps;          /* Adam steps to run */
+  int32_t batch;          /* records per step, drawn uniformly with replacement */
+  float lr, beta1, beta2, eps;
+  uint64_t seed;          /* record sampling: index = mix64(seed ^ step << 32 ^ row) % records */
+} sglc_neural_train_params;
+
+SGLC_API sglc_status sglc_neural_create(sglc_context *ctx, uint64_t seed, sglc_neural **out);
+SGLC_API sglc_status sglc_neural_destroy(sglc_neural *net);
+SGLC_API int64_t sglc_neural_param_count(void);
+SGLC_API sglc_status sglc_neural_set_params(sglc_neural *net, const float *params, int64_t count);
+SGLC_API sglc_status sglc_neural_get_params(sglc_neural *net, float *params, int64_t count);
+/* Replace the record set with `count` host records. */
+SGLC_API sglc_status sglc_neural_set_records(sglc_neural *net, const float *records, int64_t count);
+SGLC_API sglc_status sglc_neural_get_records(sglc_neural *net, float *records, int64_t first, int64_t count);
+/* Start capturing: every `stride`-th fragment the plain PBR shader shades on `ctx` (in the order
+ * the shading threads reach the capture counter) appends a record, up to `capacity` records (the
+ * rest are dropped); capacity 0 stops. */
+SGLC_API sglc_status sglc_neural_capture(sglc_context *ctx, sglc_neural *net, int64_t capacity, int32_t stride);
+SGLC_API sglc_status sglc_neural_record_count(sglc_neural *net, int64_t *count);
+/* Adam on mean squared error; `loss` receives the last step's batch loss. */
+SGLC_API sglc_status sglc_neural_train(sglc_neural *net, const sglc_neural_train_params *params, float *loss);
+/* Gradient of the mean squared error over records [first, first + count) (no update). */
+SGLC_API sglc_status sglc_neural_gradients(sglc_neural *net, int64_t first, int64_t count, float *grads,
+                                           float *loss);
+/* Network outputs (3 floats per record) for records [first, first + count). */
+SGLC_API sglc_status sglc_neural_infer(sglc_neural *net, int64_t first, int64_t count, float *out);
+/* Bind a network to a PBR program: its IBL term comes from the network (null unbinds, restoring
+ * the plain shader). The network must outlive its use by draws. */
+SGLC_API sglc_status sglc_program_set_neural_shader(sglc_context *ctx, sglc_handle prog, sglc_neural *net);
+
 /* ---- allocation-free draw ----------------------------------------------------------------- */
 /* One vertex-colour draw (position vec3 padded to 16 B + RGBA float colour, 32-B stride; the
  * vertex-colour shading model above) into caller-owned device buffers, for callers that cannot

@@ -15,6 +15,7 @@
 #include "softgl_cuda.h"
 #include "sglc_device.cuh"
 #include "sglc_kernels.h"
+#include "sglc_nn_host.h"
 
 using namespace sglc;
 
@@ -91,6 +92,7 @@ struct ProgObj {
   uint8_t defines[8] = {0};
   uint8_t uniforms[kUniformBytes] = {0};
   int samplers[kMaxSamplers] = {0};
+  const sglc_neural *neural = nullptr;   // bound neural IBL shader (PBR programs only)
 };
 
 struct UsObj {
@@ -170,6 +172,11 @@ struct Ctx {
       sortHistScan, staging;
   // capacity hints that survive between draws
   int extraVertHint = 0, polyHint = 0, appendHint = 0;
+  // neural IBL shader: training-record capture target
+  float *capRecords = nullptr;
+  unsigned long long *capCount = nullptr;
+  long long capCap = 0;
+  int capStride = 1;
 
   Object *get(int h, int kind) {
     auto it = objects.find(h);
@@ -370,6 +377,18 @@ sglc_status drawImpl(Ctx *c) {
   }
   for (int s = 0; s < 4; s++)
     if (p.samp[s].valid && p.samp[s].lodFromDerivative && p.def[s]) p.needDeriv = 1;
+  int iblEnabled = 0;
+  memcpy(&iblEnabled, prog.uniforms + 324, sizeof(int));   // UniformsMaterial.u_enableIBL (PbrSoft.h:45)
+  if (p.shading == SH_PBR && prog.neural && ct && iblEnabled) {
+    p.shading = SH_PBR_NEURAL;
+    p.nnImage = neuralImage(prog.neural);
+  }
+  if (p.shading == SH_PBR && c->capRecords) {
+    p.capRecords = c->capRecords;
+    p.capCount = c->capCount;
+    p.capCap = c->capCap;
+    p.capStride = c->capStride;
+  }
   p.depthTest = rs.depth_test;
   p.depthMask = rs.depth_mask;
   p.depthFunc = rs.depth_func;
@@ -563,6 +582,29 @@ sglc_status drawImpl(Ctx *c) {
 }
 
 }  // namespace
+
+namespace sglc {
+cudaStream_t ctxStream(sglc_context *ctx) { return reinterpret_cast<Ctx *>(ctx)->stream; }
+int ctxDevice(sglc_context *ctx) { return reinterpret_cast<Ctx *>(ctx)->device; }
+void ctxSetError(sglc_context *ctx, const char *msg) {
+  if (ctx) reinterpret_cast<Ctx *>(ctx)->err = msg;
+}
+void ctxSetCapture(sglc_context *ctx, float *records, unsigned long long *count, long long capacity, int stride) {
+  Ctx *c = reinterpret_cast<Ctx *>(ctx);
+  c->capRecords = records;
+  c->capCount = records ? count : nullptr;
+  c->capCap = records ? capacity : 0;
+  c->capStride = stride;
+}
+void ctxDetachNeural(sglc_context *ctx, const sglc_neural *net) {
+  Ctx *c = reinterpret_cast<Ctx *>(ctx);
+  for (auto &kv : c->objects)
+    if (kv.second.kind == K_PROG && kv.second.prog.neural == net) kv.second.prog.neural = nullptr;
+  c->capRecords = nullptr;
+  c->capCount = nullptr;
+  c->capCap = 0;
+}
+}  // namespace sglc
 
 extern "C" {
 
@@ -833,6 +875,15 @@ sglc_status sglc_program_set_shaders(sglc_context *ctx, sglc_handle prog, int32_
     for (size_t i = 0; i < s->defines.size(); i++)
       if (n == s->defines[i]) P.defines[i] = 1;
   memset(P.uniforms, 0, sizeof(P.uniforms));
+  return SGLC_OK;
+}
+
+sglc_status sglc_program_set_neural_shader(sglc_context *ctx, sglc_handle prog, sglc_neural *net) {
+  CTX;
+  GET(p, prog, K_PROG);
+  if (net && (!p->prog.shader || p->prog.shader->model != SH_PBR))
+    return c->fail(SGLC_ERR_INVALID_VALUE, "set_neural_shader: the program must use the PBR shading model");
+  p->prog.neural = net;
   return SGLC_OK;
 }
 

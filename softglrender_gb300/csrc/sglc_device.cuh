@@ -21,7 +21,7 @@ constexpr int kBlock = 32;           // RendererSoft::rasterBlockSize_ (Renderer
 enum { LAYOUT_LINEAR = 0, LAYOUT_TILED = 1, LAYOUT_MORTON = 2 };
 enum { FILTER_NEAREST = 0, FILTER_LINEAR, FILTER_NN, FILTER_LN, FILTER_NL, FILTER_LL };
 enum { WRAP_REPEAT = 0, WRAP_MIRRORED, WRAP_EDGE, WRAP_BORDER };
-enum { SH_BASE = 1, SH_BLINN = 2, SH_PBR = 3, SH_BLINN_DIR = 100, SH_VCOLOR = 101 };
+enum { SH_BASE = 1, SH_BLINN = 2, SH_PBR = 3, SH_BLINN_DIR = 100, SH_VCOLOR = 101, SH_PBR_NEURAL = 102 };
 
 // one texture as seen by a sampler: all layers x levels in one allocation
 struct DevTex {
@@ -132,6 +132,13 @@ struct DrawParams {
   unsigned long long *fragCounter;   // FS invocations (instrumented runs only), else null
   int needDeriv;                  // the FS reads texcoord derivatives (a bound 2D sampler with a LOD callback)
   const int *tileOrder;           // raster CTA -> tile, heaviest tile lists first (null: identity)
+  // neural IBL shader (sglc_nn.cuh): training-record capture by the plain PBR shader, and the
+  // BF16 weight image read by the fused neural variant
+  float *capRecords;              // null: no capture
+  unsigned long long *capCount;
+  long long capCap;
+  int capStride;
+  const uint8_t *nnImage;
 };
 
 // ------------------------------------------------------------------------------------------------

@@ -535,7 +535,8 @@ void launchVertexAndClip(const DrawParams &p, cudaStream_t st) {
     case SH_BASE: launchGeometry<SH_BASE>(p, st); break;
     case SH_BLINN: launchGeometry<SH_BLINN>(p, st); break;
     case SH_BLINN_DIR: launchGeometry<SH_BLINN_DIR>(p, st); break;
-    case SH_PBR: launchGeometry<SH_PBR>(p, st); break;
+    case SH_PBR:
+    case SH_PBR_NEURAL: launchGeometry<SH_PBR>(p, st); break;
     case SH_VCOLOR: launchGeometry<SH_VCOLOR>(p, st); break;
   }
 }

@@ -1,0 +1,147 @@
+// The neural IBL shader: a small MLP that stands in for the image-based-lighting term of the PBR
+// fragment shader (PbrSoft.h:296-309: irradiance fetch, prefiltered-cube fetch at a roughness
+// LOD, FresnelSchlickRoughness and EnvBRDFApprox). The direct point light, gamma and emissive stay
+// analytic. Shared by the training / inference kernels (sglc_nn.cu) and the fused raster variant.
+//
+// Network: 12 inputs -> frequency encoding (156 features, padded to 160) -> 64 ReLU -> 64 ReLU -> 3.
+// Inputs: normal N (3), view direction V (3), roughness, metallic, albedo texel (3, sRGB as
+// sampled), max(dot(N, V), 0). Output: sqrt of the IBL ambient term before the ambient-occlusion
+// factor; the shader squares it back (ambient = max(y, 0)^2).
+// Encoding of input x_i: for k = 0..5 feature 24k + 2i = sin(2^k pi x_i), 24k + 2i + 1 =
+// cos(2^k pi x_i), computed from sincospi(x_i) by the double-angle recurrences s' = 2 s c,
+// c' = 1 - 2 s s; feature 144 + i = x_i. Feature 156 is the constant 1 on training tiles (its weight
+// column stays zero, so the forward pass ignores it, and the weight gradient's row 156 is the first
+// layer's bias gradient); features 157-159 are zero.
+//
+// Parameters (FP32 master copy, flat order): W1[64][156], b1[64], W2[64][64], b2[64], W3[3][64],
+// b3[3]. The device keeps a BF16 "image" of the weights in the core-matrix tile layout of
+// sglc_tc.cuh, ready to copy into shared memory: W1 as a [64][160] tile, W2 [64][64], W3 [16][64]
+// (rows 3-15 zero), followed by the FP32 biases b1 (64), b2 (64), b3 (3) and one zero.
+#pragma once
+
+#include <cstdint>
+#include <cuda_bf16.h>
+#include "sglc_tc.cuh"
+
+namespace sglc {
+namespace nn {
+
+constexpr int kIn = 12;
+constexpr int kFreq = 6;
+constexpr int kFeat = kIn * (1 + 2 * kFreq);   // 156
+constexpr int kK1 = 160;                       // padded first-layer K
+constexpr int kHid = 64;
+constexpr int kOut = 3;
+constexpr int kOutPad = 16;
+constexpr int kOneFeature = 156;
+
+// offsets into the flat parameter vector
+constexpr int kW1 = 0;
+constexpr int kB1 = kW1 + kHid * kFeat;        // 9984
+constexpr int kW2 = kB1 + kHid;
+constexpr int kB2 = kW2 + kHid * kHid;
+constexpr int kW3 = kB2 + kHid;
+constexpr int kB3 = kW3 + kOut * kHid;
+constexpr int kParams = kB3 + kOut;            // 14403
+constexpr int kPartialStride = 14408;          // per-CTA gradient partial: params, loss, pad
+
+// weight image (bytes)
+constexpr int kImgW1 = 0;
+constexpr int kImgW2 = kImgW1 + kHid * kK1 * 2;          // 20480
+constexpr int kImgW3 = kImgW2 + kHid * kHid * 2;         // 28672
+constexpr int kImgBias = kImgW3 + kOutPad * kHid * 2;    // 30720
+constexpr int kImgBytes = kImgBias + (64 + 64 + 4) * 4;  // 31248
+static_assert(kImgBytes % 16 == 0, "image copies in 16-byte pieces");
+
+// training record: 12 inputs, 3 targets (sqrt of the ambient term), 1 pad
+constexpr int kRecordFloats = 16;
+
+// Encode one fragment's 12 inputs into row `row` of a core-matrix tile (BF16), one 16-byte store per
+// 8 features: the 8-feature chunks [C0, C1) go to tile columns 8 * (chunk - C0) of a tile with
+// `tileC` columns (the whole row: C0 = 0, C1 = 20, tileC = 160).
+template<int C0, int C1>
+__device__ __forceinline__ void encodeChunks(const float *x, uint8_t *tile, int row, int tileC, bool oneFeature) {
+  float s[kIn], c[kIn];
+#pragma unroll
+  for (int i = 0; i < kIn; i++) sincospif(x[i], &s[i], &c[i]);
+#pragma unroll
+  for (int k = 0; k < kFreq; k++) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) {   // features 24k + 8q .. +7 = inputs 4q .. 4q+3, (sin, cos) pairs
+      const int chunk = 3 * k + q;
+      if (chunk >= C0 && chunk < C1) {
+        uint4 v = make_uint4(tc::packBf16(s[4 * q], c[4 * q]), tc::packBf16(s[4 * q + 1], c[4 * q + 1]),
+                             tc::packBf16(s[4 * q + 2], c[4 * q + 2]), tc::packBf16(s[4 * q + 3], c[4 * q + 3]));
+        *reinterpret_cast<uint4 *>(tile + tc::tileOffset(row, 8 * (chunk - C0), tileC)) = v;
+      }
+    }
+    if (k + 1 < kFreq) {
+#pragma unroll
+      for (int i = 0; i < kIn; i++) {
+        float s2 = 2.0f * s[i] * c[i];
+        float c2 = 1.0f - 2.0f * s[i] * s[i];
+        s[i] = s2;
+        c[i] = c2;
+      }
+    }
+  }
+  if (18 >= C0 && 18 < C1) {
+    uint4 a = make_uint4(tc::packBf16(x[0], x[1]), tc::packBf16(x[2], x[3]), tc::packBf16(x[4], x[5]),
+                         tc::packBf16(x[6], x[7]));
+    *reinterpret_cast<uint4 *>(tile + tc::tileOffset(row, 8 * (18 - C0), tileC)) = a;
+  }
+  if (19 >= C0 && 19 < C1) {
+    uint4 b = make_uint4(tc::packBf16(x[8], x[9]), tc::packBf16(x[10], x[11]),
+                         tc::packBf16(oneFeature ? 1.f : 0.f, 0.f), 0u);
+    *reinterpret_cast<uint4 *>(tile + tc::tileOffset(row, 8 * (19 - C0), tileC)) = b;
+  }
+}
+
+__device__ __forceinline__ void encodeRow(const float *x, uint8_t *tile, int row, bool oneFeature) {
+  encodeChunks<0, 20>(x, tile, row, kK1, oneFeature);
+}
+
+// Epilogue of a hidden layer for one row: 64 accumulator columns from TMEM (this thread's lane),
+// + bias, ReLU, BF16 into row `row` of `out` (a tile with `outC` columns, starting at column
+// `outCol`). Returns the ReLU mask (bit j: unit j active).
+__device__ __forceinline__ unsigned long long hiddenEpilogue(uint32_t taddr, const float *bias, uint8_t *out,
+                                                             int row, int outC, int outCol) {
+  unsigned long long mask = 0ull;
+#pragma unroll
+  for (int h = 0; h < 4; h++) {
+    float a[16];
+    tc::ld16(taddr + 16 * h, a);
+    tc::ldWait();
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      float v = a[j] + bias[16 * h + j];
+      v = v > 0.f ? v : 0.f;
+      if (v > 0.f) mask |= 1ull << (16 * h + j);
+      a[j] = v;
+    }
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      uint4 v = make_uint4(tc::packBf16(a[8 * q], a[8 * q + 1]), tc::packBf16(a[8 * q + 2], a[8 * q + 3]),
+                           tc::packBf16(a[8 * q + 4], a[8 * q + 5]), tc::packBf16(a[8 * q + 6], a[8 * q + 7]));
+      *reinterpret_cast<uint4 *>(out + tc::tileOffset(row, outCol + 16 * h + 8 * q, outC)) = v;
+    }
+  }
+  return mask;
+}
+
+// MMA issue helper (one thread). Descriptors follow the tile layout of sglc_tc.cuh.
+// D[128 x N] (+)= A[128 x K] * B[K x N]: A = K columns of a tile with aC columns starting at column
+// aCol (K-major); B = a weight tile [N][bC] (K-major) from column bCol.
+__device__ __forceinline__ void issueKMajor(uint32_t dTmem, uint32_t aBase, int aC, int aCol, uint32_t bBase, int bC,
+                                            int bCol, int N, int K, bool accumulate) {
+  const uint32_t idesc = tc::instrDesc(128, N, false, false);
+#pragma unroll 1
+  for (int k = 0; k < K; k += 16) {
+    uint64_t ad = tc::smemDesc(aBase + tc::tileOffset(0, aCol + k, aC), 128, (uint32_t) aC / 8 * 128);
+    uint64_t bd = tc::smemDesc(bBase + tc::tileOffset(0, bCol + k, bC), 128, (uint32_t) bC / 8 * 128);
+    tc::mma(dTmem, ad, bd, idesc, accumulate || k > 0);
+  }
+}
+
+}  // namespace nn
+}  // namespace sglc

@@ -376,6 +376,59 @@ __device__ __forceinline__ uint32_t depthOps(const DrawParams &p, const Cover &c
   return (i0 ? 1u : 0u) | (i1 ? 2u : 0u) | (i2 ? 4u : 0u) | (i3 ? 8u : 0u);
 }
 
+// Pass 1 of a batch of up to 32 tile primitives (lane = primitive): a conservative edge-function
+// test of each triangle against the sample box of every pixel of the warp's 8x4 rectangle. Returns
+// this lane's pixel's candidate mask (bit = batch index); `prim` = this lane's primitive id.
+__device__ __forceinline__ unsigned pass1Candidates(const DrawParams &p, int base, int end, int lane, int rx0, int ry0,
+                                                    float lo, float hi, float vpExtent, int &prim) {
+  int i = base + lane;
+  prim = -1;
+  bool hit = false;
+  int4 r = make_int4(0, -1, 0, -1);
+  float ea[3] = {0.f, 0.f, 0.f}, eb[3] = {0.f, 0.f, 0.f}, ek[3] = {0.f, 0.f, 0.f}, et[3] = {0.f, 0.f, 0.f};
+  bool anyPix = false;
+  if (i < end) {
+    prim = __ldg(p.valA + i);
+    const TriSetup *tp = p.tri + prim;
+    r = __ldg(reinterpret_cast<const int4 *>(&tp->rx0));
+    hit = !(r.y < rx0 || r.x > rx0 + 7 || r.w < ry0 || r.z > ry0 + 3);
+    if (hit) {
+      float4 q0 = __ldg(reinterpret_cast<const float4 *>(tp));        // v0x v0y v2x v1x
+      float4 q1 = __ldg(reinterpret_cast<const float4 *>(tp) + 1);    // v0x v2y v1y v0y
+      float X[3] = {q0.x, q0.w, q0.z}, Y[3] = {q0.y, q1.z, q1.y};     // v0, v1, v2
+      float area = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
+      float mag = fabsf(X[1] - X[0]) + fabsf(Y[1] - Y[0]) + fabsf(X[2] - X[0]) + fabsf(Y[2] - Y[0]);
+      anyPix = !(fabsf(area) > 1e-3f * mag * mag + 1e-6f);   // near-degenerate: skip the edge pre-test
+      float o = area > 0.f ? 1.f : -1.f;
+#pragma unroll
+      for (int e = 0; e < 3; e++) {
+        // E(x, y) = a x + b y + c >= 0 inside; its maximum over a pixel's sample box is at the
+        // corner picked by the signs of a, b: E_max(px, py) = a px + b py + k
+        float sx = X[e], sy = Y[e], dx = X[(e + 1) % 3] - sx, dy = Y[(e + 1) % 3] - sy;
+        float a = -o * dy, b = o * dx, c = o * (dy * sx - dx * sy);
+        ea[e] = a;
+        eb[e] = b;
+        ek[e] = a * (a > 0.f ? hi : lo) + b * (b > 0.f ? hi : lo) + c;
+        et[e] = 1e-5f * ((fabsf(a) + fabsf(b)) * (vpExtent + fabsf(sx) + fabsf(sy)) + fabsf(c) + 1.f);
+      }
+    }
+  }
+  unsigned cand = 0;   // this lane's pixel: candidate triangles of the batch, bit = batch index
+#pragma unroll 4
+  for (int pp = 0; pp < 32; pp++) {
+    int cx = rx0 + (pp & 7), cy = ry0 + (pp >> 3);
+    bool c = hit && cx >= r.x && cx <= r.y && cy >= r.z && cy <= r.w;
+    if (c && !anyPix) {
+      float fx = (float) cx, fy = (float) cy;
+      c = (ea[0] * fx + eb[0] * fy + ek[0] >= -et[0]) && (ea[1] * fx + eb[1] * fy + ek[1] >= -et[1]) &&
+          (ea[2] * fx + eb[2] * fy + ek[2] >= -et[2]);
+    }
+    unsigned mm = __ballot_sync(0xffffffffu, c);
+    if (lane == pp) cand = mm;
+  }
+  return cand;
+}
+
 template<int SH, int S, bool HAS_COLOR, bool HAS_DEPTH>
 __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawParams p) {
   __shared__ FragQueue queues[HAS_COLOR ? 8 : 1];
@@ -418,52 +471,8 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
   const float lo = S == 4 ? 0.125f : 0.5f, hi = S == 4 ? 0.875f : 0.5f;
   const float vpExtent = fabsf(p.vp.w) + fabsf(p.vp.h) + 2.f * (float) (rx0 + ry0) + 64.f;
   for (int base = start; base < end; base += 32) {
-    // ---- pass 1 (lane = triangle of this batch): which pixels of the warp rectangle may it cover?
-    int i = base + lane;
-    int prim = -1;
-    bool hit = false;
-    int4 r = make_int4(0, -1, 0, -1);
-    float ea[3] = {0.f, 0.f, 0.f}, eb[3] = {0.f, 0.f, 0.f}, ek[3] = {0.f, 0.f, 0.f}, et[3] = {0.f, 0.f, 0.f};
-    bool anyPix = false;
-    if (i < end) {
-      prim = __ldg(p.valA + i);
-      const TriSetup *tp = p.tri + prim;
-      r = __ldg(reinterpret_cast<const int4 *>(&tp->rx0));
-      hit = !(r.y < rx0 || r.x > rx0 + 7 || r.w < ry0 || r.z > ry0 + 3);
-      if (hit) {
-        float4 q0 = __ldg(reinterpret_cast<const float4 *>(tp));        // v0x v0y v2x v1x
-        float4 q1 = __ldg(reinterpret_cast<const float4 *>(tp) + 1);    // v0x v2y v1y v0y
-        float X[3] = {q0.x, q0.w, q0.z}, Y[3] = {q0.y, q1.z, q1.y};     // v0, v1, v2
-        float area = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
-        float mag = fabsf(X[1] - X[0]) + fabsf(Y[1] - Y[0]) + fabsf(X[2] - X[0]) + fabsf(Y[2] - Y[0]);
-        anyPix = !(fabsf(area) > 1e-3f * mag * mag + 1e-6f);   // near-degenerate: skip the edge pre-test
-        float o = area > 0.f ? 1.f : -1.f;
-#pragma unroll
-        for (int e = 0; e < 3; e++) {
-          // E(x, y) = a x + b y + c >= 0 inside; its maximum over a pixel's sample box is at the
-          // corner picked by the signs of a, b: E_max(px, py) = a px + b py + k
-          float sx = X[e], sy = Y[e], dx = X[(e + 1) % 3] - sx, dy = Y[(e + 1) % 3] - sy;
-          float a = -o * dy, b = o * dx, c = o * (dy * sx - dx * sy);
-          ea[e] = a;
-          eb[e] = b;
-          ek[e] = a * (a > 0.f ? hi : lo) + b * (b > 0.f ? hi : lo) + c;
-          et[e] = 1e-5f * ((fabsf(a) + fabsf(b)) * (vpExtent + fabsf(sx) + fabsf(sy)) + fabsf(c) + 1.f);
-        }
-      }
-    }
-    unsigned cand = 0;   // this lane's pixel: candidate triangles of the batch, bit = batch index
-#pragma unroll 4
-    for (int pp = 0; pp < 32; pp++) {
-      int cx = rx0 + (pp & 7), cy = ry0 + (pp >> 3);
-      bool c = hit && cx >= r.x && cx <= r.y && cy >= r.z && cy <= r.w;
-      if (c && !anyPix) {
-        float fx = (float) cx, fy = (float) cy;
-        c = (ea[0] * fx + eb[0] * fy + ek[0] >= -et[0]) && (ea[1] * fx + eb[1] * fy + ek[1] >= -et[1]) &&
-            (ea[2] * fx + eb[2] * fy + ek[2] >= -et[2]);
-      }
-      unsigned mm = __ballot_sync(0xffffffffu, c);
-      if (lane == pp) cand = mm;
-    }
+    int prim;
+    unsigned cand = pass1Candidates(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim);
     if (!(inC || inD)) cand = 0;
     // ---- pass 2 (lane = pixel): exact coverage and depth for each candidate, in primitive order
     int nIter = __reduce_max_sync(0xffffffffu, __popc(cand));

@@ -6,6 +6,7 @@ namespace sglc {
 
 void launchRasterBlinn(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 void launchRasterPbr(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
+void launchRasterNeural(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
   int grid = p.tilesX * p.tilesY;
@@ -21,6 +22,7 @@ void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_
     case SH_BLINN:
     case SH_BLINN_DIR: launchRasterBlinn(p, hasColor, hasDepth, st); break;
     case SH_PBR: launchRasterPbr(p, hasColor, hasDepth, st); break;
+    case SH_PBR_NEURAL: launchRasterNeural(p, hasColor, hasDepth, st); break;
   }
 }
 

@@ -182,25 +182,57 @@ __device__ inline float4 fsBlinnPhong(const DrawParams &p, const FragIn &f) {
   return make_float4(c.x, c.y, c.z, base.w);
 }
 
-__device__ inline float4 fsPbr(const DrawParams &p, const FragIn &f) {
+// Training record of the neural IBL shader (sglc_nn.cuh): the network's 12 inputs and the square
+// root of the IBL term it learns, appended while the host has capture enabled.
+static __device__ __noinline__ void captureRecord(const DrawParams &p, f3 N, f3 V, float roughness, float metallic,
+                                           float4 albedo, float NdotV, f3 ibl) {
+  unsigned long long slot = atomicAdd(p.capCount, 1ull);
+  if (slot % (unsigned) p.capStride) return;
+  slot /= (unsigned) p.capStride;
+  if (slot >= (unsigned long long) p.capCap) return;
+  float4 *r = reinterpret_cast<float4 *>(p.capRecords + slot * 16);
+  r[0] = make_float4(N.x, N.y, N.z, V.x);
+  r[1] = make_float4(V.y, V.z, roughness, metallic);
+  r[2] = make_float4(albedo.x, albedo.y, albedo.z, NdotV);
+  r[3] = make_float4(sqrtf(fmaxf(ibl.x, 0.f)), sqrtf(fmaxf(ibl.y, 0.f)), sqrtf(fmaxf(ibl.z, 0.f)), 0.f);
+}
+
+// The PBR fragment shader's surface terms (PbrSoft.h:229-294): material texels, the normal-mapped
+// normal, the view direction, the direct point light and the emissive texel.
+struct PbrSurface {
+  float4 arg;          // albedo texel (or base colour)
+  f3 albedo;           // linear albedo
+  float metallic, roughness, ao;
+  f3 N, V, F0, Lo;
+  f3 emissive;
+};
+
+__device__ __forceinline__ PbrSurface pbrSurface(const DrawParams &p, const FragIn &f) {
   const float PI = 3.14159265359f;
   const float rangeInv = 1.0f / 5.f;
+  PbrSurface s;
   float4 arg = p.def[0] ? tex2D(p, 0, f.v[0], f.v[1], f) : uV4(p, 352);
+  s.arg = arg;
   f3 albedo = mk3(powf(arg.x, 2.2f), powf(arg.y, 2.2f), powf(arg.z, 2.2f));
+  s.albedo = albedo;
   float metallic = 0.0f, roughness = 1.0f;
   if (p.def[4]) {
     float4 mr = tex2D(p, 4, f.v[0], f.v[1], f);
     metallic = mr.z;
     roughness = mr.y;
   }
+  s.metallic = metallic;
+  s.roughness = roughness;
   float ao = 1.f;
   if (p.def[3]) ao = tex2D(p, 3, f.v[0], f.v[1], f).x;
+  s.ao = ao;
   f3 N = normalFromMap(p, f, 20, 24);
   f3 V = normalize3(f.v.v3(12));
-  f3 mV = -V;
-  f3 R = mV - N * dot3(N, mV) * 2.0f;
+  s.N = N;
+  s.V = V;
   f3 F0 = mk3(0.04f, 0.04f, 0.04f);
   F0 = F0 * (1.0f - metallic) + albedo * metallic;
+  s.F0 = F0;
   f3 Lo = mk3(0, 0, 0);
   if (uI32(p, 320)) {
     f3 ldir = f.v.v3(16);
@@ -234,8 +266,31 @@ __device__ inline float4 fsPbr(const DrawParams &p, const FragIn &f) {
     float NdL = gmax(dot3(N, L), 0.0f);
     Lo = Lo + (kD * albedo / PI + specular) * radiance * NdL;
   }
+  s.Lo = Lo;
+  s.emissive = mk3(0.f, 0.f, 0.f);
+  if (p.def[2]) {
+    float4 e = tex2D(p, 2, f.v[0], f.v[1], f);
+    s.emissive = mk3(e.x, e.y, e.z);
+  }
+  return s;
+}
+
+// gamma correction and emissive (PbrSoft.h:311-321)
+__device__ __forceinline__ float4 pbrFinish(const DrawParams &p, f3 ambient, f3 Lo, f3 emissive, float alpha) {
+  f3 color = ambient + Lo;
+  color = pow3(color, 1.0f / 2.2f);
+  if (p.def[2]) color = color + emissive;
+  return make_float4(color.x, color.y, color.z, alpha);
+}
+
+__device__ inline float4 fsPbr(const DrawParams &p, const FragIn &f) {
+  PbrSurface s = pbrSurface(p, f);
+  const f3 N = s.N, V = s.V, F0 = s.F0, albedo = s.albedo;
+  const float metallic = s.metallic, roughness = s.roughness, ao = s.ao;
   f3 ambient;
   if (uI32(p, 324)) {
+    f3 mV = -V;
+    f3 R = mV - N * dot3(N, mV) * 2.0f;
     float NdotV = gmax(dot3(N, V), 0.0f);
     float p5 = powf(gclamp(1.0f - NdotV, 0.0f, 1.0f), 5.0f);
     float omr = 1.0f - roughness;
@@ -254,17 +309,13 @@ __device__ inline float4 fsPbr(const DrawParams &p, const FragIn &f) {
     ABy *= gmax(0.f, gmin(1.f, 50.0f * F.y));
     f3 env = F * ABx + ABy;
     f3 specular = mk3(pre.x, pre.y, pre.z) * env;
-    ambient = (kD * diffuse + specular) * ao;
+    f3 ibl = kD * diffuse + specular;
+    if (p.capRecords) captureRecord(p, N, V, roughness, metallic, s.arg, NdotV, ibl);
+    ambient = ibl * ao;
   } else {
     ambient = ld3(p.u + 256) * albedo * ao;
   }
-  f3 color = ambient + Lo;
-  color = pow3(color, 1.0f / 2.2f);
-  if (p.def[2]) {
-    float4 e = tex2D(p, 2, f.v[0], f.v[1], f);
-    color = color + mk3(e.x, e.y, e.z);
-  }
-  return make_float4(color.x, color.y, color.z, arg.w);
+  return pbrFinish(p, ambient, s.Lo, s.emissive, s.arg.w);
 }
 
 template<int SH>

@@ -18,12 +18,17 @@ def declared():
     return sorted(set(re.findall(r"SGLC_API\s+[\w\s\*]+?\b(sglc_\w+)\s*\(", text)))
 
 
-# product-only extension (no Renderer counterpart): not exported by the checkers, bound by its own test
+# product-only extensions (no Renderer counterpart): not exported by the checkers; the allocation-free
+# draw is bound by its own test, the neural shader by softglrender_gb300/neural.py
 PRODUCT_ONLY = {"sglc_draw_vertex_color_noalloc"}
 
 
+def neural_abi():
+    return [n for n in declared() if n.startswith("sglc_neural_") or n == "sglc_program_set_neural_shader"]
+
+
 def renderer_abi():
-    return [n for n in declared() if n not in PRODUCT_ONLY]
+    return [n for n in declared() if n not in PRODUCT_ONLY and n not in neural_abi()]
 
 
 def exported(path):
@@ -51,7 +56,9 @@ def test_cuda_library_exports_every_symbol():
 
 def test_python_binding_covers_every_symbol():
     from softglrender_gb300.api import ABI_FUNCTIONS
+    from softglrender_gb300.neural import NEURAL_FUNCTIONS
     assert sorted("sglc_" + n for n in ABI_FUNCTIONS) == renderer_abi()
+    assert sorted("sglc_" + n for n in NEURAL_FUNCTIONS) == sorted(neural_abi())
 
 
 def test_oracle_exports_same_abi(oracle_lib):
