@@ -34,6 +34,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-neural", action="store_true", help="skip training / timing the neural IBL shader")
     return ap.parse_args()
 
 
@@ -216,13 +217,11 @@ def main():
         inst.render()
     r.waitIdle()
 
-    # ---- device-resident throughput: K frames, L2 flushed between frames (not timed) ----------
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    barrier(pg)
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
-        for i in range(args.steps):
+    def timed_frames(steps):
+        """Per-frame device time (ms) of `steps` frames, L2 flushed (untimed) before each."""
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        for i in range(steps):
             with torch.cuda.stream(stream):
                 flush.zero_()
                 starts[i].record(stream)
@@ -231,24 +230,34 @@ def main():
                 ends[i].record(stream)
         r.waitIdle()
         torch.cuda.synchronize()
+        return [s.elapsed_time(e) for s, e in zip(starts, ends)]
+
+    def raster_ms_median(n=5):
+        r.setStatsLevel(1)
+        rast, geo, binn = [], [], []
+        for _ in range(n):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            inst.render()
+            s = r.drawStats()
+            rast.append(s["raster_ms"])
+            geo.append(s["geometry_ms"])
+            binn.append(s["binning_ms"])
+        r.setStatsLevel(0)
+        return float(np.median(rast)), float(np.median(geo)), float(np.median(binn))
+
+    # ---- device-resident throughput: K frames, L2 flushed between frames (not timed) ----------
     barrier(pg)
-    frame_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        frame_ms = timed_frames(args.steps)
+    barrier(pg)
     total_s = max_over_ranks(sum(frame_ms) / 1e3, pg, f"cuda:{local}" if pg and torch.cuda.is_available() else None)
     fps = world * args.steps / total_s
     ms_per_step = total_s / args.steps * 1e3
 
     # ---- raster-kernel roofline: CUDA events around the raster launch on the renderer's stream ----
-    r.setStatsLevel(1)
-    rast, geo, binn = [], [], []
-    for _ in range(5):
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        inst.render()
-        s = r.drawStats()
-        rast.append(s["raster_ms"])
-        geo.append(s["geometry_ms"])
-        binn.append(s["binning_ms"])
-    r.setStatsLevel(0)
+    raster_ms, geo_ms, bin_ms = raster_ms_median()
     p0 = scene.passes[0]
     W, H, Sm = p0.width, p0.height, p0.samples
     d0 = p0.draws[0]
@@ -256,9 +265,40 @@ def main():
     varying_stride = 32
     raster_bytes = (W * H * Sm * 8 + W * H * 4 + texture_bytes(scene) + st["primitives"] * 128 +
                     nv * varying_stride * 4 + st["bin_entries"] * 4)
-    raster_ms = float(np.median(rast))
     peak, peak_kind = measured_peak_hbm()
     achieved = raster_bytes / (raster_ms * 1e-3) / 1e9
+
+    # ---- neural IBL shader: trained on 2^22 captured fragments of 64 orbit views (tensor-core
+    # forward / backward / Adam), judged against the plain shader on 16 held-out views; its
+    # throughput is measured on the same frames as `value` --------------------------------------
+    neural = None
+    if not args.no_neural:
+        from softglrender_gb300 import neural as NN
+        _, net, rep = NN.train_neural_ibl(r, {}, inst=inst)
+        progs = NN.pbr_programs(inst)
+        for prog in progs:
+            net.bind(prog)
+        for _ in range(3):
+            inst.render()
+        torch.cuda.synchronize()
+        n_ms = timed_frames(args.steps)
+        n_raster, _, _ = raster_ms_median()
+        for prog in progs:   # the rest of the bench (end to end) runs the plain shader
+            NN.NeuralShader.unbind(r, prog)
+        n_fps = args.steps / (sum(n_ms) / 1e3)
+        neural = {
+            "frames_per_s": round(n_fps, 3), "mfrag_per_s": round(frags * n_fps / 1e6, 2),
+            "raster_ms": round(n_raster, 4), "speedup_vs_plain_frames": round(n_fps / (args.steps / (sum(frame_ms) / 1e3)), 3),
+            "speedup_vs_plain_raster": round(raster_ms / n_raster, 3),
+            "psnr_db_mean": round(rep.psnr_mean, 2), "psnr_db_min": round(min(rep.psnr_views), 2),
+            "max_abs_lsb": int(max(rep.maxabs_views)), "threshold_db": 40.0, "bound": bool(rep.bound),
+            "psnr_db_without_network": round(float(np.mean(rep.psnr_without)), 2),
+            "psnr_db_untrained": round(float(np.mean(rep.psnr_untrained)), 2),
+            "records": rep.records, "capture_stride": rep.capture_stride, "train_steps": rep.train_steps,
+            "train_s": round(rep.train_s, 3), "capture_s": round(rep.capture_s, 3), "final_loss": rep.final_loss,
+            "views": {"train": 64, "held_out": 16},
+        }
+        net.destroy()
 
     # ---- end to end through the public API with host buffers ----------------------------------
     pinned_v = torch.empty(d0.vertexes.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(np.float32)
@@ -302,8 +342,7 @@ def main():
         "mfrag_per_s": round(frags * fps / 1e6, 2),
         "fragments_per_frame": frags,
         "mtris_per_s": round(scene.triangles * fps / 1e6, 2),
-        "stage_ms": {"geometry": round(float(np.median(geo)), 4), "binning": round(float(np.median(binn)), 4),
-                     "raster": round(raster_ms, 4)},
+        "stage_ms": {"geometry": round(geo_ms, 4), "binning": round(bin_ms, 4), "raster": round(raster_ms, 4)},
         "e2e": {"value": round(e2e_fps, 3), "unit": "frames/s", "h2d_bytes_per_step": int(pinned_v.nbytes + len(model_bytes)),
                 "d2h_bytes_per_step": int(out.nbytes)},
         "gpu_launches": launches_per_frame * args.steps,
@@ -315,6 +354,8 @@ def main():
                      "algorithmic_bytes_per_launch": int(raster_bytes)},
         "clocks": clocks.summary(),
     }
+    if neural is not None:
+        result["neural"] = neural
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         t0 = time.perf_counter()

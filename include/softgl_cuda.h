@@ -232,6 +232,15 @@ SGLC_API sglc_status sglc_wait_idle(sglc_context *ctx);
 SGLC_API sglc_status sglc_set_enable_early_z(sglc_context *ctx, int32_t enable);
 
 /* ---- extensions (no reference counterpart) --------------------------------------------------- */
+/* Batched views: the bound vertex array, program and pipeline states drawn once per view, view v
+ * into framebuffers[v] with the uniform blocks of resources[v] (samplers are taken from
+ * resources[0] and shared). The result is identical to, for each view in order:
+ * beginRenderPass(framebuffers[v], clear) (no clear when `clear` is null); setShaderResources(
+ * resources[v]); draw(); endRenderPass(). All views' attachments must have view 0's sizes, formats
+ * and sample count. The GPU runs every view in one pipeline pass (one launch per stage over all
+ * (view, triangle) and (view, tile) work items). */
+SGLC_API sglc_status sglc_draw_views(sglc_context *ctx, const sglc_handle *framebuffers, const sglc_handle *resources,
+                                     int32_t count, const sglc_clear_states *clear);
 /* Counters of the last draw (synchronises). */
 SGLC_API sglc_status sglc_get_draw_stats(sglc_context *ctx, sglc_draw_stats *out);
 /* 0: no instrumentation; 1: per-stage device timings of each draw; 2: also count fragments. */

@@ -488,6 +488,21 @@ sglc_status sglr_end_render_pass(sglc_context *ctx) {
   return SGLC_OK;
 }
 
+// The batched draw on the reference: the views drawn one after another in their own render passes
+// (RendererSoft has no batching).
+sglc_status sglr_draw_views(sglc_context *ctx, const sglc_handle *fbs, const sglc_handle *res, int32_t count,
+                            const sglc_clear_states *clear) {
+  sglc_clear_states none{0, 0, {0.f, 0.f, 0.f, 0.f}, 1.f};
+  for (int v = 0; v < count; v++) {
+    sglc_status s = sglr_begin_render_pass(ctx, fbs[v], clear ? clear : &none);
+    if (!s) s = sglr_set_shader_resources(ctx, res[v]);
+    if (!s) s = sglr_draw(ctx);
+    if (!s) s = sglr_end_render_pass(ctx);
+    if (s) return s;
+  }
+  return SGLC_OK;
+}
+
 sglc_status sglr_wait_idle(sglc_context *ctx) {
   reinterpret_cast<Ctx *>(ctx)->renderer.waitIdle();
   return SGLC_OK;

@@ -1629,6 +1629,19 @@ sglc_status sglo_draw(sglc_context *ctx) {
   return doDraw(c);
 }
 sglc_status sglo_end_render_pass(sglc_context *) { return SGLC_OK; }
+// The batched draw is, by definition, the views drawn one after another in their own render passes.
+sglc_status sglo_draw_views(sglc_context *ctx, const sglc_handle *fbs, const sglc_handle *res, int32_t count,
+                            const sglc_clear_states *clear) {
+  sglc_clear_states none{0, 0, {0.f, 0.f, 0.f, 0.f}, 1.f};
+  for (int v = 0; v < count; v++) {
+    sglc_status s = sglo_begin_render_pass(ctx, fbs[v], clear ? clear : &none);
+    if (!s) s = sglo_set_shader_resources(ctx, res[v]);
+    if (!s) s = sglo_draw(ctx);
+    if (!s) s = sglo_end_render_pass(ctx);
+    if (s) return s;
+  }
+  return SGLC_OK;
+}
 sglc_status sglo_wait_idle(sglc_context *) { return SGLC_OK; }
 sglc_status sglo_set_enable_early_z(sglc_context *ctx, int32_t e) {
   CTX;

@@ -198,6 +198,7 @@ _SIGS = {
     "get_draw_stats": [C.c_void_p, C.POINTER(_DrawStats)],
     "get_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
     "set_stats_level": [C.c_void_p, C.c_int32],
+    "draw_views": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32, C.c_void_p],
     "set_tile_size": [C.c_void_p, C.c_int32],
 }
 
@@ -472,6 +473,20 @@ class Renderer:
 
     def endRenderPass(self) -> None:
         self._call("end_render_pass")
+
+    def drawViews(self, framebuffers: Sequence[FrameBuffer], resources: Sequence[ShaderResources],
+                  clear: Optional[ClearStates] = None) -> None:
+        """Batched views (extension): the bound vertex array / program / states drawn into each
+        framebuffer with the matching resources' uniform blocks; equal to one render pass per view."""
+        n = len(framebuffers)
+        assert len(resources) == n
+        fbs = (C.c_int32 * n)(*[f.handle for f in framebuffers])
+        res = (C.c_int32 * n)(*[r.handle for r in resources])
+        cs = None
+        if clear is not None:
+            cs = _ClearStates(int(clear.depthFlag), int(clear.colorFlag), (C.c_float * 4)(*clear.clearColor),
+                              clear.clearDepth)
+        self._call("draw_views", fbs, res, n, C.byref(cs) if cs is not None else None)
 
     def waitIdle(self) -> None:
         self._call("wait_idle")

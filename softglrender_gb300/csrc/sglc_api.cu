@@ -169,7 +169,7 @@ struct Ctx {
   // scratch
   DevBuf vClip, vFrag, vMask, vVary, vAttrExtra, prims, clipExtra, clipAppendOff, clipPoly, clipPolyTri, counters;
   DevBuf tri, tileCount, pairOff, keyA, keyB, valA, valB, tileStart, tileEnd, tileOrder, scanScratch, sortHist,
-      sortHistScan, staging;
+      sortHistScan, staging, batchU, batchTargets;
   // capacity hints that survive between draws
   int extraVertHint = 0, polyHint = 0, appendHint = 0;
   // neural IBL shader: training-record capture target
@@ -329,8 +329,16 @@ TexObj *attachmentTex(Ctx *c, int h) {
   return o ? &o->tex : nullptr;
 }
 
-sglc_status drawImpl(Ctx *c) {
-  Object *fo = c->get(c->fb, K_FB), *vo = c->get(c->vao, K_VAO), *po = c->get(c->prog, K_PROG);
+// A batched draw (sglc_draw_views): per-view framebuffers and uniform bytes, one clear for all.
+struct BatchViews {
+  int count = 0;
+  const sglc_handle *fbs = nullptr;
+  std::vector<uint8_t> uniforms;   // count x kUniformBytes
+  const sglc_clear_states *clear = nullptr;
+};
+
+sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
+  Object *fo = c->get(bv ? bv->fbs[0] : c->fb, K_FB), *vo = c->get(c->vao, K_VAO), *po = c->get(c->prog, K_PROG);
   if (!fo || !vo || !po) return SGLC_OK;   // RendererSoft::draw is a silent no-op (RendererSoft.cpp:137-139)
   Object *so = c->get(c->states, K_STATES);
   if (!so) return c->fail(SGLC_ERR_INVALID_VALUE, "draw: no pipeline states bound");
@@ -384,6 +392,7 @@ sglc_status drawImpl(Ctx *c) {
     p.nnImage = neuralImage(prog.neural);
   }
   if (p.shading == SH_PBR && c->capRecords) {
+    p.shading = SH_PBR_CAPTURE;
     p.capRecords = c->capRecords;
     p.capCount = c->capCount;
     p.capCap = c->capCap;
@@ -445,7 +454,42 @@ sglc_status drawImpl(Ctx *c) {
     p.dms = dt->desc.multi_sample;
   }
   p.samples = ct ? (ct->desc.multi_sample ? 4 : 1) : (dt->desc.multi_sample ? 4 : 1);
-  if (c->clear.active && c->clear.fb == c->fb) {
+  std::vector<ViewTarget> targets;
+  if (bv) {
+    // every view's attachments must match view 0's (size, format, samples, presence)
+    for (int v = 0; v < bv->count; v++) {
+      Object *o = c->get(bv->fbs[v], K_FB);
+      if (!o) return c->fail(SGLC_ERR_INVALID_HANDLE, "draw_views: invalid framebuffer");
+      FbObj &f = o->fb;
+      TexObj *vc = f.colorReady ? attachmentTex(c, f.colorTex) : nullptr;
+      TexObj *vd = f.depthReady ? attachmentTex(c, f.depthTex) : nullptr;
+      if (vc && (!vc->allocated || f.colorLevel >= vc->levels || vc->desc.format != SGLC_FORMAT_RGBA8)) vc = nullptr;
+      if (vd && (!vd->allocated || vd->desc.format != SGLC_FORMAT_FLOAT32)) vd = nullptr;
+      if ((vc != nullptr) != (ct != nullptr) || (vd != nullptr) != (dt != nullptr) ||
+          (vc && (vc->w[f.colorLevel] != p.cw || vc->h[f.colorLevel] != p.ch || vc->desc.multi_sample != p.cms)) ||
+          (vd && (vd->w[0] != p.dw || vd->h[0] != p.dh || vd->desc.multi_sample != p.dms)))
+        return c->fail(SGLC_ERR_INVALID_VALUE, "draw_views: every view needs attachments like view 0's");
+      ViewTarget t{};
+      if (vc) {
+        t.color = vc->dev + (size_t) f.colorLayer * vc->layerStride + vc->offset[f.colorLevel];
+        t.resolved = vc->resolved;
+        if (vc->desc.multi_sample) vc->resolvedValid = true;
+      }
+      if (vd) t.depth = reinterpret_cast<float *>(vd->dev);
+      targets.push_back(t);
+    }
+    sglc_status st = flushClear(c);
+    if (st) return st;
+    const sglc_clear_states *cs = bv->clear;
+    if (cs && (cs->color_flag || cs->depth_flag)) {
+      p.pendingClear = 1;
+      p.clearColorFlag = cs->color_flag && ct;
+      p.clearDepthFlag = cs->depth_flag && dt;
+      p.clearColor = u8c(cs->clear_color[0] * 255) | (u8c(cs->clear_color[1] * 255) << 8) |
+                     (u8c(cs->clear_color[2] * 255) << 16) | (u8c(cs->clear_color[3] * 255) << 24);
+      p.clearDepth = cs->clear_depth;
+    }
+  } else if (c->clear.active && c->clear.fb == c->fb) {
     p.pendingClear = 1;
     p.clearColorFlag = c->clear.colorFlag && ct;
     p.clearDepthFlag = c->clear.depthFlag && dt;
@@ -466,6 +510,27 @@ sglc_status drawImpl(Ctx *c) {
   p.tilesX = (fw + p.tile - 1) / p.tile;
   p.tilesY = (fh + p.tile - 1) / p.tile;
   int numTiles = p.tilesX * p.tilesY;
+  p.views = 1;
+  p.nvView = p.nv;
+  p.ntriView = p.ntri;
+  p.tilesPerView = numTiles;
+  if (bv) {
+    if ((long long) p.ntri * bv->count * 3 > (1ll << 30) || (long long) p.nv * bv->count > (1ll << 30) ||
+        (long long) numTiles * bv->count > (1ll << 30))
+      return c->fail(SGLC_ERR_INVALID_VALUE, "draw_views: batch too large");
+    p.views = bv->count;
+    p.nv *= bv->count;
+    p.ntri *= bv->count;
+    numTiles *= bv->count;
+    CK(c->batchU.ensure(bv->uniforms.size()));
+    CK(c->batchTargets.ensure(sizeof(ViewTarget) * targets.size()));
+    CK(cudaMemcpyAsync(c->batchU.ptr, bv->uniforms.data(), bv->uniforms.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->batchTargets.ptr, targets.data(), sizeof(ViewTarget) * targets.size(), cudaMemcpyHostToDevice,
+                       c->stream));
+    p.viewU = c->batchU.as<uint8_t>();
+    p.viewTarget = c->batchTargets.as<ViewTarget>();
+    if (p.shading == SH_PBR_CAPTURE) p.shading = SH_PBR;   // no training capture in batched draws
+  }
 
   for (int attempt = 0; attempt < 4; attempt++) {
     int extraVerts = std::max(std::max(4096, p.ntri / 2), c->extraVertHint);
@@ -1089,6 +1154,50 @@ sglc_status sglc_set_pipeline_states(sglc_context *ctx, sglc_handle st) {
 sglc_status sglc_draw(sglc_context *ctx) {
   CTX;
   return drawImpl(c);
+}
+
+sglc_status sglc_draw_views(sglc_context *ctx, const sglc_handle *framebuffers, const sglc_handle *resources,
+                            int32_t count, const sglc_clear_states *clear) {
+  CTX;
+  if (count <= 0 || !framebuffers || !resources)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "draw_views: need at least one view");
+  Object *po = c->get(c->prog, K_PROG);
+  if (!po || !po->prog.shader) return c->fail(SGLC_ERR_INVALID_VALUE, "draw_views: no shader program bound");
+  ProgObj &P = po->prog;
+  BatchViews bv;
+  bv.count = count;
+  bv.fbs = framebuffers;
+  bv.clear = clear;
+  bv.uniforms.resize((size_t) count * kUniformBytes);
+  for (int v = 0; v < count; v++) {
+    Object *fo = c->get(framebuffers[v], K_FB);
+    Object *r = c->get(resources[v], K_RES);
+    if (!fo || !r) return c->fail(SGLC_ERR_INVALID_HANDLE, "draw_views: invalid framebuffer or resources handle");
+    for (int h : {fo->fb.colorReady ? fo->fb.colorTex : 0, fo->fb.depthReady ? fo->fb.depthTex : 0}) {
+      Object *t = c->get(h, K_TEX);
+      if (t && !t->tex.allocated) {
+        sglc_status st = allocTexture(c, t->tex);
+        if (st) return st;
+      }
+    }
+    // this view's uniforms: the program's current uniforms with the view's blocks applied, as
+    // ShaderProgram::bindResources does for a single draw (ShaderProgram.h:27-54)
+    uint8_t *dst = bv.uniforms.data() + (size_t) v * kUniformBytes;
+    memcpy(dst, P.uniforms, kUniformBytes);
+    for (auto &kv : r->resBlocks) {
+      Object *u = c->get(kv.second, K_UB);
+      if (!u) continue;
+      for (auto &d : P.shader->uniforms) {
+        if (d.samplerSlot >= 0 || u->ubName != d.name) continue;
+        size_t n = std::min(u->ubData.size(), (size_t) (P.shader->uniformSize - d.offset));
+        memcpy(dst + d.offset, u->ubData.data(), n);
+      }
+    }
+  }
+  // samplers are shared by all views: view 0's resources bind them
+  sglc_status st = sglc_set_shader_resources(ctx, resources[0]);
+  if (st) return st;
+  return drawImpl(c, &bv);
 }
 
 sglc_status sglc_end_render_pass(sglc_context *ctx) {

@@ -21,7 +21,9 @@ constexpr int kBlock = 32;           // RendererSoft::rasterBlockSize_ (Renderer
 enum { LAYOUT_LINEAR = 0, LAYOUT_TILED = 1, LAYOUT_MORTON = 2 };
 enum { FILTER_NEAREST = 0, FILTER_LINEAR, FILTER_NN, FILTER_LN, FILTER_NL, FILTER_LL };
 enum { WRAP_REPEAT = 0, WRAP_MIRRORED, WRAP_EDGE, WRAP_BORDER };
-enum { SH_BASE = 1, SH_BLINN = 2, SH_PBR = 3, SH_BLINN_DIR = 100, SH_VCOLOR = 101, SH_PBR_NEURAL = 102 };
+// SH_PBR_CAPTURE: the plain PBR shader that also appends neural-shader training records (a separate
+// instantiation, so the plain kernel carries no capture code); SH_PBR_NEURAL: the neural IBL variant
+enum { SH_BASE = 1, SH_BLINN = 2, SH_PBR = 3, SH_BLINN_DIR = 100, SH_VCOLOR = 101, SH_PBR_NEURAL = 102, SH_PBR_CAPTURE = 103 };
 
 // one texture as seen by a sampler: all layers x levels in one allocation
 struct DevTex {
@@ -63,9 +65,17 @@ struct __align__(16) TriSetup {
   int vid0, vid1, vid2;           // varying rows
   int front;
   int rx0, rx1, ry0, ry1;         // pixel rectangle the quads can touch (inclusive)
-  int pad[2];
+  int view;                       // view of a batched draw (0 for a single draw)
+  int pad;
 };
 static_assert(sizeof(TriSetup) == 128, "TriSetup is two 64-B lines");
+
+// attachments of one view of a batched draw
+struct ViewTarget {
+  uint32_t *color;
+  uint32_t *resolved;
+  float *depth;
+};
 
 // everything a draw's kernels read; passed by value as a __grid_constant__ parameter
 struct DrawParams {
@@ -139,7 +149,21 @@ struct DrawParams {
   long long capCap;
   int capStride;
   const uint8_t *nnImage;
+  // batched views (sglc_draw_views): one pipeline pass over `views` copies of the draw that differ
+  // only in uniforms and attachments. nv / ntri above count all views' vertices / triangles;
+  // view v owns vertices [v * nvView, (v + 1) * nvView), triangles [v * ntriView, ...) and raster
+  // tiles [v * tilesPerView, ...). A single draw is views = 1 with null per-view arrays.
+  int views;
+  int nvView, ntriView;
+  int tilesPerView;
+  const uint8_t *viewU;            // views x kUniformBytes, or null: DrawParams::u
+  const ViewTarget *viewTarget;    // per-view attachments, or null: color / resolved / depth above
 };
+
+// uniforms of view v
+__device__ __forceinline__ const uint8_t *viewUniforms(const DrawParams &p, int view) {
+  return p.viewU ? p.viewU + (size_t) view * kUniformBytes : p.u;
+}
 
 // ------------------------------------------------------------------------------------------------
 // exact helpers

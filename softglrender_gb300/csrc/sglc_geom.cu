@@ -53,9 +53,10 @@ template<int SH>
 __global__ void __launch_bounds__(256) k_vertex(const __grid_constant__ DrawParams p) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.nv) return;
-  const float *a = p.attr + (size_t) i * p.strideF;
+  const int view = p.views > 1 ? i / p.nvView : 0;
+  const float *a = p.attr + (size_t) (i - view * p.nvView) * p.strideF;
   float *v = p.vVary + (size_t) i * p.varyStride;
-  float4 c = runVS<SH>(p, a, v);
+  float4 c = runVS<SH>(p, viewUniforms(p, view), a, v);
   p.vClip[i] = c;
   p.vMask[i] = (uint8_t) clipMaskOf(c);
   p.vFrag[i] = toScreen(p, c);
@@ -65,11 +66,11 @@ __global__ void __launch_bounds__(256) k_vertex(const __grid_constant__ DrawPara
 // assembly + clipping
 // ------------------------------------------------------------------------------------------------
 __device__ __forceinline__ const float *attrOf(const DrawParams &p, int idx) {
-  return idx < p.nv ? p.attr + (size_t) idx * p.strideF : p.vAttrExtra + (size_t) (idx - p.nv) * p.strideF;
+  return idx < p.nv ? p.attr + (size_t) (idx % p.nvView) * p.strideF : p.vAttrExtra + (size_t) (idx - p.nv) * p.strideF;
 }
 
 template<int SH>
-__device__ int newClipVertex(const DrawParams &p, int i0, int i1, float t) {
+__device__ int newClipVertex(const DrawParams &p, int view, int i0, int i1, float t) {
   int k = atomicAdd(&p.counters[CNT_NEWVERT], 1);
   int idx = p.nv + k;
   if (idx >= p.vCap) {
@@ -80,7 +81,7 @@ __device__ int newClipVertex(const DrawParams &p, int i0, int i1, float t) {
   float *dst = p.vAttrExtra + (size_t) k * p.strideF;
   for (int j = 0; j < p.strideF; j++) dst[j] = A0[j] * (1.f - t) + A1[j] * t;   // glm::mix
   float *v = p.vVary + (size_t) idx * p.varyStride;
-  float4 c = runVS<SH>(p, dst, v);
+  float4 c = runVS<SH>(p, viewUniforms(p, view), dst, v);
   p.vClip[idx] = c;
   p.vMask[idx] = (uint8_t) clipMaskOf(c);
   p.vFrag[idx] = toScreen(p, c);
@@ -91,16 +92,23 @@ template<int SH>
 __global__ void __launch_bounds__(128) k_clip(const __grid_constant__ DrawParams p) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.ntri) return;
-  int i0 = p.indices[3 * t], i1 = p.indices[3 * t + 1], i2 = p.indices[3 * t + 2];
+  const int view = p.views > 1 ? t / p.ntriView : 0;
+  const int lt = t - view * p.ntriView;
+  const int viewBits = view << 8;   // primitive flags: bit 0 discard, bits 8+ view
+  int i0 = p.indices[3 * lt], i1 = p.indices[3 * lt + 1], i2 = p.indices[3 * lt + 2];
   p.clipExtra[t] = 0;
-  if ((unsigned) i0 >= (unsigned) p.nv || (unsigned) i1 >= (unsigned) p.nv || (unsigned) i2 >= (unsigned) p.nv) {
+  if ((unsigned) i0 >= (unsigned) p.nvView || (unsigned) i1 >= (unsigned) p.nvView ||
+      (unsigned) i2 >= (unsigned) p.nvView) {
     atomicOr(&p.counters[CNT_FLAGS], OVF_BADINDEX);
     p.prims[t] = make_int4(0, 0, 0, 1);
     return;
   }
+  i0 += view * p.nvView;
+  i1 += view * p.nvView;
+  i2 += view * p.nvView;
   int mask = p.vMask[i0] | p.vMask[i1] | p.vMask[i2];
   if (mask == 0) {
-    p.prims[t] = make_int4(i0, i1, i2, 0);
+    p.prims[t] = make_int4(i0, i1, i2, viewBits);
     return;
   }
   // Sutherland-Hodgman over the flagged planes (RendererSoft.cpp:489-559)
@@ -135,7 +143,7 @@ __global__ void __launch_bounds__(128) k_clip(const __grid_constant__ DrawParams
       if (dPre >= 0) out[nout++] = pre;
       if (signbit(dPre) != signbit(d)) {
         float tt = d < 0 ? dPre / (dPre - d) : -dPre / (d - dPre);
-        int nvid = newClipVertex<SH>(p, pre, cur, tt);
+        int nvid = newClipVertex<SH>(p, view, pre, cur, tt);
         if (nvid < 0) {
           p.prims[t] = make_int4(0, 0, 0, 1);
           return;
@@ -157,7 +165,7 @@ __global__ void __launch_bounds__(128) k_clip(const __grid_constant__ DrawParams
     p.prims[t] = make_int4(0, 0, 0, 1);
     return;
   }
-  p.prims[t] = make_int4(in[0], in[1], in[2], 0);
+  p.prims[t] = make_int4(in[0], in[1], in[2], viewBits);
   if (nin > 3) {
     int slot = atomicAdd(&p.counters[CNT_POLY], 1);
     if (slot >= p.clipPolyCap) {
@@ -188,13 +196,14 @@ __global__ void k_clip_append(const __grid_constant__ DrawParams p) {
   int ids[11] = {a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
   int nin = a.x;
   int base = p.ntri + p.clipAppendOff[t];
+  const int viewBits = (p.views > 1 ? t / p.ntriView : 0) << 8;
   for (int k = 3; k < nin; k++) {
     int dst = base + k - 3;
     if (dst >= p.primCap) {
       atomicOr(&p.counters[CNT_FLAGS], OVF_PRIMS);
       return;
     }
-    p.prims[dst] = make_int4(ids[0], ids[k - 1], ids[k], 0);
+    p.prims[dst] = make_int4(ids[0], ids[k - 1], ids[k], viewBits);
   }
 }
 
@@ -245,6 +254,7 @@ __global__ void __launch_bounds__(256) k_setup(const __grid_constant__ DrawParam
       T.bcx = bcx; T.bcy = bcy;
       T.vid0 = pr.x; T.vid1 = pr.y; T.vid2 = pr.z;
       T.front = front;
+      T.view = pr.w >> 8;
       if (bcx > 0 && bcy > 0) {
         int bsx0 = (int) (minX + 0.f), bsy0 = (int) (minY + 0.f);
         int bsxL = (int) (minX + (float) ((bcx - 1) * kBlock)), bsyL = (int) (minY + (float) ((bcy - 1) * kBlock));
@@ -270,6 +280,7 @@ __global__ void __launch_bounds__(256) k_bin_emit(const __grid_constant__ DrawPa
   if (i >= np || p.tileCount[i] == 0) return;
   const TriSetup &T = p.tri[i];
   int off = p.pairOff[i];
+  const uint32_t viewBase = (uint32_t) T.view * (uint32_t) p.tilesPerView;
   int tx0 = T.rx0 / p.tile, tx1 = T.rx1 / p.tile, ty0 = T.ry0 / p.tile, ty1 = T.ry1 / p.tile;
   for (int ty = ty0; ty <= ty1; ty++)
     for (int tx = tx0; tx <= tx1; tx++) {
@@ -277,7 +288,7 @@ __global__ void __launch_bounds__(256) k_bin_emit(const __grid_constant__ DrawPa
         atomicOr(&p.counters[CNT_FLAGS], OVF_PAIRS);
         return;
       }
-      p.keyA[off] = (uint32_t) (ty * p.tilesX + tx);
+      p.keyA[off] = viewBase + (uint32_t) (ty * p.tilesX + tx);
       p.valA[off] = i;
       off++;
     }
@@ -536,6 +547,7 @@ void launchVertexAndClip(const DrawParams &p, cudaStream_t st) {
     case SH_BLINN: launchGeometry<SH_BLINN>(p, st); break;
     case SH_BLINN_DIR: launchGeometry<SH_BLINN_DIR>(p, st); break;
     case SH_PBR:
+    case SH_PBR_CAPTURE:
     case SH_PBR_NEURAL: launchGeometry<SH_PBR>(p, st); break;
     case SH_VCOLOR: launchGeometry<SH_VCOLOR>(p, st); break;
   }
@@ -584,7 +596,7 @@ void launchTileRanges(const DrawParams &p, int nPairs, const int *nPtr, cudaStre
 }
 
 void launchTileOrder(const DrawParams &p, int *order, cudaStream_t st) {
-  k_tile_order<<<1, 1024, 0, st>>>(p.tileStart, p.tileEnd, p.tilesX * p.tilesY, order);
+  k_tile_order<<<1, 1024, 0, st>>>(p.tileStart, p.tileEnd, p.views * p.tilesPerView, order);
 }
 
 void launchFill32(uint32_t *dst, uint32_t value, size_t n, cudaStream_t st) {

@@ -220,6 +220,10 @@ extern "C" SGLC_API sglc_status sglc_draw_vertex_color_noalloc(const sglc_noallo
   p.tilesX = (d->width + kTile - 1) / kTile;
   p.tilesY = (d->height + kTile - 1) / kTile;
   int numTiles = p.tilesX * p.tilesY;
+  p.views = 1;
+  p.nvView = p.nv;
+  p.ntriView = p.ntri;
+  p.tilesPerView = numTiles;
   int *scan = reinterpret_cast<int *>(scratch + oScan);
   int *hist = reinterpret_cast<int *>(scratch + oHist);
   int *histScan = reinterpret_cast<int *>(scratch + oHistScan);

@@ -237,13 +237,14 @@ __device__ __forceinline__ bool depthPass(const DrawParams &p, float z, float de
 
 // Phase B for one fragment: quad derivatives of the texture coordinates, then the FS.
 template<int SH, int S>
-__device__ __noinline__ float4 shadeFragment(const DrawParams &p, int tri, int qx, int qy, int px, int py, float sb0,
-                                             float sb1, float sb2) {
+__device__ __noinline__ float4 shadeFragment(const DrawParams &p, const uint8_t *U, int tri, int qx, int qy, int px,
+                                             int py, float sb0, float sb1, float sb2) {
   Tri t = loadTri(p.tri + tri);
   const float *r0 = p.vVary + (size_t) t.vid0 * p.varyStride;
   const float *r1 = p.vVary + (size_t) t.vid1 * p.varyStride;
   const float *r2 = p.vVary + (size_t) t.vid2 * p.varyStride;
   FragIn f;
+  f.U = U;
   f.v = Vary{r0, r1, r2, sb0, sb1, sb2};
   f.dudx = f.dvdx = f.dudy = f.dvdy = 0.f;
   if (p.needDeriv) {
@@ -267,8 +268,8 @@ __device__ __noinline__ float4 shadeFragment(const DrawParams &p, int tri, int q
 }
 
 template<int SH, int S, bool HAS_DEPTH>
-__device__ __forceinline__ void flushQueue(const DrawParams &p, FragQueue &q, int &count, unsigned long long &mine,
-                                           int lane, int rx0, int ry0, bool inC, Samples4 &fb) {
+__device__ __forceinline__ void flushQueue(const DrawParams &p, const uint8_t *U, FragQueue &q, int &count,
+                                           unsigned long long &mine, int lane, int rx0, int ry0, bool inC, Samples4 &fb) {
   __syncwarp();
   // phase B: shade the queued fragments 32 at a time
   for (int base = 0; base < count; base += 32) {
@@ -278,7 +279,7 @@ __device__ __forceinline__ void flushQueue(const DrawParams &p, FragQueue &q, in
       int l = m & 31;
       int px = rx0 + (l & 7), py = ry0 + (l >> 3);
       int qx = px - ((m >> 9) & 1), qy = py - ((m >> 10) & 1);
-      q.col[e] = shadeFragment<SH, S>(p, q.tri[e], qx, qy, px, py, q.b0[e], q.b1[e], q.b2[e]);
+      q.col[e] = shadeFragment<SH, S>(p, U, q.tri[e], qx, qy, px, py, q.b0[e], q.b1[e], q.b2[e]);
     }
   }
   __syncwarp();
@@ -433,13 +434,19 @@ template<int SH, int S, bool HAS_COLOR, bool HAS_DEPTH>
 __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawParams p) {
   __shared__ FragQueue queues[HAS_COLOR ? 8 : 1];
   const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
-  const int tx = tile % p.tilesX, ty = tile / p.tilesX;
+  const int view = p.views > 1 ? tile / p.tilesPerView : 0;
+  const int vtile = tile - view * p.tilesPerView;
+  const int tx = vtile % p.tilesX, ty = vtile / p.tilesX;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
   const bool inC = HAS_COLOR && px < p.cw && py < p.ch;
   const bool inD = HAS_DEPTH && px < p.dw && py < p.dh;
   FragQueue &q = queues[HAS_COLOR ? warp : 0];
+  const uint8_t *U = viewUniforms(p, view);
+  uint32_t *colorBuf = p.viewTarget ? p.viewTarget[view].color : p.color;
+  uint32_t *resolvedBuf = p.viewTarget ? p.viewTarget[view].resolved : p.resolved;
+  float *depthBuf = p.viewTarget ? p.viewTarget[view].depth : p.depth;
   int count = 0;
   unsigned long long mine = 0ull;   // queue entries of this lane's pixel
   const unsigned lt = (1u << lane) - 1u;
@@ -449,10 +456,10 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
     if (p.pendingClear && p.clearColorFlag) {
       fb.c0 = fb.c1 = fb.c2 = fb.c3 = p.clearColor;
     } else if (S == 4) {
-      uint4 v = *reinterpret_cast<const uint4 *>(p.color + pix * 4);
+      uint4 v = *reinterpret_cast<const uint4 *>(colorBuf + pix * 4);
       fb.c0 = v.x; fb.c1 = v.y; fb.c2 = v.z; fb.c3 = v.w;
     } else {
-      fb.c0 = p.color[pix];
+      fb.c0 = colorBuf[pix];
     }
   }
   if (inD) {
@@ -460,10 +467,10 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
     if (p.pendingClear && p.clearDepthFlag) {
       fb.d0 = fb.d1 = fb.d2 = fb.d3 = p.clearDepth;
     } else if (S == 4) {
-      float4 v = *reinterpret_cast<const float4 *>(p.depth + pix * 4);
+      float4 v = *reinterpret_cast<const float4 *>(depthBuf + pix * 4);
       fb.d0 = v.x; fb.d1 = v.y; fb.d2 = v.z; fb.d3 = v.w;
     } else {
-      fb.d0 = p.depth[pix];
+      fb.d0 = depthBuf[pix];
     }
   }
   const int start = p.tileStart[tile], end = p.tileEnd[tile];
@@ -499,7 +506,7 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
           mask = depthOps<S, HAS_DEPTH>(p, cv, inD, fb);
         }
         if (HAS_COLOR) {
-          if (count + 32 > kQueue) flushQueue<SH, S, HAS_DEPTH>(p, q, count, mine, lane, rx0, ry0, inC, fb);
+          if (count + 32 > kQueue) flushQueue<SH, S, HAS_DEPTH>(p, U, q, count, mine, lane, rx0, ry0, inC, fb);
           unsigned want = __ballot_sync(0xffffffffu, mask != 0);
           if (mask) {
             int e = count + __popc(want & lt);
@@ -515,11 +522,11 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
       }
     }
   }
-  if (HAS_COLOR && count > 0) flushQueue<SH, S, HAS_DEPTH>(p, q, count, mine, lane, rx0, ry0, inC, fb);
+  if (HAS_COLOR && count > 0) flushQueue<SH, S, HAS_DEPTH>(p, U, q, count, mine, lane, rx0, ry0, inC, fb);
   if (inC) {
     size_t pix = (size_t) py * p.cw + px;
     if (S == 4) {
-      *reinterpret_cast<uint4 *>(p.color + pix * 4) = make_uint4(fb.c0, fb.c1, fb.c2, fb.c3);
+      *reinterpret_cast<uint4 *>(colorBuf + pix * 4) = make_uint4(fb.c0, fb.c1, fb.c2, fb.c3);
       // multiSampleResolve (RendererSoft.cpp:880-912): mean of four u8 samples, truncated
       uint32_t rsv = 0;
 #pragma unroll
@@ -528,24 +535,24 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
                        ((fb.c3 >> (8 * ch)) & 255u);
         rsv |= ((sum >> 2) & 255u) << (8 * ch);
       }
-      p.resolved[pix] = rsv;
+      resolvedBuf[pix] = rsv;
     } else {
-      p.color[pix] = fb.c0;
+      colorBuf[pix] = fb.c0;
     }
   }
   if (inD) {
     size_t pix = (size_t) py * p.dw + px;
     if (S == 4) {
-      *reinterpret_cast<float4 *>(p.depth + pix * 4) = make_float4(fb.d0, fb.d1, fb.d2, fb.d3);
+      *reinterpret_cast<float4 *>(depthBuf + pix * 4) = make_float4(fb.d0, fb.d1, fb.d2, fb.d3);
     } else {
-      p.depth[pix] = fb.d0;
+      depthBuf[pix] = fb.d0;
     }
   }
 }
 
 template<int SH>
 void launchRasterModel(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
-  int grid = p.tilesX * p.tilesY;
+  int grid = p.views * p.tilesPerView;
   if (p.samples == 4) {
     if (hasDepth) k_raster<SH, 4, true, true><<<grid, 256, 0, st>>>(p);
     else k_raster<SH, 4, true, false><<<grid, 256, 0, st>>>(p);

@@ -7,9 +7,10 @@ namespace sglc {
 void launchRasterBlinn(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 void launchRasterPbr(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 void launchRasterNeural(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
+void launchRasterPbrCapture(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
-  int grid = p.tilesX * p.tilesY;
+  int grid = p.views * p.tilesPerView;
   if (!hasColor) {   // depth-only pass: the fragment shader is skipped (RendererSoft.cpp:346-348)
     if (!hasDepth) return;
     if (p.samples == 4) k_raster<SH_BASE, 4, false, true><<<grid, 256, 0, st>>>(p);
@@ -23,6 +24,7 @@ void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_
     case SH_BLINN_DIR: launchRasterBlinn(p, hasColor, hasDepth, st); break;
     case SH_PBR: launchRasterPbr(p, hasColor, hasDepth, st); break;
     case SH_PBR_NEURAL: launchRasterNeural(p, hasColor, hasDepth, st); break;
+    case SH_PBR_CAPTURE: launchRasterPbrCapture(p, hasColor, hasDepth, st); break;
   }
 }
 

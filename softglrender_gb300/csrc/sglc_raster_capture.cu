@@ -1,0 +1,10 @@
+// Raster instantiations: PBR + IBL that also captures neural-shader training records.
+#include "sglc_raster.cuh"
+
+namespace sglc {
+
+void launchRasterPbrCapture(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
+  launchRasterModel<SH_PBR_CAPTURE>(p, hasColor, hasDepth, st);
+}
+
+}  // namespace sglc

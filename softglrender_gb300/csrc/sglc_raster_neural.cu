@@ -48,13 +48,14 @@ struct NeuralPre {
 };
 
 template<int S>
-__device__ __noinline__ NeuralPre neuralPre(const DrawParams &p, int tri, int qx, int qy, int px, int py, float sb0,
-                                            float sb1, float sb2) {
+__device__ __noinline__ NeuralPre neuralPre(const DrawParams &p, const uint8_t *U, int tri, int qx, int qy, int px,
+                                            int py, float sb0, float sb1, float sb2) {
   Tri t = loadTri(p.tri + tri);
   const float *r0 = p.vVary + (size_t) t.vid0 * p.varyStride;
   const float *r1 = p.vVary + (size_t) t.vid1 * p.varyStride;
   const float *r2 = p.vVary + (size_t) t.vid2 * p.varyStride;
   FragIn f;
+  f.U = U;
   f.v = Vary{r0, r1, r2, sb0, sb1, sb2};
   f.dudx = f.dvdx = f.dudy = f.dvdy = 0.f;
   if (p.needDeriv) {
@@ -72,7 +73,7 @@ __device__ __noinline__ NeuralPre neuralPre(const DrawParams &p, int tri, int qx
     f.dudy = u[2] - u[0];
     f.dvdy = v[2] - v[0];
   }
-  PbrSurface s = pbrSurface(p, f);
+  PbrSurface s = pbrSurface<true>(p, f);
   NeuralPre o;
   o.x[0] = s.N.x; o.x[1] = s.N.y; o.x[2] = s.N.z;
   o.x[3] = s.V.x; o.x[4] = s.V.y; o.x[5] = s.V.z;
@@ -95,6 +96,7 @@ struct NeuralCta {
   uint32_t tmem;        // TMEM base of the CTA
   uint32_t lanes;       // this thread's TMEM lane (+ its warpgroup's column base)
   int *chunks;
+  const uint8_t *U;     // uniforms of the CTA's view
   uint32_t phase;
   int row;              // row of this thread in its warpgroup tile
 };
@@ -132,7 +134,7 @@ __device__ __forceinline__ void neuralFlush(const DrawParams &p, NeuralCta &n, F
       int l = m & 31;
       int px = rx0 + (l & 7), py = ry0 + (l >> 3);
       int qx = px - ((m >> 9) & 1), qy = py - ((m >> 10) & 1);
-      pre = neuralPre<S>(p, q.tri[e], qx, qy, px, py, q.b0[e], q.b1[e], q.b2[e]);
+      pre = neuralPre<S>(p, n.U, q.tri[e], qx, qy, px, py, q.b0[e], q.b1[e], q.b2[e]);
     } else {
 #pragma unroll
       for (int i = 0; i < kIn; i++) pre.x[i] = 0.f;
@@ -211,7 +213,12 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
   uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t) 1023);
   FragQueueN *queues = reinterpret_cast<FragQueueN *>(sm + kRnQueues);
   const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
-  const int tx = tile % p.tilesX, ty = tile / p.tilesX;
+  const int view = p.views > 1 ? tile / p.tilesPerView : 0;
+  const int vtile = tile - view * p.tilesPerView;
+  const int tx = vtile % p.tilesX, ty = vtile / p.tilesX;
+  uint32_t *colorBuf = p.viewTarget ? p.viewTarget[view].color : p.color;
+  uint32_t *resolvedBuf = p.viewTarget ? p.viewTarget[view].resolved : p.resolved;
+  float *depthBuf = p.viewTarget ? p.viewTarget[view].depth : p.depth;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
@@ -231,6 +238,7 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
   n.bar = reinterpret_cast<uint64_t *>(sm + kRnBar);
   n.chunks = reinterpret_cast<int *>(sm + kRnChunks);
   n.phase = 0;
+  n.U = viewUniforms(p, view);
   n.row = (warp & 3) * 32 + lane;
   uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(sm + kRnTmem);
   for (int i = threadIdx.x; i < kImgBytes / 16; i += 256)
@@ -255,10 +263,10 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
     if (p.pendingClear && p.clearColorFlag) {
       fb.c0 = fb.c1 = fb.c2 = fb.c3 = p.clearColor;
     } else if (S == 4) {
-      uint4 v = *reinterpret_cast<const uint4 *>(p.color + pix * 4);
+      uint4 v = *reinterpret_cast<const uint4 *>(colorBuf + pix * 4);
       fb.c0 = v.x; fb.c1 = v.y; fb.c2 = v.z; fb.c3 = v.w;
     } else {
-      fb.c0 = p.color[pix];
+      fb.c0 = colorBuf[pix];
     }
   }
   if (inD) {
@@ -266,10 +274,10 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
     if (p.pendingClear && p.clearDepthFlag) {
       fb.d0 = fb.d1 = fb.d2 = fb.d3 = p.clearDepth;
     } else if (S == 4) {
-      float4 v = *reinterpret_cast<const float4 *>(p.depth + pix * 4);
+      float4 v = *reinterpret_cast<const float4 *>(depthBuf + pix * 4);
       fb.d0 = v.x; fb.d1 = v.y; fb.d2 = v.z; fb.d3 = v.w;
     } else {
-      fb.d0 = p.depth[pix];
+      fb.d0 = depthBuf[pix];
     }
   }
   const int start = p.tileStart[tile], end = p.tileEnd[tile];
@@ -323,7 +331,7 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
   if (inC) {
     size_t pix = (size_t) py * p.cw + px;
     if (S == 4) {
-      *reinterpret_cast<uint4 *>(p.color + pix * 4) = make_uint4(fb.c0, fb.c1, fb.c2, fb.c3);
+      *reinterpret_cast<uint4 *>(colorBuf + pix * 4) = make_uint4(fb.c0, fb.c1, fb.c2, fb.c3);
       uint32_t rsv = 0;
 #pragma unroll
       for (int c = 0; c < 4; c++) {
@@ -331,17 +339,17 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
                        ((fb.c3 >> (8 * c)) & 255u);
         rsv |= ((sum >> 2) & 255u) << (8 * c);
       }
-      p.resolved[pix] = rsv;
+      resolvedBuf[pix] = rsv;
     } else {
-      p.color[pix] = fb.c0;
+      colorBuf[pix] = fb.c0;
     }
   }
   if (inD) {
     size_t pix = (size_t) py * p.dw + px;
     if (S == 4) {
-      *reinterpret_cast<float4 *>(p.depth + pix * 4) = make_float4(fb.d0, fb.d1, fb.d2, fb.d3);
+      *reinterpret_cast<float4 *>(depthBuf + pix * 4) = make_float4(fb.d0, fb.d1, fb.d2, fb.d3);
     } else {
-      p.depth[pix] = fb.d0;
+      depthBuf[pix] = fb.d0;
     }
   }
   tc::fenceBefore();
@@ -361,7 +369,7 @@ static void launchNeural(const DrawParams &p, int grid, cudaStream_t st) {
 }
 
 void launchRasterNeural(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
-  int grid = p.tilesX * p.tilesY;
+  int grid = p.views * p.tilesPerView;
   (void) hasColor;   // the neural shader writes colour; depth-only draws never select it
   if (p.samples == 4) {
     if (hasDepth) launchNeural<4, true>(p, grid, st);

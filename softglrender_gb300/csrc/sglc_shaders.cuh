@@ -16,19 +16,21 @@
 
 namespace sglc {
 
-__device__ __forceinline__ const float *uMVP(const DrawParams &p) { return reinterpret_cast<const float *>(p.u + 80); }
-__device__ __forceinline__ const float *uModel(const DrawParams &p) { return reinterpret_cast<const float *>(p.u + 16); }
-__device__ __forceinline__ const float *uITModel(const DrawParams &p) { return reinterpret_cast<const float *>(p.u + 144); }
-__device__ __forceinline__ const float *uShadowMVP(const DrawParams &p) { return reinterpret_cast<const float *>(p.u + 192); }
-__device__ __forceinline__ int uI32(const DrawParams &p, int off) { return *reinterpret_cast<const int32_t *>(p.u + off); }
-__device__ __forceinline__ float uF32(const DrawParams &p, int off) { return *reinterpret_cast<const float *>(p.u + off); }
-__device__ __forceinline__ float4 uV4(const DrawParams &p, int off) { return *reinterpret_cast<const float4 *>(p.u + off); }
+// Uniform reads. U = the draw's ShaderUniforms bytes (DrawParams::u) or, in a batched draw, the
+// view's copy of them.
+__device__ __forceinline__ const float *uMVP(const uint8_t *U) { return reinterpret_cast<const float *>(U + 80); }
+__device__ __forceinline__ const float *uModel(const uint8_t *U) { return reinterpret_cast<const float *>(U + 16); }
+__device__ __forceinline__ const float *uITModel(const uint8_t *U) { return reinterpret_cast<const float *>(U + 144); }
+__device__ __forceinline__ const float *uShadowMVP(const uint8_t *U) { return reinterpret_cast<const float *>(U + 192); }
+__device__ __forceinline__ int uI32(const uint8_t *U, int off) { return *reinterpret_cast<const int32_t *>(U + off); }
+__device__ __forceinline__ float uF32(const uint8_t *U, int off) { return *reinterpret_cast<const float *>(U + off); }
+__device__ __forceinline__ float4 uV4(const uint8_t *U, int off) { return *reinterpret_cast<const float4 *>(U + off); }
 
 // VS: writes clip position and the varyings of one vertex. a = raw attribute floats.
 template<int SH>
-__device__ __forceinline__ float4 runVS(const DrawParams &p, const float *a, float *v) {
+__device__ __forceinline__ float4 runVS(const DrawParams &p, const uint8_t *U, const float *a, float *v) {
   float4 position = make_float4(a[0], a[1], a[2], 1.0f);
-  float4 pos = mul44(uMVP(p), position);
+  float4 pos = mul44(uMVP(U), position);
   if (SH == SH_VCOLOR) {
     v[0] = a[4]; v[1] = a[5]; v[2] = a[6]; v[3] = a[7];
   } else if (SH == SH_BLINN || SH == SH_BLINN_DIR || SH == SH_PBR) {
@@ -36,22 +38,22 @@ __device__ __forceinline__ float4 runVS(const DrawParams &p, const float *a, flo
     v[0] = a[4];
     v[1] = a[5];
     if (bp) {
-      float4 s = mul44(uShadowMVP(p), position);
+      float4 s = mul44(uShadowMVP(U), position);
       v[20] = s.x; v[21] = s.y; v[22] = s.z; v[23] = s.w;
     }
-    float4 w4 = mul44(uModel(p), position);
+    float4 w4 = mul44(uModel(U), position);
     f3 world = mk3(w4.x, w4.y, w4.z);
-    f3 nvec = mul33(uModel(p), mk3(a[8], a[9], a[10]));
-    f3 lpos = ld3(p.u + 288);
+    f3 nvec = mul33(uModel(U), mk3(a[8], a[9], a[10]));
+    f3 lpos = ld3(U + 288);
     f3 ldir = (SH == SH_BLINN_DIR) ? lpos : lpos - world;
-    f3 cdir = ld3(p.u + 272) - world;
+    f3 cdir = ld3(U + 272) - world;
     v[4] = nvec.x; v[5] = nvec.y; v[6] = nvec.z;
     v[8] = world.x; v[9] = world.y; v[10] = world.z;
     v[12] = cdir.x; v[13] = cdir.y; v[14] = cdir.z;
     v[16] = ldir.x; v[17] = ldir.y; v[18] = ldir.z;
     if (p.def[1]) {   // NORMAL_MAP
-      f3 N = normalize3(mul33(uITModel(p), mk3(a[8], a[9], a[10])));
-      f3 T = normalize3(mul33(uITModel(p), mk3(a[12], a[13], a[14])));
+      f3 N = normalize3(mul33(uITModel(U), mk3(a[8], a[9], a[10])));
+      f3 T = normalize3(mul33(uITModel(U), mk3(a[12], a[13], a[14])));
       f3 Tn = normalize3(T - dot3(T, N) * N);
       const int o = bp ? 24 : 20;
       v[o] = N.x; v[o + 1] = N.y; v[o + 2] = N.z;
@@ -76,6 +78,7 @@ struct Vary {
 };
 
 struct FragIn {
+  const uint8_t *U;   // uniforms
   Vary v;
   float dudx, dvdx, dudy, dvdy;   // texcoord differences p1-p0, p2-p0 of the quad
 };
@@ -129,7 +132,7 @@ __device__ inline float shadowCalc(const DrawParams &p, const FragIn &f, f3 norm
   float bias = gmax(0.00025f * (1.0f - dot3(normal, normalize3(f.v.v3(16)))), 0.00005f);
   const DevSampler &s = p.samp[4];
   float ox = 1.0f / (float) s.tex.w[0], oy = 1.0f / (float) s.tex.h[0];
-  int reverseZ = uI32(p, 0);
+  int reverseZ = uI32(f.U, 0);
   float shadow = 0.0f;
   for (int x = -1; x <= 1; ++x)
     for (int y = -1; y <= 1; ++y) {
@@ -144,16 +147,16 @@ template<bool DIRECTIONAL>
 __device__ inline float4 fsBlinnPhong(const DrawParams &p, const FragIn &f) {
   const float specExp = DIRECTIONAL ? 32.f : 128.f;
   const float rangeInv = 1.0f / 5.f;
-  float4 base = p.def[0] ? tex2D(p, 0, f.v[0], f.v[1], f) : uV4(p, 352);
+  float4 base = p.def[0] ? tex2D(p, 0, f.v[0], f.v[1], f) : uV4(f.U, 352);
   f3 N = normalFromMap(p, f, 24, 28);
   float ao = 1.f;
   if (p.def[3]) ao = tex2D(p, 3, f.v[0], f.v[1], f).x;
   f3 baseRgb = mk3(base.x, base.y, base.z);
-  f3 ambient = baseRgb * ld3(p.u + 256) * ao;
+  f3 ambient = baseRgb * ld3(f.U + 256) * ao;
   f3 diffuseC = mk3(0, 0, 0), specC = mk3(0, 0, 0), emis = mk3(0, 0, 0);
-  if (uI32(p, 320)) {
+  if (uI32(f.U, 320)) {
     f3 ldirRaw = f.v.v3(16);
-    f3 lightColor = ld3(p.u + 304);
+    f3 lightColor = ld3(f.U + 304);
     f3 L = normalize3(ldirRaw);
     float diffuse = gmax(dot3(N, L), 0.0f);
     if (DIRECTIONAL) {
@@ -167,8 +170,8 @@ __device__ inline float4 fsBlinnPhong(const DrawParams &p, const FragIn &f) {
     f3 H = normalize3(L + C);
     float sa = gmax(dot3(N, H), 0.0f);
     float pw = powf(sa, specExp);
-    specC = uF32(p, 336) * mk3(pw, pw, pw);
-    if (uI32(p, 328)) {
+    specC = uF32(f.U, 336) * mk3(pw, pw, pw);
+    if (uI32(f.U, 328)) {
       float shadow = 1.0f - shadowCalc(p, f, N);
       diffuseC = diffuseC * shadow;
       specC = specC * shadow;
@@ -184,7 +187,7 @@ __device__ inline float4 fsBlinnPhong(const DrawParams &p, const FragIn &f) {
 
 // Training record of the neural IBL shader (sglc_nn.cuh): the network's 12 inputs and the square
 // root of the IBL term it learns, appended while the host has capture enabled.
-static __device__ __noinline__ void captureRecord(const DrawParams &p, f3 N, f3 V, float roughness, float metallic,
+static __device__ __forceinline__ void captureRecord(const DrawParams &p, f3 N, f3 V, float roughness, float metallic,
                                            float4 albedo, float NdotV, f3 ibl) {
   unsigned long long slot = atomicAdd(p.capCount, 1ull);
   if (slot % (unsigned) p.capStride) return;
@@ -207,11 +210,14 @@ struct PbrSurface {
   f3 emissive;
 };
 
+// EMISSIVE: also fetch the emissive texel here (the neural variant finishes the colour later, when
+// the fragment inputs are gone); the plain shader fetches it at the end, as PbrSoft.h:315-318 does.
+template<bool EMISSIVE>
 __device__ __forceinline__ PbrSurface pbrSurface(const DrawParams &p, const FragIn &f) {
   const float PI = 3.14159265359f;
   const float rangeInv = 1.0f / 5.f;
   PbrSurface s;
-  float4 arg = p.def[0] ? tex2D(p, 0, f.v[0], f.v[1], f) : uV4(p, 352);
+  float4 arg = p.def[0] ? tex2D(p, 0, f.v[0], f.v[1], f) : uV4(f.U, 352);
   s.arg = arg;
   f3 albedo = mk3(powf(arg.x, 2.2f), powf(arg.y, 2.2f), powf(arg.z, 2.2f));
   s.albedo = albedo;
@@ -234,13 +240,13 @@ __device__ __forceinline__ PbrSurface pbrSurface(const DrawParams &p, const Frag
   F0 = F0 * (1.0f - metallic) + albedo * metallic;
   s.F0 = F0;
   f3 Lo = mk3(0, 0, 0);
-  if (uI32(p, 320)) {
+  if (uI32(f.U, 320)) {
     f3 ldir = f.v.v3(16);
     f3 L = normalize3(ldir);
     f3 H = normalize3(V + L);
     f3 lDir = ldir * rangeInv;
     float att = gclamp(1.0f - dot3(lDir, lDir), 0.0f, 1.0f);
-    f3 radiance = ld3(p.u + 304) * att;
+    f3 radiance = ld3(f.U + 304) * att;
     float a = roughness * roughness;
     float a2 = a * a;
     float NdotH = gmax(dot3(N, H), 0.0f);
@@ -268,7 +274,7 @@ __device__ __forceinline__ PbrSurface pbrSurface(const DrawParams &p, const Frag
   }
   s.Lo = Lo;
   s.emissive = mk3(0.f, 0.f, 0.f);
-  if (p.def[2]) {
+  if (EMISSIVE && p.def[2]) {
     float4 e = tex2D(p, 2, f.v[0], f.v[1], f);
     s.emissive = mk3(e.x, e.y, e.z);
   }
@@ -283,12 +289,13 @@ __device__ __forceinline__ float4 pbrFinish(const DrawParams &p, f3 ambient, f3 
   return make_float4(color.x, color.y, color.z, alpha);
 }
 
+template<bool CAPTURE>
 __device__ inline float4 fsPbr(const DrawParams &p, const FragIn &f) {
-  PbrSurface s = pbrSurface(p, f);
+  PbrSurface s = pbrSurface<false>(p, f);
   const f3 N = s.N, V = s.V, F0 = s.F0, albedo = s.albedo;
   const float metallic = s.metallic, roughness = s.roughness, ao = s.ao;
   f3 ambient;
-  if (uI32(p, 324)) {
+  if (uI32(f.U, 324)) {
     f3 mV = -V;
     f3 R = mV - N * dot3(N, mV) * 2.0f;
     float NdotV = gmax(dot3(N, V), 0.0f);
@@ -310,21 +317,26 @@ __device__ inline float4 fsPbr(const DrawParams &p, const FragIn &f) {
     f3 env = F * ABx + ABy;
     f3 specular = mk3(pre.x, pre.y, pre.z) * env;
     f3 ibl = kD * diffuse + specular;
-    if (p.capRecords) captureRecord(p, N, V, roughness, metallic, s.arg, NdotV, ibl);
+    if (CAPTURE) captureRecord(p, N, V, roughness, metallic, s.arg, NdotV, ibl);
     ambient = ibl * ao;
   } else {
-    ambient = ld3(p.u + 256) * albedo * ao;
+    ambient = ld3(f.U + 256) * albedo * ao;
   }
-  return pbrFinish(p, ambient, s.Lo, s.emissive, s.arg.w);
+  f3 emissive = mk3(0.f, 0.f, 0.f);
+  if (p.def[2]) {
+    float4 e = tex2D(p, 2, f.v[0], f.v[1], f);
+    emissive = mk3(e.x, e.y, e.z);
+  }
+  return pbrFinish(p, ambient, s.Lo, emissive, s.arg.w);
 }
 
 template<int SH>
 __device__ __forceinline__ float4 runFS(const DrawParams &p, const FragIn &f) {
-  if (SH == SH_BASE) return uV4(p, 256 + 32);
+  if (SH == SH_BASE) return uV4(f.U, 256 + 32);
   if (SH == SH_VCOLOR) return make_float4(f.v[0], f.v[1], f.v[2], f.v[3]);
   if (SH == SH_BLINN) return fsBlinnPhong<false>(p, f);
   if (SH == SH_BLINN_DIR) return fsBlinnPhong<true>(p, f);
-  return fsPbr(p, f);
+  return fsPbr<SH == SH_PBR_CAPTURE>(p, f);
 }
 
 // does the FS read texcoord derivatives (any bound 2D sampler with a mip filter and LOD callback)

@@ -12,6 +12,7 @@ threshold (per material; otherwise the plain shader stays: the fallback).
 from __future__ import annotations
 
 import ctypes as C
+import time
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional
 
@@ -118,6 +119,16 @@ class NeuralShader:
         self._check(self.fn["neural_train"](self.h, C.byref(tp), C.byref(loss)), "neural_train")
         return float(loss.value)
 
+    def fit(self, steps: int, batch: int, lr: float = 3e-3, chunks: int = 10, seed: int = 7) -> float:
+        """`steps` Adam steps with a cosine-decayed learning rate (held constant within each of
+        `chunks` equal chunks, floor 2% of `lr`). Returns the last batch loss."""
+        loss = float("nan")
+        per = max(1, steps // chunks)
+        for c in range(chunks):
+            f = 0.5 * (1.0 + np.cos(np.pi * c / chunks))
+            loss = self.train(per, batch, lr=float(max(lr * f, lr * 0.02)), seed=seed + c)
+        return loss
+
     def gradients(self, first: int, count: int):
         g = np.zeros(self.n_params, np.float32)
         loss = C.c_float(0)
@@ -150,14 +161,10 @@ def psnr(a: np.ndarray, b: np.ndarray, peak: float = 255.0) -> float:
     return float("inf") if mse == 0 else 10.0 * np.log10(peak * peak / mse)
 
 
-def set_view(inst: S.SceneInstance, scene: S.Scene) -> None:
+def set_view(inst: S.SceneInstance, blocks: Dict[str, bytes]) -> None:
     """Point an instance at another view of the same scene: re-upload its uniform blocks (camera,
     light); geometry and textures are shared."""
-    for objs, p in zip(inst.draws, scene.passes):
-        for (vao, prog, res, ps), d in zip(objs, p.draws):
-            for ub in res.blocks.values():
-                if ub.name in d.blocks:
-                    ub.setData(d.blocks[ub.name])
+    _set_blocks(inst, blocks)
 
 
 def pbr_programs(inst: S.SceneInstance) -> List[A.ShaderProgram]:
@@ -176,6 +183,8 @@ class NeuralReport:
     psnr_without: List[float] = field(default_factory=list)
     psnr_untrained: List[float] = field(default_factory=list)
     bound: bool = False
+    capture_s: float = 0.0
+    train_s: float = 0.0
 
     @property
     def psnr_mean(self) -> float:
@@ -188,17 +197,19 @@ def _resolved(inst: S.SceneInstance) -> np.ndarray:
 
 
 def train_neural_ibl(renderer: A.Renderer, scene_kwargs: Optional[dict] = None, train_views: int = 64,
-                     test_views: int = 16, records: int = 1 << 22, steps: int = 4000, batch: int = 1 << 16,
-                     lr: float = 2e-3, seed: int = 1, threshold_db: float = 40.0, baselines: bool = True,
+                     test_views: int = 16, records: int = 1 << 22, steps: int = 6000, batch: int = 1 << 14,
+                     lr: float = 3e-3, seed: int = 1, threshold_db: float = 40.0, baselines: bool = True,
                      inst: Optional[S.SceneInstance] = None, net: Optional[NeuralShader] = None):
     """Capture fragments of `train_views` orbit views of the PBR scene rendered by the plain shader,
     train the network, compare on `test_views` held-out views, and bind it to the scene's PBR
     program if the mean held-out PSNR reaches `threshold_db` (else the plain shader stays bound).
     Returns (instance, network, report)."""
     kw = dict(scene_kwargs or {})
-    views = lambda v: S.config_pbr(view=v, **kw)
+    seed_scene = kw.get("seed", 3000)
+    width, height = kw.get("width", 1920), kw.get("height", 1080)
+    views = lambda v: S.pbr_view_blocks(seed_scene, v, width, height)
     if inst is None:
-        inst = S.SceneInstance(renderer, views(0))
+        inst = S.SceneInstance(renderer, S.config_pbr(**kw))
     progs = pbr_programs(inst)
     if net is None:
         net = NeuralShader(renderer, seed)
@@ -211,6 +222,7 @@ def train_neural_ibl(renderer: A.Renderer, scene_kwargs: Optional[dict] = None, 
     frags = int(renderer.drawStats()["fragments_shaded"])
     renderer.setStatsLevel(0)
     stride = max(1, int(np.ceil(train_views * frags / float(records))))
+    t0 = time.perf_counter()
     net.capture(records, stride)
     for v in range(train_views):
         set_view(inst, views(v))
@@ -218,9 +230,11 @@ def train_neural_ibl(renderer: A.Renderer, scene_kwargs: Optional[dict] = None, 
     renderer.waitIdle()
     net.stop_capture()
     n = net.record_count()
+    capture_s = time.perf_counter() - t0
     untrained = net.get_params()
-    loss = net.train(steps, batch, lr=lr, seed=seed)
-    rep = NeuralReport(n, stride, steps, loss)
+    t0 = time.perf_counter()
+    loss = net.fit(steps, batch, lr=lr, seed=seed)
+    rep = NeuralReport(n, stride, steps, loss, capture_s=capture_s, train_s=time.perf_counter() - t0)
     test = range(train_views, train_views + test_views)
     for v in test:
         set_view(inst, views(v))
@@ -237,28 +251,27 @@ def train_neural_ibl(renderer: A.Renderer, scene_kwargs: Optional[dict] = None, 
     if baselines:
         trained = net.get_params()
         # the method without the network: the shader's own non-IBL ambient term (u_enableIBL = 0)
-        base = views(train_views)
         for v in test:
-            sc = views(v)
+            blocks = views(v)
             for prog in progs:
                 NeuralShader.unbind(renderer, prog)
-            set_view(inst, sc)
+            set_view(inst, blocks)
             inst.render()
             plain = _resolved(inst)
-            mat = dict(sc.passes[0].draws[0].blocks)
-            mat["UniformsMaterial"] = _without_ibl(mat["UniformsMaterial"])
-            _set_blocks(inst, mat)
+            without = dict(blocks)
+            without["UniformsMaterial"] = _without_ibl(blocks["UniformsMaterial"])
+            set_view(inst, without)
             inst.render()
             rep.psnr_without.append(psnr(_resolved(inst)[..., :3], plain[..., :3]))
-            set_view(inst, sc)
+            set_view(inst, blocks)
             net.set_params(untrained)
             for prog in progs:
                 net.bind(prog)
             inst.render()
             rep.psnr_untrained.append(psnr(_resolved(inst)[..., :3], plain[..., :3]))
             net.set_params(trained)
-        del base
     rep.bound = rep.psnr_mean >= threshold_db
+    set_view(inst, views(0))
     for prog in progs:
         if rep.bound:
             net.bind(prog)

@@ -635,12 +635,9 @@ def config_geometry_stress(seed: int = 2000, n_tris: int = 1_000_000, width: int
                  {"config": 2, "seed": seed, "width": width, "height": height, "samples": samples})
 
 
-def config_pbr(seed: int = 3000, width: int = 1920, height: int = 1080, samples: int = 4, lon: int = 448,
-               lat: int = 224, tex: int = 1024, prefilter: int = 512, irradiance: int = 32,
-               view: int = 0) -> Scene:
-    """Displaced sphere (value noise, amplitude 0.1) with PBR+IBL: albedo / normal / metal-roughness
-    maps (trilinear), irradiance + 5-level prefiltered specular cube maps, point light, MSAA 4x."""
-    vert, idx = uv_sphere(lon, lat, 1.0, displace_seed=seed, amplitude=0.1)
+def pbr_view_blocks(seed: int, view: int, width: int, height: int) -> Dict[str, bytes]:
+    """Uniform blocks of one seeded orbit view of the PBR scene (camera and point light follow the
+    view; geometry and textures do not depend on it)."""
     yaw = 2.0 * np.pi * hash_u01(seed, 50, view)
     pitch = (hash_u01(seed, 51, view) - 0.5) * 0.8
     dist = 2.7
@@ -649,11 +646,20 @@ def config_pbr(seed: int = 3000, width: int = 1920, height: int = 1080, samples:
     Vm = look_at(eye, [0, 0, 0], [0, 1, 0])
     Mm = np.eye(4)
     light_pos = eye * 0.9 + np.array([1.2, 1.5, 0.3])
-    blocks = {
+    return {
         "UniformsModel": uniforms_model(Mm, mm4(mm4(Pm, Vm), Mm), None, False),
         "UniformsScene": uniforms_scene([0.1, 0.1, 0.1], eye, light_pos, [2.5, 2.4, 2.2]),
         "UniformsMaterial": uniforms_material(True, True, False, 1.0, 0.5, [1, 1, 1, 1]),
     }
+
+
+def config_pbr(seed: int = 3000, width: int = 1920, height: int = 1080, samples: int = 4, lon: int = 448,
+               lat: int = 224, tex: int = 1024, prefilter: int = 512, irradiance: int = 32,
+               view: int = 0) -> Scene:
+    """Displaced sphere (value noise, amplitude 0.1) with PBR+IBL: albedo / normal / metal-roughness
+    maps (trilinear), irradiance + 5-level prefiltered specular cube maps, point light, MSAA 4x."""
+    vert, idx = uv_sphere(lon, lat, 1.0, displace_seed=seed, amplitude=0.1)
+    blocks = pbr_view_blocks(seed, view, width, height)
     trilinear = A.SamplerDesc(A.Filter_LINEAR_MIPMAP_LINEAR, A.Filter_LINEAR, A.Wrap_REPEAT, A.Wrap_REPEAT,
                               A.Wrap_REPEAT)
     tdesc = A.TextureDesc(tex, tex, A.TextureType_2D, A.TextureFormat_RGBA8,

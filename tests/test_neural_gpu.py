@@ -9,7 +9,7 @@ import pytest
 from oracle import nn_oracle as O
 from softglrender_gb300 import api as A
 from softglrender_gb300 import scenes as S
-from softglrender_gb300.neural import NeuralShader, pbr_programs, set_view, train_neural_ibl
+from softglrender_gb300.neural import NeuralShader, pbr_programs, train_neural_ibl
 
 pytestmark = pytest.mark.gpu
 
@@ -162,8 +162,8 @@ def test_neural_pipeline_gains_over_the_method_without_it(cuda_lib):
     network, and the fall-back decision must follow the threshold."""
     r = A.Renderer(cuda_lib, 0)
     kw = dict(width=320, height=180, lon=96, lat=48, tex=128, prefilter=64, irradiance=16)
-    inst, net, rep = train_neural_ibl(r, kw, train_views=8, test_views=4, records=1 << 18, steps=1500,
-                                      batch=1 << 14, lr=2e-3, seed=3)
+    inst, net, rep = train_neural_ibl(r, kw, train_views=8, test_views=4, records=1 << 18, steps=3000,
+                                      batch=1 << 14, lr=3e-3, seed=3)
     print("neural PSNR per held-out view:", [round(x, 2) for x in rep.psnr_views],
           "without IBL:", [round(x, 2) for x in rep.psnr_without],
           "untrained:", [round(x, 2) for x in rep.psnr_untrained], "loss", rep.final_loss)
