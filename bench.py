@@ -35,6 +35,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-neural", action="store_true", help="skip training / timing the neural IBL shader")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-views measurement")
     return ap.parse_args()
 
 
@@ -185,6 +186,75 @@ def run_cpu(scene, steps: int, threads: int, min_seconds: float = 0.0):
     return n / dt, n
 
 
+def bench_batched_views(r, stream, with_cpu: bool):
+    """Batched views (256 orbit views, shadow pass): autotuned frame vs the same frame drawn one
+    render pass per view on the GPU, and the CPU pipeline looped over a sample of the views."""
+    import torch
+    from softglrender_gb300.autotune import autotune
+    from softglrender_gb300.batch import BatchConfig, BatchedViews
+    cfg = BatchConfig()
+    b = BatchedViews(r, cfg)
+
+    def time_ms(fn, n):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for st, en in ev:
+            with torch.cuda.stream(stream):
+                st.record(stream)
+            fn()
+            with torch.cuda.stream(stream):
+                en.record(stream)
+        r.waitIdle()
+        torch.cuda.synchronize()
+        return float(np.median([st.elapsed_time(en) for st, en in ev]))
+
+    r.setCapacity(None)
+    for _ in range(2):
+        b.render()
+    eager_ms = time_ms(b.render, 5)
+    r.setStatsLevel(2)
+    b.render()
+    frags = int(r.drawStats()["fragments_shaded"])
+    r.setStatsLevel(0)
+    looped_ms = time_ms(b.render_looped, 2)
+    tuned = autotune(r, b.render, reps=5)
+    for _ in range(3):
+        tuned.run()
+    wall0 = time.perf_counter()
+    tuned_ms = time_ms(tuned.run, 10)
+    overflow = r.getOverflow()
+    out = {
+        "workload": "batched_views_256x256sq_shadow2048_50k", "views": cfg.views, "triangles": b.triangles,
+        "views_per_s": round(cfg.views / (tuned_ms / 1e3), 1), "ms_per_frame": round(tuned_ms, 4),
+        "mfrag_per_s": round(frags / (tuned_ms / 1e3) / 1e6, 2), "fragments_per_frame": frags,
+        "eager_exact_sizing_ms": round(eager_ms, 4), "looped_one_pass_per_view_ms": round(looped_ms, 4),
+        "speedup_vs_looped": round(looped_ms / tuned_ms, 2), "overflow_flags": overflow,
+        "autotune": tuned.result.describe(),
+    }
+    del wall0
+    tuned.destroy()
+    r.setCapacity(None)
+    if with_cpu:
+        import oracle
+        from softglrender_gb300 import api as A
+        lib = oracle.restatement()
+        rc = A.Renderer(lib, 0)
+        threads = os.cpu_count() or 1
+        lib.cdll.sglo_set_threads(rc.ctx, threads)
+        bc = BatchedViews(rc, cfg)
+        sample = list(range(16))
+        bc.render_looped(sample[:1])   # warm-up
+        t0 = time.perf_counter()
+        n = 0
+        while n < 2 or time.perf_counter() - t0 < 5.0:
+            bc.render_looped(sample)
+            n += 1
+        dt = (time.perf_counter() - t0) / n
+        rc.destroy()
+        out["cpu_baseline"] = {"views_per_s": round(len(sample) / dt, 2), "cores": threads, "kind": "port",
+                               "sample": f"shadow pass + {len(sample)} of the {cfg.views} views, {n} repetitions"}
+    return out
+
+
 def main():
     args = parse()
     world, rank, local, pg = dist_setup()
@@ -300,6 +370,12 @@ def main():
         }
         net.destroy()
 
+    # ---- batched views: 256 orbit views of a 50k-triangle sphere at 256x256 after a 2048x2048
+    # shadow pass, all views in one pipeline pass, submission chosen by the autotuner -----------
+    batched = None
+    if not args.no_batched:
+        batched = bench_batched_views(r, stream, rank == 0 and not args.no_cpu_baseline)
+
     # ---- end to end through the public API with host buffers ----------------------------------
     pinned_v = torch.empty(d0.vertexes.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(np.float32)
     pinned_v[:] = d0.vertexes.reshape(-1)
@@ -356,6 +432,8 @@ def main():
     }
     if neural is not None:
         result["neural"] = neural
+    if batched is not None:
+        result["batched_views"] = batched
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         t0 = time.perf_counter()

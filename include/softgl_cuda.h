@@ -250,6 +250,36 @@ SGLC_API sglc_status sglc_get_stream(sglc_context *ctx, void **stream);
 /* Raster tile edge in pixels (8, 16 or 32); picked by the autotuner, default 16. */
 SGLC_API sglc_status sglc_set_tile_size(sglc_context *ctx, int32_t tile);
 
+/* ---- synchronisation-free draws and CUDA graphs (no reference counterpart) ------------------- */
+/* Working-array capacities of a draw (a batched draw counts all its views together). */
+typedef struct sglc_capacity {
+  int64_t clip_vertices;         /* vertices created by frustum clipping */
+  int64_t clip_polygons;         /* triangles clipped into polygons of more than 3 vertices */
+  int64_t appended_primitives;   /* fan triangles appended after clipping */
+  int64_t bin_entries;           /* (tile, triangle) pairs */
+  int32_t heavy_first;           /* 1: raster the longest tile lists first; 0: tiles in index order */
+} sglc_capacity;
+/* With capacities set, draws size their working arrays from them instead of reading counts back
+ * from the device after the setup stage: a draw then never waits for the GPU, and draws can be
+ * captured in a CUDA graph. Work beyond a capacity is dropped and recorded in sticky overflow flags
+ * (sglc_get_overflow); the images of such a draw are then unspecified. Null restores the default
+ * (exact sizing with one count read-back per draw). */
+SGLC_API sglc_status sglc_set_capacity(sglc_context *ctx, const sglc_capacity *cap);
+/* Synchronises, returns and clears the overflow flags of the draws since the last call: bit 0 clip
+ * vertices, 1 clip polygons, 2 appended primitives, 3 bin entries, 4 an index outside the vertex
+ * array. */
+SGLC_API sglc_status sglc_get_overflow(sglc_context *ctx, int32_t *flags);
+typedef struct sglc_graph sglc_graph;
+/* Capture everything enqueued on the context between begin and end into a CUDA graph. Draws in the
+ * capture must run with capacities set, and the same sequence must have run once uncaptured so
+ * that every working array is already sized (a capture that would need to grow one fails). Reads
+ * of attachments and other synchronising calls are not allowed inside a capture. */
+SGLC_API sglc_status sglc_graph_begin(sglc_context *ctx);
+SGLC_API sglc_status sglc_graph_end(sglc_context *ctx, sglc_graph **out);
+/* Enqueue one replay of the graph on its context's stream. */
+SGLC_API sglc_status sglc_graph_launch(sglc_graph *graph);
+SGLC_API sglc_status sglc_graph_destroy(sglc_graph *graph);
+
 /* ---- neural IBL shader (no reference counterpart) ------------------------------------------- */
 /* A small MLP (12 inputs, 6-frequency encoding, 2 x 64 ReLU, 3 outputs; BF16 weights, FP32
  * accumulation on the tensor cores) that stands in for the image-based-lighting term of the PBR

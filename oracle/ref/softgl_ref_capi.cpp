@@ -503,6 +503,13 @@ sglc_status sglr_draw_views(sglc_context *ctx, const sglc_handle *fbs, const sgl
   return SGLC_OK;
 }
 
+// Capacities only change how the GPU back-end sizes its working arrays; RendererSoft has none.
+sglc_status sglr_set_capacity(sglc_context *, const sglc_capacity *) { return SGLC_OK; }
+sglc_status sglr_get_overflow(sglc_context *, int32_t *flags) {
+  if (flags) *flags = 0;
+  return SGLC_OK;
+}
+
 sglc_status sglr_wait_idle(sglc_context *ctx) {
   reinterpret_cast<Ctx *>(ctx)->renderer.waitIdle();
   return SGLC_OK;

@@ -1643,6 +1643,13 @@ sglc_status sglo_draw_views(sglc_context *ctx, const sglc_handle *fbs, const sgl
   return SGLC_OK;
 }
 sglc_status sglo_wait_idle(sglc_context *) { return SGLC_OK; }
+// Capacities only change how the GPU back-end sizes its working arrays; the CPU pipeline has no
+// capacities and never overflows.
+sglc_status sglo_set_capacity(sglc_context *, const sglc_capacity *) { return SGLC_OK; }
+sglc_status sglo_get_overflow(sglc_context *, int32_t *flags) {
+  if (flags) *flags = 0;
+  return SGLC_OK;
+}
 sglc_status sglo_set_enable_early_z(sglc_context *ctx, int32_t e) {
   CTX;
   c->earlyZ = e != 0;

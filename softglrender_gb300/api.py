@@ -199,10 +199,18 @@ _SIGS = {
     "get_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
     "set_stats_level": [C.c_void_p, C.c_int32],
     "draw_views": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32, C.c_void_p],
+    "set_capacity": [C.c_void_p, C.c_void_p],
+    "get_overflow": [C.c_void_p, C.POINTER(C.c_int32)],
     "set_tile_size": [C.c_void_p, C.c_int32],
 }
 
 ABI_FUNCTIONS = tuple(_SIGS) + ("last_error",)
+
+
+class Capacity(C.Structure):
+    """sglc_capacity: working-array capacities of synchronisation-free draws."""
+    _fields_ = [("clip_vertices", C.c_int64), ("clip_polygons", C.c_int64), ("appended_primitives", C.c_int64),
+                ("bin_entries", C.c_int64), ("heavy_first", C.c_int32)]
 
 
 class Library:
@@ -473,6 +481,15 @@ class Renderer:
 
     def endRenderPass(self) -> None:
         self._call("end_render_pass")
+
+    def setCapacity(self, cap: Optional[Capacity]) -> None:
+        """Synchronisation-free draws with these capacities (None: exact sizing, one read-back per draw)."""
+        self._call("set_capacity", C.byref(cap) if cap is not None else None)
+
+    def getOverflow(self) -> int:
+        f = C.c_int32(0)
+        self._call("get_overflow", C.byref(f))
+        return f.value
 
     def drawViews(self, framebuffers: Sequence[FrameBuffer], resources: Sequence[ShaderResources],
                   clear: Optional[ClearStates] = None) -> None:

@@ -1,0 +1,129 @@
+"""Autotuner for synchronisation-free frames: picks working-array capacities, the raster tile order
+and eager-versus-graph submission for a given frame by measuring them.
+
+1. Calibration: the frame runs once with exact sizing (one count read-back per draw); the largest
+   draw's counts (clip vertices, appended primitives, bin entries) times a headroom give the
+   capacities. A candidate that overflows (sglc_get_overflow) doubles them and is measured again.
+2. Candidates: raster tiles longest-list-first or in index order; the frame enqueued call by call
+   or captured once in a CUDA graph and replayed. Each runs `reps` times after warm-up, timed with
+   CUDA events on the renderer's stream; the fastest wins.
+The raster tile is 16 x 16 pixels with 256 threads in this build (the only tile size compiled), so
+tile size is reported, not searched.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+from typing import Callable, Dict, List, Optional
+
+import numpy as np
+
+from . import api as A
+from .graph import Graph
+
+
+@dataclass
+class TuneResult:
+    capacity: A.Capacity
+    heavy_first: int
+    graph: bool
+    ms: float
+    table: List[Dict[str, object]] = field(default_factory=list)
+    tile: int = 16
+    threads_per_tile: int = 256
+
+    def describe(self) -> Dict[str, object]:
+        c = self.capacity
+        return {"tile": self.tile, "threads_per_tile": self.threads_per_tile, "heavy_first": self.heavy_first,
+                "graph": self.graph, "ms": round(self.ms, 4),
+                "capacity": {"clip_vertices": c.clip_vertices, "clip_polygons": c.clip_polygons,
+                             "appended_primitives": c.appended_primitives, "bin_entries": c.bin_entries},
+                "candidates": self.table}
+
+
+class Tuned:
+    """A frame with its tuned submission: `run()` enqueues one frame."""
+
+    def __init__(self, r: A.Renderer, frame: Callable[[], None], result: TuneResult, graph: Optional[Graph]):
+        self.r, self.frame, self.result, self.graph = r, frame, result, graph
+
+    def run(self) -> None:
+        if self.graph is not None:
+            self.graph.launch()
+        else:
+            self.frame()
+
+    def destroy(self) -> None:
+        if self.graph is not None:
+            self.graph.destroy()
+            self.graph = None
+
+
+def _timer(r: A.Renderer):
+    import torch
+    stream = torch.cuda.ExternalStream(r.stream())
+
+    def time_ms(fn: Callable[[], None], reps: int) -> float:
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for s, e in ev:
+            with torch.cuda.stream(stream):
+                s.record(stream)
+            fn()
+            with torch.cuda.stream(stream):
+                e.record(stream)
+        r.waitIdle()
+        torch.cuda.synchronize()
+        return float(np.median([s.elapsed_time(e) for s, e in ev]))
+    return time_ms
+
+
+def autotune(r: A.Renderer, frame: Callable[[], None], headroom: float = 1.25, reps: int = 5,
+             heavy_first=(1, 0), graph=(False, True)) -> Tuned:
+    time_ms = _timer(r)
+    r.setCapacity(None)
+    frame()
+    r.waitIdle()
+    st = r.drawStats()
+    appended = max(0, int(st["primitives"]) - int(st["triangles_in"]))
+    cap = A.Capacity(max(1024, int(max(0, st["clip_vertices"]) * headroom) + 1024),
+                     max(1024, int(appended * headroom) + 1024),
+                     max(1024, int(appended * headroom) + 1024),
+                     max(4096, int(int(st["bin_entries"]) * headroom) + 4096), 1)
+    table, best, best_graph = [], None, None
+    for hf in heavy_first:
+        for use_graph in graph:
+            cap.heavy_first = hf
+            for _ in range(4):   # grow until the frame fits
+                r.setCapacity(cap)
+                frame()
+                if r.getOverflow() == 0:
+                    break
+                cap = A.Capacity(cap.clip_vertices * 2, cap.clip_polygons * 2, cap.appended_primitives * 2,
+                                 cap.bin_entries * 2, hf)
+            g = None
+            if use_graph:
+                frame()   # the uncaptured run that sizes every working array
+                r.waitIdle()
+                g = Graph(r).capture(frame)
+                run = g.launch
+            else:
+                run = frame
+            for _ in range(2):
+                run()
+            ms = time_ms(run, reps)
+            ok = r.getOverflow() == 0
+            table.append({"heavy_first": hf, "graph": use_graph, "ms": round(ms, 4), "fits": ok})
+            if ok and (best is None or ms < best.ms):
+                if best_graph is not None:
+                    best_graph.destroy()
+                best = TuneResult(A.Capacity(cap.clip_vertices, cap.clip_polygons, cap.appended_primitives,
+                                             cap.bin_entries, hf), hf, use_graph, ms)
+                best_graph = g
+            elif g is not None:
+                g.destroy()
+    if best is None:
+        r.setCapacity(None)
+        raise RuntimeError("autotune: no candidate fitted its capacities")
+    best.table = table
+    r.setCapacity(best.capacity)
+    return Tuned(r, frame, best, best_graph)

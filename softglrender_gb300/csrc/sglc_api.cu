@@ -121,8 +121,10 @@ struct Object {
 struct DevBuf {
   void *ptr = nullptr;
   size_t bytes = 0;
+  static thread_local bool capturing;   // a graph capture is in progress on this thread
   cudaError_t ensure(size_t need) {
     if (need <= bytes) return cudaSuccess;
+    if (capturing) return cudaErrorStreamCaptureUnsupported;   // run the sequence once before capturing
     if (ptr) cudaFree(ptr);
     ptr = nullptr;
     bytes = 0;
@@ -140,6 +142,8 @@ struct DevBuf {
   template<typename T>
   T *as() const { return reinterpret_cast<T *>(ptr); }
 };
+
+thread_local bool DevBuf::capturing = false;
 
 struct PendingClear {
   int fb = 0;
@@ -172,6 +176,12 @@ struct Ctx {
       sortHistScan, staging, batchU, batchTargets;
   // capacity hints that survive between draws
   int extraVertHint = 0, polyHint = 0, appendHint = 0;
+  // synchronisation-free draws (sglc_set_capacity) and graph capture
+  bool capSet = false;
+  sglc_capacity cap{};
+  DevBuf sticky;                     // overflow flags accumulated over draws
+  bool capturing = false;
+  std::vector<void *> captureHostBufs;   // pinned host sources of memcpy nodes in the capture
   // neural IBL shader: training-record capture target
   float *capRecords = nullptr;
   unsigned long long *capCount = nullptr;
@@ -524,8 +534,20 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     numTiles *= bv->count;
     CK(c->batchU.ensure(bv->uniforms.size()));
     CK(c->batchTargets.ensure(sizeof(ViewTarget) * targets.size()));
-    CK(cudaMemcpyAsync(c->batchU.ptr, bv->uniforms.data(), bv->uniforms.size(), cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(c->batchTargets.ptr, targets.data(), sizeof(ViewTarget) * targets.size(), cudaMemcpyHostToDevice,
+    const void *srcU = bv->uniforms.data(), *srcT = targets.data();
+    if (c->capturing) {   // a captured copy reads its host source at every replay: keep it alive with the graph
+      void *hu = nullptr, *ht = nullptr;
+      CK(cudaMallocHost(&hu, bv->uniforms.size()));
+      c->captureHostBufs.push_back(hu);
+      CK(cudaMallocHost(&ht, sizeof(ViewTarget) * targets.size()));
+      c->captureHostBufs.push_back(ht);
+      memcpy(hu, srcU, bv->uniforms.size());
+      memcpy(ht, srcT, sizeof(ViewTarget) * targets.size());
+      srcU = hu;
+      srcT = ht;
+    }
+    CK(cudaMemcpyAsync(c->batchU.ptr, srcU, bv->uniforms.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->batchTargets.ptr, srcT, sizeof(ViewTarget) * targets.size(), cudaMemcpyHostToDevice,
                        c->stream));
     p.viewU = c->batchU.as<uint8_t>();
     p.viewTarget = c->batchTargets.as<ViewTarget>();
@@ -533,9 +555,15 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
   }
 
   for (int attempt = 0; attempt < 4; attempt++) {
+    const bool deferred = c->capSet;
     int extraVerts = std::max(std::max(4096, p.ntri / 2), c->extraVertHint);
     int polyCap = std::max(std::max(1024, p.ntri / 4), c->polyHint);
     int appendCap = std::max(std::max(1024, p.ntri / 4), c->appendHint);
+    if (deferred) {
+      extraVerts = (int) std::max<int64_t>(1, std::min<int64_t>(c->cap.clip_vertices, 1 << 28));
+      polyCap = (int) std::max<int64_t>(1, std::min<int64_t>(c->cap.clip_polygons, 1 << 28));
+      appendCap = (int) std::max<int64_t>(1, std::min<int64_t>(c->cap.appended_primitives, 1 << 28));
+    }
     p.vCap = p.nv + extraVerts;
     p.clipPolyCap = polyCap;
     p.primCap = p.ntri + appendCap;
@@ -578,19 +606,31 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     scanExclusive(p.tileCount, p.pairOff, p.counters + 3, p.primCap, c->scanScratch.as<int>(), c->stream);
     CK(cudaGetLastError());
     if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[1], c->stream));
-    CK(cudaMemcpyAsync(c->hostCounters, p.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(c->hostCounters + 4, p.pairOff + p.primCap, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    int newVerts = c->hostCounters[0], polys = c->hostCounters[1], flags = c->hostCounters[2];
-    int np = c->hostCounters[3];
-    if (flags & 16) return c->fail(SGLC_ERR_INVALID_VALUE, "draw: index out of range of the vertex array");
-    if (flags & 7) {   // clip-vertex / polygon / primitive capacity: grow and redo (nothing written yet)
-      c->extraVertHint = std::max(extraVerts * 2, newVerts + 1024);
-      c->polyHint = std::max(polyCap * 2, polys + 1024);
-      c->appendHint = std::max(appendCap * 2, p.primCap);
-      continue;
+    int newVerts = -1, polys = -1, np = p.primCap, nPairs;
+    const int *nPairsDev = p.pairOff + p.primCap;
+    if (!deferred) {
+      CK(cudaMemcpyAsync(c->hostCounters, p.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaMemcpyAsync(c->hostCounters + 4, p.pairOff + p.primCap, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      newVerts = c->hostCounters[0];
+      polys = c->hostCounters[1];
+      int flags = c->hostCounters[2];
+      np = c->hostCounters[3];
+      if (flags & 16) return c->fail(SGLC_ERR_INVALID_VALUE, "draw: index out of range of the vertex array");
+      if (flags & 7) {   // clip-vertex / polygon / primitive capacity: grow and redo (nothing written yet)
+        c->extraVertHint = std::max(extraVerts * 2, newVerts + 1024);
+        c->polyHint = std::max(polyCap * 2, polys + 1024);
+        c->appendHint = std::max(appendCap * 2, p.primCap);
+        continue;
+      }
+      nPairs = c->hostCounters[4];
+    } else {
+      // no read-back: the bin arrays have the set capacity, the sort and ranges read the pair count
+      // (clamped to it) from the device
+      nPairs = (int) std::max<int64_t>(1, std::min<int64_t>(c->cap.bin_entries, 1 << 30));
+      launchClampCount(p.pairOff + p.primCap, nPairs, p.counters + 4, c->stream);
+      nPairsDev = p.counters + 4;
     }
-    int nPairs = c->hostCounters[4];
     CK(c->keyA.ensure(sizeof(uint32_t) * (size_t) std::max(nPairs, 1)));
     CK(c->keyB.ensure(sizeof(uint32_t) * (size_t) std::max(nPairs, 1)));
     CK(c->valA.ensure(sizeof(int) * (size_t) std::max(nPairs, 1)));
@@ -614,12 +654,14 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     launchBinEmit(p, np, c->stream);
     int keyBits = 1;
     while ((1 << keyBits) < numTiles) keyBits++;
-    const int *nPairsDev = p.pairOff + p.primCap;
     sortPairs(p, nPairs, nPairsDev, keyBits, c->sortHist.as<int>(), c->sortHistScan.as<int>(),
               c->scanScratch.as<int>(), c->stream);
     launchTileRanges(p, nPairs, nPairsDev, c->stream);
-    launchTileOrder(p, c->tileOrder.as<int>(), c->stream);
-    p.tileOrder = c->tileOrder.as<int>();
+    const bool heavyFirst = !deferred || c->cap.heavy_first;
+    if (heavyFirst) {
+      launchTileOrder(p, c->tileOrder.as<int>(), c->stream);
+      p.tileOrder = c->tileOrder.as<int>();
+    }
     if (c->statsLevel >= 2) {
       CK(cudaMemsetAsync(c->fragCounter, 0, sizeof(unsigned long long), c->stream));
       p.fragCounter = c->fragCounter;
@@ -630,17 +672,18 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       CK(cudaEventRecord(c->ev[3], c->stream));
       c->evPending = true;
     }
+    if (deferred) launchAccumulateFlags(p.counters + 2, c->sticky.as<int>(), c->stream);
     CK(cudaGetLastError());
     if (ct && ct->desc.multi_sample) ct->resolvedValid = true;
     c->stats.vertices_in = p.nv;
     c->stats.triangles_in = p.ntri;
     c->stats.clip_vertices = newVerts;
-    c->stats.primitives = np;
-    c->stats.bin_entries = nPairs;
-    // vertex, clip, 3 scan, append, count, setup, 3 scan | emit, sort, ranges, raster
+    c->stats.primitives = deferred ? -1 : np;
+    c->stats.bin_entries = deferred ? -1 : nPairs;
+    // vertex, clip, 3 scan, append, count, setup, 3 scan | emit, sort, ranges, order, raster
     int sortPasses = nPairs > 0 ? (keyBits <= 8 ? 1 : 2) : 0;
     c->stats.kernel_launches = (p.nv > 0) + (p.ntri > 0) + 3 + 2 + 1 + 3 + (np > 0) + sortPasses * 5 +
-                               (nPairs > 0) + 1 + 1 + attempt * 10;
+                               (nPairs > 0) + (heavyFirst ? 1 : 0) + 1 + attempt * 10 + (deferred ? 2 : 0);
     return SGLC_OK;
   }
   return c->fail(SGLC_ERR_OVERFLOW, "draw: clip capacity could not be satisfied");
@@ -712,9 +755,11 @@ sglc_status sglc_destroy(sglc_context *ctx) {
   DevBuf *bufs[] = {&c->vClip, &c->vFrag, &c->vMask, &c->vVary, &c->vAttrExtra, &c->prims, &c->clipExtra,
                     &c->clipAppendOff, &c->clipPoly, &c->clipPolyTri, &c->counters, &c->tri, &c->tileCount,
                     &c->pairOff, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->tileStart, &c->tileEnd, &c->tileOrder,
-                    &c->scanScratch, &c->sortHist, &c->sortHistScan, &c->staging};
+                    &c->scanScratch, &c->sortHist, &c->sortHistScan, &c->staging, &c->batchU, &c->batchTargets,
+                    &c->sticky};
   for (DevBuf *b : bufs) b->release();
   cudaFreeHost(c->hostCounters);
+  for (void *h : c->captureHostBufs) cudaFreeHost(h);
   cudaFree(c->fragCounter);
   for (int i = 0; i < 4; i++)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
@@ -1200,6 +1245,35 @@ sglc_status sglc_draw_views(sglc_context *ctx, const sglc_handle *framebuffers, 
   return drawImpl(c, &bv);
 }
 
+sglc_status sglc_set_capacity(sglc_context *ctx, const sglc_capacity *cap) {
+  CTX;
+  if (c->capturing) return c->fail(SGLC_ERR_INVALID_VALUE, "set_capacity: not allowed during a graph capture");
+  if (!cap) {
+    c->capSet = false;
+    return SGLC_OK;
+  }
+  if (cap->clip_vertices < 1 || cap->clip_polygons < 1 || cap->appended_primitives < 1 || cap->bin_entries < 1)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "set_capacity: every capacity must be at least 1");
+  CK(c->sticky.ensure(sizeof(int)));
+  CK(cudaMemsetAsync(c->sticky.ptr, 0, sizeof(int), c->stream));
+  c->cap = *cap;
+  c->capSet = true;
+  return SGLC_OK;
+}
+
+sglc_status sglc_get_overflow(sglc_context *ctx, int32_t *flags) {
+  CTX;
+  if (!flags) return c->fail(SGLC_ERR_INVALID_VALUE, "get_overflow: null output");
+  if (c->capturing) return c->fail(SGLC_ERR_INVALID_VALUE, "get_overflow: not allowed during a graph capture");
+  *flags = 0;
+  if (!c->sticky.ptr) return SGLC_OK;
+  CK(cudaMemcpyAsync(c->hostCounters + 8, c->sticky.ptr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemsetAsync(c->sticky.ptr, 0, sizeof(int), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *flags = c->hostCounters[8];
+  return SGLC_OK;
+}
+
 sglc_status sglc_end_render_pass(sglc_context *ctx) {
   CTX;
   return flushClear(c);
@@ -1255,6 +1329,84 @@ sglc_status sglc_set_tile_size(sglc_context *ctx, int32_t tile) {
   CTX;
   if (tile != 16) return c->fail(SGLC_ERR_UNSUPPORTED, "set_tile_size: this build rasterises 16x16 tiles");
   c->tile = tile;
+  return SGLC_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------------------
+// CUDA graphs
+// ------------------------------------------------------------------------------------------------
+struct sglc_graph {
+  sglc_context *ctx = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<void *> hostBufs;
+};
+
+extern "C" {
+
+sglc_status sglc_graph_begin(sglc_context *ctx) {
+  CTX;
+  if (c->capturing) return c->fail(SGLC_ERR_INVALID_VALUE, "graph_begin: a capture is already in progress");
+  if (!c->capSet) return c->fail(SGLC_ERR_INVALID_VALUE, "graph_begin: set capacities first (sglc_set_capacity)");
+  sglc_status st = flushClear(c);
+  if (st) return st;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+  c->capturing = true;
+  DevBuf::capturing = true;
+  return SGLC_OK;
+}
+
+sglc_status sglc_graph_end(sglc_context *ctx, sglc_graph **out) {
+  CTX;
+  if (!out) return c->fail(SGLC_ERR_INVALID_VALUE, "graph_end: null output");
+  *out = nullptr;
+  if (!c->capturing) return c->fail(SGLC_ERR_INVALID_VALUE, "graph_end: no capture in progress");
+  flushClear(c);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  c->capturing = false;
+  DevBuf::capturing = false;
+  std::vector<void *> bufs;
+  bufs.swap(c->captureHostBufs);
+  if (e != cudaSuccess) {
+    for (void *h : bufs) cudaFreeHost(h);
+    if (g) cudaGraphDestroy(g);
+    return c->fail(SGLC_ERR_DEVICE, std::string("graph_end: capture failed: ") + cudaGetErrorString(e) +
+                                        " (run the sequence once before capturing; no synchronising calls inside)");
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, g, 0);
+  if (e != cudaSuccess) {
+    for (void *h : bufs) cudaFreeHost(h);
+    cudaGraphDestroy(g);
+    return c->fail(SGLC_ERR_DEVICE, std::string("graph_end: instantiate: ") + cudaGetErrorString(e));
+  }
+  sglc_graph *gr = new sglc_graph();
+  gr->ctx = ctx;
+  gr->graph = g;
+  gr->exec = exec;
+  gr->hostBufs.swap(bufs);
+  *out = gr;
+  return SGLC_OK;
+}
+
+sglc_status sglc_graph_launch(sglc_graph *g) {
+  if (!g || !g->exec) return SGLC_ERR_INVALID_VALUE;
+  Ctx *c = reinterpret_cast<Ctx *>(g->ctx);
+  CK(cudaGraphLaunch(g->exec, c->stream));
+  return SGLC_OK;
+}
+
+sglc_status sglc_graph_destroy(sglc_graph *g) {
+  if (!g) return SGLC_ERR_INVALID_VALUE;
+  Ctx *c = reinterpret_cast<Ctx *>(g->ctx);
+  cudaStreamSynchronize(c->stream);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  for (void *h : g->hostBufs) cudaFreeHost(h);
+  delete g;
   return SGLC_OK;
 }
 

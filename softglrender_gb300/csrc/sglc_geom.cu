@@ -599,6 +599,14 @@ void launchTileOrder(const DrawParams &p, int *order, cudaStream_t st) {
   k_tile_order<<<1, 1024, 0, st>>>(p.tileStart, p.tileEnd, p.views * p.tilesPerView, order);
 }
 
+__global__ void k_clamp_count(const int *src, int cap, int *dst) { *dst = min(*src, cap); }
+__global__ void k_accumulate_flags(const int *flags, int *sticky) { *sticky |= *flags; }
+
+void launchClampCount(const int *src, int cap, int *dst, cudaStream_t st) { k_clamp_count<<<1, 1, 0, st>>>(src, cap, dst); }
+void launchAccumulateFlags(const int *flags, int *sticky, cudaStream_t st) {
+  k_accumulate_flags<<<1, 1, 0, st>>>(flags, sticky);
+}
+
 void launchFill32(uint32_t *dst, uint32_t value, size_t n, cudaStream_t st) {
   if (n == 0) return;
   int grid = (int) min((size_t) 152 * 8, (n + 255) / 256);

@@ -20,6 +20,10 @@ void launchTileRanges(const DrawParams &p, int nPairs, const int *nPtr, cudaStre
 void launchTileOrder(const DrawParams &p, int *order, cudaStream_t st);
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 void launchFill32(uint32_t *dst, uint32_t value, size_t n, cudaStream_t st);
+// *dst = min(*src, cap) (device-side pair count of a synchronisation-free draw)
+void launchClampCount(const int *src, int cap, int *dst, cudaStream_t st);
+// *sticky |= *flags
+void launchAccumulateFlags(const int *flags, int *sticky, cudaStream_t st);
 void launchMipLevel(const DevTex &t, int face, int level, int isFloat, cudaStream_t st);
 void launchSwizzleIn(const DevTex &t, int face, int level, const uint32_t *src, cudaStream_t st);
 void launchSwizzleOut(const DevTex &t, int face, int level, uint32_t *dst, cudaStream_t st);

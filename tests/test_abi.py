@@ -19,7 +19,8 @@ def declared():
 
 
 # product-only extensions (no Renderer counterpart): not exported by the checkers; the allocation-free
-# draw is bound by its own test, the neural shader by softglrender_gb300/neural.py
+# draw is bound by its own test, the neural shader by softglrender_gb300/neural.py, CUDA graphs by
+# softglrender_gb300/graph.py
 PRODUCT_ONLY = {"sglc_draw_vertex_color_noalloc"}
 
 
@@ -27,8 +28,12 @@ def neural_abi():
     return [n for n in declared() if n.startswith("sglc_neural_") or n == "sglc_program_set_neural_shader"]
 
 
+def graph_abi():
+    return [n for n in declared() if n.startswith("sglc_graph_")]
+
+
 def renderer_abi():
-    return [n for n in declared() if n not in PRODUCT_ONLY and n not in neural_abi()]
+    return [n for n in declared() if n not in PRODUCT_ONLY and n not in neural_abi() and n not in graph_abi()]
 
 
 def exported(path):
@@ -59,6 +64,8 @@ def test_python_binding_covers_every_symbol():
     from softglrender_gb300.neural import NEURAL_FUNCTIONS
     assert sorted("sglc_" + n for n in ABI_FUNCTIONS) == renderer_abi()
     assert sorted("sglc_" + n for n in NEURAL_FUNCTIONS) == sorted(neural_abi())
+    from softglrender_gb300.graph import GRAPH_FUNCTIONS
+    assert sorted("sglc_" + n for n in GRAPH_FUNCTIONS) == sorted(graph_abi())
 
 
 def test_oracle_exports_same_abi(oracle_lib):
