@@ -36,6 +36,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-neural", action="store_true", help="skip training / timing the neural IBL shader")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-views measurement")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch measurement")
     return ap.parse_args()
 
 
@@ -255,6 +256,78 @@ def bench_batched_views(r, stream, with_cpu: bool):
     return out
 
 
+def bench_uneven(r, stream, net, neural_bound: bool, with_cpu: bool):
+    """64 independent scenes in one CUDA-graph submission (plain shaders, and with the neural IBL
+    shader bound to the PBR scenes when it met its threshold); per-scene frames/s from eager
+    submissions; the CPU pipeline on a sample of the scenes."""
+    import torch
+    from softglrender_gb300.autotune import autotune
+    from softglrender_gb300.neural import NeuralShader
+    from softglrender_gb300.uneven import UnevenBatch, UnevenConfig
+    cfg = UnevenConfig()
+    t0 = time.perf_counter()
+    u = UnevenBatch(r, cfg)
+    setup_s = time.perf_counter() - t0
+
+    def time_ms(fn, n):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for st, en in ev:
+            with torch.cuda.stream(stream):
+                st.record(stream)
+            fn()
+            with torch.cuda.stream(stream):
+                en.record(stream)
+        r.waitIdle()
+        torch.cuda.synchronize()
+        return float(np.median([st.elapsed_time(en) for st, en in ev]))
+
+    r.setCapacity(None)
+    u.render()
+    per_scene = [time_ms(lambda s=s: u.render_scene(s), 3) for s in range(cfg.scenes)]
+    out = {"workload": "uneven_64_scenes_1k_2M_tris_128_2048", "scenes": cfg.scenes,
+           "triangles_total": int(sum(u.triangles)), "setup_s": round(setup_s, 2)}
+    tuned = autotune(r, u.render, reps=3)
+    plain_ms = time_ms(tuned.run, 5)
+    out["plain"] = {"ms_per_batch": round(plain_ms, 3), "scenes_per_s": round(cfg.scenes / (plain_ms / 1e3), 1),
+                    "autotune": {k: v for k, v in tuned.result.describe().items() if k != "candidates"}}
+    tuned.destroy()
+    r.setCapacity(None)
+    if net is not None and neural_bound:
+        for prog in u.pbr_programs():
+            net.bind(prog)
+        tuned = autotune(r, u.render, reps=3)
+        n_ms = time_ms(tuned.run, 5)
+        out["neural"] = {"ms_per_batch": round(n_ms, 3), "scenes_per_s": round(cfg.scenes / (n_ms / 1e3), 1),
+                         "pbr_scenes_use_network": True}
+        tuned.destroy()
+        r.setCapacity(None)
+        for prog in u.pbr_programs():
+            NeuralShader.unbind(r, prog)
+    else:
+        out["neural"] = {"pbr_scenes_use_network": False, "reason": "network below its PSNR threshold (fallback)"}
+    out["per_scene_fps"] = [round(1e3 / m, 1) for m in per_scene]
+    out["per_scene"] = [{"tris": u.triangles[s], "res": u.plan[s]["res"], "pbr_msaa4": bool(u.plan[s]["pbr"]),
+                         "ms": round(per_scene[s], 4)} for s in range(cfg.scenes)]
+    if with_cpu:
+        import oracle
+        from softglrender_gb300 import api as A
+        lib = oracle.restatement()
+        rc = A.Renderer(lib, 0)
+        threads = os.cpu_count() or 1
+        lib.cdll.sglo_set_threads(rc.ctx, threads)
+        sample = list(range(8))
+        uc = UnevenBatch(rc, cfg, only=sample)
+        t0 = time.perf_counter()
+        uc.render(sample)
+        dt = time.perf_counter() - t0
+        rc.destroy()
+        gpu_sample_ms = sum(per_scene[s] for s in sample)
+        out["cpu_baseline"] = {"scenes_per_s": round(len(sample) / dt, 3), "cores": threads, "kind": "port",
+                               "sample": f"scenes 0-7 of {cfg.scenes} once ({dt:.1f} s); GPU eager time of the "
+                                         f"same scenes {gpu_sample_ms:.2f} ms"}
+    return out
+
+
 def main():
     args = parse()
     world, rank, local, pg = dist_setup()
@@ -368,13 +441,21 @@ def main():
             "train_s": round(rep.train_s, 3), "capture_s": round(rep.capture_s, 3), "final_loss": rep.final_loss,
             "views": {"train": 64, "held_out": 16},
         }
-        net.destroy()
 
     # ---- batched views: 256 orbit views of a 50k-triangle sphere at 256x256 after a 2048x2048
     # shadow pass, all views in one pipeline pass, submission chosen by the autotuner -----------
     batched = None
     if not args.no_batched:
         batched = bench_batched_views(r, stream, rank == 0 and not args.no_cpu_baseline)
+
+    # ---- uneven batch: 64 scenes of 1k-2M triangles at 128^2-2048^2, Blinn-Phong / PBR MSAA 4x
+    # with the neural shader (when it met its threshold), one graph submission -----------------
+    uneven = None
+    if not args.no_uneven:
+        uneven = bench_uneven(r, stream, net if neural is not None else None,
+                              bool(neural and neural["bound"]), rank == 0 and not args.no_cpu_baseline)
+    if neural is not None:
+        net.destroy()
 
     # ---- end to end through the public API with host buffers ----------------------------------
     pinned_v = torch.empty(d0.vertexes.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(np.float32)
@@ -434,6 +515,8 @@ def main():
         result["neural"] = neural
     if batched is not None:
         result["batched_views"] = batched
+    if uneven is not None:
+        result["uneven_batch"] = uneven
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         t0 = time.perf_counter()

@@ -505,6 +505,10 @@ sglc_status sglr_draw_views(sglc_context *ctx, const sglc_handle *fbs, const sgl
 
 // Capacities only change how the GPU back-end sizes its working arrays; RendererSoft has none.
 sglc_status sglr_set_capacity(sglc_context *, const sglc_capacity *) { return SGLC_OK; }
+sglc_status sglr_get_peak_counts(sglc_context *, sglc_capacity *out) {
+  if (out) *out = sglc_capacity{0, 0, 0, 0, 1};
+  return SGLC_OK;
+}
 sglc_status sglr_get_overflow(sglc_context *, int32_t *flags) {
   if (flags) *flags = 0;
   return SGLC_OK;

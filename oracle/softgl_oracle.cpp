@@ -1646,6 +1646,10 @@ sglc_status sglo_wait_idle(sglc_context *) { return SGLC_OK; }
 // Capacities only change how the GPU back-end sizes its working arrays; the CPU pipeline has no
 // capacities and never overflows.
 sglc_status sglo_set_capacity(sglc_context *, const sglc_capacity *) { return SGLC_OK; }
+sglc_status sglo_get_peak_counts(sglc_context *, sglc_capacity *out) {
+  if (out) *out = sglc_capacity{0, 0, 0, 0, 1};
+  return SGLC_OK;
+}
 sglc_status sglo_get_overflow(sglc_context *, int32_t *flags) {
   if (flags) *flags = 0;
   return SGLC_OK;

@@ -201,6 +201,7 @@ _SIGS = {
     "draw_views": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32, C.c_void_p],
     "set_capacity": [C.c_void_p, C.c_void_p],
     "get_overflow": [C.c_void_p, C.POINTER(C.c_int32)],
+    "get_peak_counts": [C.c_void_p, C.c_void_p],
     "set_tile_size": [C.c_void_p, C.c_int32],
 }
 
@@ -485,6 +486,11 @@ class Renderer:
     def setCapacity(self, cap: Optional[Capacity]) -> None:
         """Synchronisation-free draws with these capacities (None: exact sizing, one read-back per draw)."""
         self._call("set_capacity", C.byref(cap) if cap is not None else None)
+
+    def getPeakCounts(self) -> "Capacity":
+        c = Capacity()
+        self._call("get_peak_counts", C.byref(c))
+        return c
 
     def getOverflow(self) -> int:
         f = C.c_int32(0)

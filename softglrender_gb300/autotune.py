@@ -1,9 +1,10 @@
 """Autotuner for synchronisation-free frames: picks working-array capacities, the raster tile order
 and eager-versus-graph submission for a given frame by measuring them.
 
-1. Calibration: the frame runs once with exact sizing (one count read-back per draw); the largest
-   draw's counts (clip vertices, appended primitives, bin entries) times a headroom give the
-   capacities. A candidate that overflows (sglc_get_overflow) doubles them and is measured again.
+1. Calibration: the frame runs once with exact sizing (one count read-back per draw); the peak
+   counts over its draws (clip vertices and polygons, appended primitives, bin entries) times a
+   headroom give the capacities, doubled until the frame runs without overflow (sglc_get_overflow);
+   all candidates then share them.
 2. Candidates: raster tiles longest-list-first or in index order; the frame enqueued call by call
    or captured once in a CUDA graph and replayed. Each runs `reps` times after warm-up, timed with
    CUDA events on the renderer's stream; the fastest wins.
@@ -81,25 +82,31 @@ def autotune(r: A.Renderer, frame: Callable[[], None], headroom: float = 1.25, r
              heavy_first=(1, 0), graph=(False, True)) -> Tuned:
     time_ms = _timer(r)
     r.setCapacity(None)
+    r.getPeakCounts()   # reset
     frame()
     r.waitIdle()
-    st = r.drawStats()
-    appended = max(0, int(st["primitives"]) - int(st["triangles_in"]))
-    cap = A.Capacity(max(1024, int(max(0, st["clip_vertices"]) * headroom) + 1024),
-                     max(1024, int(appended * headroom) + 1024),
-                     max(1024, int(appended * headroom) + 1024),
-                     max(4096, int(int(st["bin_entries"]) * headroom) + 4096), 1)
+    pk = r.getPeakCounts()
+    cap = A.Capacity(max(1024, int(pk.clip_vertices * headroom) + 1024),
+                     max(1024, int(pk.clip_polygons * headroom) + 1024),
+                     max(1024, int(pk.appended_primitives * headroom) + 1024),
+                     max(4096, int(pk.bin_entries * headroom) + 4096), 1)
+    # fit the capacities once (eager); every candidate then uses them unchanged, so no working array
+    # grows (and no captured graph loses its buffers) after the first capture
+    for _ in range(8):
+        r.setCapacity(cap)
+        frame()
+        if r.getOverflow() == 0:
+            break
+        cap = A.Capacity(cap.clip_vertices * 2, cap.clip_polygons * 2, cap.appended_primitives * 2,
+                         cap.bin_entries * 2, 1)
+    else:
+        r.setCapacity(None)
+        raise RuntimeError("autotune: the frame does not fit its capacities")
     table, best, best_graph = [], None, None
     for hf in heavy_first:
         for use_graph in graph:
             cap.heavy_first = hf
-            for _ in range(4):   # grow until the frame fits
-                r.setCapacity(cap)
-                frame()
-                if r.getOverflow() == 0:
-                    break
-                cap = A.Capacity(cap.clip_vertices * 2, cap.clip_polygons * 2, cap.appended_primitives * 2,
-                                 cap.bin_entries * 2, hf)
+            r.setCapacity(cap)
             g = None
             if use_graph:
                 frame()   # the uncaptured run that sizes every working array

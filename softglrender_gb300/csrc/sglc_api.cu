@@ -5,6 +5,7 @@
 // (ShaderProgram::bindResources, src/Render/ShaderProgram.h:27-54; UniformSoft.h:26-29,79-82);
 // draw() enqueues the geometry, binning and raster kernels on the context's stream.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -117,6 +118,11 @@ struct Object {
   std::map<int, int> resBlocks, resSamplers;
 };
 
+// Process-wide count of device frees by the renderer: a CUDA graph records device addresses, so a
+// graph captured before any buffer it uses was freed (a working array grown, a resource
+// released) must not be replayed; sglc_graph_launch compares this count with the capture's.
+std::atomic<unsigned long long> g_freeEpoch{0};
+
 // grow-only device buffer
 struct DevBuf {
   void *ptr = nullptr;
@@ -125,7 +131,10 @@ struct DevBuf {
   cudaError_t ensure(size_t need) {
     if (need <= bytes) return cudaSuccess;
     if (capturing) return cudaErrorStreamCaptureUnsupported;   // run the sequence once before capturing
-    if (ptr) cudaFree(ptr);
+    if (ptr) {
+      cudaFree(ptr);
+      g_freeEpoch++;
+    }
     ptr = nullptr;
     bytes = 0;
     size_t n = std::max(need, (size_t) 256);
@@ -135,7 +144,10 @@ struct DevBuf {
     return e;
   }
   void release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) {
+      cudaFree(ptr);
+      g_freeEpoch++;
+    }
     ptr = nullptr;
     bytes = 0;
   }
@@ -179,8 +191,10 @@ struct Ctx {
   // synchronisation-free draws (sglc_set_capacity) and graph capture
   bool capSet = false;
   sglc_capacity cap{};
+  sglc_capacity peak{};              // largest counts of exactly sized draws since the last query
   DevBuf sticky;                     // overflow flags accumulated over draws
   bool capturing = false;
+  unsigned long long captureEpoch = 0;
   std::vector<void *> captureHostBufs;   // pinned host sources of memcpy nodes in the capture
   // neural IBL shader: training-record capture target
   float *capRecords = nullptr;
@@ -281,6 +295,7 @@ sglc_status allocTexture(Ctx *c, TexObj &t) {
 }
 
 void freeTexture(TexObj &t) {
+  if (t.dev || t.resolved) g_freeEpoch++;
   if (t.dev) cudaFree(t.dev);
   if (t.resolved) cudaFree(t.resolved);
   t.dev = nullptr;
@@ -624,6 +639,10 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
         continue;
       }
       nPairs = c->hostCounters[4];
+      c->peak.clip_vertices = std::max<int64_t>(c->peak.clip_vertices, newVerts);
+      c->peak.clip_polygons = std::max<int64_t>(c->peak.clip_polygons, polys);
+      c->peak.appended_primitives = std::max<int64_t>(c->peak.appended_primitives, (int64_t) np - p.ntri);
+      c->peak.bin_entries = std::max<int64_t>(c->peak.bin_entries, nPairs);
     } else {
       // no read-back: the bin arrays have the set capacity, the sort and ranges read the pair count
       // (clamped to it) from the device
@@ -782,6 +801,7 @@ sglc_status sglc_release(sglc_context *ctx, sglc_handle h) {
   if (it->second.kind == K_VAO) {
     cudaFree(it->second.vao.attr);
     cudaFree(it->second.vao.idx);
+    g_freeEpoch++;
   }
   c->objects.erase(it);
   return SGLC_OK;
@@ -1261,6 +1281,15 @@ sglc_status sglc_set_capacity(sglc_context *ctx, const sglc_capacity *cap) {
   return SGLC_OK;
 }
 
+sglc_status sglc_get_peak_counts(sglc_context *ctx, sglc_capacity *out) {
+  CTX;
+  if (!out) return c->fail(SGLC_ERR_INVALID_VALUE, "get_peak_counts: null output");
+  *out = c->peak;
+  out->heavy_first = 1;
+  c->peak = sglc_capacity{};
+  return SGLC_OK;
+}
+
 sglc_status sglc_get_overflow(sglc_context *ctx, int32_t *flags) {
   CTX;
   if (!flags) return c->fail(SGLC_ERR_INVALID_VALUE, "get_overflow: null output");
@@ -1339,6 +1368,7 @@ sglc_status sglc_set_tile_size(sglc_context *ctx, int32_t tile) {
 // ------------------------------------------------------------------------------------------------
 struct sglc_graph {
   sglc_context *ctx = nullptr;
+  unsigned long long epoch = 0;   // g_freeEpoch when the capture began
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<void *> hostBufs;
@@ -1353,6 +1383,7 @@ sglc_status sglc_graph_begin(sglc_context *ctx) {
   sglc_status st = flushClear(c);
   if (st) return st;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+  c->captureEpoch = g_freeEpoch.load();
   c->capturing = true;
   DevBuf::capturing = true;
   return SGLC_OK;
@@ -1385,6 +1416,7 @@ sglc_status sglc_graph_end(sglc_context *ctx, sglc_graph **out) {
   }
   sglc_graph *gr = new sglc_graph();
   gr->ctx = ctx;
+  gr->epoch = c->captureEpoch;
   gr->graph = g;
   gr->exec = exec;
   gr->hostBufs.swap(bufs);
@@ -1395,6 +1427,9 @@ sglc_status sglc_graph_end(sglc_context *ctx, sglc_graph **out) {
 sglc_status sglc_graph_launch(sglc_graph *g) {
   if (!g || !g->exec) return SGLC_ERR_INVALID_VALUE;
   Ctx *c = reinterpret_cast<Ctx *>(g->ctx);
+  if (g_freeEpoch.load() != g->epoch)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "graph_launch: a buffer the graph uses was freed or grown since the capture; "
+                                           "capture it again");
   CK(cudaGraphLaunch(g->exec, c->stream));
   return SGLC_OK;
 }

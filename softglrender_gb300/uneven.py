@@ -1,0 +1,180 @@
+"""Uneven batch: many independent scenes of very different size rendered as one submission.
+
+Each scene is a seeded displaced sphere whose triangle count is drawn log-uniformly from
+[tri_min, tri_max] and whose square resolution is drawn from `resolutions`; even scenes use
+directional Blinn-Phong without MSAA, odd scenes PBR+IBL with 4x MSAA (the material, textures and
+IBL maps of the 1080p PBR scene, shared by all PBR scenes), optionally with the neural IBL shader
+bound when it met its PSNR threshold (per material; otherwise the plain shader stays: the
+fallback). `render()` issues the scenes one render pass each; on the GPU the whole sequence is
+captured once in a CUDA graph (softglrender_gb300/graph.py) and replayed with one launch, each
+scene's kernels running in order inside it. Meshes with the same tessellation share their
+displacement seed (the tessellation is rounded to a multiple of 16 longitude segments), which keeps
+the set-up time of 64 scenes of up to 2M triangles within seconds.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+from . import api as A
+from . import scenes as S
+
+
+@dataclass
+class UnevenConfig:
+    scenes: int = 64
+    tri_min: int = 1000
+    tri_max: int = 2_000_000
+    resolutions: Tuple[int, ...] = (128, 512, 1024, 2048)
+    seed: int = 5000
+    pbr_tex: int = 1024
+    prefilter: int = 512
+    irradiance: int = 32
+    blinn_tex: int = 512
+
+
+def scene_plan(cfg: UnevenConfig) -> List[Dict[str, int]]:
+    """(kind, longitude segments, latitude segments, resolution, samples) of every scene."""
+    plan = []
+    for s in range(cfg.scenes):
+        u = float(S.hash_u01(cfg.seed, 70, s))
+        tris = float(np.exp(np.log(cfg.tri_min) + u * (np.log(cfg.tri_max) - np.log(cfg.tri_min))))
+        lon = max(16, int(round(np.sqrt(tris) / 16.0)) * 16)   # 2 lon (lat - 1) ~ tris with lat = lon / 2
+        lat = max(8, lon // 2)
+        res = cfg.resolutions[int(S.hash_u01(cfg.seed, 71, s) * len(cfg.resolutions)) % len(cfg.resolutions)]
+        pbr = s % 2 == 1
+        plan.append({"pbr": int(pbr), "lon": lon, "lat": lat, "res": res, "samples": 4 if pbr else 1})
+    return plan
+
+
+class UnevenBatch:
+    def __init__(self, r: A.Renderer, cfg: Optional[UnevenConfig] = None, only: Optional[List[int]] = None):
+        """`only`: create just these scenes (the others are skipped by render())."""
+        self.r = r
+        self.cfg = cfg = cfg or UnevenConfig()
+        self.plan = scene_plan(cfg)
+        self.only = set(range(cfg.scenes)) if only is None else set(only)
+        meshes: Dict[int, A.VertexArrayObject] = {}
+        self.triangles = []
+        # shared materials
+        tdesc = A.TextureDesc(cfg.pbr_tex, cfg.pbr_tex, A.TextureType_2D, A.TextureFormat_RGBA8,
+                              A.TextureUsage_Sampler | A.TextureUsage_UploadData, True, False)
+        trilinear = A.SamplerDesc(A.Filter_LINEAR_MIPMAP_LINEAR, A.Filter_LINEAR, A.Wrap_REPEAT, A.Wrap_REPEAT,
+                                  A.Wrap_REPEAT)
+        pbr_samplers = []
+        for k, (name, kind) in enumerate((("u_albedoMap", "albedo"), ("u_normalMap", "normal"),
+                                          ("u_metalRoughnessMap", "metal_rough"))):
+            t = r.createTexture(tdesc)
+            t.setSamplerDesc(trilinear)
+            t.setImageData([S.noise_texture(cfg.pbr_tex, 3000 + 10 * (k + 1), kind)])
+            us = r.createUniformSampler(name, tdesc)
+            us.setTexture(t)
+            pbr_samplers.append(us)
+        pre, irr = S.ibl_maps(3000, cfg.prefilter, cfg.irradiance)
+        cdesc = A.TextureDesc(cfg.irradiance, cfg.irradiance, A.TextureType_CUBE, A.TextureFormat_RGBA8,
+                              A.TextureUsage_Sampler | A.TextureUsage_UploadData, False, False)
+        t = r.createTexture(cdesc)
+        t.setSamplerDesc(A.SamplerDesc(A.Filter_LINEAR, A.Filter_LINEAR, A.Wrap_CLAMP_TO_EDGE, A.Wrap_CLAMP_TO_EDGE,
+                                       A.Wrap_CLAMP_TO_EDGE))
+        t.setImageData(irr)
+        us = r.createUniformSampler("u_irradianceMap", cdesc)
+        us.setTexture(t)
+        pbr_samplers.append(us)
+        pdesc = A.TextureDesc(cfg.prefilter, cfg.prefilter, A.TextureType_CUBE, A.TextureFormat_RGBA8,
+                              A.TextureUsage_Sampler, True, False)
+        t = r.createTexture(pdesc)
+        t.setSamplerDesc(A.SamplerDesc(A.Filter_LINEAR_MIPMAP_LINEAR, A.Filter_LINEAR, A.Wrap_CLAMP_TO_EDGE,
+                                       A.Wrap_CLAMP_TO_EDGE, A.Wrap_CLAMP_TO_EDGE))
+        t.initImageData()
+        for lev, imgs in enumerate(pre):
+            for layer, img in enumerate(imgs):
+                t.setLevelData(layer, lev, img)
+        us = r.createUniformSampler("u_prefilterMap", pdesc)
+        us.setTexture(t)
+        pbr_samplers.append(us)
+        bdesc = A.TextureDesc(cfg.blinn_tex, cfg.blinn_tex, A.TextureType_2D, A.TextureFormat_RGBA8,
+                              A.TextureUsage_Sampler | A.TextureUsage_UploadData, True, False)
+        bt = r.createTexture(bdesc)
+        bt.setSamplerDesc(trilinear)
+        bt.setImageData([S.checkerboard(cfg.blinn_tex, 8, cfg.seed)])
+        blinn_sampler = r.createUniformSampler("u_albedoMap", bdesc)
+        blinn_sampler.setTexture(bt)
+        self.states = r.createPipelineStates(A.RenderStates(depthTest=True, depthMask=True,
+                                                            depthFunc=A.DepthFunc_LESS, cullFace=True))
+        self.items: Dict[int, dict] = {}
+        for s, pl in enumerate(self.plan):
+            if s not in self.only:
+                self.triangles.append(2 * pl["lon"] * (pl["lat"] - 1))
+                continue
+            key = pl["lon"]
+            if key not in meshes:
+                vert, idx = S.uv_sphere(pl["lon"], pl["lat"], 1.0, displace_seed=cfg.seed + key, amplitude=0.1)
+                meshes[key] = (r.createVertexArrayObject(vert, 64, idx), len(idx) // 3)
+            vao, ntri = meshes[key]
+            self.triangles.append(ntri)
+            res = pl["res"]
+            prog = r.createShaderProgram()
+            resources = r.createShaderResources()
+            if pl["pbr"]:
+                prog.addDefines(("ALBEDO_MAP", "NORMAL_MAP", "METALROUGHNESS_MAP"))
+                prog.SetShaders(A.Shading_PBR)
+                blocks = S.pbr_view_blocks(cfg.seed + 1, s, res, res)
+                for k, us in enumerate(pbr_samplers):
+                    resources.setSampler(k, us)
+            else:
+                prog.addDefines(("ALBEDO_MAP",))
+                prog.SetShaders(A.Shading_BlinnPhongDir)
+                yaw = 2.0 * np.pi * S.hash_u01(cfg.seed, 72, s)
+                eye = np.array([3.0 * S.det_sin(yaw), 0.8, 3.0 * S.det_cos(yaw)])
+                Pm = S.perspective(np.pi / 3.0, 1.0, 0.05, False)
+                Vm = S.look_at(eye, [0, 0, 0], [0, 1, 0])
+                light = S.normalize(np.array([0.5, 0.7, 0.5]))
+                blocks = {"UniformsModel": S.uniforms_model(np.eye(4), S.mm4(Pm, Vm), None, False),
+                          "UniformsScene": S.uniforms_scene([0.15, 0.15, 0.15], eye, light, [1.0, 1.0, 1.0]),
+                          "UniformsMaterial": S.uniforms_material(True, False, False, 1.0, 0.6, [1, 1, 1, 1])}
+                resources.setSampler(0, blinn_sampler)
+            for name, data in blocks.items():
+                ub = r.createUniformBlock(name, len(data))
+                ub.setData(data)
+                resources.setBlock(S._BLOCK_KEYS[name], ub)
+            ms = pl["samples"] > 1
+            ct = r.createTexture(A.TextureDesc(res, res, A.TextureType_2D, A.TextureFormat_RGBA8,
+                                               A.TextureUsage_AttachmentColor | A.TextureUsage_RendererOutput,
+                                               False, ms))
+            ct.initImageData()
+            dt = r.createTexture(A.TextureDesc(res, res, A.TextureType_2D, A.TextureFormat_FLOAT32,
+                                               A.TextureUsage_AttachmentDepth, False, ms))
+            dt.initImageData()
+            fbo = r.createFrameBuffer(offscreen=True)
+            fbo.setColorAttachment(ct, 0)
+            fbo.setDepthAttachment(dt)
+            self.items[s] = {"vao": vao, "prog": prog, "res": resources, "fbo": fbo, "color": ct, "depth": dt,
+                             "size": res, "pbr": bool(pl["pbr"])}
+        self.clear = A.ClearStates(True, True, (0.02, 0.02, 0.03, 1.0), 1.0)
+
+    def pbr_programs(self) -> List[A.ShaderProgram]:
+        return [it["prog"] for it in self.items.values() if it["pbr"]]
+
+    def render_scene(self, s: int) -> None:
+        r, it = self.r, self.items[s]
+        r.beginRenderPass(it["fbo"], self.clear)
+        r.setViewPort(0, 0, it["size"], it["size"])
+        r.setVertexArrayObject(it["vao"])
+        r.setShaderProgram(it["prog"])
+        r.setShaderResources(it["res"])
+        r.setPipelineStates(self.states)
+        r.draw()
+        r.endRenderPass()
+
+    def render(self, scenes: Optional[List[int]] = None) -> None:
+        for s in (sorted(self.items) if scenes is None else scenes):
+            self.render_scene(s)
+
+    def outputs(self, s: int):
+        it = self.items[s]
+        out = {"color": it["color"].readImage(), "depth": it["depth"].readImage()}
+        if it["pbr"]:
+            out["resolved"] = it["color"].readImage(resolved=True)
+        return out
