@@ -89,6 +89,9 @@ enum {
   SGLC_SHADING_BASE_COLOR = 1,          /* Shader/Software/BasicSoft.h:62-79 */
   SGLC_SHADING_BLINN_PHONG = 2,         /* Shader/Software/BlinnPhongSoft.h:181-325 (point light) */
   SGLC_SHADING_PBR = 3,                 /* Shader/Software/PbrSoft.h:106-323 */
+  SGLC_SHADING_SKYBOX = 4,              /* Shader/Software/SkyboxSoft.h:42-107 (equirectangular or cube) */
+  SGLC_SHADING_IBL_IRRADIANCE = 5,      /* Shader/Software/IBLIrradianceSoft.h:40-105 */
+  SGLC_SHADING_IBL_PREFILTER = 6,       /* Shader/Software/IBLPrefilterSoft.h:44-172 */
   SGLC_SHADING_BLINN_PHONG_DIR = 100,   /* Blinn-Phong, directional light, shininess 32 */
   SGLC_SHADING_VERTEX_COLOR = 101,      /* per-vertex RGBA colour */
 };

@@ -24,6 +24,9 @@
 #include "Viewer/Shader/Software/BasicSoft.h"
 #include "Viewer/Shader/Software/BlinnPhongSoft.h"
 #include "Viewer/Shader/Software/PbrSoft.h"
+#include "Viewer/Shader/Software/SkyboxSoft.h"
+#include "Viewer/Shader/Software/IBLIrradianceSoft.h"
+#include "Viewer/Shader/Software/IBLPrefilterSoft.h"
 #include "extra_shaders_soft.h"
 #include "softgl_cuda.h"
 
@@ -324,6 +327,9 @@ sglc_status sglr_program_set_shaders(sglc_context *ctx, sglc_handle prog, int32_
     case SGLC_SHADING_BASE_COLOR: SOFT_SHADERS(ShaderBasic); break;
     case SGLC_SHADING_BLINN_PHONG: SOFT_SHADERS(ShaderBlinnPhong); break;
     case SGLC_SHADING_PBR: SOFT_SHADERS(ShaderPbrIBL); break;
+    case SGLC_SHADING_SKYBOX: SOFT_SHADERS(ShaderSkybox); break;
+    case SGLC_SHADING_IBL_IRRADIANCE: SOFT_SHADERS(ShaderIBLIrradiance); break;
+    case SGLC_SHADING_IBL_PREFILTER: SOFT_SHADERS(ShaderIBLPrefilter); break;
     case SGLC_SHADING_BLINN_PHONG_DIR: SOFT_SHADERS(ShaderBlinnPhongDir); break;
     case SGLC_SHADING_VERTEX_COLOR: SOFT_SHADERS(ShaderVertexColor); break;
     default: return c->fail(SGLC_ERR_UNSUPPORTED, "unknown shading model");

@@ -136,25 +136,32 @@ struct ShaderInfo {
   std::vector<UniformDesc> uniforms;
   int uniformSize;
   int varyingsCnt;   // floats actually interpolated (sizeof(ShaderVaryings)/4)
+  int derivSlots;    // sampler slots whose LOD callback the FS installs (setupSamplerDerivative)
 };
 
 // Uniform / varying layouts of the reference shaders with GLM aligned types (probe-checked):
 // BlinnPhongSoft.h:110-150, PbrSoft.h:29-72, BasicSoft.h:24-42.
 static const ShaderInfo kShaders[] = {
-    {SGLC_SHADING_BASE_COLOR, {}, {{"UniformsModel", 0, -1}, {"UniformsMaterial", 256, -1}}, 304, 0},
+    {SGLC_SHADING_BASE_COLOR, {}, {{"UniformsModel", 0, -1}, {"UniformsMaterial", 256, -1}}, 304, 0, 0},
     {SGLC_SHADING_BLINN_PHONG, {"ALBEDO_MAP", "NORMAL_MAP", "EMISSIVE_MAP", "AO_MAP"},
      {{"UniformsModel", 0, -1}, {"UniformsScene", 256, -1}, {"UniformsMaterial", 320, -1},
       {"u_albedoMap", 368, 0}, {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3},
-      {"u_shadowMap", 400, 4}}, 416, 32},
+      {"u_shadowMap", 400, 4}}, 416, 32, 0xF},
     {SGLC_SHADING_PBR, {"ALBEDO_MAP", "NORMAL_MAP", "EMISSIVE_MAP", "AO_MAP", "METALROUGHNESS_MAP"},
      {{"UniformsModel", 0, -1}, {"UniformsScene", 256, -1}, {"UniformsMaterial", 320, -1},
       {"u_albedoMap", 368, 0}, {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3},
-      {"u_metalRoughnessMap", 400, 4}, {"u_irradianceMap", 408, 5}, {"u_prefilterMap", 416, 6}}, 432, 28},
+      {"u_metalRoughnessMap", 400, 4}, {"u_irradianceMap", 408, 5}, {"u_prefilterMap", 416, 6}}, 432, 28, 0xF},
+    // SkyboxSoft.h:24-61, IBLIrradianceSoft.h:24-56, IBLPrefilterSoft.h:24-61
+    {SGLC_SHADING_SKYBOX, {"EQUIRECTANGULAR_MAP"},
+     {{"UniformsModel", 0, -1}, {"u_equirectangularMap", 256, 0}, {"u_cubeMap", 264, 1}}, 272, 4, 0},
+    {SGLC_SHADING_IBL_IRRADIANCE, {}, {{"UniformsModel", 0, -1}, {"u_cubeMap", 256, 0}}, 264, 4, 0},
+    {SGLC_SHADING_IBL_PREFILTER, {},
+     {{"UniformsModel", 0, -1}, {"UniformsPrefilter", 256, -1}, {"u_cubeMap", 264, 0}}, 272, 4, 0},
     {SGLC_SHADING_BLINN_PHONG_DIR, {"ALBEDO_MAP", "NORMAL_MAP", "EMISSIVE_MAP", "AO_MAP"},
      {{"UniformsModel", 0, -1}, {"UniformsScene", 256, -1}, {"UniformsMaterial", 320, -1},
       {"u_albedoMap", 368, 0}, {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3},
-      {"u_shadowMap", 400, 4}}, 416, 32},
-    {SGLC_SHADING_VERTEX_COLOR, {}, {{"UniformsModel", 0, -1}, {"UniformsMaterial", 256, -1}}, 304, 4},
+      {"u_shadowMap", 400, 4}}, 416, 32, 0xF},
+    {SGLC_SHADING_VERTEX_COLOR, {}, {{"UniformsModel", 0, -1}, {"UniformsMaterial", 256, -1}}, 304, 4, 0},
 };
 
 static const ShaderInfo *findShader(int model) {
@@ -453,6 +460,16 @@ static void runVS(const DrawState &ds, const float *a, float *v, V4 *pos) {
   switch (ds.shader->model) {
     case SGLC_SHADING_BASE_COLOR:
       break;
+    case SGLC_SHADING_SKYBOX:   // SkyboxSoft.h:67-76
+      *pos = {pos->x, pos->y, pos->w, pos->w};
+      if (U_REVERSEZ(u)) pos->z = 0.f;
+      v[0] = a[0]; v[1] = a[1]; v[2] = a[2];
+      break;
+    case SGLC_SHADING_IBL_IRRADIANCE:   // IBLIrradianceSoft.h:62-67, IBLPrefilterSoft.h:67-72
+    case SGLC_SHADING_IBL_PREFILTER:
+      pos->z = pos->w;
+      v[0] = a[0]; v[1] = a[1]; v[2] = a[2];
+      break;
     case SGLC_SHADING_VERTEX_COLOR:
       v[0] = a[4];
       v[1] = a[5];
@@ -708,6 +725,96 @@ static V4 fsPbr(const DrawState &ds, const FragIn &f) {
   return {c.x, c.y, c.z, arg.w};
 }
 
+// ---- environment shaders drawn into cube faces by IBLGenerator (Environment.cpp:152-195) ---------
+static V4 fsSkybox(const DrawState &ds, const FragIn &f) {
+  // SkyboxSoft.h:84-103
+  V3 wp = load3(f.v);
+  if (ds.def[0]) {   // EQUIRECTANGULAR_MAP: SampleSphericalMap
+    V3 dir = normalize3(wp);
+    float u = std::atan2(dir.z, dir.x), v = std::asin(-dir.y);
+    u = u * 0.1591f + 0.5f;
+    v = v * 0.3183f + 0.5f;
+    return tex2D(ds, 0, u, v, f);
+  }
+  return texCube(ds, 1, wp, 0.f);
+}
+
+static V4 fsIrradiance(const DrawState &ds, const FragIn &f) {
+  // IBLIrradianceSoft.h:75-101
+  const float PI = 3.14159265359f;
+  V3 N = normalize3(load3(f.v));
+  V3 irradiance{0.f, 0.f, 0.f};
+  V3 up{0.0f, 1.0f, 0.0f};
+  V3 right = normalize3(cross3(up, N));
+  up = normalize3(cross3(N, right));
+  const float sampleDelta = 0.025f;
+  float nrSamples = 0.0f;
+  for (float phi = 0.0f; phi < 2.0f * PI; phi += sampleDelta) {
+    for (float theta = 0.0f; theta < 0.5f * PI; theta += sampleDelta) {
+      V3 ts{std::sin(theta) * std::cos(phi), std::sin(theta) * std::sin(phi), std::cos(theta)};
+      V3 sampleVec = ts.x * right + ts.y * up + ts.z * N;
+      V4 c = texCube(ds, 0, sampleVec, 0.f);
+      irradiance = irradiance + V3{c.x, c.y, c.z} * std::cos(theta) * std::sin(theta);
+      nrSamples++;
+    }
+  }
+  irradiance = PI * irradiance * (1.0f / nrSamples);
+  return {irradiance.x, irradiance.y, irradiance.z, 1.0f};
+}
+
+static float radicalInverseVdC(uint32_t bits) {
+  // IBLPrefilterSoft.h:93-100 (Hammersley point set, van der Corput radical inverse)
+  bits = (bits << 16u) | (bits >> 16u);
+  bits = ((bits & 0x55555555u) << 1u) | ((bits & 0xAAAAAAAAu) >> 1u);
+  bits = ((bits & 0x33333333u) << 2u) | ((bits & 0xCCCCCCCCu) >> 2u);
+  bits = ((bits & 0x0F0F0F0Fu) << 4u) | ((bits & 0xF0F0F0F0u) >> 4u);
+  bits = ((bits & 0x00FF00FFu) << 8u) | ((bits & 0xFF00FF00u) >> 8u);
+  return float(bits * 2.3283064365386963e-10);
+}
+
+static V4 fsPrefilter(const DrawState &ds, const FragIn &f) {
+  // IBLPrefilterSoft.h:101-170
+  const float PI = 3.14159265359f;
+  const float srcResolution = *(const float *) (ds.u + 256), roughness = *(const float *) (ds.u + 260);
+  V3 N = normalize3(load3(f.v));
+  V3 V = N;
+  const uint32_t SAMPLE_COUNT = 1024u;
+  V3 color{0.f, 0.f, 0.f};
+  float totalWeight = 0.0f;
+  for (uint32_t i = 0u; i < SAMPLE_COUNT; ++i) {
+    float xi0 = float(i) / float(SAMPLE_COUNT), xi1 = radicalInverseVdC(i);
+    float a = roughness * roughness;
+    float phi = 2.0f * PI * xi0;
+    float cosTheta = std::sqrt((1.0f - xi1) / (1.0f + (a * a - 1.0f) * xi1));
+    float sinTheta = std::sqrt(1.0f - cosTheta * cosTheta);
+    V3 H{std::cos(phi) * sinTheta, std::sin(phi) * sinTheta, cosTheta};
+    V3 upv = std::fabs(N.z) < 0.999 ? V3{0.0f, 0.0f, 1.0f} : V3{1.0f, 0.0f, 0.0f};
+    V3 tangent = normalize3(cross3(upv, N));
+    V3 bitangent = cross3(N, tangent);
+    H = normalize3(tangent * H.x + bitangent * H.y + N * H.z);
+    V3 L = normalize3(2.0f * dot3(V, H) * H - V);
+    float NdotL = gmax(dot3(N, L), 0.0f);
+    if (NdotL > 0.0f) {
+      float a2 = a * a;
+      float NdotH = gmax(dot3(N, H), 0.0f);
+      float NdotH2 = NdotH * NdotH;
+      float denom = (NdotH2 * (a2 - 1.0f) + 1.0f);
+      denom = PI * denom * denom;
+      float D = a2 / denom;
+      float HdotV = gmax(dot3(H, V), 0.0f);
+      float pdf = D * NdotH / (4.0f * HdotV) + 0.0001f;
+      float saTexel = 4.0f * PI / (6.0f * srcResolution * srcResolution);
+      float saSample = 1.0f / (float(SAMPLE_COUNT) * pdf + 0.0001f);
+      float mipLevel = roughness == 0.0f ? 0.0f : 0.5f * std::log2(saSample / saTexel);
+      V4 c = texCube(ds, 0, L, mipLevel);
+      color = color + V3{c.x, c.y, c.z} * NdotL;
+      totalWeight += NdotL;
+    }
+  }
+  color = color / totalWeight;
+  return {color.x, color.y, color.z, 1.0f};
+}
+
 static V4 runFS(const DrawState &ds, const FragIn &f) {
   switch (ds.shader->model) {
     case SGLC_SHADING_BASE_COLOR: return U_BASECOLOR(ds.u, 256);
@@ -715,6 +822,9 @@ static V4 runFS(const DrawState &ds, const FragIn &f) {
     case SGLC_SHADING_BLINN_PHONG: return fsBlinnPhong(ds, f, false);
     case SGLC_SHADING_BLINN_PHONG_DIR: return fsBlinnPhong(ds, f, true);
     case SGLC_SHADING_PBR: return fsPbr(ds, f);
+    case SGLC_SHADING_SKYBOX: return fsSkybox(ds, f);
+    case SGLC_SHADING_IBL_IRRADIANCE: return fsIrradiance(ds, f);
+    case SGLC_SHADING_IBL_PREFILTER: return fsPrefilter(ds, f);
   }
   return {0, 0, 0, 0};
 }
@@ -1083,7 +1193,7 @@ static sglc_status doDraw(Ctx *c) {
     ds.sampH[s] = us.height;
     // only samplers whose LOD callback the FS installs (setupSamplerDerivative: albedo, normal,
     // emissive, ao; BlinnPhongSoft.h:217-230, PbrSoft.h:138-151) get derivative-based LOD
-    ds.sampMip[s] = us.useMipmaps && s <= 3 && us.type == SGLC_TEXTURE_2D;
+    ds.sampMip[s] = us.useMipmaps && ((ds.shader->derivSlots >> s) & 1) && us.type == SGLC_TEXTURE_2D;
     for (int f = 0; f < 6; f++) {
       int layer = std::min(f, to->tex.layers - 1);
       ds.samp[s][f] = {&to->tex.img[layer], us.filter, us.wrap, us.border, us.format == SGLC_FORMAT_FLOAT32};

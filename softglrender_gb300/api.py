@@ -42,6 +42,9 @@ TextureUsage_AttachmentColor, TextureUsage_AttachmentDepth, TextureUsage_Rendere
 Shading_BaseColor = 1
 Shading_BlinnPhong = 2
 Shading_PBR = 3
+Shading_Skybox = 4
+Shading_IBL_Irradiance = 5
+Shading_IBL_Prefilter = 6
 Shading_BlinnPhongDir = 100
 Shading_VertexColor = 101
 

@@ -34,23 +34,30 @@ struct ShaderInfo {
   std::vector<UniformDescEntry> uniforms;
   int uniformSize;
   int varyingsCnt;
+  int derivSlots;   // sampler slots whose LOD callback the FS installs (setupSamplerDerivative)
 };
 
 // uniform / varying layouts of the reference shaders with GLM aligned types
 // (BasicSoft.h:24-42, BlinnPhongSoft.h:110-150, PbrSoft.h:29-72)
 const ShaderInfo kShaders[] = {
-    {SH_BASE, {}, {{"UniformsModel", 0, -1}, {"UniformsMaterial", 256, -1}}, 304, 0},
+    {SH_BASE, {}, {{"UniformsModel", 0, -1}, {"UniformsMaterial", 256, -1}}, 304, 0, 0},
     {SH_BLINN, {"ALBEDO_MAP", "NORMAL_MAP", "EMISSIVE_MAP", "AO_MAP"},
      {{"UniformsModel", 0, -1}, {"UniformsScene", 256, -1}, {"UniformsMaterial", 320, -1}, {"u_albedoMap", 368, 0},
-      {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3}, {"u_shadowMap", 400, 4}}, 416, 32},
+      {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3}, {"u_shadowMap", 400, 4}}, 416, 32, 0xF},
     {SH_PBR, {"ALBEDO_MAP", "NORMAL_MAP", "EMISSIVE_MAP", "AO_MAP", "METALROUGHNESS_MAP"},
      {{"UniformsModel", 0, -1}, {"UniformsScene", 256, -1}, {"UniformsMaterial", 320, -1}, {"u_albedoMap", 368, 0},
       {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3}, {"u_metalRoughnessMap", 400, 4},
-      {"u_irradianceMap", 408, 5}, {"u_prefilterMap", 416, 6}}, 432, 28},
+      {"u_irradianceMap", 408, 5}, {"u_prefilterMap", 416, 6}}, 432, 28, 0xF},
+    // SkyboxSoft.h:24-61, IBLIrradianceSoft.h:24-56, IBLPrefilterSoft.h:24-61: UniformsModel, then
+    // UniformsPrefilter (u_srcResolution, u_roughness), then the sampler pointers; varyings: v_worldPos
+    {SH_SKYBOX, {"EQUIRECTANGULAR_MAP"},
+     {{"UniformsModel", 0, -1}, {"u_equirectangularMap", 256, 0}, {"u_cubeMap", 264, 1}}, 272, 4, 0},
+    {SH_IBL_IRR, {}, {{"UniformsModel", 0, -1}, {"u_cubeMap", 256, 0}}, 264, 4, 0},
+    {SH_IBL_PRE, {}, {{"UniformsModel", 0, -1}, {"UniformsPrefilter", 256, -1}, {"u_cubeMap", 264, 0}}, 272, 4, 0},
     {SH_BLINN_DIR, {"ALBEDO_MAP", "NORMAL_MAP", "EMISSIVE_MAP", "AO_MAP"},
      {{"UniformsModel", 0, -1}, {"UniformsScene", 256, -1}, {"UniformsMaterial", 320, -1}, {"u_albedoMap", 368, 0},
-      {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3}, {"u_shadowMap", 400, 4}}, 416, 32},
-    {SH_VCOLOR, {}, {{"UniformsModel", 0, -1}, {"UniformsMaterial", 256, -1}}, 304, 4},
+      {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3}, {"u_shadowMap", 400, 4}}, 416, 32, 0xF},
+    {SH_VCOLOR, {}, {{"UniformsModel", 0, -1}, {"UniformsMaterial", 256, -1}}, 304, 4, 0},
 };
 
 const ShaderInfo *findShader(int model) {
@@ -404,7 +411,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     d.height = us.height;
     // only samplers whose LOD callback the FS installs (setupSamplerDerivative: albedo, normal,
     // emissive, ao; BlinnPhongSoft.h:217-230, PbrSoft.h:138-151) use derivative-based LOD
-    d.lodFromDerivative = us.useMipmaps && s <= 3 && us.type == SGLC_TEXTURE_2D;
+    d.lodFromDerivative = us.useMipmaps && ((prog.shader->derivSlots >> s) & 1) && us.type == SGLC_TEXTURE_2D;
     d.isFloat = us.format == SGLC_FORMAT_FLOAT32;
     d.tex = devTex(to->tex);
   }

@@ -23,7 +23,10 @@ enum { FILTER_NEAREST = 0, FILTER_LINEAR, FILTER_NN, FILTER_LN, FILTER_NL, FILTE
 enum { WRAP_REPEAT = 0, WRAP_MIRRORED, WRAP_EDGE, WRAP_BORDER };
 // SH_PBR_CAPTURE: the plain PBR shader that also appends neural-shader training records (a separate
 // instantiation, so the plain kernel carries no capture code); SH_PBR_NEURAL: the neural IBL variant
-enum { SH_BASE = 1, SH_BLINN = 2, SH_PBR = 3, SH_BLINN_DIR = 100, SH_VCOLOR = 101, SH_PBR_NEURAL = 102, SH_PBR_CAPTURE = 103 };
+enum {
+  SH_BASE = 1, SH_BLINN = 2, SH_PBR = 3, SH_SKYBOX = 4, SH_IBL_IRR = 5, SH_IBL_PRE = 6,
+  SH_BLINN_DIR = 100, SH_VCOLOR = 101, SH_PBR_NEURAL = 102, SH_PBR_CAPTURE = 103
+};
 
 // one texture as seen by a sampler: all layers x levels in one allocation
 struct DevTex {

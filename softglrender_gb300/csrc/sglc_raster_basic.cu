@@ -8,6 +8,7 @@ void launchRasterBlinn(const DrawParams &p, bool hasColor, bool hasDepth, cudaSt
 void launchRasterPbr(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 void launchRasterNeural(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 void launchRasterPbrCapture(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
+void launchRasterEnvironment(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
   int grid = p.views * p.tilesPerView;
@@ -25,6 +26,9 @@ void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_
     case SH_PBR: launchRasterPbr(p, hasColor, hasDepth, st); break;
     case SH_PBR_NEURAL: launchRasterNeural(p, hasColor, hasDepth, st); break;
     case SH_PBR_CAPTURE: launchRasterPbrCapture(p, hasColor, hasDepth, st); break;
+    case SH_SKYBOX:
+    case SH_IBL_IRR:
+    case SH_IBL_PRE: launchRasterEnvironment(p, hasColor, hasDepth, st); break;
   }
 }
 

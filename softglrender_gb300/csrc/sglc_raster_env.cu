@@ -1,0 +1,15 @@
+// Raster instantiations: the environment passes (skybox / equirectangular-to-cube, irradiance and
+// prefiltered-specular convolution) that IBLGenerator draws into cube-map faces.
+#include "sglc_raster.cuh"
+
+namespace sglc {
+
+void launchRasterEnvironment(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
+  switch (p.shading) {
+    case SH_SKYBOX: launchRasterModel<SH_SKYBOX>(p, hasColor, hasDepth, st); break;
+    case SH_IBL_IRR: launchRasterModel<SH_IBL_IRR>(p, hasColor, hasDepth, st); break;
+    case SH_IBL_PRE: launchRasterModel<SH_IBL_PRE>(p, hasColor, hasDepth, st); break;
+  }
+}
+
+}  // namespace sglc

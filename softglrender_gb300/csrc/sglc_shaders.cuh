@@ -31,7 +31,14 @@ template<int SH>
 __device__ __forceinline__ float4 runVS(const DrawParams &p, const uint8_t *U, const float *a, float *v) {
   float4 position = make_float4(a[0], a[1], a[2], 1.0f);
   float4 pos = mul44(uMVP(U), position);
-  if (SH == SH_VCOLOR) {
+  if (SH == SH_SKYBOX || SH == SH_IBL_IRR || SH == SH_IBL_PRE) {
+    // SkyboxSoft.h:67-76 (x, y, w, w; z = 0 with reversed Z), IBL*Soft.h VS (z = w): the cube sits
+    // on the far plane
+    if (SH == SH_SKYBOX) pos = make_float4(pos.x, pos.y, pos.w, pos.w);
+    else pos.z = pos.w;
+    if (SH == SH_SKYBOX && uI32(U, 0)) pos.z = 0.f;
+    v[0] = a[0]; v[1] = a[1]; v[2] = a[2];
+  } else if (SH == SH_VCOLOR) {
     v[0] = a[4]; v[1] = a[5]; v[2] = a[6]; v[3] = a[7];
   } else if (SH == SH_BLINN || SH == SH_BLINN_DIR || SH == SH_PBR) {
     const bool bp = SH != SH_PBR;
@@ -330,9 +337,104 @@ __device__ inline float4 fsPbr(const DrawParams &p, const FragIn &f) {
   return pbrFinish(p, ambient, s.Lo, emissive, s.arg.w);
 }
 
+// ---- environment shaders (IBLGenerator's cube-face passes, Environment.cpp:152-195) ------------
+// SkyboxSoft.h:84-103
+__device__ inline float4 fsSkybox(const DrawParams &p, const FragIn &f) {
+  f3 wp = f.v.v3(0);
+  if (p.def[0]) {   // EQUIRECTANGULAR_MAP: SampleSphericalMap
+    f3 dir = normalize3(wp);
+    float u = atan2f(dir.z, dir.x), v = asinf(-dir.y);
+    u = u * 0.1591f + 0.5f;
+    v = v * 0.3183f + 0.5f;
+    return tex2D(p, 0, u, v, f);
+  }
+  return texCube(p, 1, wp, 0.f);
+}
+
+// IBLIrradianceSoft.h:75-101: cosine-weighted hemisphere sum, sampleDelta 0.025
+__device__ inline float4 fsIrradiance(const DrawParams &p, const FragIn &f) {
+  const float PI = 3.14159265359f;
+  f3 N = normalize3(f.v.v3(0));
+  f3 irradiance = mk3(0.f, 0.f, 0.f);
+  f3 up = mk3(0.0f, 1.0f, 0.0f);
+  f3 right = normalize3(cross3(up, N));
+  up = normalize3(cross3(N, right));
+  const float sampleDelta = 0.025f;
+  float nrSamples = 0.0f;
+  for (float phi = 0.0f; phi < 2.0f * PI; phi += sampleDelta) {
+    float sp = sinf(phi), cp = cosf(phi);
+    for (float theta = 0.0f; theta < 0.5f * PI; theta += sampleDelta) {
+      float st = sinf(theta), ct = cosf(theta);
+      f3 ts = mk3(st * cp, st * sp, ct);
+      f3 sampleVec = right * ts.x + up * ts.y + N * ts.z;
+      float4 c = texCube(p, 0, sampleVec, 0.f);
+      irradiance = irradiance + mk3(c.x, c.y, c.z) * ct * st;
+      nrSamples++;
+    }
+  }
+  irradiance = PI * irradiance * (1.0f / nrSamples);
+  return make_float4(irradiance.x, irradiance.y, irradiance.z, 1.0f);
+}
+
+// IBLPrefilterSoft.h:101-170: GGX importance sampling, 1024 Hammersley samples, PDF-based source LOD
+__device__ __forceinline__ float radicalInverseVdC(uint32_t bits) {
+  bits = (bits << 16u) | (bits >> 16u);
+  bits = ((bits & 0x55555555u) << 1u) | ((bits & 0xAAAAAAAAu) >> 1u);
+  bits = ((bits & 0x33333333u) << 2u) | ((bits & 0xCCCCCCCCu) >> 2u);
+  bits = ((bits & 0x0F0F0F0Fu) << 4u) | ((bits & 0xF0F0F0F0u) >> 4u);
+  bits = ((bits & 0x00FF00FFu) << 8u) | ((bits & 0xFF00FF00u) >> 8u);
+  return (float) ((double) bits * 2.3283064365386963e-10);
+}
+
+__device__ inline float4 fsPrefilter(const DrawParams &p, const FragIn &f) {
+  const float PI = 3.14159265359f;
+  const float srcResolution = uF32(f.U, 256), roughness = uF32(f.U, 260);
+  f3 N = normalize3(f.v.v3(0));
+  f3 V = N;
+  const uint32_t SAMPLE_COUNT = 1024u;
+  f3 color = mk3(0.f, 0.f, 0.f);
+  float totalWeight = 0.0f;
+  const float a = roughness * roughness;
+  f3 upv = fabsf(N.z) < 0.999 ? mk3(0.0f, 0.0f, 1.0f) : mk3(1.0f, 0.0f, 0.0f);
+  f3 tangent = normalize3(cross3(upv, N));
+  f3 bitangent = cross3(N, tangent);
+  for (uint32_t i = 0u; i < SAMPLE_COUNT; ++i) {
+    float xi0 = (float) i / (float) SAMPLE_COUNT, xi1 = radicalInverseVdC(i);
+    float phi = 2.0f * PI * xi0;
+    float cosTheta = sqrtf((1.0f - xi1) / (1.0f + (a * a - 1.0f) * xi1));
+    float sinTheta = sqrtf(1.0f - cosTheta * cosTheta);
+    f3 H = mk3(cosf(phi) * sinTheta, sinf(phi) * sinTheta, cosTheta);
+    H = normalize3(tangent * H.x + bitangent * H.y + N * H.z);
+    f3 L = normalize3(2.0f * dot3(V, H) * H - V);
+    float NdotL = gmax(dot3(N, L), 0.0f);
+    if (NdotL > 0.0f) {
+      float a2 = a * a;
+      float NdotH = gmax(dot3(N, H), 0.0f);
+      float NdotH2 = NdotH * NdotH;
+      float denom = (NdotH2 * (a2 - 1.0f) + 1.0f);
+      denom = PI * denom * denom;
+      float D = a2 / denom;
+      float NdotHb = gmax(dot3(N, H), 0.0f);
+      float HdotV = gmax(dot3(H, V), 0.0f);
+      float pdf = D * NdotHb / (4.0f * HdotV) + 0.0001f;
+      float saTexel = 4.0f * PI / (6.0f * srcResolution * srcResolution);
+      float saSample = 1.0f / ((float) SAMPLE_COUNT * pdf + 0.0001f);
+      float mipLevel = roughness == 0.0f ? 0.0f : 0.5f * log2f(saSample / saTexel);
+      float4 c = texCube(p, 0, L, mipLevel);
+      color = color + mk3(c.x, c.y, c.z) * NdotL;
+      totalWeight += NdotL;
+    }
+  }
+  color = color / totalWeight;
+  return make_float4(color.x, color.y, color.z, 1.0f);
+}
+
 template<int SH>
 __device__ __forceinline__ float4 runFS(const DrawParams &p, const FragIn &f) {
   if (SH == SH_BASE) return uV4(f.U, 256 + 32);
+  if (SH == SH_SKYBOX) return fsSkybox(p, f);
+  if (SH == SH_IBL_IRR) return fsIrradiance(p, f);
+  if (SH == SH_IBL_PRE) return fsPrefilter(p, f);
   if (SH == SH_VCOLOR) return make_float4(f.v[0], f.v[1], f.v[2], f.v[3]);
   if (SH == SH_BLINN) return fsBlinnPhong<false>(p, f);
   if (SH == SH_BLINN_DIR) return fsBlinnPhong<true>(p, f);
