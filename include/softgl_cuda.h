@@ -92,6 +92,7 @@ enum {
   SGLC_SHADING_SKYBOX = 4,              /* Shader/Software/SkyboxSoft.h:42-107 (equirectangular or cube) */
   SGLC_SHADING_IBL_IRRADIANCE = 5,      /* Shader/Software/IBLIrradianceSoft.h:40-105 */
   SGLC_SHADING_IBL_PREFILTER = 6,       /* Shader/Software/IBLPrefilterSoft.h:44-172 */
+  SGLC_SHADING_FXAA = 7,                /* Shader/Software/FxaaSoft.h:37-267 (QuadFilter screen pass) */
   SGLC_SHADING_BLINN_PHONG_DIR = 100,   /* Blinn-Phong, directional light, shininess 32 */
   SGLC_SHADING_VERTEX_COLOR = 101,      /* per-vertex RGBA colour */
 };

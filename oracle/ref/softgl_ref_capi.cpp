@@ -27,6 +27,7 @@
 #include "Viewer/Shader/Software/SkyboxSoft.h"
 #include "Viewer/Shader/Software/IBLIrradianceSoft.h"
 #include "Viewer/Shader/Software/IBLPrefilterSoft.h"
+#include "Viewer/Shader/Software/FxaaSoft.h"
 #include "extra_shaders_soft.h"
 #include "softgl_cuda.h"
 
@@ -330,6 +331,7 @@ sglc_status sglr_program_set_shaders(sglc_context *ctx, sglc_handle prog, int32_
     case SGLC_SHADING_SKYBOX: SOFT_SHADERS(ShaderSkybox); break;
     case SGLC_SHADING_IBL_IRRADIANCE: SOFT_SHADERS(ShaderIBLIrradiance); break;
     case SGLC_SHADING_IBL_PREFILTER: SOFT_SHADERS(ShaderIBLPrefilter); break;
+    case SGLC_SHADING_FXAA: SOFT_SHADERS(ShaderFXAA); break;
     case SGLC_SHADING_BLINN_PHONG_DIR: SOFT_SHADERS(ShaderBlinnPhongDir); break;
     case SGLC_SHADING_VERTEX_COLOR: SOFT_SHADERS(ShaderVertexColor); break;
     default: return c->fail(SGLC_ERR_UNSUPPORTED, "unknown shading model");

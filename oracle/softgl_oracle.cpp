@@ -157,6 +157,8 @@ static const ShaderInfo kShaders[] = {
     {SGLC_SHADING_IBL_IRRADIANCE, {}, {{"UniformsModel", 0, -1}, {"u_cubeMap", 256, 0}}, 264, 4, 0},
     {SGLC_SHADING_IBL_PREFILTER, {},
      {{"UniformsModel", 0, -1}, {"UniformsPrefilter", 256, -1}, {"u_cubeMap", 264, 0}}, 272, 4, 0},
+    // FxaaSoft.h:24-53
+    {SGLC_SHADING_FXAA, {}, {{"UniformsQuadFilter", 0, -1}, {"u_screenTexture", 8, 0}}, 16, 2, 0},
     {SGLC_SHADING_BLINN_PHONG_DIR, {"ALBEDO_MAP", "NORMAL_MAP", "EMISSIVE_MAP", "AO_MAP"},
      {{"UniformsModel", 0, -1}, {"UniformsScene", 256, -1}, {"UniformsMaterial", 320, -1},
       {"u_albedoMap", 368, 0}, {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3},
@@ -459,6 +461,11 @@ static void runVS(const DrawState &ds, const float *a, float *v, V4 *pos) {
   *pos = mul44(U_MVP(u), position);
   switch (ds.shader->model) {
     case SGLC_SHADING_BASE_COLOR:
+      break;
+    case SGLC_SHADING_FXAA:   // FxaaSoft.h:60-63: the quad is already in clip space
+      *pos = position;
+      v[0] = a[4];
+      v[1] = a[5];
       break;
     case SGLC_SHADING_SKYBOX:   // SkyboxSoft.h:67-76
       *pos = {pos->x, pos->y, pos->w, pos->w};
@@ -815,6 +822,136 @@ static V4 fsPrefilter(const DrawState &ds, const FragIn &f) {
   return {color.x, color.y, color.z, 1.0f};
 }
 
+// ---- FXAA screen pass (QuadFilter.cpp:12-112, FxaaSoft.h) -------------------------------------
+static uint32_t textureOffsetImpl(const SamplerView &s, float u, float v, int ox, int oy) {
+  // textureLodOffset at LOD 0 (SamplerSoft.h:117-165, 214-238)
+  const std::vector<Level> &lv = *s.levels;
+  if (lv.empty()) return 0;
+  auto one = [&](const Level &L, bool nearest) -> uint32_t {
+    float tx = u * (float) L.w, ty = v * (float) L.h;
+    if (nearest) return pixelWrap(L, (int) std::floor(tx) + ox, (int) std::floor(ty) + oy, s.wrap, s.border);
+    return sampleBilinearPx(L, tx + (float) ox, ty + (float) oy, s.wrap, s.border, s.isFloat);
+  };
+  bool nearest = s.filter == SGLC_FILTER_NEAREST || s.filter == SGLC_FILTER_NEAREST_MIPMAP_NEAREST ||
+                 s.filter == SGLC_FILTER_NEAREST_MIPMAP_LINEAR;
+  if (s.filter == SGLC_FILTER_NEAREST_MIPMAP_LINEAR || s.filter == SGLC_FILTER_LINEAR_MIPMAP_LINEAR) {
+    uint32_t th = one(lv[0], nearest);
+    if (lv.size() < 2) return th;
+    uint32_t tl = one(lv[1], nearest);
+    return s.isFloat ? mixF(th, tl, 0.f) : mixRGBA(th, tl, 0.f);
+  }
+  return one(lv[0], nearest);
+}
+
+static inline float fxaaQuality(float q) {   // QUALITY(q), FxaaSoft.h:74
+  return q < 5.f ? 1.0f : (q > 5.f ? (q < 10.f ? 2.0f : (q < 11.f ? 4.0f : 8.0f)) : 1.5f);
+}
+static inline float rgb2luma(V3 c) { return dot3(c, V3{0.299f, 0.587f, 0.114f}); }
+static inline float fxaaClamp01(float x) { return gclamp(x, 0.0f, 1.0f); }
+static inline V3 fxaaTex(const DrawState &ds, float u, float v) {
+  RGBAf c = unpack(textureImpl(ds.samp[0][0], u, v, 0.f));
+  return {c.r / 255.f, c.g / 255.f, c.b / 255.f};
+}
+static inline V3 fxaaTexOff(const DrawState &ds, float u, float v, int ox, int oy) {
+  RGBAf c = unpack(textureOffsetImpl(ds.samp[0][0], u, v, ox, oy));
+  return {c.r / 255.f, c.g / 255.f, c.b / 255.f};
+}
+
+static V3 fxaaColor(const DrawState &ds, const FragIn &f) {
+  // FxaaSoft.h:83-262 (FXAA 3.11-style edge walk: 12 iterations, subpixel quality 0.75)
+  const float inv_x = 1.0f / *(const float *) (ds.u + 0), inv_y = 1.0f / *(const float *) (ds.u + 4);
+  const float tu = f.v[0], tv = f.v[1];
+  V3 colorCenter = fxaaTex(ds, tu, tv);
+  float lumaCenter = rgb2luma(colorCenter);
+  float lumaDown = rgb2luma(fxaaTexOff(ds, tu, tv, 0, -1));
+  float lumaUp = rgb2luma(fxaaTexOff(ds, tu, tv, 0, 1));
+  float lumaLeft = rgb2luma(fxaaTexOff(ds, tu, tv, -1, 0));
+  float lumaRight = rgb2luma(fxaaTexOff(ds, tu, tv, 1, 0));
+  float lumaMin = gmin(lumaCenter, gmin(gmin(lumaDown, lumaUp), gmin(lumaLeft, lumaRight)));
+  float lumaMax = gmax(lumaCenter, gmax(gmax(lumaDown, lumaUp), gmax(lumaLeft, lumaRight)));
+  float lumaRange = lumaMax - lumaMin;
+  if (lumaRange < gmax(0.0312f, lumaMax * 0.125f)) return colorCenter;
+  float lumaDownLeft = rgb2luma(fxaaTexOff(ds, tu, tv, -1, -1));
+  float lumaUpRight = rgb2luma(fxaaTexOff(ds, tu, tv, 1, 1));
+  float lumaUpLeft = rgb2luma(fxaaTexOff(ds, tu, tv, -1, 1));
+  float lumaDownRight = rgb2luma(fxaaTexOff(ds, tu, tv, 1, -1));
+  float lumaDownUp = lumaDown + lumaUp;
+  float lumaLeftRight = lumaLeft + lumaRight;
+  float lumaLeftCorners = lumaDownLeft + lumaUpLeft;
+  float lumaDownCorners = lumaDownLeft + lumaDownRight;
+  float lumaRightCorners = lumaDownRight + lumaUpRight;
+  float lumaUpCorners = lumaUpRight + lumaUpLeft;
+  float edgeHorizontal = std::fabs(-2.0f * lumaLeft + lumaLeftCorners) + std::fabs(-2.0f * lumaCenter + lumaDownUp) * 2.0f +
+                         std::fabs(-2.0f * lumaRight + lumaRightCorners);
+  float edgeVertical = std::fabs(-2.0f * lumaUp + lumaUpCorners) + std::fabs(-2.0f * lumaCenter + lumaLeftRight) * 2.0f +
+                       std::fabs(-2.0f * lumaDown + lumaDownCorners);
+  bool isHorizontal = (edgeHorizontal >= edgeVertical);
+  float stepLength = isHorizontal ? inv_y : inv_x;
+  float luma1 = isHorizontal ? lumaDown : lumaLeft;
+  float luma2 = isHorizontal ? lumaUp : lumaRight;
+  float gradient1 = luma1 - lumaCenter;
+  float gradient2 = luma2 - lumaCenter;
+  bool is1Steepest = std::fabs(gradient1) >= std::fabs(gradient2);
+  float gradientScaled = 0.25f * gmax(std::fabs(gradient1), std::fabs(gradient2));
+  float lumaLocalAverage = 0.0f;
+  if (is1Steepest) {
+    stepLength = -stepLength;
+    lumaLocalAverage = 0.5f * (luma1 + lumaCenter);
+  } else {
+    lumaLocalAverage = 0.5f * (luma2 + lumaCenter);
+  }
+  float cu = tu, cv = tv;
+  if (isHorizontal) cv += stepLength * 0.5f;
+  else cu += stepLength * 0.5f;
+  float offx = isHorizontal ? inv_x : 0.0f, offy = isHorizontal ? 0.0f : inv_y;
+  float u1 = cu - offx * fxaaQuality(0.f), v1 = cv - offy * fxaaQuality(0.f);
+  float u2 = cu + offx * fxaaQuality(0.f), v2 = cv + offy * fxaaQuality(0.f);
+  float lumaEnd1 = 0.f, lumaEnd2 = 0.f;
+  bool reached1 = false, reached2 = false, reachedBoth = false;
+  for (int i = 1; i < 12; i++) {
+    if (!reached1) {
+      lumaEnd1 = rgb2luma(fxaaTex(ds, u1, v1));
+      lumaEnd1 = lumaEnd1 - lumaLocalAverage;
+      reached1 = std::fabs(lumaEnd1) >= gradientScaled;
+    }
+    if (!reached2) {
+      lumaEnd2 = rgb2luma(fxaaTex(ds, u2, v2));
+      lumaEnd2 = lumaEnd2 - lumaLocalAverage;
+      reached2 = std::fabs(lumaEnd2) >= gradientScaled;
+    }
+    reachedBoth = reached1 && reached2;
+    if (!reached1) {
+      u1 -= offx * fxaaQuality((float) i);
+      v1 -= offy * fxaaQuality((float) i);
+    }
+    if (!reached2) {
+      u2 += offx * fxaaQuality((float) i);
+      v2 += offy * fxaaQuality((float) i);
+    }
+    if (reachedBoth) break;
+  }
+  float distance1 = isHorizontal ? (tu - u1) : (tv - v1);
+  float distance2 = isHorizontal ? (u2 - tu) : (v2 - tv);
+  bool isDirection1 = distance1 < distance2;
+  float distanceFinal = gmin(distance1, distance2);
+  bool isLumaCenterSmaller = lumaCenter < lumaLocalAverage;
+  bool correctVariation1 = (lumaEnd1 < 0.0f) != isLumaCenterSmaller;
+  bool correctVariation2 = (lumaEnd2 < 0.0f) != isLumaCenterSmaller;
+  bool correctVariation = isDirection1 ? correctVariation1 : correctVariation2;
+  float edgeLength = (distance1 + distance2);
+  float pixelOffset = -distanceFinal / edgeLength + 0.5f;
+  float finalOffset = correctVariation ? pixelOffset : 0.0f;
+  float lumaAverage = (1.0f / 12.0f) * (2.0f * (lumaDownUp + lumaLeftRight) + lumaLeftCorners + lumaRightCorners);
+  float subPixelOffset1 = fxaaClamp01(std::fabs(lumaAverage - lumaCenter) / lumaRange);
+  float subPixelOffset2 = (-2.0f * subPixelOffset1 + 3.0f) * subPixelOffset1 * subPixelOffset1;
+  float subPixelOffsetFinal = subPixelOffset2 * subPixelOffset2 * 0.75f;
+  finalOffset = gmax(finalOffset, subPixelOffsetFinal);
+  float fu = tu, fv = tv;
+  if (isHorizontal) fv += finalOffset * stepLength;
+  else fu += finalOffset * stepLength;
+  return fxaaTex(ds, fu, fv);
+}
+
 static V4 runFS(const DrawState &ds, const FragIn &f) {
   switch (ds.shader->model) {
     case SGLC_SHADING_BASE_COLOR: return U_BASECOLOR(ds.u, 256);
@@ -825,6 +962,10 @@ static V4 runFS(const DrawState &ds, const FragIn &f) {
     case SGLC_SHADING_SKYBOX: return fsSkybox(ds, f);
     case SGLC_SHADING_IBL_IRRADIANCE: return fsIrradiance(ds, f);
     case SGLC_SHADING_IBL_PREFILTER: return fsPrefilter(ds, f);
+    case SGLC_SHADING_FXAA: {
+      V3 c = fxaaColor(ds, f);
+      return {c.x, c.y, c.z, 1.f};
+    }
   }
   return {0, 0, 0, 0};
 }

@@ -45,6 +45,7 @@ Shading_PBR = 3
 Shading_Skybox = 4
 Shading_IBL_Irradiance = 5
 Shading_IBL_Prefilter = 6
+Shading_FXAA = 7
 Shading_BlinnPhongDir = 100
 Shading_VertexColor = 101
 

@@ -54,6 +54,8 @@ const ShaderInfo kShaders[] = {
      {{"UniformsModel", 0, -1}, {"u_equirectangularMap", 256, 0}, {"u_cubeMap", 264, 1}}, 272, 4, 0},
     {SH_IBL_IRR, {}, {{"UniformsModel", 0, -1}, {"u_cubeMap", 256, 0}}, 264, 4, 0},
     {SH_IBL_PRE, {}, {{"UniformsModel", 0, -1}, {"UniformsPrefilter", 256, -1}, {"u_cubeMap", 264, 0}}, 272, 4, 0},
+    // FxaaSoft.h:24-53: UniformsQuadFilter (vec2 u_screenSize), the screen texture; varyings: v_texCoord
+    {SH_FXAA, {}, {{"UniformsQuadFilter", 0, -1}, {"u_screenTexture", 8, 0}}, 16, 2, 0},
     {SH_BLINN_DIR, {"ALBEDO_MAP", "NORMAL_MAP", "EMISSIVE_MAP", "AO_MAP"},
      {{"UniformsModel", 0, -1}, {"UniformsScene", 256, -1}, {"UniformsMaterial", 320, -1}, {"u_albedoMap", 368, 0},
       {"u_normalMap", 376, 1}, {"u_emissiveMap", 384, 2}, {"u_aoMap", 392, 3}, {"u_shadowMap", 400, 4}}, 416, 32, 0xF},

@@ -24,7 +24,7 @@ enum { WRAP_REPEAT = 0, WRAP_MIRRORED, WRAP_EDGE, WRAP_BORDER };
 // SH_PBR_CAPTURE: the plain PBR shader that also appends neural-shader training records (a separate
 // instantiation, so the plain kernel carries no capture code); SH_PBR_NEURAL: the neural IBL variant
 enum {
-  SH_BASE = 1, SH_BLINN = 2, SH_PBR = 3, SH_SKYBOX = 4, SH_IBL_IRR = 5, SH_IBL_PRE = 6,
+  SH_BASE = 1, SH_BLINN = 2, SH_PBR = 3, SH_SKYBOX = 4, SH_IBL_IRR = 5, SH_IBL_PRE = 6, SH_FXAA = 7,
   SH_BLINN_DIR = 100, SH_VCOLOR = 101, SH_PBR_NEURAL = 102, SH_PBR_CAPTURE = 103
 };
 
@@ -342,6 +342,34 @@ static __device__ __noinline__ uint32_t textureImpl(const DevSampler &s, int fac
   uint32_t tl = nearest ? nearestSample(t, face, lo, u, v, s.wrap, s.border)
                         : bilinearSample(t, face, lo, u, v, s.wrap, s.border, isF);
   return mixTexel(th, tl, frac, isF);
+}
+
+// textureLodOffset at LOD 0 (SamplerSoft.h:117-165, 214-238): integer texel offset added to the
+// scaled coordinate (bilinear) or to the floored texel (nearest)
+static __device__ __noinline__ uint32_t textureOffsetImpl(const DevSampler &s, float u, float v, int ox, int oy) {
+  const DevTex &t = s.tex;
+  if (t.levels <= 0) return 0;
+  const bool isF = s.isFloat;
+  const int f = s.filter;
+  const bool nearest = (f & 1) == 0;
+  const int maxLevel = t.levels - 1;
+  int hi = 0, lo = 0;
+  bool two = false;
+  if (f == FILTER_NN || f == FILTER_LN) {
+    hi = min(max((int) ceilf(0.f + 0.5f) - 1, 0), maxLevel);
+  } else if (f >= FILTER_NL) {
+    hi = 0;
+    lo = min(1, maxLevel);
+    two = hi != lo;
+  }
+  auto one = [&](int level) -> uint32_t {
+    float tx = u * (float) t.w[level], ty = v * (float) t.h[level];
+    if (nearest) return pixelWrap(t, 0, level, (int) floorf(tx) + ox, (int) floorf(ty) + oy, s.wrap, s.border);
+    return bilinearPx(t, 0, level, tx + (float) ox, ty + (float) oy, s.wrap, s.border, isF);
+  };
+  uint32_t th = one(hi);
+  if (!two) return th;
+  return mixTexel(th, one(lo), 0.f, isF);
 }
 
 // BaseSamplerCube::convertXYZ2UV (SamplerSoft.h:311-373), if-chain order kept for ties

@@ -550,6 +550,7 @@ void launchVertexAndClip(const DrawParams &p, cudaStream_t st) {
     case SH_PBR_CAPTURE:
     case SH_PBR_NEURAL: launchGeometry<SH_PBR>(p, st); break;
     case SH_SKYBOX: launchGeometry<SH_SKYBOX>(p, st); break;
+    case SH_FXAA: launchGeometry<SH_FXAA>(p, st); break;
     case SH_IBL_IRR:
     case SH_IBL_PRE: launchGeometry<SH_IBL_IRR>(p, st); break;
     case SH_VCOLOR: launchGeometry<SH_VCOLOR>(p, st); break;

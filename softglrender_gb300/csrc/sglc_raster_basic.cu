@@ -28,7 +28,8 @@ void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_
     case SH_PBR_CAPTURE: launchRasterPbrCapture(p, hasColor, hasDepth, st); break;
     case SH_SKYBOX:
     case SH_IBL_IRR:
-    case SH_IBL_PRE: launchRasterEnvironment(p, hasColor, hasDepth, st); break;
+    case SH_IBL_PRE:
+    case SH_FXAA: launchRasterEnvironment(p, hasColor, hasDepth, st); break;
   }
 }
 

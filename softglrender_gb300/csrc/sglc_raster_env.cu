@@ -1,5 +1,6 @@
 // Raster instantiations: the environment passes (skybox / equirectangular-to-cube, irradiance and
-// prefiltered-specular convolution) that IBLGenerator draws into cube-map faces.
+// prefiltered-specular convolution) that IBLGenerator draws into cube-map faces, and the FXAA
+// screen pass that QuadFilter draws.
 #include "sglc_raster.cuh"
 
 namespace sglc {
@@ -9,6 +10,7 @@ void launchRasterEnvironment(const DrawParams &p, bool hasColor, bool hasDepth, 
     case SH_SKYBOX: launchRasterModel<SH_SKYBOX>(p, hasColor, hasDepth, st); break;
     case SH_IBL_IRR: launchRasterModel<SH_IBL_IRR>(p, hasColor, hasDepth, st); break;
     case SH_IBL_PRE: launchRasterModel<SH_IBL_PRE>(p, hasColor, hasDepth, st); break;
+    case SH_FXAA: launchRasterModel<SH_FXAA>(p, hasColor, hasDepth, st); break;
   }
 }
 

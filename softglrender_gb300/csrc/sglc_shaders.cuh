@@ -31,7 +31,11 @@ template<int SH>
 __device__ __forceinline__ float4 runVS(const DrawParams &p, const uint8_t *U, const float *a, float *v) {
   float4 position = make_float4(a[0], a[1], a[2], 1.0f);
   float4 pos = mul44(uMVP(U), position);
-  if (SH == SH_SKYBOX || SH == SH_IBL_IRR || SH == SH_IBL_PRE) {
+  if (SH == SH_FXAA) {   // FxaaSoft.h:60-63: the quad is already in clip space
+    pos = position;
+    v[0] = a[4];
+    v[1] = a[5];
+  } else if (SH == SH_SKYBOX || SH == SH_IBL_IRR || SH == SH_IBL_PRE) {
     // SkyboxSoft.h:67-76 (x, y, w, w; z = 0 with reversed Z), IBL*Soft.h VS (z = w): the cube sits
     // on the far plane
     if (SH == SH_SKYBOX) pos = make_float4(pos.x, pos.y, pos.w, pos.w);
@@ -429,12 +433,127 @@ __device__ inline float4 fsPrefilter(const DrawParams &p, const FragIn &f) {
   return make_float4(color.x, color.y, color.z, 1.0f);
 }
 
+// ---- FXAA post pass (QuadFilter + FxaaSoft.h) ------------------------------------------------------
+// QUALITY(q) of FxaaSoft.h:74
+__device__ __forceinline__ float fxaaQuality(float q) {
+  return q < 5.f ? 1.0f : (q > 5.f ? (q < 10.f ? 2.0f : (q < 11.f ? 4.0f : 8.0f)) : 1.5f);
+}
+__device__ __forceinline__ float rgb2luma(f3 c) { return dot3(c, mk3(0.299f, 0.587f, 0.114f)); }
+__device__ __forceinline__ float fxaaClamp01(float x) { return gclamp(x, 0.0f, 1.0f); }
+__device__ __forceinline__ f3 fxaaTex(const DrawParams &p, float u, float v) {
+  float4 c = unpack4(textureImpl(p.samp[0], 0, u, v, 0.f));
+  return mk3(c.x / 255.f, c.y / 255.f, c.z / 255.f);
+}
+__device__ __forceinline__ f3 fxaaTexOff(const DrawParams &p, float u, float v, int ox, int oy) {
+  float4 c = unpack4(textureOffsetImpl(p.samp[0], u, v, ox, oy));
+  return mk3(c.x / 255.f, c.y / 255.f, c.z / 255.f);
+}
+
+__device__ inline f3 fxaaColor(const DrawParams &p, const FragIn &f) {
+  // FxaaSoft.h:83-262 (FXAA 3.11-style edge walk: 12 iterations, subpixel quality 0.75)
+  const float inv_x = 1.0f / uF32(f.U, 0), inv_y = 1.0f / uF32(f.U, 4);
+  const float tu = f.v[0], tv = f.v[1];
+  f3 colorCenter = fxaaTex(p, tu, tv);
+  float lumaCenter = rgb2luma(colorCenter);
+  float lumaDown = rgb2luma(fxaaTexOff(p, tu, tv, 0, -1));
+  float lumaUp = rgb2luma(fxaaTexOff(p, tu, tv, 0, 1));
+  float lumaLeft = rgb2luma(fxaaTexOff(p, tu, tv, -1, 0));
+  float lumaRight = rgb2luma(fxaaTexOff(p, tu, tv, 1, 0));
+  float lumaMin = gmin(lumaCenter, gmin(gmin(lumaDown, lumaUp), gmin(lumaLeft, lumaRight)));
+  float lumaMax = gmax(lumaCenter, gmax(gmax(lumaDown, lumaUp), gmax(lumaLeft, lumaRight)));
+  float lumaRange = lumaMax - lumaMin;
+  if (lumaRange < gmax(0.0312f, lumaMax * 0.125f)) return colorCenter;
+  float lumaDownLeft = rgb2luma(fxaaTexOff(p, tu, tv, -1, -1));
+  float lumaUpRight = rgb2luma(fxaaTexOff(p, tu, tv, 1, 1));
+  float lumaUpLeft = rgb2luma(fxaaTexOff(p, tu, tv, -1, 1));
+  float lumaDownRight = rgb2luma(fxaaTexOff(p, tu, tv, 1, -1));
+  float lumaDownUp = lumaDown + lumaUp;
+  float lumaLeftRight = lumaLeft + lumaRight;
+  float lumaLeftCorners = lumaDownLeft + lumaUpLeft;
+  float lumaDownCorners = lumaDownLeft + lumaDownRight;
+  float lumaRightCorners = lumaDownRight + lumaUpRight;
+  float lumaUpCorners = lumaUpRight + lumaUpLeft;
+  float edgeHorizontal = fabsf(-2.0f * lumaLeft + lumaLeftCorners) + fabsf(-2.0f * lumaCenter + lumaDownUp) * 2.0f +
+                         fabsf(-2.0f * lumaRight + lumaRightCorners);
+  float edgeVertical = fabsf(-2.0f * lumaUp + lumaUpCorners) + fabsf(-2.0f * lumaCenter + lumaLeftRight) * 2.0f +
+                       fabsf(-2.0f * lumaDown + lumaDownCorners);
+  bool isHorizontal = (edgeHorizontal >= edgeVertical);
+  float stepLength = isHorizontal ? inv_y : inv_x;
+  float luma1 = isHorizontal ? lumaDown : lumaLeft;
+  float luma2 = isHorizontal ? lumaUp : lumaRight;
+  float gradient1 = luma1 - lumaCenter;
+  float gradient2 = luma2 - lumaCenter;
+  bool is1Steepest = fabsf(gradient1) >= fabsf(gradient2);
+  float gradientScaled = 0.25f * gmax(fabsf(gradient1), fabsf(gradient2));
+  float lumaLocalAverage = 0.0f;
+  if (is1Steepest) {
+    stepLength = -stepLength;
+    lumaLocalAverage = 0.5f * (luma1 + lumaCenter);
+  } else {
+    lumaLocalAverage = 0.5f * (luma2 + lumaCenter);
+  }
+  float cu = tu, cv = tv;
+  if (isHorizontal) cv += stepLength * 0.5f;
+  else cu += stepLength * 0.5f;
+  float offx = isHorizontal ? inv_x : 0.0f, offy = isHorizontal ? 0.0f : inv_y;
+  float u1 = cu - offx * fxaaQuality(0.f), v1 = cv - offy * fxaaQuality(0.f);
+  float u2 = cu + offx * fxaaQuality(0.f), v2 = cv + offy * fxaaQuality(0.f);
+  float lumaEnd1 = 0.f, lumaEnd2 = 0.f;
+  bool reached1 = false, reached2 = false, reachedBoth = false;
+  for (int i = 1; i < 12; i++) {
+    if (!reached1) {
+      lumaEnd1 = rgb2luma(fxaaTex(p, u1, v1));
+      lumaEnd1 = lumaEnd1 - lumaLocalAverage;
+      reached1 = fabsf(lumaEnd1) >= gradientScaled;
+    }
+    if (!reached2) {
+      lumaEnd2 = rgb2luma(fxaaTex(p, u2, v2));
+      lumaEnd2 = lumaEnd2 - lumaLocalAverage;
+      reached2 = fabsf(lumaEnd2) >= gradientScaled;
+    }
+    reachedBoth = reached1 && reached2;
+    if (!reached1) {
+      u1 -= offx * fxaaQuality((float) i);
+      v1 -= offy * fxaaQuality((float) i);
+    }
+    if (!reached2) {
+      u2 += offx * fxaaQuality((float) i);
+      v2 += offy * fxaaQuality((float) i);
+    }
+    if (reachedBoth) break;
+  }
+  float distance1 = isHorizontal ? (tu - u1) : (tv - v1);
+  float distance2 = isHorizontal ? (u2 - tu) : (v2 - tv);
+  bool isDirection1 = distance1 < distance2;
+  float distanceFinal = gmin(distance1, distance2);
+  bool isLumaCenterSmaller = lumaCenter < lumaLocalAverage;
+  bool correctVariation1 = (lumaEnd1 < 0.0f) != isLumaCenterSmaller;
+  bool correctVariation2 = (lumaEnd2 < 0.0f) != isLumaCenterSmaller;
+  bool correctVariation = isDirection1 ? correctVariation1 : correctVariation2;
+  float edgeLength = (distance1 + distance2);
+  float pixelOffset = -distanceFinal / edgeLength + 0.5f;
+  float finalOffset = correctVariation ? pixelOffset : 0.0f;
+  float lumaAverage = (1.0f / 12.0f) * (2.0f * (lumaDownUp + lumaLeftRight) + lumaLeftCorners + lumaRightCorners);
+  float subPixelOffset1 = fxaaClamp01(fabsf(lumaAverage - lumaCenter) / lumaRange);
+  float subPixelOffset2 = (-2.0f * subPixelOffset1 + 3.0f) * subPixelOffset1 * subPixelOffset1;
+  float subPixelOffsetFinal = subPixelOffset2 * subPixelOffset2 * 0.75f;
+  finalOffset = gmax(finalOffset, subPixelOffsetFinal);
+  float fu = tu, fv = tv;
+  if (isHorizontal) fv += finalOffset * stepLength;
+  else fu += finalOffset * stepLength;
+  return fxaaTex(p, fu, fv);
+}
+
 template<int SH>
 __device__ __forceinline__ float4 runFS(const DrawParams &p, const FragIn &f) {
   if (SH == SH_BASE) return uV4(f.U, 256 + 32);
   if (SH == SH_SKYBOX) return fsSkybox(p, f);
   if (SH == SH_IBL_IRR) return fsIrradiance(p, f);
   if (SH == SH_IBL_PRE) return fsPrefilter(p, f);
+  if (SH == SH_FXAA) {
+    f3 c = fxaaColor(p, f);
+    return make_float4(c.x, c.y, c.z, 1.f);
+  }
   if (SH == SH_VCOLOR) return make_float4(f.v[0], f.v[1], f.v[2], f.v[3]);
   if (SH == SH_BLINN) return fsBlinnPhong<false>(p, f);
   if (SH == SH_BLINN_DIR) return fsBlinnPhong<true>(p, f);
