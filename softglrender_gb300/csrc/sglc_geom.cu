@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(256) k_setup(const __grid_constant__ DrawParam
       }
     }
   }
-  p.tri[i] = T;
+  if (cnt) p.tri[i] = T;   // only binned primitives are read again (bin emission, raster)
   p.tileCount[i] = cnt;
 }
 
