@@ -292,3 +292,35 @@ def _set_blocks(inst: S.SceneInstance, blocks: Dict[str, bytes]) -> None:
             for ub in res.blocks.values():
                 if ub.name in blocks:
                     ub.setData(blocks[ub.name])
+
+
+def main(argv=None) -> None:
+    """`python -m softglrender_gb300.neural [--width W --height H --steps N]`: capture, train and
+    evaluate the neural IBL shader on a PBR scene, then render it with the network bound."""
+    import argparse
+    import json
+    from . import RendererCUDA
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--width", type=int, default=480)
+    ap.add_argument("--height", type=int, default=270)
+    ap.add_argument("--views", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--frames", type=int, default=3)
+    a = ap.parse_args(argv)
+    r = RendererCUDA(0)
+    kw = dict(width=a.width, height=a.height, lon=128, lat=64, tex=256, prefilter=128, irradiance=16)
+    inst, net, rep = train_neural_ibl(r, kw, train_views=a.views, test_views=2, records=1 << 18, steps=a.steps,
+                                      batch=1 << 14)
+    for prog in pbr_programs(inst):
+        net.bind(prog)
+    for _ in range(a.frames):
+        inst.render()
+    r.waitIdle()
+    print(json.dumps({"records": rep.records, "psnr_db": [round(x, 2) for x in rep.psnr_views],
+                      "loss": rep.final_loss, "bound": rep.bound}))
+    net.destroy()
+    r.destroy()
+
+
+if __name__ == "__main__":
+    main()
