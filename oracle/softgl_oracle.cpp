@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -448,6 +449,7 @@ static inline int32_t U_ENABLE_LIGHT(const uint8_t *u, int base) { return *(cons
 static inline int32_t U_ENABLE_IBL(const uint8_t *u, int base) { return *(const int32_t *) (u + base + 4); }
 static inline int32_t U_ENABLE_SHADOW(const uint8_t *u, int base) { return *(const int32_t *) (u + base + 8); }
 static inline float U_KSPEC(const uint8_t *u, int base) { return *(const float *) (u + base + 16); }
+static inline float U_POINTSIZE(const uint8_t *u, int base) { return *(const float *) (u + base + 12); }
 static inline V4 U_BASECOLOR(const uint8_t *u, int base) {
   const float *p = (const float *) (u + base + 32);
   return {p[0], p[1], p[2], p[3]};
@@ -1292,6 +1294,80 @@ static void rasterTriangle(DrawState &ds, const VertexH &a, const VertexH &b, co
   }
 }
 
+// ---- points and lines (RendererSoft.cpp:636-712) -----------------------------------------------
+static const int64_t kMaxLineSteps = 1 << 24;   // longer lines are refused (SGLC_ERR_OVERFLOW)
+
+// float -> int as the reference's (int) casts compile on x86-64 (cvttss2si): truncation, and
+// INT_MIN for NaN and for values outside the int range
+static inline int truncI(float f) {
+  if (!(f > -2147483904.f && f < 2147483648.f)) return INT32_MIN;
+  return (int) f;
+}
+
+// rasterizationPoint (RendererSoft.cpp:636-661): a pointSize x pointSize stamp; every pixel runs
+// the FS on the vertex's own varyings (no shader reads FragCoord, so one evaluation serves the
+// stamp) and the per-sample operations on every sample. The reference walks the stamp with the
+// vertex's fragPos as its loop variable, so a stamp that ran leaves fragPos.xy at its last pixel;
+// a vertex drawn again starts from there.
+static void rasterPoint(DrawState &ds, V4 &fragPos, const float *vary, float size) {
+  if (!ds.color) return;
+  float left = fragPos.x - size / 2.f + 0.5f;
+  float right = left + size;
+  float top = fragPos.y - size / 2.f + 0.5f;
+  float bottom = top + size;
+  int x0 = truncI(left), x1 = truncI(right), y0 = truncI(top), y1 = truncI(bottom);
+  if (!(x0 < x1 && y0 < y1)) return;
+  FragIn f;
+  f.v = vary;
+  f.dudx = f.dvdx = f.dudy = f.dvdy = 0.f;
+  V4 color = runFS(ds, f);
+  // pixels outside both attachments change nothing (getFrameColor / getFrameDepth return null)
+  int W = std::max(ds.color->w, ds.depth ? ds.depth->w : 0), H = std::max(ds.color->h, ds.depth ? ds.depth->h : 0);
+  for (int x = std::max(x0, 0); x < std::min(x1, W); x++)
+    for (int y = std::max(y0, 0); y < std::min(y1, H); y++)
+      for (int s = 0; s < ds.samples; s++) perSample(ds, x, y, fragPos.z, color, s);
+  fragPos.x = (float) (x1 - 1);
+  fragPos.y = (float) (y1 - 1);
+}
+
+// rasterizationLine (RendererSoft.cpp:663-712): Bresenham over the major axis; every step is a
+// lineWidth stamp with z, w and the varyings lerped by t = (x - x0) / dx (glm::mix).
+static sglc_status rasterLine(DrawState &ds, const VertexH &v0, const VertexH &v1, float width, float *tmp) {
+  int64_t x0 = truncI(v0.fragPos.x), y0 = truncI(v0.fragPos.y);
+  int64_t x1 = truncI(v1.fragPos.x), y1 = truncI(v1.fragPos.y);
+  float z0 = v0.fragPos.z, z1 = v1.fragPos.z, w0 = v0.fragPos.w, w1 = v1.fragPos.w;
+  bool steep = false;
+  if (std::llabs(x0 - x1) < std::llabs(y0 - y1)) {
+    std::swap(x0, y0);
+    std::swap(x1, y1);
+    steep = true;
+  }
+  const float *vin[2] = {v0.vary, v1.vary};
+  if (x0 > x1) {
+    std::swap(x0, x1);
+    std::swap(y0, y1);
+    std::swap(z0, z1);
+    std::swap(w0, w1);
+    std::swap(vin[0], vin[1]);
+  }
+  int64_t dx = x1 - x0, dy = y1 - y0;
+  if (dx > kMaxLineSteps) return SGLC_ERR_OVERFLOW;
+  int64_t error = 0, dError = 2 * std::llabs(dy), y = y0;
+  for (int64_t x = x0; x <= x1; x++) {
+    float t = (float) (x - x0) / (float) dx;
+    V4 pos{(float) x, (float) y, z0 * (1.f - t) + z1 * t, w0 * (1.f - t) + w1 * t};
+    if (steep) std::swap(pos.x, pos.y);
+    for (int i = 0; i < ds.varyCnt; i++) tmp[i] = vin[0][i] * (1.f - t) + vin[1][i] * t;
+    rasterPoint(ds, pos, tmp, width);
+    error += dError;
+    if (error > dx) {
+      y += (y1 > y0 ? 1 : -1);
+      error -= 2 * dx;
+    }
+  }
+  return SGLC_OK;
+}
+
 static Level *attachmentLevel(Ctx *c, int texH, int layer, int level) {
   Object *t = c->get(texH, 2);
   if (!t) return nullptr;
@@ -1301,6 +1377,31 @@ static Level *attachmentLevel(Ctx *c, int texH, int layer, int level) {
   return &lv[level];
 }
 
+// perspectiveDivideImpl + viewportTransformImpl (RendererSoft.cpp:981-992)
+static inline V4 toScreen(const Viewport &vp, V4 f) {
+  float invW = 1.f / f.w;
+  f = {f.x * invW, f.y * invW, f.z * invW, f.w * invW};
+  f.w = invW;
+  f = {f.x * vp.innerP.x, f.y * vp.innerP.y, f.z * vp.innerP.z, f.w * vp.innerP.w};
+  return {f.x + vp.innerO.x, f.y + vp.innerO.y, f.z + vp.innerO.z, f.w + vp.innerO.w};
+}
+
+// MSAA resolve after every draw (RendererSoft.cpp:161-163, 880-912)
+static void resolveMsaa(DrawState &ds) {
+  if (!ds.color || ds.color->samples <= 1) return;
+  Level &L = *ds.color;
+  L.resolved.assign((size_t) L.w * L.h, 0);
+  for (size_t i = 0; i < (size_t) L.w * L.h; i++) {
+    float s[4] = {0, 0, 0, 0};
+    for (int k = 0; k < 4; k++) {
+      RGBAf q = unpack(L.data[i * 4 + k]);
+      s[0] += q.r; s[1] += q.g; s[2] += q.b; s[3] += q.a;
+    }
+    L.resolved[i] = pack(s[0] / 4.f, s[1] / 4.f, s[2] / 4.f, s[3] / 4.f);
+  }
+  L.hasResolved = true;
+}
+
 static sglc_status doDraw(Ctx *c) {
   Object *fbo = c->get(c->fb, 1), *vo = c->get(c->vao, 3), *po = c->get(c->prog, 4), *so = c->get(c->states, 5);
   if (!fbo || !vo || !po) return SGLC_OK;   // RendererSoft::draw is a silent no-op (RendererSoft.cpp:137-139)
@@ -1308,8 +1409,13 @@ static sglc_status doDraw(Ctx *c) {
   ProgramObj &prog = po->prog;
   if (!prog.shader) return c->fail(SGLC_ERR_INVALID_VALUE, "draw: program has no shaders");
   const sglc_render_states *rs = &so->states;
-  if (rs->primitive_type != SGLC_PRIMITIVE_TRIANGLE || rs->polygon_mode != SGLC_POLYGON_FILL)
-    return c->fail(SGLC_ERR_UNSUPPORTED, "draw: only filled triangles are implemented");
+  const int prim = rs->primitive_type;
+  if (prim != SGLC_PRIMITIVE_POINT && prim != SGLC_PRIMITIVE_LINE && prim != SGLC_PRIMITIVE_TRIANGLE)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "draw: unknown primitive type");
+  if (rs->polygon_mode != SGLC_POLYGON_POINT && rs->polygon_mode != SGLC_POLYGON_LINE &&
+      rs->polygon_mode != SGLC_POLYGON_FILL)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "draw: unknown polygon mode");
+  const bool fill = prim == SGLC_PRIMITIVE_TRIANGLE && rs->polygon_mode == SGLC_POLYGON_FILL;
   DrawState ds{};
   ds.shader = prog.shader;
   ds.u = prog.uniforms.data();
@@ -1342,9 +1448,17 @@ static sglc_status doDraw(Ctx *c) {
     if (s == 4 && to->tex.img[0].size()) ds.shadowLevel0 = &to->tex.img[0][0];
   }
   // every sampler the shader may touch must be bound (the reference dereferences it)
+  if (!fill) {
+    // points and lines run the FS outside a pixel quad: the reference has no derivative context
+    // there, so a derivative-LOD sampler in use has nothing to read
+    for (int s = 0; s < 4; s++)
+      if (ds.sampBound[s] && ds.sampMip[s] && ds.def[s])
+        return c->fail(SGLC_ERR_UNSUPPORTED, "draw: points/lines with a derivative-LOD (mipmapped 2D) sampler");
+  }
   VaoObj &vao = vo->vao;
   size_t nv = vao.vertexCnt;
-  size_t ntri = vao.indices.size() / 3;
+  const int per = prim == SGLC_PRIMITIVE_POINT ? 1 : (prim == SGLC_PRIMITIVE_LINE ? 2 : 3);
+  size_t ntri = vao.indices.size() / per;
   int strideF = (int) (vao.stride / 4);
   int va = std::max(ds.varyAligned, 1);
   // vertex stage (RendererSoft.cpp:170-190, 971-979, 994-1003)
@@ -1359,20 +1473,21 @@ static sglc_status doDraw(Ctx *c) {
     runVS(ds, h.attr, h.vary, &h.clipPos);
     h.clipMask = clipMaskOf(h.clipPos);
   }
-  // primitive assembly (RendererSoft.cpp:428-437)
+  // primitive assembly (RendererSoft.cpp:409-437)
   std::vector<Prim> prims(ntri);
   for (size_t i = 0; i < ntri; i++) {
     prims[i].discard = false;
     prims[i].frontFacing = true;
-    for (int k = 0; k < 3; k++) {
-      int32_t ix = vao.indices[i * 3 + k];
+    prims[i].idx[1] = prims[i].idx[2] = 0;
+    for (int k = 0; k < per; k++) {
+      int32_t ix = vao.indices[i * per + k];
       if (ix < 0 || (size_t) ix >= nv) prims[i].discard = true;
       prims[i].idx[k] = ix;
     }
   }
   // clipping (RendererSoft.cpp:206-257, 489-559, 956-969, 1058-1083)
   std::vector<std::unique_ptr<float[]>> keep;
-  auto newVertex = [&](int i0, int i1, float tt) -> int {
+  auto newVertex = [&](int i0, int i1, float tt, bool post = false) -> int {
     std::unique_ptr<float[]> a(new float[strideF]);
     std::unique_ptr<float[]> v(new float[va]());
     const float *A0 = verts[i0].attr, *A1 = verts[i1].attr;
@@ -1382,14 +1497,49 @@ static sglc_status doDraw(Ctx *c) {
     h.vary = v.get();
     runVS(ds, h.attr, h.vary, &h.clipPos);
     h.clipMask = clipMaskOf(h.clipPos);
+    if (post) h.fragPos = toScreen(ds.vp, h.clipPos);
     keep.push_back(std::move(a));
     keep.push_back(std::move(v));
     verts.push_back(h);
     return (int) verts.size() - 1;
   };
+  // clippingLine (RendererSoft.cpp:443-487): parametric clip against the planes either end is
+  // outside of; the far end is re-made from the already re-made near end (indices[0] is updated
+  // before the second clippingNewVertex call)
+  auto clipLine = [&](Prim &l, bool post) {
+    const int m0 = verts[l.idx[0]].clipMask, m1 = verts[l.idx[1]].clipMask;
+    const V4 c0 = verts[l.idx[0]].clipPos, c1 = verts[l.idx[1]].clipPos;
+    float t0 = 0.f, t1 = 1.f;
+    int mask = m0 | m1;
+    for (int pl = 0; pl < 6 && mask; pl++) {
+      if (!(mask & (1 << pl))) continue;
+      float d0 = dot4(kClipPlanes[pl], c0), d1 = dot4(kClipPlanes[pl], c1);
+      if (d0 < 0 && d1 < 0) {
+        l.discard = true;
+        return;
+      } else if (d0 < 0) {
+        float t = -d0 / (d1 - d0);
+        t0 = (t0 < t) ? t : t0;   // std::max
+      } else {
+        float t = d0 / (d0 - d1);
+        t1 = (t < t1) ? t : t1;   // std::min
+      }
+    }
+    if (m0) l.idx[0] = newVertex(l.idx[0], l.idx[1], t0, post);
+    if (m1) l.idx[1] = newVertex(l.idx[0], l.idx[1], t1, post);
+  };
   size_t primCnt = prims.size();
   for (size_t pi = 0; pi < primCnt; pi++) {
     if (prims[pi].discard) continue;
+    if (prim == SGLC_PRIMITIVE_POINT) {   // clippingPoint (RendererSoft.cpp:439-441)
+      prims[pi].discard = verts[prims[pi].idx[0]].clipMask != 0;
+      continue;
+    }
+    if (prim == SGLC_PRIMITIVE_LINE) {
+      clipLine(prims[pi], false);
+      continue;
+    }
+    if (!fill) continue;   // triangles drawn as points / lines are not clipped as triangles
     int mask = verts[prims[pi].idx[0]].clipMask | verts[prims[pi].idx[1]].clipMask | verts[prims[pi].idx[2]].clipMask;
     if (mask == 0) continue;
     std::vector<int> in = {prims[pi].idx[0], prims[pi].idx[1], prims[pi].idx[2]}, out;
@@ -1442,27 +1592,55 @@ static sglc_status doDraw(Ctx *c) {
   std::vector<char> used(verts.size(), 0);
   for (auto &p : prims)
     if (!p.discard)
-      for (int k = 0; k < 3; k++) used[p.idx[k]] = 1;
+      for (int k = 0; k < per; k++) used[p.idx[k]] = 1;
   for (size_t i = 0; i < verts.size(); i++) {
     if (!used[i]) continue;
-    VertexH &h = verts[i];
-    V4 f = h.clipPos;
-    float invW = 1.f / f.w;
-    f = {f.x * invW, f.y * invW, f.z * invW, f.w * invW};
-    f.w = invW;
-    f = {f.x * ds.vp.innerP.x, f.y * ds.vp.innerP.y, f.z * ds.vp.innerP.z, f.w * ds.vp.innerP.w};
-    f = {f.x + ds.vp.innerO.x, f.y + ds.vp.innerO.y, f.z + ds.vp.innerO.z, f.w + ds.vp.innerO.w};
-    h.fragPos = f;
+    verts[i].fragPos = toScreen(ds.vp, verts[i].clipPos);
   }
   // face culling (RendererSoft.cpp:277-299)
   for (auto &p : prims) {
-    if (p.discard) continue;
+    if (p.discard || prim != SGLC_PRIMITIVE_TRIANGLE) continue;
     V4 v0 = verts[p.idx[0]].fragPos, v1 = verts[p.idx[1]].fragPos, v2 = verts[p.idx[2]].fragPos;
     V3 e1 = {v1.x - v0.x, v1.y - v0.y, v1.z - v0.z}, e2 = {v2.x - v0.x, v2.y - v0.y, v2.z - v0.z};
     V3 n = cross3(e1, e2);
     float area = (n.x * 0.f + n.y * 0.f) + n.z * 1.f;
     p.frontFacing = area > 0;
     if (rs->cull_face) p.discard = !p.frontFacing;
+  }
+  if (!fill) {
+    // points and lines, in primitive order (RendererSoft.cpp:301-321, 575-622)
+    const float pointSize = ds.shader->model == SGLC_SHADING_BASE_COLOR ? U_POINTSIZE(ds.u, 256) : 1.f;
+    std::vector<float> tmp(std::max(ds.varyCnt, 1));
+    sglc_status st = SGLC_OK;
+    for (size_t pi = 0; pi < prims.size() && st == SGLC_OK; pi++) {
+      Prim &p = prims[pi];
+      if (p.discard) continue;
+      if (prim == SGLC_PRIMITIVE_POINT) {
+        rasterPoint(ds, verts[p.idx[0]].fragPos, verts[p.idx[0]].vary, pointSize);
+      } else if (prim == SGLC_PRIMITIVE_LINE) {
+        st = rasterLine(ds, verts[p.idx[0]], verts[p.idx[1]], rs->line_width, tmp.data());
+      } else if (rs->polygon_mode == SGLC_POLYGON_POINT) {
+        for (int k = 0; k < 3; k++) {
+          VertexH &h = verts[p.idx[k]];
+          if (h.clipMask != 0) continue;
+          rasterPoint(ds, h.fragPos, h.vary, pointSize);
+        }
+      } else {
+        for (int k = 0; k < 3 && st == SGLC_OK; k++) {
+          Prim l;
+          l.discard = false;
+          l.idx[0] = p.idx[k];
+          l.idx[1] = p.idx[(k + 1) % 3];
+          clipLine(l, true);
+          if (l.discard) continue;
+          st = rasterLine(ds, verts[l.idx[0]], verts[l.idx[1]], rs->line_width, tmp.data());
+        }
+      }
+    }
+    c->stats.clip_vertices = (int64_t) (verts.size() - nv);
+    if (st != SGLC_OK) return c->fail(st, "draw: line longer than 2^24 steps");
+    resolveMsaa(ds);
+    return SGLC_OK;
   }
   // rasterization, row bands in parallel (each pixel sees the same ordered operations)
   int H = ds.color ? ds.color->h : (ds.depth ? ds.depth->h : 0);
@@ -1486,20 +1664,7 @@ static sglc_status doDraw(Ctx *c) {
     }
     for (auto &t : th) t.join();
   }
-  // MSAA resolve after every draw (RendererSoft.cpp:161-163, 880-912)
-  if (ds.color && ds.color->samples > 1) {
-    Level &L = *ds.color;
-    L.resolved.assign((size_t) L.w * L.h, 0);
-    for (size_t i = 0; i < (size_t) L.w * L.h; i++) {
-      float s[4] = {0, 0, 0, 0};
-      for (int k = 0; k < 4; k++) {
-        RGBAf q = unpack(L.data[i * 4 + k]);
-        s[0] += q.r; s[1] += q.g; s[2] += q.b; s[3] += q.a;
-      }
-      L.resolved[i] = pack(s[0] / 4.f, s[1] / 4.f, s[2] / 4.f, s[3] / 4.f);
-    }
-    L.hasResolved = true;
-  }
+  resolveMsaa(ds);
   return SGLC_OK;
 }
 

@@ -55,6 +55,11 @@ TEXTURE_CUBE_MAP_POSITIVE_Y, TEXTURE_CUBE_MAP_NEGATIVE_Y = 2, 3
 TEXTURE_CUBE_MAP_POSITIVE_Z, TEXTURE_CUBE_MAP_NEGATIVE_Z = 4, 5
 
 
+# sglc_status (softgl_cuda.h)
+(SGLC_OK, SGLC_ERR_INVALID_HANDLE, SGLC_ERR_INVALID_VALUE, SGLC_ERR_OUT_OF_MEMORY, SGLC_ERR_DEVICE,
+ SGLC_ERR_UNSUPPORTED, SGLC_ERR_OVERFLOW, SGLC_ERR_NO_DEVICE) = range(8)
+
+
 class SoftGLError(RuntimeError):
     def __init__(self, status: int, call: str, message: str):
         super().__init__(f"{call} failed with status {status}: {message}")

@@ -195,6 +195,8 @@ struct Ctx {
   DevBuf vClip, vFrag, vMask, vVary, vAttrExtra, prims, clipExtra, clipAppendOff, clipPoly, clipPolyTri, counters;
   DevBuf tri, tileCount, pairOff, keyA, keyB, valA, valB, tileStart, tileEnd, tileOrder, scanScratch, sortHist,
       sortHistScan, staging, batchU, batchTargets;
+  DevBuf lpSlot, lpOrigin, lpStampCount, lpStampOff, lpStampGeo, lpStampRow, lpStampColor, lpStampVary, lpFragCount,
+      lpFragOff, lpMisc;   // point and line draws
   // capacity hints that survive between draws
   int extraVertHint = 0, polyHint = 0, appendHint = 0;
   // synchronisation-free draws (sglc_set_capacity) and graph capture
@@ -371,6 +373,188 @@ struct BatchViews {
   const sglc_clear_states *clear = nullptr;
 };
 
+// Point and line draws (RendererSoft.cpp:301-321, 409-487, 575-712; kernels in sglc_lines.cu).
+// The stamp and fragment counts are read back (two synchronisations per draw), so these draws are
+// not captured in graphs.
+sglc_status drawPointsLines(Ctx *c, DrawParams &p, const sglc_render_states &rs, const VaoObj &vao, TexObj *ct,
+                            TexObj *dt) {
+  if (c->capturing) return c->fail(SGLC_ERR_UNSUPPORTED, "draw: point and line draws cannot be captured in a graph");
+  // points and lines run the FS outside a pixel quad: the reference has no derivative context
+  // there, so a derivative-LOD sampler in use has nothing to read
+  if (p.needDeriv)
+    return c->fail(SGLC_ERR_UNSUPPORTED, "draw: points/lines with a derivative-LOD (mipmapped 2D) sampler");
+  sglc_status st0 = flushClear(c);
+  if (st0) return st0;
+  c->stats = sglc_draw_stats{};
+  if (!ct) return SGLC_OK;   // rasterizationPoint draws nothing without a colour attachment (:637-639)
+  const cudaStream_t st = c->stream;
+  LineParams lp;
+  memset(&lp, 0, sizeof(lp));
+  int per = 3;
+  if (rs.primitive_type == SGLC_PRIMITIVE_POINT) {
+    lp.mode = LP_POINTS;
+    per = 1;
+  } else if (rs.primitive_type == SGLC_PRIMITIVE_LINE) {
+    lp.mode = LP_LINES;
+    per = 2;
+  } else {
+    lp.mode = rs.polygon_mode == SGLC_POLYGON_POINT ? LP_TRI_POINTS : LP_TRI_LINES;
+  }
+  const long long nIn = (long long) vao.nidx / per;
+  // PointSize is written by the base-colour VS only (BasicSoft.h:66-69); ShaderBuiltin's default is 1
+  lp.pointSize = 1.f;
+  if (p.shading == SH_BASE) memcpy(&lp.pointSize, p.u + 268, sizeof(float));   // UniformsMaterial.u_pointSize
+  lp.lineWidth = rs.line_width;
+  lp.fw = std::max(p.cw, p.dw);
+  lp.fh = std::max(p.ch, p.dh);
+  const long long extra = lp.mode == LP_LINES ? 2 * nIn : (lp.mode == LP_TRI_LINES ? 6 * nIn : 0);
+  const long long kScanMax = 4096ll * 4096ll;   // one scan handles up to 4096 blocks of 4096
+  if (3 * nIn > kScanMax || (long long) p.nv + extra > (1ll << 30))
+    return c->fail(SGLC_ERR_OVERFLOW, "draw: too many points/lines in one draw");
+  lp.nIn = (int) nIn;
+  const int nSlots = 3 * lp.nIn;
+  p.attr = vao.attr;
+  p.strideF = (int) (vao.stride / 4);
+  p.nv = (int) vao.nv;
+  p.indices = vao.idx;
+  p.ntri = 0;
+  p.views = 1;
+  p.nvView = p.nv;
+  p.ntriView = 0;
+  p.vCap = (int) (p.nv + extra);
+  CK(c->vClip.ensure(sizeof(float4) * std::max(p.vCap, 1)));
+  CK(c->vFrag.ensure(sizeof(float4) * std::max(p.vCap, 1)));
+  CK(c->vMask.ensure((size_t) std::max(p.vCap, 1)));
+  CK(c->vVary.ensure(sizeof(float) * (size_t) std::max(p.vCap, 1) * p.varyStride));
+  CK(c->vAttrExtra.ensure(sizeof(float) * (size_t) std::max<long long>(extra, 1) * std::max(p.strideF, 1)));
+  CK(c->counters.ensure(sizeof(int) * 8));
+  CK(c->lpSlot.ensure(sizeof(int4) * (size_t) std::max(nSlots, 1)));
+  CK(c->lpOrigin.ensure(sizeof(float2) * (size_t) std::max(nSlots, 1)));
+  CK(c->lpStampCount.ensure(sizeof(int) * (size_t) std::max(nSlots, 1)));
+  CK(c->lpStampOff.ensure(sizeof(int) * (size_t) (nSlots + 1)));
+  CK(c->lpMisc.ensure(64));
+  CK(c->scanScratch.ensure(sizeof(int) * (size_t) scanScratchInts(nSlots + 1) * 2));
+  p.vClip = c->vClip.as<float4>();
+  p.vFrag = c->vFrag.as<float4>();
+  p.vMask = c->vMask.as<uint8_t>();
+  p.vVary = c->vVary.as<float>();
+  p.vAttrExtra = c->vAttrExtra.as<float>();
+  p.counters = c->counters.as<int>();
+  lp.slot = c->lpSlot.as<int4>();
+  lp.pointOrigin = c->lpOrigin.as<float2>();
+  lp.stampCount = c->lpStampCount.as<int>();
+  lp.stampOff = c->lpStampOff.as<int>();
+  int *misc = c->lpMisc.as<int>();   // [0] flags, [1] sort count; [4..7] two 64-bit totals
+  lp.flags = misc;
+  lp.totals = reinterpret_cast<unsigned long long *>(misc + 4);
+  CK(cudaMemsetAsync(p.counters, 0, sizeof(int) * 8, st));
+  CK(cudaMemsetAsync(misc, 0, 64, st));
+  int launches = 2;
+  launchPointsLinesGeometry(p, lp, st);
+  // sorts (p.keyA, p.valA)[0, n); the kernels read n from *nDev
+  auto sortBy = [&](int n, const int *nDev, int keyBits) -> sglc_status {
+    int sortInts = sortScratchInts(n);
+    CK(c->sortHist.ensure(sizeof(int) * (size_t) sortInts));
+    CK(c->sortHistScan.ensure(sizeof(int) * (size_t) sortInts));
+    CK(c->scanScratch.ensure(sizeof(int) * (size_t) scanScratchInts(std::max(n + 1, sortInts)) * 2));
+    sortPairs(p, n, nDev, keyBits, c->sortHist.as<int>(), c->sortHistScan.as<int>(), c->scanScratch.as<int>(), st);
+    launches += 5 * ((keyBits + 7) / 8);
+    return SGLC_OK;
+  };
+  auto bitsFor = [](long long n) {
+    int b = 1;
+    while ((1ll << b) < n) b++;
+    return b;
+  };
+  if (lp.mode == LP_POINTS || lp.mode == LP_TRI_POINTS) {
+    // per vertex, its point slots in drawing order: every stamp's origin
+    CK(c->keyA.ensure(sizeof(uint32_t) * (size_t) std::max(nSlots, 1)));
+    CK(c->keyB.ensure(sizeof(uint32_t) * (size_t) std::max(nSlots, 1)));
+    CK(c->valA.ensure(sizeof(int) * (size_t) std::max(nSlots, 1)));
+    CK(c->valB.ensure(sizeof(int) * (size_t) std::max(nSlots, 1)));
+    p.keyA = c->keyA.as<uint32_t>();
+    p.keyB = c->keyB.as<uint32_t>();
+    p.valA = c->valA.as<int>();
+    p.valB = c->valB.as<int>();
+    launchPointKeys(lp, p.keyA, p.valA, nSlots, st);
+    c->hostCounters[8] = nSlots;   // pinned; read by the copy below before any later write
+    CK(cudaMemcpyAsync(misc + 1, c->hostCounters + 8, sizeof(int), cudaMemcpyHostToDevice, st));
+    sglc_status s = sortBy(nSlots, misc + 1, bitsFor((long long) p.nv + 1));
+    if (s) return s;
+    launchPointChain(p, lp, p.keyA, p.valA, nSlots, st);
+    launches += 2;
+  }
+  launchStampCount(p, lp, st);
+  scanExclusive(lp.stampCount, lp.stampOff, nullptr, std::max(nSlots, 1), c->scanScratch.as<int>(), st);
+  CK(cudaGetLastError());
+  // read back: flags, stamp total
+  CK(cudaMemcpyAsync(c->hostCounters, misc, 32, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  int flags = c->hostCounters[0];
+  unsigned long long nStamps64;
+  memcpy(&nStamps64, c->hostCounters + 4, 8);
+  if (flags & LP_ERR_BADINDEX) return c->fail(SGLC_ERR_INVALID_VALUE, "draw: index out of range of the vertex array");
+  if (flags & LP_ERR_LONGLINE) return c->fail(SGLC_ERR_OVERFLOW, "draw: line longer than 2^24 steps");
+  if ((long long) nStamps64 > kScanMax - 1) return c->fail(SGLC_ERR_OVERFLOW, "draw: too many point/line stamps");
+  const int nStamps = (int) nStamps64;
+  const bool lineVary = p.varyCnt > 0 && (lp.mode == LP_LINES || lp.mode == LP_TRI_LINES);
+  CK(c->lpStampGeo.ensure(sizeof(float4) * (size_t) std::max(nStamps, 1)));
+  CK(c->lpStampRow.ensure(sizeof(int) * (size_t) std::max(nStamps, 1)));
+  CK(c->lpStampColor.ensure(sizeof(float4) * (size_t) std::max(nStamps, 1)));
+  if (lineVary) CK(c->lpStampVary.ensure(sizeof(float) * (size_t) std::max(nStamps, 1) * p.varyStride));
+  CK(c->lpFragCount.ensure(sizeof(int) * (size_t) std::max(nStamps, 1)));
+  CK(c->lpFragOff.ensure(sizeof(int) * (size_t) (nStamps + 1)));
+  CK(c->scanScratch.ensure(sizeof(int) * (size_t) scanScratchInts(nStamps + 1) * 2));
+  lp.stampGeo = c->lpStampGeo.as<float4>();
+  lp.stampRow = c->lpStampRow.as<int>();
+  lp.stampColor = c->lpStampColor.as<float4>();
+  lp.stampVary = lineVary ? c->lpStampVary.as<float>() : nullptr;
+  lp.fragCount = c->lpFragCount.as<int>();
+  lp.fragOff = c->lpFragOff.as<int>();
+  launchStampEmit(p, lp, st);
+  launchStampShade(p, lp, nStamps, st);
+  launchFragCount(lp, nStamps, st);
+  scanExclusive(lp.fragCount, lp.fragOff, nullptr, std::max(nStamps, 1), c->scanScratch.as<int>(), st);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(c->hostCounters, misc, 32, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  unsigned long long nFrags64;
+  memcpy(&nFrags64, c->hostCounters + 6, 8);
+  // the sort's histogram scan covers 256 digits x (n / 2048) blocks
+  if ((long long) nFrags64 > 2048ll * (kScanMax / 256) - 2048)
+    return c->fail(SGLC_ERR_OVERFLOW, "draw: too many point/line fragments");
+  const int nFrags = (int) nFrags64;
+  launches += 3 + 3 + 3;
+  if (nFrags > 0) {
+    CK(c->keyA.ensure(sizeof(uint32_t) * (size_t) nFrags));
+    CK(c->keyB.ensure(sizeof(uint32_t) * (size_t) nFrags));
+    CK(c->valA.ensure(sizeof(int) * (size_t) nFrags));
+    CK(c->valB.ensure(sizeof(int) * (size_t) nFrags));
+    p.keyA = c->keyA.as<uint32_t>();
+    p.keyB = c->keyB.as<uint32_t>();
+    p.valA = c->valA.as<int>();
+    p.valB = c->valB.as<int>();
+    launchFragEmit(lp, nStamps, p.keyA, p.valA, st);
+    sglc_status s = sortBy(nFrags, lp.fragOff + nStamps, bitsFor((long long) lp.fw * lp.fh));
+    if (s) return s;
+    launchFragApply(p, lp, p.keyA, p.valA, nFrags, dt != nullptr, st);
+    launches += 2;
+  }
+  if (p.samples == 4) {
+    launchResolve(p, st);
+    ct->resolvedValid = true;
+    launches += 1;
+  }
+  CK(cudaGetLastError());
+  c->stats.vertices_in = p.nv;
+  c->stats.triangles_in = nIn;
+  c->stats.primitives = nStamps;
+  c->stats.bin_entries = nFrags;
+  c->stats.clip_vertices = -1;
+  c->stats.kernel_launches = launches;
+  return SGLC_OK;
+}
+
 sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
   Object *fo = c->get(bv ? bv->fbs[0] : c->fb, K_FB), *vo = c->get(c->vao, K_VAO), *po = c->get(c->prog, K_PROG);
   if (!fo || !vo || !po) return SGLC_OK;   // RendererSoft::draw is a silent no-op (RendererSoft.cpp:137-139)
@@ -379,8 +563,12 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
   ProgObj &prog = po->prog;
   if (!prog.shader) return c->fail(SGLC_ERR_INVALID_VALUE, "draw: program has no shaders");
   const sglc_render_states &rs = so->states;
-  if (rs.primitive_type != SGLC_PRIMITIVE_TRIANGLE || rs.polygon_mode != SGLC_POLYGON_FILL)
-    return c->fail(SGLC_ERR_UNSUPPORTED, "draw: only filled triangles are implemented by this back-end");
+  if (rs.primitive_type < SGLC_PRIMITIVE_POINT || rs.primitive_type > SGLC_PRIMITIVE_TRIANGLE)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "draw: unknown primitive type");
+  if (rs.polygon_mode < SGLC_POLYGON_POINT || rs.polygon_mode > SGLC_POLYGON_FILL)
+    return c->fail(SGLC_ERR_INVALID_VALUE, "draw: unknown polygon mode");
+  const bool pointsLines = rs.primitive_type != SGLC_PRIMITIVE_TRIANGLE || rs.polygon_mode != SGLC_POLYGON_FILL;
+  if (pointsLines && bv) return c->fail(SGLC_ERR_UNSUPPORTED, "draw_views: only filled triangles are batched");
   FbObj &fb = fo->fb;
   TexObj *ct = fb.colorReady ? attachmentTex(c, fb.colorTex) : nullptr;
   TexObj *dt = fb.depthReady ? attachmentTex(c, fb.depthTex) : nullptr;
@@ -421,11 +609,12 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     if (p.samp[s].valid && p.samp[s].lodFromDerivative && p.def[s]) p.needDeriv = 1;
   int iblEnabled = 0;
   memcpy(&iblEnabled, prog.uniforms + 324, sizeof(int));   // UniformsMaterial.u_enableIBL (PbrSoft.h:45)
+  if (pointsLines) iblEnabled = 0;   // points and lines run the exact shader, never the neural one
   if (p.shading == SH_PBR && prog.neural && ct && iblEnabled) {
     p.shading = SH_PBR_NEURAL;
     p.nnImage = neuralImage(prog.neural);
   }
-  if (p.shading == SH_PBR && c->capRecords) {
+  if (p.shading == SH_PBR && c->capRecords && !pointsLines) {
     p.shading = SH_PBR_CAPTURE;
     p.capRecords = c->capRecords;
     p.capCount = c->capCount;
@@ -523,6 +712,8 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
                      (u8c(cs->clear_color[2] * 255) << 16) | (u8c(cs->clear_color[3] * 255) << 24);
       p.clearDepth = cs->clear_depth;
     }
+  } else if (pointsLines) {
+    return drawPointsLines(c, p, rs, vao, ct, dt);
   } else if (c->clear.active && c->clear.fb == c->fb) {
     p.pendingClear = 1;
     p.clearColorFlag = c->clear.colorFlag && ct;
@@ -784,7 +975,8 @@ sglc_status sglc_destroy(sglc_context *ctx) {
                     &c->clipAppendOff, &c->clipPoly, &c->clipPolyTri, &c->counters, &c->tri, &c->tileCount,
                     &c->pairOff, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->tileStart, &c->tileEnd, &c->tileOrder,
                     &c->scanScratch, &c->sortHist, &c->sortHistScan, &c->staging, &c->batchU, &c->batchTargets,
-                    &c->sticky};
+                    &c->sticky, &c->lpSlot, &c->lpOrigin, &c->lpStampCount, &c->lpStampOff, &c->lpStampGeo,
+                    &c->lpStampRow, &c->lpStampColor, &c->lpStampVary, &c->lpFragCount, &c->lpFragOff, &c->lpMisc};
   for (DevBuf *b : bufs) b->release();
   cudaFreeHost(c->hostCounters);
   for (void *h : c->captureHostBufs) cudaFreeHost(h);

@@ -163,6 +163,39 @@ struct DrawParams {
   const ViewTarget *viewTarget;    // per-view attachments, or null: color / resolved / depth above
 };
 
+// Point and line draws (sglc_lines.cu; RendererSoft.cpp:301-321, 409-487, 575-712). Every input
+// primitive owns three slots (a point draw uses one, a line draw one, a triangle drawn as points or
+// as lines up to three), so slot order is the reference's drawing order. A slot becomes stamps (one
+// for a point, one per Bresenham step for a line); a stamp becomes one fragment per covered pixel;
+// the fragments are stably sorted by pixel and every pixel applies its own in stamp order.
+enum { LP_POINTS = 0, LP_LINES = 1, LP_TRI_POINTS = 2, LP_TRI_LINES = 3 };
+enum { LP_SLOT_NONE = 0, LP_SLOT_POINT = 1, LP_SLOT_LINE = 2 };
+enum { LP_ERR_BADINDEX = 1, LP_ERR_LONGLINE = 2 };
+constexpr int kMaxLineSteps = 1 << 24;   // longer lines are refused
+
+struct LineParams {
+  int mode;                       // LP_*
+  int nIn;                        // input primitives (points, lines or triangles)
+  float pointSize, lineWidth;
+  int4 *slot;                     // [3 nIn] kind, vertex a, vertex b, 0
+  float2 *pointOrigin;            // [3 nIn] fragPos.xy a point slot is stamped from
+  int *stampCount, *stampOff;     // [3 nIn], [3 nIn + 1]
+  float4 *stampGeo;               // x, y, z, size
+  int *stampRow;                  // >= 0: row of stampVary; < 0: -(vertex + 1), a row of vVary
+  float4 *stampColor;             // FS output
+  float *stampVary;               // lerped varyings of line steps, varyStride floats per stamp
+  int *fragCount, *fragOff;       // per stamp
+  int fw, fh;                     // pixel grid: the larger of the attachments
+  int *flags;                     // LP_ERR_*
+  unsigned long long *totals;     // [0] stamps, [1] fragments (64-bit, overflow checks)
+};
+
+// (int) f as x86-64 converts it (cvttss2si): truncation; INT_MIN for NaN and out-of-range values
+__device__ __forceinline__ int truncI(float f) {
+  if (!(f > -2147483904.f && f < 2147483648.f)) return (int) 0x80000000u;
+  return (int) f;
+}
+
 // uniforms of view v
 __device__ __forceinline__ const uint8_t *viewUniforms(const DrawParams &p, int view) {
   return p.viewU ? p.viewU + (size_t) view * kUniformBytes : p.u;

@@ -535,26 +535,120 @@ void scanExclusive(const int *in, int *out, const int *nPtr, int nMax, int *bloc
 
 int scanScratchInts(int nMax) { return max(1, cdiv(nMax, kScanTile)) + 1; }
 
+// ------------------------------------------------------------------------------------------------
+// points and lines: assembly, clipping and culling into drawing-order slots
+// ------------------------------------------------------------------------------------------------
+// clippingLine (RendererSoft.cpp:443-487): parametric clip against the planes either end is outside
+// of; the far end is re-made from the already re-made near end, as the reference updates
+// indices[0] before its second clippingNewVertex call. Returns false when the line is culled (or
+// the vertex capacity ran out, flagged).
+template<int SH>
+__device__ bool clipLine(const DrawParams &p, int &a, int &b) {
+  const int m0 = p.vMask[a], m1 = p.vMask[b];
+  const float4 c0 = p.vClip[a], c1 = p.vClip[b];
+  float t0 = 0.f, t1 = 1.f;
+  const int mask = m0 | m1;
+  for (int pl = 0; pl < 6 && mask; pl++) {
+    if (!(mask & (1 << pl))) continue;
+    float d0 = dot4(kPlanes[pl], c0), d1 = dot4(kPlanes[pl], c1);
+    if (d0 < 0 && d1 < 0) return false;
+    if (d0 < 0) {
+      float t = -d0 / (d1 - d0);
+      t0 = (t0 < t) ? t : t0;   // std::max
+    } else {
+      float t = d0 / (d0 - d1);
+      t1 = (t < t1) ? t : t1;   // std::min
+    }
+  }
+  if (m0) {
+    a = newClipVertex<SH>(p, 0, a, b, t0);
+    if (a < 0) return false;
+  }
+  if (m1) {
+    b = newClipVertex<SH>(p, 0, a, b, t1);
+    if (b < 0) return false;
+  }
+  return true;
+}
+
+// One thread per input primitive: processPointAssembly / processLineAssembly /
+// processPolygonAssembly (:409-437), clippingPoint / clippingLine (:439-487), face culling of
+// triangles (:277-299) and the per-triangle point / edge loops of rasterizationPolygonsPoint /
+// rasterizationPolygonsLine (:575-622). Triangles drawn as points or lines are not clipped as
+// triangles; their edges are clipped as lines, their corners as points.
+template<int SH>
+__global__ void __launch_bounds__(128) k_lp_assemble(const __grid_constant__ DrawParams p,
+                                                     const __grid_constant__ LineParams lp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= lp.nIn) return;
+  int4 *out = lp.slot + (size_t) 3 * i;
+  int4 s[3] = {make_int4(0, 0, 0, 0), make_int4(0, 0, 0, 0), make_int4(0, 0, 0, 0)};
+  const int per = lp.mode == LP_POINTS ? 1 : (lp.mode == LP_LINES ? 2 : 3);
+  int idx[3] = {0, 0, 0};
+  bool ok = true;
+  for (int k = 0; k < per; k++) {
+    idx[k] = p.indices[(size_t) per * i + k];
+    if ((unsigned) idx[k] >= (unsigned) p.nv) ok = false;
+  }
+  if (!ok) {
+    atomicOr(lp.flags, LP_ERR_BADINDEX);
+  } else if (lp.mode == LP_POINTS) {
+    if (p.vMask[idx[0]] == 0) s[0] = make_int4(LP_SLOT_POINT, idx[0], 0, 0);
+  } else if (lp.mode == LP_LINES) {
+    int a = idx[0], b = idx[1];
+    if (clipLine<SH>(p, a, b)) s[0] = make_int4(LP_SLOT_LINE, a, b, 0);
+  } else {
+    float4 a = p.vFrag[idx[0]], b = p.vFrag[idx[1]], c = p.vFrag[idx[2]];
+    f3 e1 = mk3(b.x - a.x, b.y - a.y, b.z - a.z), e2 = mk3(c.x - a.x, c.y - a.y, c.z - a.z);
+    f3 n = cross3(e1, e2);
+    float area = (n.x * 0.f + n.y * 0.f) + n.z * 1.f;
+    if (!(p.cullFace && !(area > 0))) {
+      for (int k = 0; k < 3; k++) {
+        if (lp.mode == LP_TRI_POINTS) {
+          if (p.vMask[idx[k]] == 0) s[k] = make_int4(LP_SLOT_POINT, idx[k], 0, 0);
+        } else {
+          int va = idx[k], vb = idx[(k + 1) % 3];
+          if (clipLine<SH>(p, va, vb)) s[k] = make_int4(LP_SLOT_LINE, va, vb, 0);
+        }
+      }
+    }
+  }
+  out[0] = s[0];
+  out[1] = s[1];
+  out[2] = s[2];
+}
+
 template<int SH>
 static void launchGeometry(const DrawParams &p, cudaStream_t st) {
   if (p.nv > 0) k_vertex<SH><<<cdiv(p.nv, 256), 256, 0, st>>>(p);
   if (p.ntri > 0) k_clip<SH><<<cdiv(p.ntri, 128), 128, 0, st>>>(p);
 }
 
-void launchVertexAndClip(const DrawParams &p, cudaStream_t st) {
-  switch (p.shading) {
-    case SH_BASE: launchGeometry<SH_BASE>(p, st); break;
-    case SH_BLINN: launchGeometry<SH_BLINN>(p, st); break;
-    case SH_BLINN_DIR: launchGeometry<SH_BLINN_DIR>(p, st); break;
-    case SH_PBR:
-    case SH_PBR_CAPTURE:
-    case SH_PBR_NEURAL: launchGeometry<SH_PBR>(p, st); break;
-    case SH_SKYBOX: launchGeometry<SH_SKYBOX>(p, st); break;
-    case SH_FXAA: launchGeometry<SH_FXAA>(p, st); break;
-    case SH_IBL_IRR:
-    case SH_IBL_PRE: launchGeometry<SH_IBL_IRR>(p, st); break;
-    case SH_VCOLOR: launchGeometry<SH_VCOLOR>(p, st); break;
+template<int SH>
+static void pointsLinesGeometry(const DrawParams &p, const LineParams &lp, cudaStream_t st) {
+  if (p.nv > 0) k_vertex<SH><<<cdiv(p.nv, 256), 256, 0, st>>>(p);
+  if (lp.nIn > 0) k_lp_assemble<SH><<<cdiv(lp.nIn, 128), 128, 0, st>>>(p, lp);
+}
+
+#define SGLC_GEOMETRY_SWITCH(FN, ...)                                 \
+  switch (p.shading) {                                                \
+    case SH_BASE: FN<SH_BASE>(__VA_ARGS__); break;                    \
+    case SH_BLINN: FN<SH_BLINN>(__VA_ARGS__); break;                  \
+    case SH_BLINN_DIR: FN<SH_BLINN_DIR>(__VA_ARGS__); break;          \
+    case SH_PBR:                                                      \
+    case SH_PBR_CAPTURE:                                              \
+    case SH_PBR_NEURAL: FN<SH_PBR>(__VA_ARGS__); break;               \
+    case SH_SKYBOX: FN<SH_SKYBOX>(__VA_ARGS__); break;                \
+    case SH_FXAA: FN<SH_FXAA>(__VA_ARGS__); break;                    \
+    case SH_IBL_IRR:                                                  \
+    case SH_IBL_PRE: FN<SH_IBL_IRR>(__VA_ARGS__); break;              \
+    case SH_VCOLOR: FN<SH_VCOLOR>(__VA_ARGS__); break;                \
   }
+
+void launchVertexAndClip(const DrawParams &p, cudaStream_t st) { SGLC_GEOMETRY_SWITCH(launchGeometry, p, st) }
+
+void launchPointsLinesGeometry(const DrawParams &p, const LineParams &lp, cudaStream_t st) {
+  SGLC_GEOMETRY_SWITCH(pointsLinesGeometry, p, lp, st)
 }
 
 void launchClipAppend(const DrawParams &p, cudaStream_t st) {
@@ -580,7 +674,7 @@ void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, in
   int nb = cdiv(nPairs, kSortTile);
   uint32_t *kin = p.keyA, *kout = p.keyB;
   int *vin = p.valA, *vout = p.valB;
-  int passes = keyBits <= 8 ? 1 : 2;
+  int passes = keyBits <= 8 ? 1 : (keyBits <= 16 ? 2 : (keyBits <= 24 ? 3 : 4));
   for (int pass = 0; pass < passes; pass++) {
     int shift = pass * 8;
     k_radix_hist<<<nb, kSortThreads, 0, st>>>(kin, nPtr, shift, hist, nb);
@@ -589,7 +683,7 @@ void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, in
     uint32_t *tk = kin; kin = kout; kout = tk;
     int *tv = vin; vin = vout; vout = tv;
   }
-  if (passes == 1) {   // result must land in A
+  if (passes & 1) {   // result must land in A
     cudaMemcpyAsync(p.keyA, p.keyB, sizeof(uint32_t) * (size_t) nPairs, cudaMemcpyDeviceToDevice, st);
     cudaMemcpyAsync(p.valA, p.valB, sizeof(int) * (size_t) nPairs, cudaMemcpyDeviceToDevice, st);
   }

@@ -28,4 +28,18 @@ void launchMipLevel(const DevTex &t, int face, int level, int isFloat, cudaStrea
 void launchSwizzleIn(const DevTex &t, int face, int level, const uint32_t *src, cudaStream_t st);
 void launchSwizzleOut(const DevTex &t, int face, int level, uint32_t *dst, cudaStream_t st);
 
+// point and line draws (sglc_lines.cu, sglc_lines_shade.cu, k_lp_assemble in sglc_geom.cu)
+void launchPointsLinesGeometry(const DrawParams &p, const LineParams &lp, cudaStream_t st);
+void launchPointKeys(const LineParams &lp, uint32_t *keys, int *vals, int n, cudaStream_t st);
+void launchPointChain(const DrawParams &p, const LineParams &lp, const uint32_t *keys, const int *vals, int n,
+                      cudaStream_t st);
+void launchStampCount(const DrawParams &p, const LineParams &lp, cudaStream_t st);
+void launchStampEmit(const DrawParams &p, const LineParams &lp, cudaStream_t st);
+void launchStampShade(const DrawParams &p, const LineParams &lp, int nStamps, cudaStream_t st);
+void launchFragCount(const LineParams &lp, int nStamps, cudaStream_t st);
+void launchFragEmit(const LineParams &lp, int nStamps, uint32_t *keys, int *vals, cudaStream_t st);
+void launchFragApply(const DrawParams &p, const LineParams &lp, const uint32_t *keys, const int *vals, int n,
+                     bool hasDepth, cudaStream_t st);
+void launchResolve(const DrawParams &p, cudaStream_t st);
+
 }  // namespace sglc

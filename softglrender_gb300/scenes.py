@@ -690,5 +690,107 @@ def config_pbr(seed: int = 3000, width: int = 1920, height: int = 1080, samples:
                  {"config": 3, "seed": seed, "width": width, "height": height, "samples": samples})
 
 
+def config_lines(seed: int = 6000, width: int = 640, height: int = 400, samples: int = 1, lon: int = 24,
+                 lat: int = 12, segments: int = 40, blend: bool = True, cull: bool = True) -> Scene:
+    """Points, lines and wireframe in one pass, as the reference viewer draws them with the
+    base-colour shader (Viewer.cpp:244-270; ModelLoader.cpp:40-84), plus vertex-coloured segments:
+
+    d0  a sphere in PolygonMode_LINE (wireframe), partly outside the side planes
+    d1  the world-axis grid (Primitive_LINE) on a floor plane that runs behind the camera, so the
+        near plane clips it
+    d2  seeded vertex-coloured segments, lineWidth 2, alpha blended (per-pixel order matters)
+    d3  point lights (Primitive_POINT, pointSize 10) with repeated indices: a stamp leaves the
+        vertex at its last pixel, so a repeated point walks
+    d4  a small sphere in PolygonMode_POINT (pointSize 3): every shared vertex walks too
+    d5  degenerate lines whose two ends fall in one pixel (t = 0 / 0), depth test off
+    """
+    aspect = width / height
+    eye = np.array([0.35, 0.55, 1.75])
+    Pm = perspective(np.pi / 3.0, aspect, 0.05, False)
+    Vm = look_at(eye, [0.0, 0.0, 0.0], [0, 1, 0])
+    VP = mm4(Pm, Vm)
+    model = uniforms_model(np.eye(4), VP, None, False)
+
+    def base(point_size, color):
+        return {"UniformsModel": model,
+                "UniformsMaterial": uniforms_material(False, False, False, point_size, 0.0, color)}
+
+    def rows_of(pos):
+        r = np.zeros((len(pos), 16), np.float32)
+        r[:, 0:3] = pos
+        return r
+
+    depth_less = dict(depthTest=True, depthMask=True, depthFunc=A.DepthFunc_LESS)
+    # d0: wireframe sphere
+    vert, idx = uv_sphere(lon, lat, 1.0, displace_seed=seed, amplitude=0.1)
+    d0 = DrawSpec(vert, 64, idx, A.Shading_BaseColor, (),
+                  A.RenderStates(cullFace=cull, polygonMode=A.PolygonMode_LINE, **depth_less),
+                  base(1.0, [0.9, 0.9, 0.85, 1.0]))
+    # d1: floor grid (ModelLoader::loadWorldAxis layout: lines along x and z, 0.2 apart, to +-3.2)
+    g = []
+    for i in range(-16, 17, 2):
+        g += [[-3.2, -1.1, 0.2 * i], [3.2, -1.1, 0.2 * i], [0.2 * i, -1.1, -3.2], [0.2 * i, -1.1, 3.2]]
+    gpos = np.array(g, np.float64)
+    d1 = DrawSpec(rows_of(gpos), 64, np.arange(len(gpos), dtype=np.int32), A.Shading_BaseColor, (),
+                  A.RenderStates(primitiveType=A.Primitive_LINE, **depth_less), base(1.0, [0.25, 0.25, 0.25, 1.0]))
+    # d2: vertex-coloured segments (rows: pos.xyz_, rgba), each at least a few pixels long
+    t = np.arange(segments, dtype=np.uint64)
+    a = np.stack([hash_u01(seed, 10 + k, t) * 2.4 - 1.2 for k in range(3)], axis=-1)
+    d = normalize(np.stack([hash_u01(seed, 20 + k, t) * 2.0 - 1.0 for k in range(3)], axis=-1))
+    b = a + d * (0.3 + 1.2 * hash_u01(seed, 30, t))[:, None]
+    crow = np.zeros((2 * segments, 8), np.float32)
+    crow[0::2, 0:3] = a
+    crow[1::2, 0:3] = b
+    for k in range(3):
+        crow[0::2, 4 + k] = hash_u01(seed, 40 + k, t)
+        crow[1::2, 4 + k] = hash_u01(seed, 50 + k, t)
+    crow[:, 7] = 0.6
+    bp = A.BlendParameters()
+    bp.SetBlendFactor(A.BlendFactor_SRC_ALPHA, A.BlendFactor_ONE_MINUS_SRC_ALPHA)
+    d2 = DrawSpec(crow, 32, np.arange(2 * segments, dtype=np.int32), A.Shading_VertexColor, (),
+                  A.RenderStates(blend=blend, blendParams=bp, primitiveType=A.Primitive_LINE, lineWidth=2.0,
+                                 **depth_less), base(1.0, [1, 1, 1, 1]))
+    # d3: point lights, some near the frame edges, with repeats
+    lp = np.stack([hash_u01(seed, 60 + k, np.arange(12, dtype=np.uint64)) * 3.0 - 1.5 for k in range(3)], axis=-1)
+    lp[0] = [1.2, 1.0, 0.5]
+    pidx = np.array([0, 0, 0, 1, 2, 3, 3, 4, 5, 6, 7, 8, 9, 10, 11, 11, 11, 11, 5], np.int32)
+    d3 = DrawSpec(rows_of(lp), 64, pidx, A.Shading_BaseColor, (),
+                  A.RenderStates(primitiveType=A.Primitive_POINT, **depth_less), base(10.0, [1.0, 0.85, 0.3, 1.0]))
+    # d4: small sphere drawn as points
+    sv, si = uv_sphere(12, 6, 0.35)
+    sv = sv.copy()
+    sv[:, 0:3] += np.array([-0.9, 0.75, 0.2], np.float32)
+    d4 = DrawSpec(sv, 64, si, A.Shading_BaseColor, (),
+                  A.RenderStates(cullFace=False, polygonMode=A.PolygonMode_POINT, **depth_less),
+                  base(3.0, [0.3, 0.9, 0.4, 1.0]))
+    # d5: degenerate lines (both ends in one pixel), depth test off
+    q = np.stack([hash_u01(seed, 70 + k, np.arange(6, dtype=np.uint64)) * 1.6 - 0.8 for k in range(3)], axis=-1)
+    qq = np.repeat(q, 2, axis=0)
+    qq[1::2] += 1e-4
+    d5 = DrawSpec(rows_of(qq), 64, np.arange(len(qq), dtype=np.int32), A.Shading_BaseColor, (),
+                  A.RenderStates(primitiveType=A.Primitive_LINE), base(1.0, [0.2, 0.5, 1.0, 1.0]))
+    clear = A.ClearStates(True, True, (0.05, 0.05, 0.08, 1.0), 1.0)
+    return Scene("lines", [PassSpec(width, height, samples, clear, [d0, d1, d2, d3, d4, d5])],
+                 {"seed": seed, "width": width, "height": height, "samples": samples})
+
+
+def config_wireframe(seed: int = 6100, width: int = 1920, height: int = 1080, samples: int = 1, lon: int = 448,
+                     lat: int = 224, distance: float = 2.4) -> Scene:
+    """The viewer's wireframe mode on the benchmark sphere: base colour, PolygonMode_LINE, back faces
+    culled, depth LESS (Viewer.cpp:264-270)."""
+    vert, idx = uv_sphere(lon, lat, 1.0, displace_seed=seed, amplitude=0.1)
+    eye = np.array([0.0, 0.3, distance])
+    Pm = perspective(np.pi / 3.0, width / height, 0.05, False)
+    Vm = look_at(eye, [0.0, 0.0, 0.0], [0, 1, 0])
+    blocks = {"UniformsModel": uniforms_model(np.eye(4), mm4(Pm, Vm), None, False),
+              "UniformsMaterial": uniforms_material(False, False, False, 1.0, 0.0, [0.9, 0.9, 0.9, 1.0])}
+    st = A.RenderStates(depthTest=True, depthMask=True, depthFunc=A.DepthFunc_LESS, cullFace=True,
+                        polygonMode=A.PolygonMode_LINE)
+    draw = DrawSpec(vert, 64, idx, A.Shading_BaseColor, (), st, blocks)
+    clear = A.ClearStates(True, True, (0.0, 0.0, 0.0, 1.0), 1.0)
+    return Scene("wireframe", [PassSpec(width, height, samples, clear, [draw])],
+                 {"seed": seed, "width": width, "height": height, "samples": samples})
+
+
 def output_digest(arrs: Dict[str, np.ndarray]) -> Dict[str, str]:
     return {k: hashlib.sha256(np.ascontiguousarray(v).tobytes()).hexdigest()[:16] for k, v in sorted(arrs.items())}

@@ -108,11 +108,22 @@ def test_unknown_shading_model_unsupported(lib):
 
 
 @pytest.mark.parametrize("lib", _backends(), indirect=True)
-def test_lines_and_points_report_unsupported(lib):
-    scene = soup(10, 32, 32, 1, [A.RenderStates(primitiveType=A.Primitive_LINE)])
-    with pytest.raises(A.SoftGLError) as e:
-        render(lib, scene)
-    assert e.value.status == 5
+def test_unknown_primitive_type_or_polygon_mode_rejected(lib):
+    for states in (A.RenderStates(primitiveType=7), A.RenderStates(polygonMode=-1)):
+        scene = soup(10, 32, 32, 1, [states])
+        with pytest.raises(A.SoftGLError) as e:
+            render(lib, scene)
+        assert e.value.status == A.SGLC_ERR_INVALID_VALUE
+
+
+@pytest.mark.parametrize("lib", _backends(), indirect=True)
+def test_line_soup_draws(lib):
+    """A triangle soup's index buffer drawn as lines (pairs of indices) and as points."""
+    for states in (A.RenderStates(primitiveType=A.Primitive_LINE), A.RenderStates(primitiveType=A.Primitive_POINT)):
+        scene = soup(40, 48, 32, 1, [states])
+        outs, _ = render(lib, scene)
+        c = outs[0]["color"]
+        assert np.any(c != c[0, 0])
 
 
 @pytest.mark.parametrize("lib", _backends(), indirect=True)
