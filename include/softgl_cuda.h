@@ -191,6 +191,17 @@ SGLC_API sglc_status sglc_texture_set_level_data(sglc_context *ctx, sglc_handle 
  * (RGBA8: 16 B/pixel; FLOAT32: 16 B/pixel) and 1 returns the resolved RGBA8 image. */
 SGLC_API sglc_status sglc_texture_read_image(sglc_context *ctx, sglc_handle tex, int32_t layer, int32_t level,
                                              int32_t resolved, void *out, size_t bytes);
+/* TextureSoft::storeToFile / TextureSoft::loadFromFile (TextureSoft.h:166-215), the format of the
+ * viewer's IBL texture cache (IBLGenerator::storeToCache / loadFromCache, Environment.cpp:205-239):
+ * for every layer, for every mip level, the level's raw texels in the storage order of its buffer
+ * layout (Buffer::convertIndex, Buffer.h:31-33, 151-157, 193-202), padding texels of the Tiled 4x4 /
+ * Morton 32x32 layouts included; 4 B per texel (RGBA8 or FLOAT32), 4 samples per texel for a
+ * multi-sample texture. Attachments and multi-sample textures are stored Linear. A texture with no
+ * image data writes and reads nothing. Load reads exactly the bytes it needs (a longer file is
+ * accepted, a shorter one fails with SGLC_ERR_INVALID_VALUE and leaves the texture unchanged);
+ * an unopenable path fails with SGLC_ERR_INVALID_VALUE. */
+SGLC_API sglc_status sglc_texture_store_to_file(sglc_context *ctx, sglc_handle tex, const char *path);
+SGLC_API sglc_status sglc_texture_load_from_file(sglc_context *ctx, sglc_handle tex, const char *path);
 
 /* ---- vertex array (Renderer::createVertexArrayObject, Renderer.h:37; VertexSoft.h:16-31) ---- */
 SGLC_API sglc_status sglc_create_vertex_array(sglc_context *ctx, const void *vertexes, size_t vertexes_len,

@@ -11,6 +11,7 @@
  * shader-pair loading that ViewerSoftware::loadShaders does (src/Viewer/ViewerSoftware.h:54-69),
  * and read-back of attachments in linear order (Buffer::get, src/Base/Buffer.h:86-99).
  */
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -277,6 +278,28 @@ sglc_status sglr_texture_read_image(sglc_context *ctx, sglc_handle tex, int32_t 
     ok = readTexture(dynamic_cast<TextureSoft<float> *>(t->tex.get()), layer, level, resolved, (uint8_t *) out, bytes);
   }
   return ok ? SGLC_OK : c->fail(SGLC_ERR_INVALID_VALUE, "read_image: bad level or size");
+}
+
+sglc_status sglr_texture_store_to_file(sglc_context *ctx, sglc_handle tex, const char *path) {
+  auto *c = reinterpret_cast<Ctx *>(ctx);
+  Object *t = c->get(tex);
+  CTX_CHECK(t && t->tex && path);
+  FILE *probe = fopen(path, "ab");   // storeToFile only logs a failed open
+  if (!probe) return c->fail(SGLC_ERR_INVALID_VALUE, "store_to_file: failed to open file");
+  fclose(probe);
+  if (t->tex->format == TextureFormat_RGBA8) dynamic_cast<TextureSoft<RGBA> *>(t->tex.get())->storeToFile(path);
+  else dynamic_cast<TextureSoft<float> *>(t->tex.get())->storeToFile(path);
+  return SGLC_OK;
+}
+
+sglc_status sglr_texture_load_from_file(sglc_context *ctx, sglc_handle tex, const char *path) {
+  auto *c = reinterpret_cast<Ctx *>(ctx);
+  Object *t = c->get(tex);
+  CTX_CHECK(t && t->tex && path);
+  bool ok;
+  if (t->tex->format == TextureFormat_RGBA8) ok = dynamic_cast<TextureSoft<RGBA> *>(t->tex.get())->loadFromFile(path);
+  else ok = dynamic_cast<TextureSoft<float> *>(t->tex.get())->loadFromFile(path);
+  return ok ? SGLC_OK : c->fail(SGLC_ERR_INVALID_VALUE, "load_from_file: failed");
 }
 
 sglc_status sglr_create_vertex_array(sglc_context *ctx, const void *vertexes, size_t vertexes_len, size_t stride,

@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -1701,6 +1702,42 @@ static void allocLevels(TextureObj &t, bool withMips) {
   }
 }
 
+// ---- texture files (TextureSoft::storeToFile / loadFromFile, TextureSoft.h:166-215) ------------
+// Storage layout of a texture: attachments and multi-sample textures are Linear, others keep the
+// layout of their description (the product's per-texture choice of the reference's compile-time
+// Buffer layout).
+static int storageLayout(const TextureObj &t) {
+  bool attachment = (t.desc.usage & (4u | 8u)) != 0;
+  if (attachment || t.desc.multi_sample) return SGLC_LAYOUT_LINEAR;
+  return t.desc.layout;
+}
+
+// Buffer::initLayout + convertIndex (Buffer.h:26-33, 144-157, 175-202): the storage extent and the
+// storage index of texel (x, y)
+static size_t storageTexels(int layout, int w, int h) {
+  if (layout == SGLC_LAYOUT_TILED) return (size_t) ((w + 3) / 4) * 4 * (size_t) ((h + 3) / 4) * 4;
+  if (layout == SGLC_LAYOUT_MORTON) return (size_t) ((w + 31) / 32) * 32 * (size_t) ((h + 31) / 32) * 32;
+  return (size_t) w * h;
+}
+
+static inline uint32_t spreadBits5(uint32_t v) {
+  uint32_t r = 0;
+  for (int b = 0; b < 5; b++) r |= ((v >> b) & 1u) << (2 * b);
+  return r;
+}
+
+static size_t storageIndex(int layout, int w, int x, int y) {
+  if (layout == SGLC_LAYOUT_TILED) {
+    size_t tile = (size_t) (y >> 2) * (size_t) ((w + 3) / 4) + (size_t) (x >> 2);
+    return (tile << 4) + ((size_t) (y & 3) << 2) + (size_t) (x & 3);
+  }
+  if (layout == SGLC_LAYOUT_MORTON) {
+    size_t tile = (size_t) (y >> 5) * (size_t) ((w + 31) / 32) + (size_t) (x >> 5);
+    return (tile << 10) + (spreadBits5((uint32_t) (x & 31)) | (spreadBits5((uint32_t) (y & 31)) << 1));
+  }
+  return (size_t) y * w + x;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1831,6 +1868,58 @@ sglc_status sglo_texture_read_image(sglc_context *ctx, sglc_handle tex, int32_t 
   }
   if (bytes < n * 4 * L.samples) return c->fail(SGLC_ERR_INVALID_VALUE, "read_image: size");
   memcpy(out, L.data.data(), n * 4 * L.samples);
+  return SGLC_OK;
+}
+
+sglc_status sglo_texture_store_to_file(sglc_context *ctx, sglc_handle tex, const char *path) {
+  CTX;
+  GET(t, tex, 2);
+  if (!path) return c->fail(SGLC_ERR_INVALID_VALUE, "store_to_file: null path");
+  TextureObj &T = t->tex;
+  const int layout = storageLayout(T);
+  std::vector<uint32_t> raw;
+  for (int layer = 0; layer < T.layers; layer++)
+    for (const Level &L : T.img[layer]) {
+      size_t base = raw.size();
+      raw.resize(base + storageTexels(layout, L.w, L.h) * L.samples, 0u);
+      for (int y = 0; y < L.h; y++)
+        for (int x = 0; x < L.w; x++)
+          for (int s = 0; s < L.samples; s++)
+            raw[base + storageIndex(layout, L.w, x, y) * L.samples + s] = L.data[((size_t) y * L.w + x) * L.samples + s];
+    }
+  FILE *f = fopen(path, "wb");
+  if (!f) return c->fail(SGLC_ERR_INVALID_VALUE, (std::string("store_to_file: failed to open file: ") + path).c_str());
+  size_t wrote = raw.empty() ? 0 : fwrite(raw.data(), 4, raw.size(), f);
+  int closed = fclose(f);
+  if (wrote != raw.size() || closed != 0)
+    return c->fail(SGLC_ERR_INVALID_VALUE, (std::string("store_to_file: failed to write file: ") + path).c_str());
+  return SGLC_OK;
+}
+
+sglc_status sglo_texture_load_from_file(sglc_context *ctx, sglc_handle tex, const char *path) {
+  CTX;
+  GET(t, tex, 2);
+  if (!path) return c->fail(SGLC_ERR_INVALID_VALUE, "load_from_file: null path");
+  TextureObj &T = t->tex;
+  const int layout = storageLayout(T);
+  FILE *f = fopen(path, "rb");
+  if (!f) return c->fail(SGLC_ERR_INVALID_VALUE, (std::string("load_from_file: failed to open file: ") + path).c_str());
+  size_t total = 0;
+  for (int layer = 0; layer < T.layers; layer++)
+    for (const Level &L : T.img[layer]) total += storageTexels(layout, L.w, L.h) * L.samples;
+  std::vector<uint32_t> raw(total);
+  size_t got = total ? fread(raw.data(), 4, total, f) : 0;
+  fclose(f);
+  if (got != total) return c->fail(SGLC_ERR_INVALID_VALUE, (std::string("load_from_file: failed to read file: ") + path).c_str());
+  size_t base = 0;
+  for (int layer = 0; layer < T.layers; layer++)
+    for (Level &L : T.img[layer]) {
+      for (int y = 0; y < L.h; y++)
+        for (int x = 0; x < L.w; x++)
+          for (int s = 0; s < L.samples; s++)
+            L.data[((size_t) y * L.w + x) * L.samples + s] = raw[base + storageIndex(layout, L.w, x, y) * L.samples + s];
+      base += storageTexels(layout, L.w, L.h) * L.samples;
+    }
   return SGLC_OK;
 }
 

@@ -15,6 +15,7 @@ returns instead (RendererSoft.cpp:33,137-139), which a caller gets by catching t
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 from typing import Dict, Optional, Sequence
 
@@ -179,6 +180,8 @@ _SIGS = {
     "texture_set_image_data": [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p), C.c_size_t],
     "texture_set_level_data": [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t],
     "texture_read_image": [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t],
+    "texture_store_to_file": [C.c_void_p, C.c_int32, C.c_char_p],
+    "texture_load_from_file": [C.c_void_p, C.c_int32, C.c_char_p],
     "create_vertex_array": [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p, C.c_size_t,
                             C.POINTER(C.c_int32)],
     "vertex_array_update": [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t],
@@ -284,6 +287,7 @@ class Texture(_Resource):
         self.width, self.height = desc.width, desc.height
         self.type, self.format = desc.type, desc.format
         self.useMipmaps, self.multiSample = desc.useMipmaps, desc.multiSample
+        self.tag = ""   # Texture::tag (Texture.h:98): names the IBL cache entry
 
     @property
     def layerCount(self) -> int:
@@ -327,6 +331,21 @@ class Texture(_Resource):
         self.renderer._call("texture_read_image", self.handle, layer, level, int(resolved),
                             out.ctypes.data_as(C.c_void_p), out.nbytes)
         return out
+
+
+    def storeToFile(self, path: str) -> None:
+        """TextureSoft::storeToFile: every layer and level, raw texels in storage layout order."""
+        self.renderer._call("texture_store_to_file", self.handle, os.fsencode(path))
+
+    def loadFromFile(self, path: str) -> bool:
+        """TextureSoft::loadFromFile: False (texture unchanged) when the file is missing or short."""
+        try:
+            self.renderer._call("texture_load_from_file", self.handle, os.fsencode(path))
+        except SoftGLError as e:
+            if e.status != SGLC_ERR_INVALID_VALUE:
+                raise
+            return False
+        return True
 
 
 class VertexArrayObject(_Resource):

@@ -1148,6 +1148,83 @@ sglc_status sglc_texture_read_image(sglc_context *ctx, sglc_handle tex, int32_t 
   return SGLC_OK;
 }
 
+// raw texels of one level in its storage layout, padding included (Buffer::getRawDataBytesSize)
+static size_t levelStorageTexels(const TexObj &T, int level) {
+  int w = T.w[level], h = T.h[level];
+  size_t n;
+  if (T.desc.layout == LAYOUT_TILED) n = (size_t) ((w + 3) / 4) * 4 * ((h + 3) / 4) * 4;
+  else if (T.desc.layout == LAYOUT_MORTON) n = (size_t) ((w + 31) / 32) * 32 * ((h + 31) / 32) * 32;
+  else n = (size_t) w * h;
+  return n * T.samplesPerTexel;
+}
+
+// TextureSoft::storeToFile (TextureSoft.h:195-215): layers x levels of raw storage, in order
+sglc_status sglc_texture_store_to_file(sglc_context *ctx, sglc_handle tex, const char *path) {
+  CTX;
+  GET(t, tex, K_TEX);
+  if (!path) return c->fail(SGLC_ERR_INVALID_VALUE, "store_to_file: null path");
+  if (c->capturing) return c->fail(SGLC_ERR_UNSUPPORTED, "store_to_file: not capturable in a graph");
+  TexObj &T = t->tex;
+  sglc_status s = flushClear(c);
+  if (s) return s;
+  std::vector<uint32_t> host;
+  if (T.allocated) {
+    size_t total = 0;
+    for (int l = 0; l < T.levels; l++) total += levelStorageTexels(T, l);
+    host.resize(total * (size_t) T.layers);
+    size_t o = 0;
+    for (int layer = 0; layer < T.layers; layer++)
+      for (int l = 0; l < T.levels; l++) {
+        size_t n = levelStorageTexels(T, l);
+        CK(cudaMemcpyAsync(host.data() + o, T.dev + (size_t) layer * T.layerStride + T.offset[l], n * 4,
+                           cudaMemcpyDeviceToHost, c->stream));
+        o += n;
+      }
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  FILE *f = fopen(path, "wb");
+  if (!f) return c->fail(SGLC_ERR_INVALID_VALUE, std::string("store_to_file: failed to open file: ") + path);
+  size_t wrote = host.empty() ? 0 : fwrite(host.data(), 4, host.size(), f);
+  int closed = fclose(f);
+  if (wrote != host.size() || closed != 0)
+    return c->fail(SGLC_ERR_INVALID_VALUE, std::string("store_to_file: failed to write file: ") + path);
+  return SGLC_OK;
+}
+
+// TextureSoft::loadFromFile (TextureSoft.h:166-193)
+sglc_status sglc_texture_load_from_file(sglc_context *ctx, sglc_handle tex, const char *path) {
+  CTX;
+  GET(t, tex, K_TEX);
+  if (!path) return c->fail(SGLC_ERR_INVALID_VALUE, "load_from_file: null path");
+  if (c->capturing) return c->fail(SGLC_ERR_UNSUPPORTED, "load_from_file: not capturable in a graph");
+  TexObj &T = t->tex;
+  FILE *f = fopen(path, "rb");
+  if (!f) return c->fail(SGLC_ERR_INVALID_VALUE, std::string("load_from_file: failed to open file: ") + path);
+  if (!T.allocated) {   // no image data: nothing to read
+    fclose(f);
+    return SGLC_OK;
+  }
+  size_t total = 0;
+  for (int l = 0; l < T.levels; l++) total += levelStorageTexels(T, l);
+  total *= (size_t) T.layers;
+  std::vector<uint32_t> host(total);
+  size_t got = total ? fread(host.data(), 4, total, f) : 0;
+  fclose(f);
+  if (got != total) return c->fail(SGLC_ERR_INVALID_VALUE, std::string("load_from_file: failed to read file: ") + path);
+  sglc_status s = flushClear(c);
+  if (s) return s;
+  size_t o = 0;
+  for (int layer = 0; layer < T.layers; layer++)
+    for (int l = 0; l < T.levels; l++) {
+      size_t n = levelStorageTexels(T, l);
+      CK(cudaMemcpyAsync(T.dev + (size_t) layer * T.layerStride + T.offset[l], host.data() + o, n * 4,
+                         cudaMemcpyHostToDevice, c->stream));
+      o += n;
+    }
+  CK(cudaStreamSynchronize(c->stream));   // the host staging vector goes out of scope
+  return SGLC_OK;
+}
+
 sglc_status sglc_create_vertex_array(sglc_context *ctx, const void *vertexes, size_t vlen, size_t stride,
                                      const int32_t *indices, size_t ilen, sglc_handle *out) {
   CTX;

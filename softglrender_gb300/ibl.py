@@ -7,6 +7,8 @@ draws of the corresponding shading models (their fragment shaders run on the CUD
 """
 from __future__ import annotations
 
+import hashlib
+import os
 from typing import Optional
 
 import numpy as np
@@ -47,9 +49,21 @@ def _face_mvp(face: int) -> np.ndarray:
     return S.mm4(P, R)
 
 
+def cache_key(tex: A.Texture) -> str:
+    """IBLGenerator::getTextureHashKey (Environment.cpp:197-199): MD5 of tag + width + height, as
+    32 lower-case hex digits."""
+    return hashlib.md5((tex.tag + str(tex.width) + str(tex.height)).encode()).hexdigest()
+
+
 class IBLGenerator:
-    def __init__(self, r: A.Renderer):
+    """`cache_dir` (IBL_TEX_CACHE_DIR, Environment.cpp:17): when set, every generated map is looked
+    up in the cache first (loadFromCache) and stored there after it is drawn (storeToCache),
+    one <md5>.tex file per map in the TextureSoft::storeToFile format."""
+
+    def __init__(self, r: A.Renderer, cache_dir: Optional[str] = None):
         self.r = r
+        self.cache_dir = cache_dir
+        self.cache_hits = 0
         rows, idx = cube_mesh()
         self.vao = r.createVertexArrayObject(rows, 64, idx)
         self.fbo = r.createFrameBuffer(offscreen=True)
@@ -89,6 +103,25 @@ class IBLGenerator:
             r.draw()
             r.endRenderPass()
 
+    def cache_path(self, tex: A.Texture) -> str:
+        """IBLGenerator::getCacheFilePath (Environment.cpp:201-204)."""
+        return os.path.join(self.cache_dir, cache_key(tex) + ".tex")
+
+    def _load_from_cache(self, tex: A.Texture) -> bool:
+        """IBLGenerator::loadFromCache (Environment.cpp:206-222)."""
+        if self.cache_dir is None or not os.path.exists(self.cache_path(tex)):
+            return False
+        ok = tex.loadFromFile(self.cache_path(tex))
+        self.cache_hits += int(ok)
+        return ok
+
+    def _store_to_cache(self, tex: A.Texture) -> None:
+        """IBLGenerator::storeToCache (Environment.cpp:224-239)."""
+        if self.cache_dir is None:
+            return
+        os.makedirs(self.cache_dir, exist_ok=True)
+        tex.storeToFile(self.cache_path(tex))
+
     def _cube(self, size: int, mipmaps: bool) -> A.Texture:
         t = self.r.createTexture(A.TextureDesc(size, size, A.TextureType_CUBE, A.TextureFormat_RGBA8,
                                                A.TextureUsage_AttachmentColor | A.TextureUsage_Sampler,
@@ -102,21 +135,33 @@ class IBLGenerator:
     def convert_equirectangular(self, equirect: A.Texture, size: int) -> A.Texture:
         """IBLGenerator::convertEquirectangular: the skybox shader with EQUIRECTANGULAR_MAP."""
         out = self._cube(size, False)
+        out.tag = equirect.tag + ".cubeMap"
+        if self._load_from_cache(out):
+            return out
         self._draw_faces(A.Shading_Skybox, ("EQUIRECTANGULAR_MAP",), "u_equirectangularMap", equirect, out)
+        self._store_to_cache(out)
         return out
 
     def irradiance(self, cube: A.Texture, size: int = K_IRRADIANCE_SIZE) -> A.Texture:
         """IBLGenerator::generateIrradianceMap."""
         out = self._cube(size, False)
+        out.tag = cube.tag + ".irradianceMap"
+        if self._load_from_cache(out):
+            return out
         self._draw_faces(A.Shading_IBL_Irradiance, (), "u_cubeMap", cube, out)
+        self._store_to_cache(out)
         return out
 
     def prefilter(self, cube: A.Texture, size: int = K_PREFILTER_SIZE, levels: int = K_PREFILTER_LEVELS) -> A.Texture:
         """IBLGenerator::generatePrefilterMap: roughness level / (levels - 1) for mip `level`."""
         out = self._cube(size, True)
+        out.tag = cube.tag + ".prefilterMap"
+        if self._load_from_cache(out):
+            return out
         for level in range(levels):
             block = np.array([float(cube.width), level / float(levels - 1)], np.float32).tobytes()
             self._draw_faces(A.Shading_IBL_Prefilter, (), "u_cubeMap", cube, out, level, block)
+        self._store_to_cache(out)
         return out
 
 
