@@ -99,6 +99,14 @@ void TextureCUDA::dumpImage(const char *path, uint32_t layer, uint32_t level) {
   }
 }
 
+bool TextureCUDA::loadFromFile(const char *path) {
+  return renderer->check(sglc_texture_load_from_file(renderer->ctx(), handle, path), "loadFromFile");
+}
+
+void TextureCUDA::storeToFile(const char *path) {
+  renderer->check(sglc_texture_store_to_file(renderer->ctx(), handle, path), "storeToFile");
+}
+
 bool FrameBufferCUDA::isValid() {
   int32_t v = 0;
   renderer->check(sglc_framebuffer_is_valid(renderer->ctx(), handle, &v), "isValid");

@@ -27,6 +27,9 @@ class TextureCUDA : public Texture {
   void setImageData(const std::vector<std::shared_ptr<Buffer<RGBA>>> &buffers) override;
   void setImageData(const std::vector<std::shared_ptr<Buffer<float>>> &buffers) override;
   void dumpImage(const char *path, uint32_t layer, uint32_t level) override;
+  // TextureSoft::loadFromFile / storeToFile (TextureSoft.h:166-215): the IBL cache format
+  bool loadFromFile(const char *path);
+  void storeToFile(const char *path);
 
   RendererCUDA *renderer;
   sglc_handle handle;
