@@ -264,6 +264,10 @@ SGLC_API sglc_status sglc_set_stats_level(sglc_context *ctx, int32_t level);
 SGLC_API sglc_status sglc_get_stream(sglc_context *ctx, void **stream);
 /* Raster tile edge in pixels (8, 16 or 32); picked by the autotuner, default 16. */
 SGLC_API sglc_status sglc_set_tile_size(sglc_context *ctx, int32_t tile);
+/* 1 (default): shading models with a heavy fragment shader (Blinn-Phong, PBR, skybox / IBL, FXAA)
+ * rasterise in three kernels: coverage and depth, then the fragment shader over every fragment, then
+ * the colour operations in each pixel's order. 0: one fused raster kernel. Same images either way. */
+SGLC_API sglc_status sglc_set_deferred_shading(sglc_context *ctx, int32_t enable);
 
 /* ---- synchronisation-free draws and CUDA graphs (no reference counterpart) ------------------- */
 /* Working-array capacities of a draw (a batched draw counts all its views together). */
@@ -273,6 +277,8 @@ typedef struct sglc_capacity {
   int64_t appended_primitives;   /* fan triangles appended after clipping */
   int64_t bin_entries;           /* (tile, triangle) pairs */
   int32_t heavy_first;           /* 1: raster the longest tile lists first; 0: tiles in index order */
+  int64_t fragments;             /* fragment records of deferred shading (0: those draws use the
+                                    single raster kernel) */
 } sglc_capacity;
 /* With capacities set, draws size their working arrays from them instead of reading counts back
  * from the device after the setup stage: a draw then never waits for the GPU, and draws can be
@@ -285,7 +291,7 @@ SGLC_API sglc_status sglc_set_capacity(sglc_context *ctx, const sglc_capacity *c
 SGLC_API sglc_status sglc_get_peak_counts(sglc_context *ctx, sglc_capacity *out);
 /* Synchronises, returns and clears the overflow flags of the draws since the last call: bit 0 clip
  * vertices, 1 clip polygons, 2 appended primitives, 3 bin entries, 4 an index outside the vertex
- * array. */
+ * array, 5 fragment records. */
 SGLC_API sglc_status sglc_get_overflow(sglc_context *ctx, int32_t *flags);
 typedef struct sglc_graph sglc_graph;
 /* Capture everything enqueued on the context between begin and end into a CUDA graph. Draws in the

@@ -215,6 +215,7 @@ _SIGS = {
     "get_overflow": [C.c_void_p, C.POINTER(C.c_int32)],
     "get_peak_counts": [C.c_void_p, C.c_void_p],
     "set_tile_size": [C.c_void_p, C.c_int32],
+    "set_deferred_shading": [C.c_void_p, C.c_int32],
 }
 
 ABI_FUNCTIONS = tuple(_SIGS) + ("last_error",)
@@ -223,7 +224,7 @@ ABI_FUNCTIONS = tuple(_SIGS) + ("last_error",)
 class Capacity(C.Structure):
     """sglc_capacity: working-array capacities of synchronisation-free draws."""
     _fields_ = [("clip_vertices", C.c_int64), ("clip_polygons", C.c_int64), ("appended_primitives", C.c_int64),
-                ("bin_entries", C.c_int64), ("heavy_first", C.c_int32)]
+                ("bin_entries", C.c_int64), ("heavy_first", C.c_int32), ("fragments", C.c_int64)]
 
 
 class Library:
@@ -561,3 +562,8 @@ class Renderer:
 
     def setTileSize(self, tile: int) -> None:
         self._call("set_tile_size", tile)
+
+    def setDeferredShading(self, enable: bool) -> None:
+        """Extension: rasterise heavy shading models in coverage / shade / ROP kernels (default) or
+        in one fused kernel; the images are the same."""
+        self._call("set_deferred_shading", int(enable))

@@ -38,7 +38,8 @@ class TuneResult:
         return {"tile": self.tile, "threads_per_tile": self.threads_per_tile, "heavy_first": self.heavy_first,
                 "graph": self.graph, "ms": round(self.ms, 4),
                 "capacity": {"clip_vertices": c.clip_vertices, "clip_polygons": c.clip_polygons,
-                             "appended_primitives": c.appended_primitives, "bin_entries": c.bin_entries},
+                             "appended_primitives": c.appended_primitives, "bin_entries": c.bin_entries,
+                             "fragments": c.fragments},
                 "candidates": self.table}
 
 
@@ -89,7 +90,8 @@ def autotune(r: A.Renderer, frame: Callable[[], None], headroom: float = 1.25, r
     cap = A.Capacity(max(1024, int(pk.clip_vertices * headroom) + 1024),
                      max(1024, int(pk.clip_polygons * headroom) + 1024),
                      max(1024, int(pk.appended_primitives * headroom) + 1024),
-                     max(4096, int(pk.bin_entries * headroom) + 4096), 1)
+                     max(4096, int(pk.bin_entries * headroom) + 4096), 1,
+                     int(pk.fragments * headroom) + 4096 if pk.fragments else 0)
     # fit the capacities once (eager); every candidate then uses them unchanged, so no working array
     # grows (and no captured graph loses its buffers) after the first capture
     for _ in range(8):
@@ -98,7 +100,7 @@ def autotune(r: A.Renderer, frame: Callable[[], None], headroom: float = 1.25, r
         if r.getOverflow() == 0:
             break
         cap = A.Capacity(cap.clip_vertices * 2, cap.clip_polygons * 2, cap.appended_primitives * 2,
-                         cap.bin_entries * 2, 1)
+                         cap.bin_entries * 2, 1, cap.fragments * 2)
     else:
         r.setCapacity(None)
         raise RuntimeError("autotune: the frame does not fit its capacities")
@@ -124,7 +126,7 @@ def autotune(r: A.Renderer, frame: Callable[[], None], headroom: float = 1.25, r
                 if best_graph is not None:
                     best_graph.destroy()
                 best = TuneResult(A.Capacity(cap.clip_vertices, cap.clip_polygons, cap.appended_primitives,
-                                             cap.bin_entries, hf), hf, use_graph, ms)
+                                             cap.bin_entries, hf, cap.fragments), hf, use_graph, ms)
                 best_graph = g
             elif g is not None:
                 g.destroy()

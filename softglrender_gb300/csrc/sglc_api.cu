@@ -195,6 +195,8 @@ struct Ctx {
   DevBuf vClip, vFrag, vMask, vVary, vAttrExtra, prims, clipExtra, clipAppendOff, clipPoly, clipPolyTri, counters;
   DevBuf tri, tileCount, pairOff, keyA, keyB, valA, valB, tileStart, tileEnd, tileOrder, scanScratch, sortHist,
       sortHistScan, staging, batchU, batchTargets;
+  DevBuf recA, recB, recColor, chunkNext, chunkFill, warpHead;   // deferred shading
+  bool deferredShading = true;
   DevBuf lpSlot, lpOrigin, lpStampCount, lpStampOff, lpStampGeo, lpStampRow, lpStampColor, lpStampVary, lpFragCount,
       lpFragOff, lpMisc;   // point and line draws
   // capacity hints that survive between draws
@@ -822,10 +824,12 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     CK(cudaGetLastError());
     if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[1], c->stream));
     int newVerts = -1, polys = -1, np = p.primCap, nPairs;
+    unsigned long long fragBound = 0;   // upper bound on fragment records (exact sizing only)
     const int *nPairsDev = p.pairOff + p.primCap;
     if (!deferred) {
       CK(cudaMemcpyAsync(c->hostCounters, p.counters, sizeof(int) * 4, cudaMemcpyDeviceToHost, c->stream));
       CK(cudaMemcpyAsync(c->hostCounters + 4, p.pairOff + p.primCap, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaMemcpyAsync(c->hostCounters + 6, p.counters + kCntBound, 8, cudaMemcpyDeviceToHost, c->stream));
       CK(cudaStreamSynchronize(c->stream));
       newVerts = c->hostCounters[0];
       polys = c->hostCounters[1];
@@ -843,6 +847,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       c->peak.clip_polygons = std::max<int64_t>(c->peak.clip_polygons, polys);
       c->peak.appended_primitives = std::max<int64_t>(c->peak.appended_primitives, (int64_t) np - p.ntri);
       c->peak.bin_entries = std::max<int64_t>(c->peak.bin_entries, nPairs);
+      memcpy(&fragBound, c->hostCounters + 6, 8);
     } else {
       // no read-back: the bin arrays have the set capacity, the sort and ranges read the pair count
       // (clamped to it) from the device
@@ -885,8 +890,34 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       CK(cudaMemsetAsync(c->fragCounter, 0, sizeof(unsigned long long), c->stream));
       p.fragCounter = c->fragCounter;
     }
+    // deferred shading: records = the bound from setup, plus a partly filled last chunk per warp
+    bool deferShade = c->deferredShading && ct && deferredShadingModel(p.shading);
+    long long chunks = 0;
+    if (deferShade) {
+      const long long warps = (long long) numTiles * 8;
+      chunks = deferred ? (c->cap.fragments + kChunk - 1) / kChunk
+                        : (long long) (fragBound / kChunk) + warps + 1;
+      if (!deferred) c->peak.fragments = std::max<int64_t>(c->peak.fragments, chunks * kChunk);
+      if (chunks < 1 || chunks * kChunk > (1ll << 27)) deferShade = false;   // single kernel instead
+    }
+    if (deferShade) {
+      CK(c->recA.ensure(sizeof(int4) * (size_t) chunks * kChunk));
+      CK(c->recB.ensure(sizeof(float2) * (size_t) chunks * kChunk));
+      CK(c->recColor.ensure(sizeof(float4) * (size_t) chunks * kChunk));
+      CK(c->chunkNext.ensure(sizeof(int) * (size_t) chunks));
+      CK(c->chunkFill.ensure(sizeof(int) * (size_t) chunks));
+      CK(c->warpHead.ensure(sizeof(int) * (size_t) numTiles * 8));
+      p.recA = c->recA.as<int4>();
+      p.recB = c->recB.as<float2>();
+      p.recColor = c->recColor.as<float4>();
+      p.chunkNext = c->chunkNext.as<int>();
+      p.chunkFill = c->chunkFill.as<int>();
+      p.warpHead = c->warpHead.as<int>();
+      p.chunkCap = (int) chunks;
+    }
     if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[2], c->stream));
-    launchRaster(p, ct != nullptr, dt != nullptr, c->stream);
+    if (deferShade) launchRasterDeferred(p, dt != nullptr, c->stream);
+    else launchRaster(p, ct != nullptr, dt != nullptr, c->stream);
     if (c->statsLevel >= 1) {
       CK(cudaEventRecord(c->ev[3], c->stream));
       c->evPending = true;
@@ -902,7 +933,8 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     // vertex, clip, 3 scan, append, count, setup, 3 scan | emit, sort, ranges, order, raster
     int sortPasses = nPairs > 0 ? (keyBits <= 8 ? 1 : 2) : 0;
     c->stats.kernel_launches = (p.nv > 0) + (p.ntri > 0) + 3 + 2 + 1 + 3 + (np > 0) + sortPasses * 5 +
-                               (nPairs > 0) + (heavyFirst ? 1 : 0) + 1 + attempt * 10 + (deferred ? 2 : 0);
+                               (nPairs > 0) + (heavyFirst ? 1 : 0) + 1 + attempt * 10 + (deferred ? 2 : 0) +
+                               (deferShade ? 2 : 0);
     return SGLC_OK;
   }
   return c->fail(SGLC_ERR_OVERFLOW, "draw: clip capacity could not be satisfied");
@@ -976,7 +1008,8 @@ sglc_status sglc_destroy(sglc_context *ctx) {
                     &c->pairOff, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->tileStart, &c->tileEnd, &c->tileOrder,
                     &c->scanScratch, &c->sortHist, &c->sortHistScan, &c->staging, &c->batchU, &c->batchTargets,
                     &c->sticky, &c->lpSlot, &c->lpOrigin, &c->lpStampCount, &c->lpStampOff, &c->lpStampGeo,
-                    &c->lpStampRow, &c->lpStampColor, &c->lpStampVary, &c->lpFragCount, &c->lpFragOff, &c->lpMisc};
+                    &c->lpStampRow, &c->lpStampColor, &c->lpStampVary, &c->lpFragCount, &c->lpFragOff, &c->lpMisc,
+                    &c->recA, &c->recB, &c->recColor, &c->chunkNext, &c->chunkFill, &c->warpHead};
   for (DevBuf *b : bufs) b->release();
   cudaFreeHost(c->hostCounters);
   for (void *h : c->captureHostBufs) cudaFreeHost(h);
@@ -1629,6 +1662,12 @@ sglc_status sglc_set_stats_level(sglc_context *ctx, int32_t level) {
 sglc_status sglc_get_stream(sglc_context *ctx, void **stream) {
   CTX;
   *stream = c->stream;
+  return SGLC_OK;
+}
+
+sglc_status sglc_set_deferred_shading(sglc_context *ctx, int32_t enable) {
+  CTX;
+  c->deferredShading = enable != 0;
   return SGLC_OK;
 }
 

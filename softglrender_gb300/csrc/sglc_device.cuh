@@ -161,7 +161,20 @@ struct DrawParams {
   int tilesPerView;
   const uint8_t *viewU;            // views x kUniformBytes, or null: DrawParams::u
   const ViewTarget *viewTarget;    // per-view attachments, or null: color / resolved / depth above
+  // deferred shading (k_raster_cov -> k_shade -> k_rop in sglc_raster.cuh): fragment records in
+  // chunks of kChunk, one linked chunk list per raster warp, in the warp's fragment order
+  int4 *recA;                     // triangle, meta, px | py << 16, b0 bits
+  float2 *recB;                   // b1, b2
+  float4 *recColor;               // fragment shader output
+  int *chunkNext, *chunkFill;     // per chunk: successor (-1: none), records in it
+  int *warpHead;                  // per raster warp (tile * 8 + warp): first chunk, -1: none
+  int chunkCap;
 };
+
+constexpr int kChunk = 32;         // fragment records per chunk
+constexpr int kCntChunks = 5;      // DrawParams::counters[5]: chunks allocated
+constexpr int kCntBound = 6;       // counters[6..7]: 64-bit upper bound on a draw's fragment records
+constexpr int kOvfFrags = 32;      // counters[2] flag: the fragment record pool ran out
 
 // Point and line draws (sglc_lines.cu; RendererSoft.cpp:301-321, 409-487, 575-712). Every input
 // primitive owns three slots (a point draw uses one, a line draw one, a triangle drawn as points or

@@ -213,10 +213,8 @@ __global__ void k_clip_append(const __grid_constant__ DrawParams p) {
 __device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }   // std::min
 __device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }   // std::max
 
-__global__ void __launch_bounds__(256) k_setup(const __grid_constant__ DrawParams p) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int np = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
-  if (i >= np) return;
+// one primitive's setup; returns its upper bound on emitted fragments
+__device__ __forceinline__ unsigned long long setupPrim(const DrawParams &p, int i) {
   int4 pr = p.prims[i];
   TriSetup T;
   int cnt = 0;
@@ -272,6 +270,19 @@ __global__ void __launch_bounds__(256) k_setup(const __grid_constant__ DrawParam
   }
   if (cnt) p.tri[i] = T;   // only binned primitives are read again (bin emission, raster)
   p.tileCount[i] = cnt;
+  // upper bound on the fragments the raster can emit for this primitive: each pixel of its quad
+  // rectangle once, plus one more per row / column where two 32x32 blocks overlap
+  return cnt ? (unsigned long long) (T.rx1 - T.rx0 + 1 + T.bcx) * (unsigned long long) (T.ry1 - T.ry0 + 1 + T.bcy)
+             : 0ull;
+}
+
+__global__ void __launch_bounds__(256) k_setup(const __grid_constant__ DrawParams p) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int np = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
+  unsigned long long bound = i < np ? setupPrim(p, i) : 0ull;
+  for (int o = 16; o > 0; o >>= 1) bound += __shfl_down_sync(0xffffffffu, bound, o);
+  if ((threadIdx.x & 31) == 0 && bound)
+    atomicAdd(reinterpret_cast<unsigned long long *>(p.counters + kCntBound), bound);
 }
 
 __global__ void __launch_bounds__(256) k_bin_emit(const __grid_constant__ DrawParams p) {

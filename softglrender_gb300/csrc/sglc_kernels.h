@@ -19,6 +19,9 @@ void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, in
 void launchTileRanges(const DrawParams &p, int nPairs, const int *nPtr, cudaStream_t st);
 void launchTileOrder(const DrawParams &p, int *order, cudaStream_t st);
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
+// deferred shading (coverage -> shade -> ROP) for the shading models it is built for
+bool deferredShadingModel(int shading);
+void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st);
 void launchFill32(uint32_t *dst, uint32_t value, size_t n, cudaStream_t st);
 // *dst = min(*src, cap) (device-side pair count of a synchronisation-free draw)
 void launchClampCount(const int *src, int cap, int *dst, cudaStream_t st);

@@ -378,8 +378,12 @@ __device__ __forceinline__ uint32_t depthOps(const DrawParams &p, const Cover &c
 }
 
 // Pass 1 of a batch of up to 32 tile primitives (lane = primitive): a conservative edge-function
-// test of each triangle against the sample box of every pixel of the warp's 8x4 rectangle. Returns
-// this lane's pixel's candidate mask (bit = batch index); `prim` = this lane's primitive id.
+// test of each triangle against the sample box of every pixel of the warp's 8x4 rectangle, and for
+// 4x MSAA against each of the four sample points of a pixel whose box passes (a triangle covering
+// no sample point cannot cover the pixel; slivers that cross a pixel between its samples are
+// dropped here rather than in the exact per-pixel test). Returns this lane's pixel's candidate mask
+// (bit = batch index); `prim` = this lane's primitive id.
+template<int S>
 __device__ __forceinline__ unsigned pass1Candidates(const DrawParams &p, int base, int end, int lane, int rx0, int ry0,
                                                     float lo, float hi, float vpExtent, int &prim) {
   int i = base + lane;
@@ -387,20 +391,31 @@ __device__ __forceinline__ unsigned pass1Candidates(const DrawParams &p, int bas
   bool hit = false;
   int4 r = make_int4(0, -1, 0, -1);
   float ea[3] = {0.f, 0.f, 0.f}, eb[3] = {0.f, 0.f, 0.f}, ek[3] = {0.f, 0.f, 0.f}, et[3] = {0.f, 0.f, 0.f};
+  float es[3][4] = {};   // 4x MSAA: edge value at each sample offset, less a px + b py
   bool anyPix = false;
   if (i < end) {
     prim = __ldg(p.valA + i);
     const TriSetup *tp = p.tri + prim;
     r = __ldg(reinterpret_cast<const int4 *>(&tp->rx0));
     hit = !(r.y < rx0 || r.x > rx0 + 7 || r.w < ry0 || r.z > ry0 + 3);
+    float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
+    float uz = 0.f;
     if (hit) {
-      float4 q0 = __ldg(reinterpret_cast<const float4 *>(tp));        // v0x v0y v2x v1x
-      float4 q1 = __ldg(reinterpret_cast<const float4 *>(tp) + 1);    // v0x v2y v1y v0y
+      q0 = __ldg(reinterpret_cast<const float4 *>(tp));        // v0x v0y v2x v1x
+      q1 = __ldg(reinterpret_cast<const float4 *>(tp) + 1);    // v0x v2y v1y v0y
+      // the barycentric denominator does not depend on the point (baryCover): a triangle whose
+      // |uz| is below FLT_EPSILON covers nothing (RendererSoft.cpp:1035-1037)
+      uz = (q0.z - q0.x) * (q1.z - q0.y) - (q0.w - q0.x) * (q1.y - q0.y);
+      if (fabsf(uz) < 1.19209290e-07f) hit = false;
+    }
+    if (hit) {
       float X[3] = {q0.x, q0.w, q0.z}, Y[3] = {q0.y, q1.z, q1.y};     // v0, v1, v2
-      float area = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
       float mag = fabsf(X[1] - X[0]) + fabsf(Y[1] - Y[0]) + fabsf(X[2] - X[0]) + fabsf(Y[2] - Y[0]);
-      anyPix = !(fabsf(area) > 1e-3f * mag * mag + 1e-6f);   // near-degenerate: skip the edge pre-test
-      float o = area > 0.f ? 1.f : -1.f;
+      anyPix = !(fabsf(uz) > 1e-6f * mag * mag + 1e-6f);   // near-degenerate: skip the edge pre-test
+      // orientation from the reference's own denominator: its coverage signs are ux/uz, uy/uz and
+      // 1 - (ux + uy)/uz, so the edge functions take the sign uz was computed with (uz is twice the
+      // signed area with the opposite sign of (v1 - v0) x (v2 - v0))
+      float o = uz > 0.f ? -1.f : 1.f;
 #pragma unroll
       for (int e = 0; e < 3; e++) {
         // E(x, y) = a x + b y + c >= 0 inside; its maximum over a pixel's sample box is at the
@@ -411,6 +426,10 @@ __device__ __forceinline__ unsigned pass1Candidates(const DrawParams &p, int bas
         eb[e] = b;
         ek[e] = a * (a > 0.f ? hi : lo) + b * (b > 0.f ? hi : lo) + c;
         et[e] = 1e-5f * ((fabsf(a) + fabsf(b)) * (vpExtent + fabsf(sx) + fabsf(sy)) + fabsf(c) + 1.f);
+        if (S == 4) {
+#pragma unroll
+          for (int k = 0; k < 4; k++) es[e][k] = a * kLoc4xR[k].x + b * kLoc4xR[k].y + c;
+        }
       }
     }
   }
@@ -421,8 +440,15 @@ __device__ __forceinline__ unsigned pass1Candidates(const DrawParams &p, int bas
     bool c = hit && cx >= r.x && cx <= r.y && cy >= r.z && cy <= r.w;
     if (c && !anyPix) {
       float fx = (float) cx, fy = (float) cy;
-      c = (ea[0] * fx + eb[0] * fy + ek[0] >= -et[0]) && (ea[1] * fx + eb[1] * fy + ek[1] >= -et[1]) &&
-          (ea[2] * fx + eb[2] * fy + ek[2] >= -et[2]);
+      float g0 = ea[0] * fx + eb[0] * fy, g1 = ea[1] * fx + eb[1] * fy, g2 = ea[2] * fx + eb[2] * fy;
+      c = (g0 + ek[0] >= -et[0]) && (g1 + ek[1] >= -et[1]) && (g2 + ek[2] >= -et[2]);
+      if (S == 4 && c) {
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+          any = any || ((g0 + es[0][k] >= -et[0]) && (g1 + es[1][k] >= -et[1]) && (g2 + es[2][k] >= -et[2]));
+        c = any;
+      }
     }
     unsigned mm = __ballot_sync(0xffffffffu, c);
     if (lane == pp) cand = mm;
@@ -479,7 +505,7 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
   const float vpExtent = fabsf(p.vp.w) + fabsf(p.vp.h) + 2.f * (float) (rx0 + ry0) + 64.f;
   for (int base = start; base < end; base += 32) {
     int prim;
-    unsigned cand = pass1Candidates(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim);
+    unsigned cand = pass1Candidates<S>(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim);
     if (!(inC || inD)) cand = 0;
     // ---- pass 2 (lane = pixel): exact coverage and depth for each candidate, in primitive order
     int nIter = __reduce_max_sync(0xffffffffu, __popc(cand));
@@ -561,6 +587,312 @@ void launchRasterModel(const DrawParams &p, bool hasColor, bool hasDepth, cudaSt
     else k_raster<SH, 1, true, false><<<grid, 256, 0, st>>>(p);
   }
   (void) hasColor;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Deferred shading: the per-pixel sequence of k_raster split over three kernels, so that the large
+// fragment shader runs in a kernel of its own (full SIMD width, one code path per SM, no coverage
+// code competing for the instruction cache) and the coverage kernel carries no shader registers.
+//
+//   k_raster_cov  coverage, early-Z and depth exactly as k_raster; each fragment that reaches the
+//                 colour stage is appended, in the warp's order, to the warp's chunk list
+//   k_shade       the fragment shader once per record (any order: it is a pure function)
+//   k_rop         every warp walks its chunk list and applies each record's colour operations to
+//                 its pixel in list order, then stores colour and the MSAA resolve
+//
+// A pixel belongs to one warp in both k_raster_cov and k_rop, and that warp's list keeps the
+// pixel's fragments in the order k_raster would apply them, so the result is the same bit for bit.
+// ------------------------------------------------------------------------------------------------
+
+// meta of a record: lane | sample mask << 5 | (px - qx) << 9 | (py - qy) << 10 | view << 11
+__device__ __forceinline__ int allocChunk(const DrawParams &p, int lane) {
+  int c = 0;
+  if (lane == 0) {
+    c = atomicAdd(&p.counters[kCntChunks], 1);
+    if (c >= p.chunkCap) {
+      atomicOr(&p.counters[2], kOvfFrags);
+      c = -1;
+    } else {
+      p.chunkNext[c] = -1;
+    }
+  }
+  return __shfl_sync(0xffffffffu, c, 0);
+}
+
+// one evaluated (pixel, candidate) pair of the load-balanced pass 2
+struct CovSlot {
+  Cover cv;
+  int x0, x1, y0, y1, nx, nq;
+  int prim;
+};
+
+template<int S, bool HAS_DEPTH>
+__global__ void __launch_bounds__(256, 3) k_raster_cov(const __grid_constant__ DrawParams p) {
+  __shared__ CovSlot covSlots[8][32];
+  const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
+  const int view = p.views > 1 ? tile / p.tilesPerView : 0;
+  const int vtile = tile - view * p.tilesPerView;
+  const int tx = vtile % p.tilesX, ty = vtile / p.tilesX;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
+  const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
+  const bool inD = HAS_DEPTH && px < p.dw && py < p.dh;
+  float *depthBuf = p.viewTarget ? p.viewTarget[view].depth : p.depth;
+  const unsigned lt = (1u << lane) - 1u;
+  Samples4 fb = {0u, 0u, 0u, 0u, 0.f, 0.f, 0.f, 0.f};
+  if (inD) {
+    size_t pix = (size_t) py * p.dw + px;
+    if (p.pendingClear && p.clearDepthFlag) {
+      fb.d0 = fb.d1 = fb.d2 = fb.d3 = p.clearDepth;
+    } else if (S == 4) {
+      float4 v = *reinterpret_cast<const float4 *>(depthBuf + pix * 4);
+      fb.d0 = v.x; fb.d1 = v.y; fb.d2 = v.z; fb.d3 = v.w;
+    } else {
+      fb.d0 = depthBuf[pix];
+    }
+  }
+  const bool inPix = (px < p.cw && py < p.ch) || inD;
+  const uint32_t pixWord = (uint32_t) px | ((uint32_t) py << 16);
+  int head = -1, ch = -1, cnt = 0;
+  bool dead = false;
+  unsigned long long total = 0;
+  const int start = p.tileStart[tile], end = p.tileEnd[tile];
+  const float lo = S == 4 ? 0.125f : 0.5f, hi = S == 4 ? 0.875f : 0.5f;
+  const float vpExtent = fabsf(p.vp.w) + fabsf(p.vp.h) + 2.f * (float) (rx0 + ry0) + 64.f;
+  CovSlot *slots = covSlots[warp];
+  for (int base = start; base < end; base += 32) {
+    int prim;
+    unsigned cand = pass1Candidates<S>(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim);
+    if (!inPix) cand = 0;
+    // pass 2, load-balanced: the (pixel, candidate) pairs of the batch, pixel-major in candidate
+    // order, are evaluated 32 at a time by all lanes (coverage does not depend on the depth buffer);
+    // then each pixel's owner lane runs the depth operations of its pairs in order
+    const int cnum = __popc(cand);
+    int off = cnum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int v = __shfl_up_sync(0xffffffffu, off, o);
+      if (lane >= o) off += v;
+    }
+    const int pairs = __shfl_sync(0xffffffffu, off, 31);
+    off -= cnum;   // exclusive
+    for (int r0 = 0; r0 < pairs; r0 += 32) {
+      const int kk = r0 + lane;
+      // owner pixel of pair kk: the last lane whose offset is <= kk
+      int L = 0;
+#pragma unroll
+      for (int step = 16; step; step >>= 1) {
+        int o2 = __shfl_sync(0xffffffffu, off, (L + step) & 31);
+        if (L + step < 32 && o2 <= kk) L += step;
+      }
+      const unsigned candL = __shfl_sync(0xffffffffu, cand, L);
+      const int offL = __shfl_sync(0xffffffffu, off, L);
+      // the (kk - offL)-th candidate of pixel L
+      int nth = kk - offL, pos = 0;
+      unsigned m = candL;
+#pragma unroll
+      for (int w = 16; w; w >>= 1) {
+        int c1 = __popc(m & ((1u << w) - 1u));
+        if (nth >= c1) {
+          nth -= c1;
+          m >>= w;
+          pos += w;
+        }
+      }
+      const int pr = __shfl_sync(0xffffffffu, prim, pos & 31);
+      CovSlot sl;
+      sl.nq = 0;
+      if (kk < pairs) {
+        const int lpx = rx0 + (L & 7), lpy = ry0 + (L >> 3);
+        const TriSetup *tp = p.tri + pr;
+        int x0 = 0, x1 = 0, y0 = 0, y1 = 0, nx = 0;
+        int nq = quadsOf(tp, lpx, lpy, x0, x1, y0, y1, nx);
+        Cover cv;
+        cv.mask = 0u;
+        if (nq) cv = coverSamples<S>(p, loadTriCov(tp), lpx, lpy);
+        if (!cv.mask) nq = 0;
+        sl.cv = cv;
+        sl.x0 = x0; sl.x1 = x1; sl.y0 = y0; sl.y1 = y1;
+        sl.nx = nx;
+        sl.nq = nq;
+        sl.prim = pr;
+      }
+      slots[lane] = sl;
+      __syncwarp();
+      // owner phase: this lane's pairs of the round, in order
+      const int s0 = max(off, r0) - r0, s1 = min(off + cnum, r0 + 32) - r0;
+      const int nOwn = max(0, s1 - s0);
+      const int maxOwn = __reduce_max_sync(0xffffffffu, nOwn);
+      for (int q = 0; q < maxOwn; q++) {
+        const CovSlot *e = q < nOwn ? &slots[s0 + q] : nullptr;
+        const int nq = e ? e->nq : 0;
+        const int nqMax = __reduce_max_sync(0xffffffffu, nq);
+        for (int k = 0; k < nqMax; k++) {   // a pixel can lie in two overlapping blocks' quads
+          uint32_t mask = 0;
+          int qx = 0, qy = 0;
+          if (k < nq) {
+            qy = (k / e->nx) ? e->y1 : e->y0;
+            qx = (k % e->nx) ? e->x1 : e->x0;
+            mask = depthOps<S, HAS_DEPTH>(p, e->cv, inD, fb);
+          }
+          unsigned want = __ballot_sync(0xffffffffu, mask != 0);
+          if (!want || dead) continue;
+          const int n = __popc(want);
+          if (head < 0) {
+            ch = head = allocChunk(p, lane);
+            cnt = 0;
+            if (ch < 0) {
+              dead = true;
+              continue;
+            }
+          }
+          int nch = -1;
+          if (cnt + n > kChunk) nch = allocChunk(p, lane);
+          if (mask) {
+            int ei = cnt + __popc(want & lt);
+            int c2 = ei < kChunk ? ch : nch;
+            if (c2 >= 0) {
+              size_t r = (size_t) c2 * kChunk + (ei < kChunk ? ei : ei - kChunk);
+              uint32_t meta = (uint32_t) lane | (mask << 5) | ((uint32_t) (px - qx) << 9) |
+                              ((uint32_t) (py - qy) << 10) | ((uint32_t) view << 11);
+              p.recA[r] = make_int4(e->prim, (int) meta, (int) pixWord, __float_as_int(e->cv.b0));
+              p.recB[r] = make_float2(e->cv.b1, e->cv.b2);
+            }
+          }
+          total += (unsigned long long) n;
+          if (cnt + n > kChunk) {
+            if (lane == 0) {
+              p.chunkFill[ch] = kChunk;
+              if (nch >= 0) p.chunkNext[ch] = nch;
+            }
+            cnt = cnt + n - kChunk;
+            ch = nch;
+            if (nch < 0) dead = true;
+          } else {
+            cnt += n;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  if (lane == 0) {
+    p.warpHead[tile * 8 + warp] = head;
+    if (ch >= 0) p.chunkFill[ch] = cnt;
+    if (p.fragCounter && total) atomicAdd(p.fragCounter, total);
+  }
+  if (inD) {
+    size_t pix = (size_t) py * p.dw + px;
+    if (S == 4) {
+      *reinterpret_cast<float4 *>(depthBuf + pix * 4) = make_float4(fb.d0, fb.d1, fb.d2, fb.d3);
+    } else {
+      depthBuf[pix] = fb.d0;
+    }
+  }
+}
+
+// the fragment shader over every record (grid-stride over the chunks the coverage kernel used)
+template<int SH, int S>
+__global__ void __launch_bounds__(128) k_shade(const __grid_constant__ DrawParams p) {
+  const long long n = (long long) min(p.counters[kCntChunks], p.chunkCap) * kChunk;
+  for (long long r = (long long) blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long) gridDim.x * blockDim.x) {
+    const int ch = (int) (r / kChunk), slot = (int) (r % kChunk);
+    if (slot >= p.chunkFill[ch]) continue;
+    const int4 a = p.recA[r];
+    const float2 b = p.recB[r];
+    const uint32_t meta = (uint32_t) a.y;
+    const int px = a.z & 0xffff, py = (int) ((uint32_t) a.z >> 16);
+    const int qx = px - (int) ((meta >> 9) & 1u), qy = py - (int) ((meta >> 10) & 1u);
+    p.recColor[r] = shadeFragment<SH, S>(p, viewUniforms(p, (int) (meta >> 11)), a.x, qx, qy, px, py,
+                                         __int_as_float(a.w), b.x, b.y);
+  }
+}
+
+// colour operations in each warp's list order, then colour store and MSAA resolve
+template<int S>
+__global__ void __launch_bounds__(256) k_rop(const __grid_constant__ DrawParams p) {
+  __shared__ float4 scol[8][kChunk];
+  __shared__ uint32_t smeta[8][kChunk];
+  __shared__ uint32_t sown[8][kChunk];
+  const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
+  const int view = p.views > 1 ? tile / p.tilesPerView : 0;
+  const int vtile = tile - view * p.tilesPerView;
+  const int tx = vtile % p.tilesX, ty = vtile / p.tilesX;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
+  const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
+  const bool inC = px < p.cw && py < p.ch;
+  uint32_t *colorBuf = p.viewTarget ? p.viewTarget[view].color : p.color;
+  uint32_t *resolvedBuf = p.viewTarget ? p.viewTarget[view].resolved : p.resolved;
+  Samples4 fb = {0u, 0u, 0u, 0u, 0.f, 0.f, 0.f, 0.f};
+  const size_t pix = (size_t) py * p.cw + px;
+  if (inC) {
+    if (p.pendingClear && p.clearColorFlag) {
+      fb.c0 = fb.c1 = fb.c2 = fb.c3 = p.clearColor;
+    } else if (S == 4) {
+      uint4 v = *reinterpret_cast<const uint4 *>(colorBuf + pix * 4);
+      fb.c0 = v.x; fb.c1 = v.y; fb.c2 = v.z; fb.c3 = v.w;
+    } else {
+      fb.c0 = colorBuf[pix];
+    }
+  }
+  int ch = p.warpHead[tile * 8 + warp];
+  while (ch >= 0) {
+    const int fill = p.chunkFill[ch];
+    const size_t r = (size_t) ch * kChunk + lane;
+    uint32_t meta = 0u;
+    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (lane < fill) {
+      meta = (uint32_t) p.recA[r].y;
+      c = p.recColor[r];
+    }
+    sown[warp][lane] = 0u;
+    __syncwarp();
+    if (lane < fill) atomicOr(&sown[warp][meta & 31u], 1u << lane);
+    smeta[warp][lane] = meta;
+    scol[warp][lane] = c;
+    __syncwarp();
+    unsigned mine = sown[warp][lane];
+    while (mine) {
+      const int e = __ffs(mine) - 1;
+      mine &= mine - 1;
+      const float4 color = scol[warp][e];
+      const uint32_t mask = (smeta[warp][e] >> 5) & 15u;
+      if (mask & 1u) perSample<true, false>(p, inC, true, fb.c0, fb.d0, 0.f, color);
+      if (S == 4) {
+        if (mask & 2u) perSample<true, false>(p, inC, true, fb.c1, fb.d1, 0.f, color);
+        if (mask & 4u) perSample<true, false>(p, inC, true, fb.c2, fb.d2, 0.f, color);
+        if (mask & 8u) perSample<true, false>(p, inC, true, fb.c3, fb.d3, 0.f, color);
+      }
+    }
+    const int next = fill == kChunk ? p.chunkNext[ch] : -1;
+    __syncwarp();
+    ch = next;
+  }
+  if (inC) {
+    if (S == 4) {
+      *reinterpret_cast<uint4 *>(colorBuf + pix * 4) = make_uint4(fb.c0, fb.c1, fb.c2, fb.c3);
+      // multiSampleResolve (RendererSoft.cpp:880-912): mean of four u8 samples, truncated
+      uint32_t rsv = 0;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        uint32_t sum = ((fb.c0 >> (8 * k)) & 255u) + ((fb.c1 >> (8 * k)) & 255u) + ((fb.c2 >> (8 * k)) & 255u) +
+                       ((fb.c3 >> (8 * k)) & 255u);
+        rsv |= ((sum >> 2) & 255u) << (8 * k);
+      }
+      resolvedBuf[pix] = rsv;
+    } else {
+      colorBuf[pix] = fb.c0;
+    }
+  }
+}
+
+// the shading kernel of one model; the coverage and ROP kernels are model-independent
+template<int SH>
+void launchShadeModel(const DrawParams &p, cudaStream_t st) {
+  const int grid = 152 * 16;
+  if (p.samples == 4) k_shade<SH, 4><<<grid, 128, 0, st>>>(p);
+  else k_shade<SH, 1><<<grid, 128, 0, st>>>(p);
 }
 
 }  // namespace sglc

@@ -9,6 +9,47 @@ void launchRasterPbr(const DrawParams &p, bool hasColor, bool hasDepth, cudaStre
 void launchRasterNeural(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 void launchRasterPbrCapture(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 void launchRasterEnvironment(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
+void launchShadeBlinn(const DrawParams &p, cudaStream_t st);
+void launchShadePbr(const DrawParams &p, cudaStream_t st);
+void launchShadePbrCapture(const DrawParams &p, cudaStream_t st);
+void launchShadeEnvironment(const DrawParams &p, cudaStream_t st);
+
+bool deferredShadingModel(int shading) {
+  switch (shading) {
+    case SH_BLINN:
+    case SH_BLINN_DIR:
+    case SH_PBR:
+    case SH_PBR_CAPTURE:
+    case SH_SKYBOX:
+    case SH_IBL_IRR:
+    case SH_IBL_PRE:
+    case SH_FXAA: return true;
+  }
+  return false;   // base / vertex colour: the shader is a load; the neural variant has its own kernel
+}
+
+void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st) {
+  const int grid = p.views * p.tilesPerView;
+  if (p.samples == 4) {
+    if (hasDepth) k_raster_cov<4, true><<<grid, 256, 0, st>>>(p);
+    else k_raster_cov<4, false><<<grid, 256, 0, st>>>(p);
+  } else {
+    if (hasDepth) k_raster_cov<1, true><<<grid, 256, 0, st>>>(p);
+    else k_raster_cov<1, false><<<grid, 256, 0, st>>>(p);
+  }
+  switch (p.shading) {
+    case SH_BLINN:
+    case SH_BLINN_DIR: launchShadeBlinn(p, st); break;
+    case SH_PBR: launchShadePbr(p, st); break;
+    case SH_PBR_CAPTURE: launchShadePbrCapture(p, st); break;
+    case SH_SKYBOX:
+    case SH_IBL_IRR:
+    case SH_IBL_PRE:
+    case SH_FXAA: launchShadeEnvironment(p, st); break;
+  }
+  if (p.samples == 4) k_rop<4><<<grid, 256, 0, st>>>(p);
+  else k_rop<1><<<grid, 256, 0, st>>>(p);
+}
 
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
   int grid = p.views * p.tilesPerView;

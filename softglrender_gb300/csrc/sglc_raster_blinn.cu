@@ -8,4 +8,9 @@ void launchRasterBlinn(const DrawParams &p, bool hasColor, bool hasDepth, cudaSt
   else launchRasterModel<SH_BLINN_DIR>(p, hasColor, hasDepth, st);
 }
 
+void launchShadeBlinn(const DrawParams &p, cudaStream_t st) {
+  if (p.shading == SH_BLINN) launchShadeModel<SH_BLINN>(p, st);
+  else launchShadeModel<SH_BLINN_DIR>(p, st);
+}
+
 }  // namespace sglc

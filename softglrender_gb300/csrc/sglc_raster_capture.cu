@@ -7,4 +7,6 @@ void launchRasterPbrCapture(const DrawParams &p, bool hasColor, bool hasDepth, c
   launchRasterModel<SH_PBR_CAPTURE>(p, hasColor, hasDepth, st);
 }
 
+void launchShadePbrCapture(const DrawParams &p, cudaStream_t st) { launchShadeModel<SH_PBR_CAPTURE>(p, st); }
+
 }  // namespace sglc

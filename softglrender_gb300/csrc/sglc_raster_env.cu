@@ -14,4 +14,13 @@ void launchRasterEnvironment(const DrawParams &p, bool hasColor, bool hasDepth, 
   }
 }
 
+void launchShadeEnvironment(const DrawParams &p, cudaStream_t st) {
+  switch (p.shading) {
+    case SH_SKYBOX: launchShadeModel<SH_SKYBOX>(p, st); break;
+    case SH_IBL_IRR: launchShadeModel<SH_IBL_IRR>(p, st); break;
+    case SH_IBL_PRE: launchShadeModel<SH_IBL_PRE>(p, st); break;
+    case SH_FXAA: launchShadeModel<SH_FXAA>(p, st); break;
+  }
+}
+
 }  // namespace sglc

@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
   const float vpExtent = fabsf(p.vp.w) + fabsf(p.vp.h) + 2.f * (float) (rx0 + ry0) + 64.f;
   for (int base = start; base < end; base += 32) {
     int prim;
-    unsigned cand = pass1Candidates(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim);
+    unsigned cand = pass1Candidates<S>(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim);
     if (!(inC || inD)) cand = 0;
     // pass 2 in CTA-wide steps: one candidate per lane per step (up to 2 quads = 64 queue entries)
     while (__syncthreads_or(cand != 0u)) {

@@ -7,4 +7,6 @@ void launchRasterPbr(const DrawParams &p, bool hasColor, bool hasDepth, cudaStre
   launchRasterModel<SH_PBR>(p, hasColor, hasDepth, st);
 }
 
+void launchShadePbr(const DrawParams &p, cudaStream_t st) { launchShadeModel<SH_PBR>(p, st); }
+
 }  // namespace sglc
