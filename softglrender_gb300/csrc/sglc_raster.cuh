@@ -384,17 +384,14 @@ __device__ __forceinline__ uint32_t depthOps(const DrawParams &p, const Cover &c
 // dropped here rather than in the exact per-pixel test). Returns this lane's pixel's candidate mask
 // (bit = batch index); `prim` = this lane's primitive id.
 template<int S>
-__device__ __forceinline__ unsigned pass1Candidates(const DrawParams &p, int base, int end, int lane, int rx0, int ry0,
-                                                    float lo, float hi, float vpExtent, int &prim) {
-  int i = base + lane;
-  prim = -1;
+__device__ __forceinline__ unsigned pass1Prim(const DrawParams &p, int prim, int lane, int rx0, int ry0, float lo, float hi,
+                                              float vpExtent) {
   bool hit = false;
   int4 r = make_int4(0, -1, 0, -1);
   float ea[3] = {0.f, 0.f, 0.f}, eb[3] = {0.f, 0.f, 0.f}, ek[3] = {0.f, 0.f, 0.f}, et[3] = {0.f, 0.f, 0.f};
   float es[3][4] = {};   // 4x MSAA: edge value at each sample offset, less a px + b py
   bool anyPix = false;
-  if (i < end) {
-    prim = __ldg(p.valA + i);
+  if (prim >= 0) {
     const TriSetup *tp = p.tri + prim;
     r = __ldg(reinterpret_cast<const int4 *>(&tp->rx0));
     hit = !(r.y < rx0 || r.x > rx0 + 7 || r.w < ry0 || r.z > ry0 + 3);
@@ -454,6 +451,21 @@ __device__ __forceinline__ unsigned pass1Candidates(const DrawParams &p, int bas
     if (lane == pp) cand = mm;
   }
   return cand;
+}
+
+// pass 1 for the batch of tile-list entries [base, base + 32): lane i tests entry base + i
+template<int S>
+__device__ __forceinline__ unsigned pass1Candidates(const DrawParams &p, int base, int end, int lane, int rx0, int ry0,
+                                                    float lo, float hi, float vpExtent, int &prim) {
+  int i = base + lane;
+  prim = i < end ? __ldg(p.valA + i) : -1;
+  return pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent);
+}
+
+// does a tile-list primitive's pixel rectangle touch the warp's 8x4 rectangle
+__device__ __forceinline__ bool touchesRect(const DrawParams &p, int prim, int rx0, int ry0) {
+  int4 r = __ldg(reinterpret_cast<const int4 *>(&p.tri[prim].rx0));
+  return !(r.y < rx0 || r.x > rx0 + 7 || r.w < ry0 || r.z > ry0 + 3);
 }
 
 template<int SH, int S, bool HAS_COLOR, bool HAS_DEPTH>
@@ -627,8 +639,9 @@ struct CovSlot {
 };
 
 template<int S, bool HAS_DEPTH>
-__global__ void __launch_bounds__(256, 3) k_raster_cov(const __grid_constant__ DrawParams p) {
+__global__ void __launch_bounds__(256, S == 4 ? 2 : 3) k_raster_cov(const __grid_constant__ DrawParams p) {
   __shared__ CovSlot covSlots[8][32];
+  __shared__ int covQueue[8][64];
   const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
   const int view = p.views > 1 ? tile / p.tilesPerView : 0;
   const int vtile = tile - view * p.tilesPerView;
@@ -660,9 +673,30 @@ __global__ void __launch_bounds__(256, 3) k_raster_cov(const __grid_constant__ D
   const float lo = S == 4 ? 0.125f : 0.5f, hi = S == 4 ? 0.875f : 0.5f;
   const float vpExtent = fabsf(p.vp.w) + fabsf(p.vp.h) + 2.f * (float) (rx0 + ry0) + 64.f;
   CovSlot *slots = covSlots[warp];
-  for (int base = start; base < end; base += 32) {
-    int prim;
-    unsigned cand = pass1Candidates<S>(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim);
+  int *queue = covQueue[warp];
+  int qn = 0;
+  for (int base = start; base < end || qn > 0;) {
+    // dense batches: the tile-list primitives whose rectangle touches this warp's pixels, in list
+    // order, 32 at a time (most of a tile's list misses any one 8x4 rectangle)
+    while (qn < 32 && base < end) {
+      const int i = base + lane;
+      const int pr0 = i < end ? __ldg(p.valA + i) : -1;
+      const bool t = pr0 >= 0 && touchesRect(p, pr0, rx0, ry0);
+      const unsigned bm = __ballot_sync(0xffffffffu, t);
+      if (t) queue[qn + __popc(bm & lt)] = pr0;
+      qn += __popc(bm);
+      base += 32;
+    }
+    __syncwarp();
+    const int nb = min(qn, 32);
+    const int prim = lane < nb ? queue[lane] : -1;
+    const int rest = qn - nb;
+    const int keep = lane < rest ? queue[nb + lane] : 0;
+    __syncwarp();
+    if (lane < rest) queue[lane] = keep;
+    qn = rest;
+    __syncwarp();
+    unsigned cand = pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent);
     if (!inPix) cand = 0;
     // pass 2, load-balanced: the (pixel, candidate) pairs of the batch, pixel-major in candidate
     // order, are evaluated 32 at a time by all lanes (coverage does not depend on the depth buffer);
