@@ -134,9 +134,10 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes (read + write) of one raster launch from the committed ncu summary, or None."""
-    path = os.path.join(ROOT, "profiles", "k_raster_pbr_ibl_1080p_msaa4.md")
+def profiled_traffic(name="k_raster_cov_pbr_ibl_1080p_msaa4.md"):
+    """DRAM bytes (read + write) of one launch of the roofline kernel from its committed ncu summary,
+    or None."""
+    path = os.path.join(ROOT, "profiles", name)
     try:
         with open(path) as f:
             for line in f:
@@ -375,9 +376,11 @@ def main():
         torch.cuda.synchronize()
         return [s.elapsed_time(e) for s, e in zip(starts, ends)]
 
-    def raster_ms_median(n=5):
+    def raster_ms_median(n=5, parts=None):
+        """Median device times of the raster stage, geometry and binning (CUDA events on the
+        renderer's stream); `parts` collects the deferred-shading kernels' times."""
         r.setStatsLevel(1)
-        rast, geo, binn = [], [], []
+        rast, geo, binn, cov, shd, rop = [], [], [], [], [], []
         for _ in range(n):
             with torch.cuda.stream(stream):
                 flush.zero_()
@@ -386,7 +389,13 @@ def main():
             rast.append(s["raster_ms"])
             geo.append(s["geometry_ms"])
             binn.append(s["binning_ms"])
+            cov.append(s["coverage_ms"])
+            shd.append(s["shading_ms"])
+            rop.append(s["rop_ms"])
         r.setStatsLevel(0)
+        if parts is not None:
+            parts.update({"coverage": float(np.median(cov)), "shading": float(np.median(shd)),
+                          "rop": float(np.median(rop))})
         return float(np.median(rast)), float(np.median(geo)), float(np.median(binn))
 
     # ---- device-resident throughput: K frames, L2 flushed between frames (not timed) ----------
@@ -400,16 +409,21 @@ def main():
     ms_per_step = total_s / args.steps * 1e3
 
     # ---- raster-kernel roofline: CUDA events around the raster launch on the renderer's stream ----
-    raster_ms, geo_ms, bin_ms = raster_ms_median()
+    parts = {}
+    raster_ms, geo_ms, bin_ms = raster_ms_median(parts=parts)
     p0 = scene.passes[0]
     W, H, Sm = p0.width, p0.height, p0.samples
     d0 = p0.draws[0]
     nv = len(d0.vertexes)
-    varying_stride = 32
-    raster_bytes = (W * H * Sm * 8 + W * H * 4 + texture_bytes(scene) + st["primitives"] * 128 +
-                    nv * varying_stride * 4 + st["bin_entries"] * 4)
+    tiles = ((W + 15) // 16) * ((H + 15) // 16)
+    # the dominant kernel of the raster stage is the coverage / depth kernel of deferred shading;
+    # its algorithmic bytes per launch: every depth sample written once (the pass's clear is fused,
+    # nothing read), per bin entry the primitive id and its 128-B setup record, per fragment a
+    # 24-B record, per tile its list range and 8 warp list heads
+    cov_bytes = W * H * Sm * 4 + st["bin_entries"] * (4 + 128) + frags * 24 + tiles * (8 + 32)
+    cov_ms = parts["coverage"]
     peak, peak_kind = measured_peak_hbm()
-    achieved = raster_bytes / (raster_ms * 1e-3) / 1e9
+    achieved = cov_bytes / (cov_ms * 1e-3) / 1e9
 
     # ---- neural IBL shader: trained on 2^22 captured fragments of 64 orbit views (tensor-core
     # forward / backward / Adam), judged against the plain shader on 16 held-out views; its
@@ -499,16 +513,18 @@ def main():
         "mfrag_per_s": round(frags * fps / 1e6, 2),
         "fragments_per_frame": frags,
         "mtris_per_s": round(scene.triangles * fps / 1e6, 2),
-        "stage_ms": {"geometry": round(geo_ms, 4), "binning": round(bin_ms, 4), "raster": round(raster_ms, 4)},
+        "stage_ms": {"geometry": round(geo_ms, 4), "binning": round(bin_ms, 4), "raster": round(raster_ms, 4),
+                     "raster_coverage": round(parts["coverage"], 4), "raster_shading": round(parts["shading"], 4),
+                     "raster_rop": round(parts["rop"], 4)},
         "e2e": {"value": round(e2e_fps, 3), "unit": "frames/s", "h2d_bytes_per_step": int(pinned_v.nbytes + len(model_bytes)),
                 "d2h_bytes_per_step": int(out.nbytes)},
         "gpu_launches": launches_per_frame * args.steps,
-        "roofline": {"bound": "hbm", "kernel": "k_raster<PBR,4>", "achieved": round(achieved, 1),
+        "roofline": {"bound": "hbm", "kernel": "k_raster_cov<4,depth>", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": peak_kind, "traffic": profiled_traffic(),
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
-                                       "profiles/k_raster_pbr_ibl_1080p_msaa4.md",
-                     "algorithmic_bytes_per_launch": int(raster_bytes)},
+                                       "profiles/k_raster_cov_pbr_ibl_1080p_msaa4.md",
+                     "algorithmic_bytes_per_launch": int(cov_bytes), "kernel_ms": round(cov_ms, 4)},
         "clocks": clocks.summary(),
     }
     if neural is not None:

@@ -157,6 +157,9 @@ typedef struct sglc_draw_stats {
   float binning_ms;           /* pair emission + sort + tile ranges, including the count read-back */
   float raster_ms;            /* tile raster + shading + ROP + resolve */
   int32_t kernel_launches;    /* kernels this back-end launched for the draw */
+  float coverage_ms;          /* deferred shading: coverage + depth kernel (stats level >= 1; else 0) */
+  float shading_ms;           /* deferred shading: fragment-shader kernel */
+  float rop_ms;               /* deferred shading: colour operations + resolve kernel */
 } sglc_draw_stats;
 
 /* ---- context (Renderer::create / destroy, Renderer.h:27-28) ---------------------------------- */

@@ -96,7 +96,8 @@ class _DrawStats(C.Structure):
     _fields_ = [("vertices_in", C.c_int64), ("triangles_in", C.c_int64), ("clip_vertices", C.c_int64),
                 ("primitives", C.c_int64), ("bin_entries", C.c_int64), ("fragments_shaded", C.c_int64),
                 ("geometry_ms", C.c_float), ("binning_ms", C.c_float), ("raster_ms", C.c_float),
-                ("kernel_launches", C.c_int32)]
+                ("kernel_launches", C.c_int32), ("coverage_ms", C.c_float), ("shading_ms", C.c_float),
+                ("rop_ms", C.c_float)]
 
 
 # ---- reference value types ---------------------------------------------------------------------

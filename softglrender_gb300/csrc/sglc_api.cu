@@ -188,7 +188,8 @@ struct Ctx {
   sglc_draw_stats stats{};
   int *hostCounters = nullptr;   // pinned
   int statsLevel = 0;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  bool evDeferred = false;   // ev[4], ev[5] bracket the deferred-shading kernels of the last draw
   bool evPending = false;
   unsigned long long *fragCounter = nullptr;
   // scratch
@@ -916,7 +917,10 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       p.chunkCap = (int) chunks;
     }
     if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[2], c->stream));
-    if (deferShade) launchRasterDeferred(p, dt != nullptr, c->stream);
+    c->evDeferred = deferShade && c->statsLevel >= 1;
+    if (deferShade)
+      launchRasterDeferred(p, dt != nullptr, c->stream, c->evDeferred ? c->ev[4] : nullptr,
+                           c->evDeferred ? c->ev[5] : nullptr);
     else launchRaster(p, ct != nullptr, dt != nullptr, c->stream);
     if (c->statsLevel >= 1) {
       CK(cudaEventRecord(c->ev[3], c->stream));
@@ -982,7 +986,7 @@ sglc_status sglc_create(sglc_context **out, int32_t device) {
   bool ok = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) == cudaSuccess &&
             cudaMallocHost(&c->hostCounters, 64) == cudaSuccess &&
             cudaMalloc(&c->fragCounter, sizeof(unsigned long long)) == cudaSuccess;
-  for (int i = 0; i < 4 && ok; i++) ok = cudaEventCreate(&c->ev[i]) == cudaSuccess;
+  for (int i = 0; i < 6 && ok; i++) ok = cudaEventCreate(&c->ev[i]) == cudaSuccess;
   if (!ok) {
     delete c;
     return SGLC_ERR_DEVICE;
@@ -1014,7 +1018,7 @@ sglc_status sglc_destroy(sglc_context *ctx) {
   cudaFreeHost(c->hostCounters);
   for (void *h : c->captureHostBufs) cudaFreeHost(h);
   cudaFree(c->fragCounter);
-  for (int i = 0; i < 4; i++)
+  for (int i = 0; i < 6; i++)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -1640,6 +1644,12 @@ sglc_status sglc_get_draw_stats(sglc_context *ctx, sglc_draw_stats *out) {
     CK(cudaEventElapsedTime(&c->stats.geometry_ms, c->ev[0], c->ev[1]));
     CK(cudaEventElapsedTime(&c->stats.binning_ms, c->ev[1], c->ev[2]));
     CK(cudaEventElapsedTime(&c->stats.raster_ms, c->ev[2], c->ev[3]));
+    c->stats.coverage_ms = c->stats.shading_ms = c->stats.rop_ms = 0.f;
+    if (c->evDeferred) {
+      CK(cudaEventElapsedTime(&c->stats.coverage_ms, c->ev[2], c->ev[4]));
+      CK(cudaEventElapsedTime(&c->stats.shading_ms, c->ev[4], c->ev[5]));
+      CK(cudaEventElapsedTime(&c->stats.rop_ms, c->ev[5], c->ev[3]));
+    }
     if (c->statsLevel >= 2) {
       unsigned long long n = 0;
       CK(cudaMemcpy(&n, c->fragCounter, sizeof(n), cudaMemcpyDeviceToHost));

@@ -21,7 +21,9 @@ void launchTileOrder(const DrawParams &p, int *order, cudaStream_t st);
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
 // deferred shading (coverage -> shade -> ROP) for the shading models it is built for
 bool deferredShadingModel(int shading);
-void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st);
+// evCov / evShade (may be null) are recorded after the coverage and the shading kernel
+void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st, cudaEvent_t evCov = nullptr,
+                          cudaEvent_t evShade = nullptr);
 void launchFill32(uint32_t *dst, uint32_t value, size_t n, cudaStream_t st);
 // *dst = min(*src, cap) (device-side pair count of a synchronisation-free draw)
 void launchClampCount(const int *src, int cap, int *dst, cudaStream_t st);

@@ -13,6 +13,7 @@ void launchShadeBlinn(const DrawParams &p, cudaStream_t st);
 void launchShadePbr(const DrawParams &p, cudaStream_t st);
 void launchShadePbrCapture(const DrawParams &p, cudaStream_t st);
 void launchShadeEnvironment(const DrawParams &p, cudaStream_t st);
+void launchShadeNeural(const DrawParams &p, cudaStream_t st);
 
 bool deferredShadingModel(int shading) {
   switch (shading) {
@@ -23,12 +24,13 @@ bool deferredShadingModel(int shading) {
     case SH_SKYBOX:
     case SH_IBL_IRR:
     case SH_IBL_PRE:
-    case SH_FXAA: return true;
+    case SH_FXAA:
+    case SH_PBR_NEURAL: return true;
   }
-  return false;   // base / vertex colour: the shader is a load; the neural variant has its own kernel
+  return false;   // base / vertex colour: the shader is a load
 }
 
-void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st) {
+void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st, cudaEvent_t evCov, cudaEvent_t evShade) {
   const int grid = p.views * p.tilesPerView;
   if (p.samples == 4) {
     if (hasDepth) k_raster_cov<4, true><<<grid, 256, 0, st>>>(p);
@@ -37,16 +39,19 @@ void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st) {
     if (hasDepth) k_raster_cov<1, true><<<grid, 256, 0, st>>>(p);
     else k_raster_cov<1, false><<<grid, 256, 0, st>>>(p);
   }
+  if (evCov) cudaEventRecord(evCov, st);
   switch (p.shading) {
     case SH_BLINN:
     case SH_BLINN_DIR: launchShadeBlinn(p, st); break;
     case SH_PBR: launchShadePbr(p, st); break;
     case SH_PBR_CAPTURE: launchShadePbrCapture(p, st); break;
+    case SH_PBR_NEURAL: launchShadeNeural(p, st); break;
     case SH_SKYBOX:
     case SH_IBL_IRR:
     case SH_IBL_PRE:
     case SH_FXAA: launchShadeEnvironment(p, st); break;
   }
+  if (evShade) cudaEventRecord(evShade, st);
   if (p.samples == 4) k_rop<4><<<grid, 256, 0, st>>>(p);
   else k_rop<1><<<grid, 256, 0, st>>>(p);
 }

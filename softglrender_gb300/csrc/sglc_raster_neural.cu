@@ -358,6 +358,129 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
   if (warp == 0) tc::tmemFree(n.tmem, 256);
 }
 
+// ------------------------------------------------------------------------------------------------
+// Deferred neural shading: the network over the fragment records of k_raster_cov (sglc_raster.cuh),
+// 256 records (two M = 128 tiles) per step, persistent CTAs; nothing couples it to coverage, so
+// every step is a full tile. Colour goes to the records' colour slots for k_rop.
+// ------------------------------------------------------------------------------------------------
+constexpr int kSnX = 0;                               // 2 x [128][80] BF16 input / hidden tiles
+constexpr int kSnImg = kSnX + 2 * 128 * 80 * 2;
+constexpr int kSnBar = kSnImg + kImgBytes;
+constexpr int kSnTmem = kSnBar + 8;
+// at least 80 KB so that no more than two CTAs (2 x 256 TMEM columns) share an SM
+constexpr int kSnBytes = (kSnTmem + 4 + 1024) > 80 * 1024 ? (kSnTmem + 4 + 1024) : 80 * 1024;
+static_assert(kSnBytes * 3 > 227 * 1024 && kSnBytes * 2 <= 227 * 1024, "exactly two CTAs per SM");
+
+template<int S>
+__global__ void __launch_bounds__(256, 2) k_shade_neural(const __grid_constant__ DrawParams p) {
+  extern __shared__ __align__(1024) uint8_t smraw[];
+  uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t) 1023);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  NeuralCta n;
+  n.xTile = sm + kSnX + (warp >> 2) * 128 * 80 * 2;
+  n.sX[0] = tc::smemAddr(sm + kSnX);
+  n.sX[1] = tc::smemAddr(sm + kSnX + 128 * 80 * 2);
+  uint8_t *img = sm + kSnImg;
+  n.sW1 = tc::smemAddr(img + kImgW1);
+  n.sW2 = tc::smemAddr(img + kImgW2);
+  n.sW3 = tc::smemAddr(img + kImgW3);
+  n.bias = reinterpret_cast<const float *>(img + kImgBias);
+  n.bar = reinterpret_cast<uint64_t *>(sm + kSnBar);
+  n.chunks = nullptr;
+  n.phase = 0;
+  n.U = nullptr;
+  n.row = (warp & 3) * 32 + lane;
+  uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(sm + kSnTmem);
+  for (int i = threadIdx.x; i < kImgBytes / 16; i += 256)
+    reinterpret_cast<uint4 *>(img)[i] = __ldg(reinterpret_cast<const uint4 *>(p.nnImage) + i);
+  if (threadIdx.x == 0) tc::barInit(n.bar, 1);
+  if (warp == 0) tc::tmemAlloc(tmemSlot, 256);
+  tc::fenceBefore();
+  __syncthreads();
+  tc::fenceAfter();
+  n.tmem = *tmemSlot;
+  n.lanes = n.tmem + ((uint32_t) ((warp & 3) * 32) << 16) + 128u * (uint32_t) (warp >> 2);
+
+  const long long nSlots = (long long) min(p.counters[kCntChunks], p.chunkCap) * kChunk;
+  for (long long t0 = (long long) blockIdx.x * 256; t0 < nSlots; t0 += (long long) gridDim.x * 256) {
+    const long long r = t0 + threadIdx.x;
+    bool valid = r < nSlots && (int) (r % kChunk) < p.chunkFill[r / kChunk];
+    NeuralPre pre;
+    if (valid) {
+      const int4 a = p.recA[r];
+      const float2 b = p.recB[r];
+      const uint32_t meta = (uint32_t) a.y;
+      const int px = a.z & 0xffff, py = (int) ((uint32_t) a.z >> 16);
+      const int qx = px - (int) ((meta >> 9) & 1u), qy = py - (int) ((meta >> 10) & 1u);
+      pre = neuralPre<S>(p, viewUniforms(p, (int) (meta >> 11)), a.x, qx, qy, px, py, __int_as_float(a.w), b.x, b.y);
+    } else {
+#pragma unroll
+      for (int i = 0; i < kIn; i++) pre.x[i] = 0.f;
+      pre.lo0 = pre.lo1 = pre.lo2 = pre.alpha = pre.ao = pre.e0 = pre.e1 = pre.e2 = 0.f;
+    }
+    // layer 1, features 0-79
+    encodeChunks<0, 10>(pre.x, n.xTile, n.row, 80, false);
+    ntHandOff();
+    if (threadIdx.x == 0) {
+      tc::fenceAfter();
+      for (int w = 0; w < 2; w++) issueKMajor(n.tmem + 128 * w, n.sX[w], 80, 0, n.sW1, kK1, 0, 64, 80, false);
+      tc::commit(n.bar);
+    }
+    ntWait(n);
+    // layer 1, features 80-159 (the tile is free again)
+    encodeChunks<10, 20>(pre.x, n.xTile, n.row, 80, false);
+    ntHandOff();
+    if (threadIdx.x == 0) {
+      tc::fenceAfter();
+      for (int w = 0; w < 2; w++) issueKMajor(n.tmem + 128 * w, n.sX[w], 80, 0, n.sW1, kK1, 80, 64, 80, true);
+      tc::commit(n.bar);
+    }
+    ntWait(n);
+    hiddenEpilogue(n.lanes, n.bias, n.xTile, n.row, 64, 0);
+    ntHandOff();
+    if (threadIdx.x == 0) {
+      tc::fenceAfter();
+      for (int w = 0; w < 2; w++) issueKMajor(n.tmem + 128 * w + 64, n.sX[w], 64, 0, n.sW2, 64, 0, 64, 64, false);
+      tc::commit(n.bar);
+    }
+    ntWait(n);
+    hiddenEpilogue(n.lanes + 64, n.bias + 64, n.xTile, n.row, 64, 0);
+    ntHandOff();
+    if (threadIdx.x == 0) {
+      tc::fenceAfter();
+      for (int w = 0; w < 2; w++) issueKMajor(n.tmem + 128 * w, n.sX[w], 64, 0, n.sW3, 64, 0, 16, 64, false);
+      tc::commit(n.bar);
+    }
+    ntWait(n);
+    float y[16];
+    tc::ld16(n.lanes, y);
+    tc::ldWait();
+    tc::fenceBefore();
+    if (valid) {
+      float a0 = gmax(y[0] + n.bias[128], 0.f), a1 = gmax(y[1] + n.bias[129], 0.f), a2 = gmax(y[2] + n.bias[130], 0.f);
+      f3 ambient = mk3(a0 * a0, a1 * a1, a2 * a2) * pre.ao;
+      p.recColor[r] = pbrFinish(p, ambient, mk3(pre.lo0, pre.lo1, pre.lo2), mk3(pre.e0, pre.e1, pre.e2), pre.alpha);
+    }
+    __syncthreads();   // the tiles are rewritten by the next step
+  }
+  tc::fenceBefore();
+  __syncthreads();
+  tc::fenceAfter();
+  if (warp == 0) tc::tmemFree(n.tmem, 256);
+}
+
+void launchShadeNeural(const DrawParams &p, cudaStream_t st) {
+  static bool attr[2] = {false, false};
+  const int k = p.samples == 4 ? 1 : 0;
+  if (!attr[k]) {
+    if (k) cudaFuncSetAttribute(k_shade_neural<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSnBytes);
+    else cudaFuncSetAttribute(k_shade_neural<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSnBytes);
+    attr[k] = true;
+  }
+  if (k) k_shade_neural<4><<<152 * 2, 256, kSnBytes, st>>>(p);
+  else k_shade_neural<1><<<152 * 2, 256, kSnBytes, st>>>(p);
+}
+
 template<int S, bool D>
 static void launchNeural(const DrawParams &p, int grid, cudaStream_t st) {
   static bool attr = false;
