@@ -271,9 +271,8 @@ __device__ __forceinline__ unsigned long long setupPrim(const DrawParams &p, int
   if (cnt) p.tri[i] = T;   // only binned primitives are read again (bin emission, raster)
   p.tileCount[i] = cnt;
   // upper bound on the fragments the raster can emit for this primitive: each pixel of its quad
-  // rectangle once, plus one more per row / column where two 32x32 blocks overlap
-  return cnt ? (unsigned long long) (T.rx1 - T.rx0 + 1 + T.bcx) * (unsigned long long) (T.ry1 - T.ry0 + 1 + T.bcy)
-             : 0ull;
+  // rectangle once, plus one more per row / column where two adjacent 32x32 blocks overlap
+  return cnt ? (unsigned long long) (T.rx1 - T.rx0 + T.bcx) * (unsigned long long) (T.ry1 - T.ry0 + T.bcy) : 0ull;
 }
 
 __global__ void __launch_bounds__(256) k_setup(const __grid_constant__ DrawParams p) {
