@@ -586,7 +586,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
   memset(&p, 0, sizeof(p));
   p.shading = prog.shader->model;
   p.varyCnt = prog.shader->varyingsCnt;
-  p.varyStride = std::max(8, ((p.varyCnt * 4 + 31) / 32) * 8);
+  p.varyStride = std::max(8, ((p.varyCnt * 4 + 31) / 32) * 8);   // <= 32: k_vertex stages a row in registers
   memcpy(p.def, prog.defines, 8);
   memcpy(p.u, prog.uniforms, kUniformBytes);
   for (int s = 0; s < kMaxSamplers; s++) {

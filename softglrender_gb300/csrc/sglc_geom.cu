@@ -51,15 +51,34 @@ __device__ __forceinline__ float4 toScreen(const DrawParams &p, float4 c) {
 // ------------------------------------------------------------------------------------------------
 template<int SH>
 __global__ void __launch_bounds__(256) k_vertex(const __grid_constant__ DrawParams p) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.nv) return;
-  const int view = p.views > 1 ? i / p.nvView : 0;
-  const float *a = p.attr + (size_t) (i - view * p.nvView) * p.strideF;
-  float *v = p.vVary + (size_t) i * p.varyStride;
-  float4 c = runVS<SH>(p, viewUniforms(p, view), a, v);
-  p.vClip[i] = c;
-  p.vMask[i] = (uint8_t) clipMaskOf(c);
-  p.vFrag[i] = toScreen(p, c);
+  // each warp's 32 varying rows are contiguous in memory: they are staged in shared memory and
+  // written as one contiguous run of 16-byte stores (varyStride <= 32 floats for every model)
+  __shared__ float4 stage[8][32 * 8];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = p.varyStride / 4;
+  float v[32];
+#pragma unroll
+  for (int k = 0; k < 32; k++) v[k] = 0.f;
+  if (i < p.nv) {
+    const int view = p.views > 1 ? i / p.nvView : 0;
+    const float *a = p.attr + (size_t) (i - view * p.nvView) * p.strideF;
+    float4 c = runVS<SH>(p, viewUniforms(p, view), a, v);
+    p.vClip[i] = c;
+    p.vMask[i] = (uint8_t) clipMaskOf(c);
+    p.vFrag[i] = toScreen(p, c);
+  }
+  float4 *st = stage[warp];
+#pragma unroll
+  for (int k = 0; k < 8; k++)
+    if (k < q) st[lane * q + k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+  __syncwarp();
+  const int i0 = i - lane;
+  const int rows = min(32, p.nv - i0);
+  if (rows > 0) {
+    float4 *dst = reinterpret_cast<float4 *>(p.vVary + (size_t) i0 * p.varyStride);
+    for (int e = lane; e < rows * q; e += 32) dst[e] = st[e];
+  }
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -639,7 +639,7 @@ struct CovSlot {
 };
 
 template<int S, bool HAS_DEPTH>
-__global__ void __launch_bounds__(256, S == 4 ? 2 : 3) k_raster_cov(const __grid_constant__ DrawParams p) {
+__global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid_constant__ DrawParams p) {
   __shared__ CovSlot covSlots[8][32];
   __shared__ int covQueue[8][64];
   const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
