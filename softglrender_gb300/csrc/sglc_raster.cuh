@@ -385,7 +385,7 @@ __device__ __forceinline__ uint32_t depthOps(const DrawParams &p, const Cover &c
 // (bit = batch index); `prim` = this lane's primitive id.
 template<int S>
 __device__ __forceinline__ unsigned pass1Prim(const DrawParams &p, int prim, int lane, int rx0, int ry0, float lo, float hi,
-                                              float vpExtent) {
+                                              float vpExtent, unsigned *candS) {
   bool hit = false;
   int4 r = make_int4(0, -1, 0, -1);
   float ea[3] = {0.f, 0.f, 0.f}, eb[3] = {0.f, 0.f, 0.f}, ek[3] = {0.f, 0.f, 0.f}, et[3] = {0.f, 0.f, 0.f};
@@ -430,36 +430,61 @@ __device__ __forceinline__ unsigned pass1Prim(const DrawParams &p, int prim, int
       }
     }
   }
-  unsigned cand = 0;   // this lane's pixel: candidate triangles of the batch, bit = batch index
-#pragma unroll 4
-  for (int pp = 0; pp < 32; pp++) {
-    int cx = rx0 + (pp & 7), cy = ry0 + (pp >> 3);
-    bool c = hit && cx >= r.x && cx <= r.y && cy >= r.z && cy <= r.w;
-    if (c && !anyPix) {
-      float fx = (float) cx, fy = (float) cy;
-      float g0 = ea[0] * fx + eb[0] * fy, g1 = ea[1] * fx + eb[1] * fy, g2 = ea[2] * fx + eb[2] * fy;
-      c = (g0 + ek[0] >= -et[0]) && (g1 + ek[1] >= -et[1]) && (g2 + ek[2] >= -et[2]);
-      if (S == 4 && c) {
-        bool any = false;
+  const int x0 = max(r.x, rx0), x1 = min(r.y, rx0 + 7), y0 = max(r.z, ry0), y1 = min(r.w, ry0 + 3);
+  const int w = hit && x1 >= x0 && y1 >= y0 ? x1 - x0 + 1 : 0;
+  const int n = w ? w * (y1 - y0 + 1) : 0;
+  const int nMax = __reduce_max_sync(0xffffffffu, n);
+  auto test = [&](int px, int py) -> bool {
+    if (anyPix) return true;
+    float fx = (float) px, fy = (float) py;
+    float g0 = ea[0] * fx + eb[0] * fy, g1 = ea[1] * fx + eb[1] * fy, g2 = ea[2] * fx + eb[2] * fy;
+    bool c = (g0 + ek[0] >= -et[0]) && (g1 + ek[1] >= -et[1]) && (g2 + ek[2] >= -et[2]);
+    if (S == 4 && c) {
+      bool any = false;
 #pragma unroll
-        for (int k = 0; k < 4; k++)
-          any = any || ((g0 + es[0][k] >= -et[0]) && (g1 + es[1][k] >= -et[1]) && (g2 + es[2][k] >= -et[2]));
-        c = any;
+      for (int q = 0; q < 4; q++)
+        any = any || ((g0 + es[0][q] >= -et[0]) && (g1 + es[1][q] >= -et[1]) && (g2 + es[2][q] >= -et[2]));
+      c = any;
+    }
+    return c;
+  };
+  if (nMax > 12) {
+    // large primitives: every pixel of the rectangle in turn, one ballot per pixel
+    unsigned cand = 0;
+#pragma unroll 4
+    for (int pp = 0; pp < 32; pp++) {
+      int px = rx0 + (pp & 7), py = ry0 + (pp >> 3);
+      bool c = px >= x0 && px <= x1 && py >= y0 && py <= y1 && w && test(px, py);
+      unsigned mm = __ballot_sync(0xffffffffu, c);
+      if (lane == pp) cand = mm;
+    }
+    return cand;
+  }
+  // small primitives: each lane (primitive) visits only the pixels of the warp's 8x4 rectangle inside
+  // its own pixel rectangle and sets its bit in those pixels' candidate masks (bit = batch index)
+  candS[lane] = 0u;
+  __syncwarp();
+  int cx = x0, cy = y0;
+  for (int k = 0; k < nMax; k++) {
+    if (k < n) {
+      if (test(cx, cy)) atomicOr(&candS[(cy - ry0) * 8 + (cx - rx0)], 1u << lane);
+      if (++cx > x1) {
+        cx = x0;
+        cy++;
       }
     }
-    unsigned mm = __ballot_sync(0xffffffffu, c);
-    if (lane == pp) cand = mm;
   }
-  return cand;
+  __syncwarp();
+  return candS[lane];
 }
 
 // pass 1 for the batch of tile-list entries [base, base + 32): lane i tests entry base + i
 template<int S>
 __device__ __forceinline__ unsigned pass1Candidates(const DrawParams &p, int base, int end, int lane, int rx0, int ry0,
-                                                    float lo, float hi, float vpExtent, int &prim) {
+                                                    float lo, float hi, float vpExtent, int &prim, unsigned *candS) {
   int i = base + lane;
   prim = i < end ? __ldg(p.valA + i) : -1;
-  return pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent);
+  return pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent, candS);
 }
 
 // does a tile-list primitive's pixel rectangle touch the warp's 8x4 rectangle
@@ -471,6 +496,7 @@ __device__ __forceinline__ bool touchesRect(const DrawParams &p, int prim, int r
 template<int SH, int S, bool HAS_COLOR, bool HAS_DEPTH>
 __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawParams p) {
   __shared__ FragQueue queues[HAS_COLOR ? 8 : 1];
+  __shared__ unsigned candMasks[8][32];
   const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
   const int view = p.views > 1 ? tile / p.tilesPerView : 0;
   const int vtile = tile - view * p.tilesPerView;
@@ -517,7 +543,7 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
   const float vpExtent = fabsf(p.vp.w) + fabsf(p.vp.h) + 2.f * (float) (rx0 + ry0) + 64.f;
   for (int base = start; base < end; base += 32) {
     int prim;
-    unsigned cand = pass1Candidates<S>(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim);
+    unsigned cand = pass1Candidates<S>(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim, candMasks[warp]);
     if (!(inC || inD)) cand = 0;
     // ---- pass 2 (lane = pixel): exact coverage and depth for each candidate, in primitive order
     int nIter = __reduce_max_sync(0xffffffffu, __popc(cand));
@@ -641,6 +667,7 @@ struct CovSlot {
 template<int S, bool HAS_DEPTH>
 __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid_constant__ DrawParams p) {
   __shared__ CovSlot covSlots[8][32];
+  __shared__ unsigned candMasks[8][32];
   __shared__ int covQueue[8][64];
   const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
   const int view = p.views > 1 ? tile / p.tilesPerView : 0;
@@ -696,7 +723,7 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
     if (lane < rest) queue[lane] = keep;
     qn = rest;
     __syncwarp();
-    unsigned cand = pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent);
+    unsigned cand = pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent, candMasks[warp]);
     if (!inPix) cand = 0;
     // pass 2, load-balanced: the (pixel, candidate) pairs of the batch, pixel-major in candidate
     // order, are evaluated 32 at a time by all lanes (coverage does not depend on the depth buffer);
