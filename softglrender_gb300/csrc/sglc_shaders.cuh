@@ -145,9 +145,14 @@ __device__ inline float shadowCalc(const DrawParams &p, const FragIn &f, f3 norm
   float ox = 1.0f / (float) s.tex.w[0], oy = 1.0f / (float) s.tex.h[0];
   int reverseZ = uI32(f.U, 0);
   float shadow = 0.0f;
+  // a NEAREST shadow map is read at level 0 whatever the LOD: the nine taps inline the nearest
+  // lookup (the same arithmetic as textureImpl's) instead of nine sampler calls
+  const bool nearest0 = s.filter == FILTER_NEAREST && s.tex.levels > 0;
   for (int x = -1; x <= 1; ++x)
     for (int y = -1; y <= 1; ++y) {
-      float pcf = __uint_as_float(textureImpl(s, 0, px + (float) x * ox, py + (float) y * oy, 0.f));
+      const float u = px + (float) x * ox, v = py + (float) y * oy;
+      float pcf = nearest0 ? __uint_as_float(nearestSample(s.tex, 0, 0, u, v, s.wrap, s.border))
+                           : __uint_as_float(textureImpl(s, 0, u, v, 0.f));
       if (reverseZ) shadow += cur + bias < pcf ? 1.0f : 0.0f;
       else shadow += cur - bias > pcf ? 1.0f : 0.0f;
     }
