@@ -289,8 +289,9 @@ typedef struct sglc_capacity {
  * (sglc_get_overflow); the images of such a draw are then unspecified. Null restores the default
  * (exact sizing with one count read-back per draw). */
 SGLC_API sglc_status sglc_set_capacity(sglc_context *ctx, const sglc_capacity *cap);
-/* The largest counts the draws since the last call needed (draws with exact sizing only), as
- * capacities (heavy_first = 1); resets them. Used to calibrate sglc_set_capacity. */
+/* The largest counts the draws since the last call needed (draws with exact sizing only; fragments:
+ * the records deferred-shading draws used, in whole chunks of 32), as capacities (heavy_first = 1);
+ * resets them. Used to calibrate sglc_set_capacity. */
 SGLC_API sglc_status sglc_get_peak_counts(sglc_context *ctx, sglc_capacity *out);
 /* Synchronises, returns and clears the overflow flags of the draws since the last call: bit 0 clip
  * vertices, 1 clip polygons, 2 appended primitives, 3 bin entries, 4 an index outside the vertex

@@ -197,6 +197,7 @@ struct Ctx {
   DevBuf tri, tileCount, pairOff, keyA, keyB, valA, valB, tileStart, tileEnd, tileOrder, scanScratch, sortHist,
       sortHistScan, staging, batchU, batchTargets;
   DevBuf recA, recB, recColor, chunkNext, chunkFill, warpHead;   // deferred shading
+  DevBuf peakChunks;   // largest number of fragment-record chunks a deferred draw used (device)
   bool deferredShading = true;
   DevBuf lpSlot, lpOrigin, lpStampCount, lpStampOff, lpStampGeo, lpStampRow, lpStampColor, lpStampVary, lpFragCount,
       lpFragOff, lpMisc;   // point and line draws
@@ -898,8 +899,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       const long long warps = (long long) numTiles * 8;
       chunks = deferred ? (c->cap.fragments + kChunk - 1) / kChunk
                         : (long long) (fragBound / kChunk) + warps + 1;
-      if (!deferred) c->peak.fragments = std::max<int64_t>(c->peak.fragments, chunks * kChunk);
-      if (chunks < 1 || chunks * kChunk > (1ll << 27)) deferShade = false;   // single kernel instead
+      if (chunks < 1 || chunks * kChunk > (1ll << 28)) deferShade = false;   // single kernel instead
     }
     if (deferShade) {
       CK(c->recA.ensure(sizeof(int4) * (size_t) chunks * kChunk));
@@ -915,12 +915,19 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       p.chunkFill = c->chunkFill.as<int>();
       p.warpHead = c->warpHead.as<int>();
       p.chunkCap = (int) chunks;
+      if (!c->peakChunks.ptr) {
+        CK(c->peakChunks.ensure(sizeof(int)));
+        CK(cudaMemsetAsync(c->peakChunks.ptr, 0, sizeof(int), c->stream));
+      }
     }
     if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[2], c->stream));
     c->evDeferred = deferShade && c->statsLevel >= 1;
-    if (deferShade)
+    if (deferShade) {
       launchRasterDeferred(p, dt != nullptr, c->stream, c->evDeferred ? c->ev[4] : nullptr,
                            c->evDeferred ? c->ev[5] : nullptr);
+      // chunks actually used (the pool is sized from an upper bound): calibrates capacities
+      launchMaxInto(p.counters + kCntChunks, c->peakChunks.as<int>(), c->stream);
+    }
     else launchRaster(p, ct != nullptr, dt != nullptr, c->stream);
     if (c->statsLevel >= 1) {
       CK(cudaEventRecord(c->ev[3], c->stream));
@@ -935,10 +942,10 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     c->stats.primitives = deferred ? -1 : np;
     c->stats.bin_entries = deferred ? -1 : nPairs;
     // vertex, clip, 3 scan, append, count, setup, 3 scan | emit, sort, ranges, order, raster
-    int sortPasses = nPairs > 0 ? (keyBits <= 8 ? 1 : 2) : 0;
+    int sortPasses = nPairs > 0 ? (keyBits + 7) / 8 : 0;
     c->stats.kernel_launches = (p.nv > 0) + (p.ntri > 0) + 3 + 2 + 1 + 3 + (np > 0) + sortPasses * 5 +
                                (nPairs > 0) + (heavyFirst ? 1 : 0) + 1 + attempt * 10 + (deferred ? 2 : 0) +
-                               (deferShade ? 2 : 0);
+                               (deferShade ? 3 : 0);
     return SGLC_OK;
   }
   return c->fail(SGLC_ERR_OVERFLOW, "draw: clip capacity could not be satisfied");
@@ -1013,7 +1020,8 @@ sglc_status sglc_destroy(sglc_context *ctx) {
                     &c->scanScratch, &c->sortHist, &c->sortHistScan, &c->staging, &c->batchU, &c->batchTargets,
                     &c->sticky, &c->lpSlot, &c->lpOrigin, &c->lpStampCount, &c->lpStampOff, &c->lpStampGeo,
                     &c->lpStampRow, &c->lpStampColor, &c->lpStampVary, &c->lpFragCount, &c->lpFragOff, &c->lpMisc,
-                    &c->recA, &c->recB, &c->recColor, &c->chunkNext, &c->chunkFill, &c->warpHead};
+                    &c->recA, &c->recB, &c->recColor, &c->chunkNext, &c->chunkFill, &c->warpHead,
+                    &c->peakChunks};
   for (DevBuf *b : bufs) b->release();
   cudaFreeHost(c->hostCounters);
   for (void *h : c->captureHostBufs) cudaFreeHost(h);
@@ -1601,6 +1609,13 @@ sglc_status sglc_get_peak_counts(sglc_context *ctx, sglc_capacity *out) {
   if (!out) return c->fail(SGLC_ERR_INVALID_VALUE, "get_peak_counts: null output");
   *out = c->peak;
   out->heavy_first = 1;
+  out->fragments = 0;
+  if (c->peakChunks.ptr) {   // fragment records the deferred draws used, in whole chunks
+    CK(cudaMemcpyAsync(c->hostCounters + 10, c->peakChunks.ptr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemsetAsync(c->peakChunks.ptr, 0, sizeof(int), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    out->fragments = (int64_t) c->hostCounters[10] * kChunk;
+  }
   c->peak = sglc_capacity{};
   return SGLC_OK;
 }

@@ -730,6 +730,9 @@ __global__ void k_clamp_count(const int *src, int cap, int *dst) { *dst = min(*s
 __global__ void k_accumulate_flags(const int *flags, int *sticky) { *sticky |= *flags; }
 
 void launchClampCount(const int *src, int cap, int *dst, cudaStream_t st) { k_clamp_count<<<1, 1, 0, st>>>(src, cap, dst); }
+__global__ void k_max_into(const int *src, int *dst) { *dst = max(*dst, *src); }
+void launchMaxInto(const int *src, int *dst, cudaStream_t st) { k_max_into<<<1, 1, 0, st>>>(src, dst); }
+
 void launchAccumulateFlags(const int *flags, int *sticky, cudaStream_t st) {
   k_accumulate_flags<<<1, 1, 0, st>>>(flags, sticky);
 }

@@ -29,6 +29,8 @@ void launchFill32(uint32_t *dst, uint32_t value, size_t n, cudaStream_t st);
 void launchClampCount(const int *src, int cap, int *dst, cudaStream_t st);
 // *sticky |= *flags
 void launchAccumulateFlags(const int *flags, int *sticky, cudaStream_t st);
+// *dst = max(*dst, *src)
+void launchMaxInto(const int *src, int *dst, cudaStream_t st);
 void launchMipLevel(const DevTex &t, int face, int level, int isFloat, cudaStream_t st);
 void launchSwizzleIn(const DevTex &t, int face, int level, const uint32_t *src, cudaStream_t st);
 void launchSwizzleOut(const DevTex &t, int face, int level, uint32_t *dst, cudaStream_t st);
