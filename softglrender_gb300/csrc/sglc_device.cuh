@@ -363,7 +363,7 @@ __device__ __forceinline__ uint32_t bilinearSample(const DevTex &t, int face, in
   return bilinearPx(t, face, level, u * (float) t.w[level], v * (float) t.h[level], wrap, border, isF);
 }
 
-static __device__ __noinline__ uint32_t textureImpl(const DevSampler &s, int face, float u, float v, float lod) {
+static __device__ __forceinline__ uint32_t textureImpl(const DevSampler &s, int face, float u, float v, float lod) {
   const DevTex &t = s.tex;
   if (t.levels <= 0) return 0;
   const bool isF = s.isFloat;

@@ -852,9 +852,10 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
   }
 }
 
-// the fragment shader over every record (grid-stride over the chunks the coverage kernel used)
+// the fragment shader over every record (grid-stride over the chunks the coverage kernel used);
+// 8 CTAs of 4 warps per SM: the sampler is inlined and latency-bound, more warps beat a few spills
 template<int SH, int S>
-__global__ void __launch_bounds__(128) k_shade(const __grid_constant__ DrawParams p) {
+__global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ DrawParams p) {
   const long long n = (long long) min(p.counters[kCntChunks], p.chunkCap) * kChunk;
   for (long long r = (long long) blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long) gridDim.x * blockDim.x) {
     const int ch = (int) (r / kChunk), slot = (int) (r % kChunk);
