@@ -896,7 +896,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     bool deferShade = c->deferredShading && ct && deferredShadingModel(p.shading);
     long long chunks = 0;
     if (deferShade) {
-      const long long warps = (long long) numTiles * 8;
+      const long long warps = ((long long) numTiles + 3 * 64) * 8;   // split tiles have 4 x 8 warps
       chunks = deferred ? (c->cap.fragments + kChunk - 1) / kChunk
                         : (long long) (fragBound / kChunk) + warps + 1;
       if (chunks < 1 || chunks * kChunk > (1ll << 28)) deferShade = false;   // single kernel instead
@@ -907,7 +907,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       CK(c->recColor.ensure(sizeof(float4) * (size_t) chunks * kChunk));
       CK(c->chunkNext.ensure(sizeof(int) * (size_t) chunks));
       CK(c->chunkFill.ensure(sizeof(int) * (size_t) chunks));
-      CK(c->warpHead.ensure(sizeof(int) * (size_t) numTiles * 8));
+      CK(c->warpHead.ensure(sizeof(int) * (size_t) numTiles * 32));
       p.recA = c->recA.as<int4>();
       p.recB = c->recB.as<float2>();
       p.recColor = c->recColor.as<float4>();
@@ -915,6 +915,8 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       p.chunkFill = c->chunkFill.as<int>();
       p.warpHead = c->warpHead.as<int>();
       p.chunkCap = (int) chunks;
+      p.heavySlots = 64;    // with the heavy-first order: its first 64 tiles may be split in 4
+      p.heavyMin = 256;     // primitives in a tile's list above which it is split
       if (!c->peakChunks.ptr) {
         CK(c->peakChunks.ensure(sizeof(int)));
         CK(cudaMemsetAsync(c->peakChunks.ptr, 0, sizeof(int), c->stream));

@@ -167,8 +167,11 @@ struct DrawParams {
   float2 *recB;                   // b1, b2
   float4 *recColor;               // fragment shader output
   int *chunkNext, *chunkFill;     // per chunk: successor (-1: none), records in it
-  int *warpHead;                  // per raster warp (tile * 8 + warp): first chunk, -1: none
+  int *warpHead;                  // per raster warp ((tile * 4 + part) * 8 + warp): first chunk, -1: none
   int chunkCap;
+  // the heaviest tiles (the first heavySlots of the heavy-first order whose list is longer than
+  // heavyMin) are split over 4 CTAs, each warp owning one 8-pixel row instead of an 8x4 block
+  int heavySlots, heavyMin;
 };
 
 constexpr int kChunk = 32;         // fragment records per chunk

@@ -385,7 +385,7 @@ __device__ __forceinline__ uint32_t depthOps(const DrawParams &p, const Cover &c
 // (bit = batch index); `prim` = this lane's primitive id.
 template<int S>
 __device__ __forceinline__ unsigned pass1Prim(const DrawParams &p, int prim, int lane, int rx0, int ry0, float lo, float hi,
-                                              float vpExtent, unsigned *candS) {
+                                              float vpExtent, unsigned *candS, int rh = 4) {
   bool hit = false;
   int4 r = make_int4(0, -1, 0, -1);
   float ea[3] = {0.f, 0.f, 0.f}, eb[3] = {0.f, 0.f, 0.f}, ek[3] = {0.f, 0.f, 0.f}, et[3] = {0.f, 0.f, 0.f};
@@ -394,7 +394,7 @@ __device__ __forceinline__ unsigned pass1Prim(const DrawParams &p, int prim, int
   if (prim >= 0) {
     const TriSetup *tp = p.tri + prim;
     r = __ldg(reinterpret_cast<const int4 *>(&tp->rx0));
-    hit = !(r.y < rx0 || r.x > rx0 + 7 || r.w < ry0 || r.z > ry0 + 3);
+    hit = !(r.y < rx0 || r.x > rx0 + 7 || r.w < ry0 || r.z > ry0 + rh - 1);
     float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
     float uz = 0.f;
     if (hit) {
@@ -430,7 +430,7 @@ __device__ __forceinline__ unsigned pass1Prim(const DrawParams &p, int prim, int
       }
     }
   }
-  const int x0 = max(r.x, rx0), x1 = min(r.y, rx0 + 7), y0 = max(r.z, ry0), y1 = min(r.w, ry0 + 3);
+  const int x0 = max(r.x, rx0), x1 = min(r.y, rx0 + 7), y0 = max(r.z, ry0), y1 = min(r.w, ry0 + rh - 1);
   const int w = hit && x1 >= x0 && y1 >= y0 ? x1 - x0 + 1 : 0;
   const int n = w ? w * (y1 - y0 + 1) : 0;
   const int nMax = __reduce_max_sync(0xffffffffu, n);
@@ -453,7 +453,7 @@ __device__ __forceinline__ unsigned pass1Prim(const DrawParams &p, int prim, int
     unsigned cand = 0;
 #pragma unroll 4
     for (int pp = 0; pp < 32; pp++) {
-      int px = rx0 + (pp & 7), py = ry0 + (pp >> 3);
+      int px = rx0 + (pp & 7), py = ry0 + (pp >> 3);   // rows beyond rh fall outside [y0, y1]
       bool c = px >= x0 && px <= x1 && py >= y0 && py <= y1 && w && test(px, py);
       unsigned mm = __ballot_sync(0xffffffffu, c);
       if (lane == pp) cand = mm;
@@ -488,9 +488,9 @@ __device__ __forceinline__ unsigned pass1Candidates(const DrawParams &p, int bas
 }
 
 // does a tile-list primitive's pixel rectangle touch the warp's 8x4 rectangle
-__device__ __forceinline__ bool touchesRect(const DrawParams &p, int prim, int rx0, int ry0) {
+__device__ __forceinline__ bool touchesRect(const DrawParams &p, int prim, int rx0, int ry0, int rh = 4) {
   int4 r = __ldg(reinterpret_cast<const int4 *>(&p.tri[prim].rx0));
-  return !(r.y < rx0 || r.x > rx0 + 7 || r.w < ry0 || r.z > ry0 + 3);
+  return !(r.y < rx0 || r.x > rx0 + 7 || r.w < ry0 || r.z > ry0 + rh - 1);
 }
 
 template<int SH, int S, bool HAS_COLOR, bool HAS_DEPTH>
@@ -657,6 +657,30 @@ __device__ __forceinline__ int allocChunk(const DrawParams &p, int lane) {
   return __shfl_sync(0xffffffffu, c, 0);
 }
 
+// The tile (and part) a coverage / ROP CTA works on. CTAs [0, 4 H) take the first H tiles of the
+// heavy-first order, four per tile: a tile with more than heavyMin primitives is split by rows (part
+// p = row p of every warp's 8x4 block, so each warp owns 8 pixels); a lighter one is done whole by its
+// first CTA. CTAs [4 H, tiles + 3 H) take the rest of the order one tile each.
+struct TileJob {
+  int tile, part, rows;   // rows of each warp's block: 4 (whole tile) or 1 (split)
+  bool skip;
+};
+
+__device__ __forceinline__ TileJob tileJob(const DrawParams &p) {
+  const int H = p.tileOrder ? p.heavySlots : 0;
+  const int nTiles = p.views * p.tilesPerView;
+  const int b = blockIdx.x;
+  if (b < 4 * H) {
+    const int slot = b >> 2, part = b & 3;
+    if (slot >= nTiles) return {0, 0, 4, true};
+    const int tile = p.tileOrder[slot];
+    if (p.tileEnd[tile] - p.tileStart[tile] > p.heavyMin) return {tile, part, 1, false};
+    return {tile, 0, 4, part != 0};
+  }
+  const int k = b - 3 * H;
+  return {p.tileOrder ? p.tileOrder[k] : k, 0, 4, false};
+}
+
 // one evaluated (pixel, candidate) pair of the load-balanced pass 2
 struct CovSlot {
   Cover cv;
@@ -669,14 +693,17 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
   __shared__ CovSlot covSlots[8][32];
   __shared__ unsigned candMasks[8][32];
   __shared__ int covQueue[8][64];
-  const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
+  const TileJob job = tileJob(p);
+  if (job.skip) return;
+  const int tile = job.tile, rh = job.rows;
   const int view = p.views > 1 ? tile / p.tilesPerView : 0;
   const int vtile = tile - view * p.tilesPerView;
   const int tx = vtile % p.tilesX, ty = vtile / p.tilesX;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
+  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4 + job.part;
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
-  const bool inD = HAS_DEPTH && px < p.dw && py < p.dh;
+  const bool own = (lane >> 3) < rh;   // this lane has a pixel (all 32 in a whole tile, 8 in a split one)
+  const bool inD = HAS_DEPTH && own && px < p.dw && py < p.dh;
   float *depthBuf = p.viewTarget ? p.viewTarget[view].depth : p.depth;
   const unsigned lt = (1u << lane) - 1u;
   Samples4 fb = {0u, 0u, 0u, 0u, 0.f, 0.f, 0.f, 0.f};
@@ -691,7 +718,7 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
       fb.d0 = depthBuf[pix];
     }
   }
-  const bool inPix = (px < p.cw && py < p.ch) || inD;
+  const bool inPix = (own && px < p.cw && py < p.ch) || inD;
   const uint32_t pixWord = (uint32_t) px | ((uint32_t) py << 16);
   int head = -1, ch = -1, cnt = 0;
   bool dead = false;
@@ -708,7 +735,7 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
     while (qn < 32 && base < end) {
       const int i = base + lane;
       const int pr0 = i < end ? __ldg(p.valA + i) : -1;
-      const bool t = pr0 >= 0 && touchesRect(p, pr0, rx0, ry0);
+      const bool t = pr0 >= 0 && touchesRect(p, pr0, rx0, ry0, rh);
       const unsigned bm = __ballot_sync(0xffffffffu, t);
       if (t) queue[qn + __popc(bm & lt)] = pr0;
       qn += __popc(bm);
@@ -723,7 +750,7 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
     if (lane < rest) queue[lane] = keep;
     qn = rest;
     __syncwarp();
-    unsigned cand = pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent, candMasks[warp]);
+    unsigned cand = pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent, candMasks[warp], rh);
     if (!inPix) cand = 0;
     // pass 2, load-balanced: the (pixel, candidate) pairs of the batch, pixel-major in candidate
     // order, are evaluated 32 at a time by all lanes (coverage does not depend on the depth buffer);
@@ -838,7 +865,7 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
     }
   }
   if (lane == 0) {
-    p.warpHead[tile * 8 + warp] = head;
+    p.warpHead[(tile * 4 + job.part) * 8 + warp] = head;
     if (ch >= 0) p.chunkFill[ch] = cnt;
     if (p.fragCounter && total) atomicAdd(p.fragCounter, total);
   }
@@ -876,14 +903,16 @@ __global__ void __launch_bounds__(256) k_rop(const __grid_constant__ DrawParams 
   __shared__ float4 scol[8][kChunk];
   __shared__ uint32_t smeta[8][kChunk];
   __shared__ uint32_t sown[8][kChunk];
-  const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
+  const TileJob job = tileJob(p);
+  if (job.skip) return;
+  const int tile = job.tile;
   const int view = p.views > 1 ? tile / p.tilesPerView : 0;
   const int vtile = tile - view * p.tilesPerView;
   const int tx = vtile % p.tilesX, ty = vtile / p.tilesX;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
+  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4 + job.part;
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
-  const bool inC = px < p.cw && py < p.ch;
+  const bool inC = (lane >> 3) < job.rows && px < p.cw && py < p.ch;
   uint32_t *colorBuf = p.viewTarget ? p.viewTarget[view].color : p.color;
   uint32_t *resolvedBuf = p.viewTarget ? p.viewTarget[view].resolved : p.resolved;
   Samples4 fb = {0u, 0u, 0u, 0u, 0.f, 0.f, 0.f, 0.f};
@@ -898,7 +927,7 @@ __global__ void __launch_bounds__(256) k_rop(const __grid_constant__ DrawParams 
       fb.c0 = colorBuf[pix];
     }
   }
-  int ch = p.warpHead[tile * 8 + warp];
+  int ch = p.warpHead[(tile * 4 + job.part) * 8 + warp];
   while (ch >= 0) {
     const int fill = p.chunkFill[ch];
     const size_t r = (size_t) ch * kChunk + lane;

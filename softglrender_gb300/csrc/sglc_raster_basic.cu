@@ -31,7 +31,7 @@ bool deferredShadingModel(int shading) {
 }
 
 void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st, cudaEvent_t evCov, cudaEvent_t evShade) {
-  const int grid = p.views * p.tilesPerView;
+  const int grid = p.views * p.tilesPerView + 3 * (p.tileOrder ? p.heavySlots : 0);   // see tileJob
   if (p.samples == 4) {
     if (hasDepth) k_raster_cov<4, true><<<grid, 256, 0, st>>>(p);
     else k_raster_cov<4, false><<<grid, 256, 0, st>>>(p);
