@@ -196,7 +196,7 @@ struct Ctx {
   DevBuf vClip, vFrag, vMask, vVary, vAttrExtra, prims, clipExtra, clipAppendOff, clipPoly, clipPolyTri, counters;
   DevBuf tri, tileCount, pairOff, keyA, keyB, valA, valB, tileStart, tileEnd, tileOrder, scanScratch, sortHist,
       sortHistScan, staging, batchU, batchTargets;
-  DevBuf recA, recB, recColor, chunkNext, chunkFill, warpHead;   // deferred shading
+  DevBuf recA, recB, recColor, chunkNext, chunkFill, warpHead, recDense;   // deferred shading
   DevBuf peakChunks;   // largest number of fragment-record chunks a deferred draw used (device)
   bool deferredShading = true;
   DevBuf lpSlot, lpOrigin, lpStampCount, lpStampOff, lpStampGeo, lpStampRow, lpStampColor, lpStampVary, lpFragCount,
@@ -796,7 +796,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     CK(c->clipAppendOff.ensure(sizeof(int) * (size_t) (p.ntri + 1)));
     CK(c->clipPoly.ensure(sizeof(int4) * 3 * (size_t) polyCap));
     CK(c->clipPolyTri.ensure(sizeof(int) * (size_t) polyCap));
-    CK(c->counters.ensure(sizeof(int) * 8));
+    CK(c->counters.ensure(sizeof(int) * 16));
     CK(c->tri.ensure(sizeof(TriSetup) * (size_t) p.primCap));
     CK(c->tileCount.ensure(sizeof(int) * (size_t) p.primCap));
     CK(c->pairOff.ensure(sizeof(int) * (size_t) (p.primCap + 1)));
@@ -816,7 +816,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     p.tileCount = c->tileCount.as<int>();
     p.pairOff = c->pairOff.as<int>();
 
-    CK(cudaMemsetAsync(p.counters, 0, sizeof(int) * 8, c->stream));
+    CK(cudaMemsetAsync(p.counters, 0, sizeof(int) * 16, c->stream));
     if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[0], c->stream));
     launchVertexAndClip(p, c->stream);
     scanExclusive(p.clipExtra, p.clipAppendOff, nullptr, std::max(p.ntri, 1), c->scanScratch.as<int>(), c->stream);
@@ -908,12 +908,14 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       CK(c->chunkNext.ensure(sizeof(int) * (size_t) chunks));
       CK(c->chunkFill.ensure(sizeof(int) * (size_t) chunks));
       CK(c->warpHead.ensure(sizeof(int) * (size_t) numTiles * 32));
+      CK(c->recDense.ensure(sizeof(int) * (size_t) chunks * kChunk));
       p.recA = c->recA.as<int4>();
       p.recB = c->recB.as<float2>();
       p.recColor = c->recColor.as<float4>();
       p.chunkNext = c->chunkNext.as<int>();
       p.chunkFill = c->chunkFill.as<int>();
       p.warpHead = c->warpHead.as<int>();
+      p.recDense = c->recDense.as<int>();
       p.chunkCap = (int) chunks;
       p.heavySlots = 64;    // with the heavy-first order: its first 64 tiles may be split in 4
       p.heavyMin = 256;     // primitives in a tile's list above which it is split
@@ -1022,7 +1024,7 @@ sglc_status sglc_destroy(sglc_context *ctx) {
                     &c->scanScratch, &c->sortHist, &c->sortHistScan, &c->staging, &c->batchU, &c->batchTargets,
                     &c->sticky, &c->lpSlot, &c->lpOrigin, &c->lpStampCount, &c->lpStampOff, &c->lpStampGeo,
                     &c->lpStampRow, &c->lpStampColor, &c->lpStampVary, &c->lpFragCount, &c->lpFragOff, &c->lpMisc,
-                    &c->recA, &c->recB, &c->recColor, &c->chunkNext, &c->chunkFill, &c->warpHead,
+                    &c->recA, &c->recB, &c->recColor, &c->chunkNext, &c->chunkFill, &c->warpHead, &c->recDense,
                     &c->peakChunks};
   for (DevBuf *b : bufs) b->release();
   cudaFreeHost(c->hostCounters);

@@ -168,6 +168,7 @@ struct DrawParams {
   float4 *recColor;               // fragment shader output
   int *chunkNext, *chunkFill;     // per chunk: successor (-1: none), records in it
   int *warpHead;                  // per raster warp ((tile * 4 + part) * 8 + warp): first chunk, -1: none
+  int *recDense;                  // record ids in append-round order, no gaps (-1: a dropped record)
   int chunkCap;
   // the heaviest tiles (the first heavySlots of the heavy-first order whose list is longer than
   // heavyMin) are split over 4 CTAs, each warp owning one 8-pixel row instead of an 8x4 block
@@ -177,6 +178,7 @@ struct DrawParams {
 constexpr int kChunk = 32;         // fragment records per chunk
 constexpr int kCntChunks = 5;      // DrawParams::counters[5]: chunks allocated
 constexpr int kCntBound = 6;       // counters[6..7]: 64-bit upper bound on a draw's fragment records
+constexpr int kCntDense = 8;       // counters[8]: entries of the dense record list
 constexpr int kOvfFrags = 32;      // counters[2] flag: the fragment record pool ran out
 
 // Point and line draws (sglc_lines.cu; RendererSoft.cpp:301-321, 409-487, 575-712). Every input

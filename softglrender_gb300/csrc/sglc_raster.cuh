@@ -869,6 +869,32 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
     if (ch >= 0) p.chunkFill[ch] = cnt;
     if (p.fragCounter && total) atomicAdd(p.fragCounter, total);
   }
+  // the dense record list: one contiguous run per CTA (one atomic), each warp's records in its
+  // list order inside it, so the shading kernel reads no unfilled chunk slots and keeps each warp's
+  // records together
+  __shared__ int wRecs[8], ctaBase;
+  int recs = 0;
+  for (int c = head; c >= 0;) {   // this warp's chunks: every one full but the last
+    const int f = c == ch ? cnt : kChunk;
+    recs += f;
+    c = c == ch ? -1 : p.chunkNext[c];
+  }
+  if (lane == 0) wRecs[warp] = recs;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int sum = 0;
+    for (int w = 0; w < 8; w++) sum += wRecs[w];
+    ctaBase = sum ? atomicAdd(&p.counters[kCntDense], sum) : 0;
+  }
+  __syncthreads();
+  int d = ctaBase;
+  for (int w = 0; w < warp; w++) d += wRecs[w];
+  for (int c = head; c >= 0;) {
+    const int f = c == ch ? cnt : kChunk;
+    if (lane < f && d + lane < p.chunkCap * kChunk) p.recDense[d + lane] = c * kChunk + lane;
+    d += f;
+    c = c == ch ? -1 : p.chunkNext[c];
+  }
   if (inD) {
     size_t pix = (size_t) py * p.dw + px;
     if (S == 4) {
@@ -879,14 +905,15 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
   }
 }
 
-// the fragment shader over every record (grid-stride over the chunks the coverage kernel used);
-// 8 CTAs of 4 warps per SM: the sampler is inlined and latency-bound, more warps beat a few spills
+// the fragment shader over every record (grid-stride over the dense record list, so no lane idles
+// on the unfilled tail of a warp's last chunk); 8 CTAs of 4 warps per SM: the sampler is inlined
+// and latency-bound, more warps beat a few spills
 template<int SH, int S>
 __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ DrawParams p) {
-  const long long n = (long long) min(p.counters[kCntChunks], p.chunkCap) * kChunk;
-  for (long long r = (long long) blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long) gridDim.x * blockDim.x) {
-    const int ch = (int) (r / kChunk), slot = (int) (r % kChunk);
-    if (slot >= p.chunkFill[ch]) continue;
+  const int n = min(p.counters[kCntDense], p.chunkCap * kChunk);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int r = p.recDense[i];
+    if (r < 0) continue;
     const int4 a = p.recA[r];
     const float2 b = p.recB[r];
     const uint32_t meta = (uint32_t) a.y;

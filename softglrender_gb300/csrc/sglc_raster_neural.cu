@@ -414,10 +414,11 @@ __global__ void __launch_bounds__(256, 2) k_shade_neural(const __grid_constant__
     tc::fenceAfter();
   };
 
-  const long long nSlots = (long long) min(p.counters[kCntChunks], p.chunkCap) * kChunk;
-  for (long long t0 = ((long long) blockIdx.x * 2 + wg) * 128; t0 < nSlots; t0 += (long long) gridDim.x * 256) {
-    const long long r = t0 + wgThread;
-    const bool valid = r < nSlots && (int) (r % kChunk) < p.chunkFill[r / kChunk];
+  const int nRec = min(p.counters[kCntDense], p.chunkCap * kChunk);
+  for (int t0 = (blockIdx.x * 2 + wg) * 128; t0 < nRec; t0 += gridDim.x * 256) {
+    const int di = t0 + wgThread;
+    const int r = di < nRec ? p.recDense[di] : -1;
+    const bool valid = r >= 0;
     NeuralPre pre;
     if (valid) {
       const int4 a = p.recA[r];
