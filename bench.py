@@ -433,7 +433,7 @@ def main():
     achieved = cov_bytes / (cov_ms * 1e-3) / 1e9
 
     # ---- neural IBL shader: trained on 2^22 captured fragments of 64 orbit views (tensor-core
-    # forward / backward / Adam), judged against the plain shader on 16 held-out views; its
+    # forward / backward / Adam), compared with the plain shader on 16 held-out views; its
     # throughput is measured on the same frames as `value` --------------------------------------
     neural = None
     if not args.no_neural:

@@ -256,6 +256,20 @@ __device__ __forceinline__ uint32_t pack4(float r, float g, float b, float a) {
 __device__ __forceinline__ float4 unpack4(uint32_t c) {
   return make_float4((float) (c & 255u), (float) ((c >> 8) & 255u), (float) ((c >> 16) & 255u), (float) (c >> 24));
 }
+// x / 255 for an unpacked RGBA8 channel (x an integer 0..255), correctly rounded without a divide:
+// the product with the rounded reciprocal, then one correction by the exact residual x - q*255
+// (Markstein's FMA correction step). It equals the IEEE quotient for all 256 inputs, which
+// tests/test_unit_division.py checks one by one.
+__device__ __forceinline__ float div255(float x) {
+  const float r = 1.f / 255.f;
+  const float q = x * r;
+  return __fmaf_rn(__fmaf_rn(-q, 255.f, x), r, q);
+}
+// the shaders' texel / 255 (ShaderSoft.h:80-103)
+__device__ __forceinline__ float4 unpackUnit4(uint32_t c) {
+  const float4 v = unpack4(c);
+  return make_float4(div255(v.x), div255(v.y), div255(v.z), div255(v.w));
+}
 
 // column-major glm::mat4 * vec4 (type_mat4x4.inl:540-572)
 __device__ __forceinline__ float4 mul44(const float *m, float4 v) {

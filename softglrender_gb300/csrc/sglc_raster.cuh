@@ -205,8 +205,7 @@ __device__ __forceinline__ void perSample(const DrawParams &p, bool inC, bool in
   if (p.blend) {
     float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
     if (inC) {
-      float4 q = unpack4(col);
-      d = make_float4(q.x / 255.f, q.y / 255.f, q.z / 255.f, q.w / 255.f);
+      d = unpackUnit4(col);
     }
     float r0 = blendFn(p, 0, c0 * blendFactor(p, 0, c0, c3, d.x, d.w), d.x * blendFactor(p, 1, c0, c3, d.x, d.w));
     float r1 = blendFn(p, 0, c1 * blendFactor(p, 0, c1, c3, d.y, d.w), d.y * blendFactor(p, 1, c1, c3, d.y, d.w));
@@ -706,6 +705,23 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
   const bool inD = HAS_DEPTH && own && px < p.dw && py < p.dh;
   float *depthBuf = p.viewTarget ? p.viewTarget[view].depth : p.depth;
   const unsigned lt = (1u << lane) - 1u;
+  const int start = p.tileStart[tile], end = p.tileEnd[tile];
+  if (start >= end) {
+    // an empty list (most tiles of a frame): no records, so no part in the dense list (the whole
+    // CTA leaves here); only the warps' empty record lists and, on a pass's first draw, the
+    // cleared depth
+    if (lane == 0) p.warpHead[(tile * 4 + job.part) * 8 + warp] = -1;
+    if (inD && p.pendingClear && p.clearDepthFlag) {
+      const size_t pix = (size_t) py * p.dw + px;
+      if (S == 4) {
+        *reinterpret_cast<float4 *>(depthBuf + pix * 4) = make_float4(p.clearDepth, p.clearDepth, p.clearDepth,
+                                                                      p.clearDepth);
+      } else {
+        depthBuf[pix] = p.clearDepth;
+      }
+    }
+    return;
+  }
   Samples4 fb = {0u, 0u, 0u, 0u, 0.f, 0.f, 0.f, 0.f};
   if (inD) {
     size_t pix = (size_t) py * p.dw + px;
@@ -723,7 +739,6 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
   int head = -1, ch = -1, cnt = 0;
   bool dead = false;
   unsigned long long total = 0;
-  const int start = p.tileStart[tile], end = p.tileEnd[tile];
   const float lo = S == 4 ? 0.125f : 0.5f, hi = S == 4 ? 0.875f : 0.5f;
   const float vpExtent = fabsf(p.vp.w) + fabsf(p.vp.h) + 2.f * (float) (rx0 + ry0) + 64.f;
   CovSlot *slots = covSlots[warp];
