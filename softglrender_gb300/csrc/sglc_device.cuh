@@ -9,11 +9,47 @@
 #pragma once
 
 #include <cstdint>
+#include <utility>
 #include <cuda_runtime.h>
 
 namespace sglc {
 
 constexpr int kMaxLevels = 16;
+
+// Chained launches (programmatic dependent launch). The kernels of one draw form a chain in one
+// stream; each is launched with programmatic stream serialisation, so its CTAs may be scheduled
+// while the previous kernel's last CTAs are still running, instead of after that kernel has
+// drained and the next launch has been processed. A chained kernel's first statement is
+// chainEnter(): griddepcontrol.wait blocks until the previous grid has completed and its memory
+// writes are visible (it returns at once for a kernel launched without the attribute), and
+// griddepcontrol.launch_dependents lets the next kernel be scheduled once every CTA of this grid
+// has started. Both are hardware-managed; no kernel spins on memory.
+__device__ __forceinline__ void chainEnter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// launches `kernel` (whose first statement is chainEnter()) as the next link of the stream's chain.
+// Only eager submissions are chained: in a captured CUDA graph the launch gaps are already short,
+// and a graph of plain kernel nodes replays a GB300 frame slightly faster (0.491 against 0.498 ms
+// for the 1080p PBR frame) than one with programmatic edges, while eager chaining gains 9 %.
+template<typename... K, typename... A>
+inline cudaError_t launchChained(void (*kernel)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                 A &&...args) {
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &capture) != cudaSuccess) capture = cudaStreamCaptureStatusActive;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = capture == cudaStreamCaptureStatusNone ? 1 : 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
 constexpr int kMaxSamplers = 8;
 constexpr int kUniformBytes = 448;
 constexpr int kBlock = 32;           // RendererSoft::rasterBlockSize_ (RendererSoft.h:128)

@@ -51,6 +51,7 @@ __device__ __forceinline__ float4 toScreen(const DrawParams &p, float4 c) {
 // ------------------------------------------------------------------------------------------------
 template<int SH>
 __global__ void __launch_bounds__(256) k_vertex(const __grid_constant__ DrawParams p) {
+  chainEnter();
   // each warp's 32 varying rows are contiguous in memory: they are staged in shared memory and
   // written as one contiguous run of 16-byte stores (varyStride <= 32 floats for every model)
   __shared__ float4 stage[8][32 * 8];
@@ -109,6 +110,7 @@ __device__ int newClipVertex(const DrawParams &p, int view, int i0, int i1, floa
 
 template<int SH>
 __global__ void __launch_bounds__(128) k_clip(const __grid_constant__ DrawParams p) {
+  chainEnter();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.ntri) return;
   const int view = p.views > 1 ? t / p.ntriView : 0;
@@ -202,10 +204,12 @@ __global__ void __launch_bounds__(128) k_clip(const __grid_constant__ DrawParams
 
 // number of primitives after clipping, kept on the device for the count-driven kernels
 __global__ void k_prim_count(const __grid_constant__ DrawParams p) {
+  chainEnter();
   p.counters[3] = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
 }
 
 __global__ void k_clip_append(const __grid_constant__ DrawParams p) {
+  chainEnter();
   int slot = blockIdx.x * blockDim.x + threadIdx.x;
   int n = min(p.counters[CNT_POLY], p.clipPolyCap);
   if (slot >= n) return;
@@ -295,6 +299,7 @@ __device__ __forceinline__ unsigned long long setupPrim(const DrawParams &p, int
 }
 
 __global__ void __launch_bounds__(256) k_setup(const __grid_constant__ DrawParams p) {
+  chainEnter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int np = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
   unsigned long long bound = i < np ? setupPrim(p, i) : 0ull;
@@ -304,6 +309,7 @@ __global__ void __launch_bounds__(256) k_setup(const __grid_constant__ DrawParam
 }
 
 __global__ void __launch_bounds__(256) k_bin_emit(const __grid_constant__ DrawParams p) {
+  chainEnter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int np = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
   if (i >= np || p.tileCount[i] == 0) return;
@@ -332,6 +338,7 @@ constexpr int kSortTile = kSortThreads * kSortItems; // 2048 items per CTA
 
 __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint32_t *keys, const int *nPtr, int shift,
                                                              int *hist, int numBlocks) {
+  chainEnter();
   __shared__ int h[256];
   int n = *nPtr;
   for (int d = threadIdx.x; d < 256; d += blockDim.x) h[d] = 0;
@@ -350,6 +357,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint32_t *key
 __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t *keysIn, const int *valsIn,
                                                                 uint32_t *keysOut, int *valsOut, const int *nPtr,
                                                                 int shift, const int *histOff, int numBlocks) {
+  chainEnter();
   __shared__ int wcount[8][256];
   int n = *nPtr;
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -396,6 +404,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t *
 }
 
 __global__ void k_tile_ranges(const uint32_t *keys, const int *nPtr, int *tileStart, int *tileEnd) {
+  chainEnter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int n = *nPtr;
   if (i >= n) return;
@@ -409,6 +418,7 @@ __global__ void k_tile_ranges(const uint32_t *keys, const int *nPtr, int *tileSt
 // is arbitrary (tiles are independent).
 __global__ void __launch_bounds__(1024) k_tile_order(const int *tileStart, const int *tileEnd, int numTiles,
                                                      int *order) {
+  chainEnter();
   __shared__ int cnt[33], off[33];
   if (threadIdx.x < 33) cnt[threadIdx.x] = 0;
   __syncthreads();
@@ -467,6 +477,7 @@ __device__ __forceinline__ int blockExclusiveScan(int v, int *total) {
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_local(const int *in, int *out, const int *nPtr, int nMax,
                                                              int *blockSums) {
+  chainEnter();
   int n = nPtr ? min(*nPtr, nMax) : nMax;
   int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
   int v[kScanItems], s = 0;
@@ -486,6 +497,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_local(const int *in, int 
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_sums(int *blockSums, int numBlocks) {
+  chainEnter();
   // single CTA: exclusive scan of up to kScanTile block sums, in place; total at [numBlocks]
   int base = threadIdx.x * kScanItems;
   int v[kScanItems], s = 0;
@@ -505,6 +517,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_sums(int *blockSums, int 
 }
 
 __global__ void k_scan_add(int *out, const int *nPtr, int nMax, const int *blockSums, int numBlocks) {
+  chainEnter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int n = nPtr ? min(*nPtr, nMax) : nMax;
   if (i < nMax) out[i] += blockSums[i / kScanTile];
@@ -557,9 +570,9 @@ static inline int cdiv(long a, long b) { return (int) ((a + b - 1) / b); }
 
 void scanExclusive(const int *in, int *out, const int *nPtr, int nMax, int *blockSums, cudaStream_t st) {
   int nb = max(1, cdiv(nMax, kScanTile));
-  k_scan_local<<<nb, kScanThreads, 0, st>>>(in, out, nPtr, nMax, blockSums);
-  k_scan_sums<<<1, kScanThreads, 0, st>>>(blockSums, nb);
-  k_scan_add<<<max(1, cdiv(nMax, 256)), 256, 0, st>>>(out, nPtr, nMax, blockSums, nb);
+  launchChained(k_scan_local, dim3(nb), dim3(kScanThreads), 0, st, in, out, nPtr, nMax, blockSums);
+  launchChained(k_scan_sums, dim3(1), dim3(kScanThreads), 0, st, blockSums, nb);
+  launchChained(k_scan_add, dim3(max(1, cdiv(nMax, 256))), dim3(256), 0, st, out, nPtr, nMax, blockSums, nb);
 }
 
 int scanScratchInts(int nMax) { return max(1, cdiv(nMax, kScanTile)) + 1; }
@@ -649,13 +662,13 @@ __global__ void __launch_bounds__(128) k_lp_assemble(const __grid_constant__ Dra
 
 template<int SH>
 static void launchGeometry(const DrawParams &p, cudaStream_t st) {
-  if (p.nv > 0) k_vertex<SH><<<cdiv(p.nv, 256), 256, 0, st>>>(p);
-  if (p.ntri > 0) k_clip<SH><<<cdiv(p.ntri, 128), 128, 0, st>>>(p);
+  if (p.nv > 0) launchChained(k_vertex<SH>, dim3(cdiv(p.nv, 256)), dim3(256), 0, st, p);
+  if (p.ntri > 0) launchChained(k_clip<SH>, dim3(cdiv(p.ntri, 128)), dim3(128), 0, st, p);
 }
 
 template<int SH>
 static void pointsLinesGeometry(const DrawParams &p, const LineParams &lp, cudaStream_t st) {
-  if (p.nv > 0) k_vertex<SH><<<cdiv(p.nv, 256), 256, 0, st>>>(p);
+  if (p.nv > 0) launchChained(k_vertex<SH>, dim3(cdiv(p.nv, 256)), dim3(256), 0, st, p);
   if (lp.nIn > 0) k_lp_assemble<SH><<<cdiv(lp.nIn, 128), 128, 0, st>>>(p, lp);
 }
 
@@ -681,16 +694,16 @@ void launchPointsLinesGeometry(const DrawParams &p, const LineParams &lp, cudaSt
 }
 
 void launchClipAppend(const DrawParams &p, cudaStream_t st) {
-  k_clip_append<<<max(1, cdiv(p.clipPolyCap, 256)), 256, 0, st>>>(p);
-  k_prim_count<<<1, 1, 0, st>>>(p);
+  launchChained(k_clip_append, dim3(max(1, cdiv(p.clipPolyCap, 256))), dim3(256), 0, st, p);
+  launchChained(k_prim_count, dim3(1), dim3(1), 0, st, p);
 }
 
 void launchSetup(const DrawParams &p, int primCount, cudaStream_t st) {
-  if (primCount > 0) k_setup<<<cdiv(primCount, 256), 256, 0, st>>>(p);
+  if (primCount > 0) launchChained(k_setup, dim3(cdiv(primCount, 256)), dim3(256), 0, st, p);
 }
 
 void launchBinEmit(const DrawParams &p, int primCount, cudaStream_t st) {
-  if (primCount > 0) k_bin_emit<<<cdiv(primCount, 256), 256, 0, st>>>(p);
+  if (primCount > 0) launchChained(k_bin_emit, dim3(cdiv(primCount, 256)), dim3(256), 0, st, p);
 }
 
 int sortScratchInts(int nPairs) { return 256 * max(1, cdiv(nPairs, kSortTile)) + 1; }
@@ -706,9 +719,9 @@ void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, in
   int passes = keyBits <= 8 ? 1 : (keyBits <= 16 ? 2 : (keyBits <= 24 ? 3 : 4));
   for (int pass = 0; pass < passes; pass++) {
     int shift = pass * 8;
-    k_radix_hist<<<nb, kSortThreads, 0, st>>>(kin, nPtr, shift, hist, nb);
+    launchChained(k_radix_hist, dim3(nb), dim3(kSortThreads), 0, st, kin, nPtr, shift, hist, nb);
     scanExclusive(hist, histScan, nullptr, 256 * nb, scanScratch, st);
-    k_radix_scatter<<<nb, kSortThreads, 0, st>>>(kin, vin, kout, vout, nPtr, shift, histScan, nb);
+    launchChained(k_radix_scatter, dim3(nb), dim3(kSortThreads), 0, st, kin, vin, kout, vout, nPtr, shift, histScan, nb);
     uint32_t *tk = kin; kin = kout; kout = tk;
     int *tv = vin; vin = vout; vout = tv;
   }
@@ -719,22 +732,31 @@ void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, in
 }
 
 void launchTileRanges(const DrawParams &p, int nPairs, const int *nPtr, cudaStream_t st) {
-  if (nPairs > 0) k_tile_ranges<<<cdiv(nPairs, 256), 256, 0, st>>>(p.keyA, nPtr, p.tileStart, p.tileEnd);
+  if (nPairs > 0) launchChained(k_tile_ranges, dim3(cdiv(nPairs, 256)), dim3(256), 0, st, p.keyA, nPtr, p.tileStart, p.tileEnd);
 }
 
 void launchTileOrder(const DrawParams &p, int *order, cudaStream_t st) {
-  k_tile_order<<<1, 1024, 0, st>>>(p.tileStart, p.tileEnd, p.views * p.tilesPerView, order);
+  launchChained(k_tile_order, dim3(1), dim3(1024), 0, st, p.tileStart, p.tileEnd, p.views * p.tilesPerView, order);
 }
 
-__global__ void k_clamp_count(const int *src, int cap, int *dst) { *dst = min(*src, cap); }
-__global__ void k_accumulate_flags(const int *flags, int *sticky) { *sticky |= *flags; }
+__global__ void k_clamp_count(const int *src, int cap, int *dst) {
+  chainEnter();
+  *dst = min(*src, cap);
+}
+__global__ void k_accumulate_flags(const int *flags, int *sticky) {
+  chainEnter();
+  *sticky |= *flags;
+}
 
-void launchClampCount(const int *src, int cap, int *dst, cudaStream_t st) { k_clamp_count<<<1, 1, 0, st>>>(src, cap, dst); }
-__global__ void k_max_into(const int *src, int *dst) { *dst = max(*dst, *src); }
-void launchMaxInto(const int *src, int *dst, cudaStream_t st) { k_max_into<<<1, 1, 0, st>>>(src, dst); }
+void launchClampCount(const int *src, int cap, int *dst, cudaStream_t st) { launchChained(k_clamp_count, dim3(1), dim3(1), 0, st, src, cap, dst); }
+__global__ void k_max_into(const int *src, int *dst) {
+  chainEnter();
+  *dst = max(*dst, *src);
+}
+void launchMaxInto(const int *src, int *dst, cudaStream_t st) { launchChained(k_max_into, dim3(1), dim3(1), 0, st, src, dst); }
 
 void launchAccumulateFlags(const int *flags, int *sticky, cudaStream_t st) {
-  k_accumulate_flags<<<1, 1, 0, st>>>(flags, sticky);
+  launchChained(k_accumulate_flags, dim3(1), dim3(1), 0, st, flags, sticky);
 }
 
 void launchFill32(uint32_t *dst, uint32_t value, size_t n, cudaStream_t st) {

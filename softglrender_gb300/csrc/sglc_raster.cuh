@@ -170,6 +170,18 @@ __device__ __forceinline__ bool depthCmp(float a, float b, int func) {
   return (bits >> func) & 1u;
 }
 
+// DepthFunction values (RenderStates.h:13-22), each the index of its bit in depthCmp
+constexpr int DEPTH_LESS = 1, DEPTH_LEQUAL = 3, DEPTH_GREATER = 4, DEPTH_GEQUAL = 6;
+
+// The depth a sample keeps when a fragment of clamped depth b meets stored depth a, for the four
+// functions whose depth write keeps a running extremum: b if it passes the test against a, else a.
+// On non-NaN values it is associative (the earliest minimum for LESS, the latest for LEQUAL, and
+// likewise for the maximum), which is what lets pass 2 evaluate a pixel's fragments as a scan.
+__device__ __forceinline__ float depthKeep(float a, float b, int func) {
+  const bool take = func == DEPTH_LESS ? b < a : (func == DEPTH_LEQUAL ? b <= a : (func == DEPTH_GREATER ? b > a : b >= a));
+  return take ? b : a;
+}
+
 // calcBlendFactor: one of {0, 1, x, 1 - x}, x chosen among the four blend operands
 __device__ __forceinline__ float blendFactor(const DrawParams &p, int k, float src, float srcA, float dst, float dstA) {
   int op = p.bfOp[k];
@@ -494,6 +506,7 @@ __device__ __forceinline__ bool touchesRect(const DrawParams &p, int prim, int r
 
 template<int SH, int S, bool HAS_COLOR, bool HAS_DEPTH>
 __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawParams p) {
+  chainEnter();
   __shared__ FragQueue queues[HAS_COLOR ? 8 : 1];
   __shared__ unsigned candMasks[8][32];
   const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
@@ -617,11 +630,11 @@ template<int SH>
 void launchRasterModel(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
   int grid = p.views * p.tilesPerView;
   if (p.samples == 4) {
-    if (hasDepth) k_raster<SH, 4, true, true><<<grid, 256, 0, st>>>(p);
-    else k_raster<SH, 4, true, false><<<grid, 256, 0, st>>>(p);
+    if (hasDepth) launchChained(k_raster<SH, 4, true, true>, dim3(grid), dim3(256), 0, st, p);
+    else launchChained(k_raster<SH, 4, true, false>, dim3(grid), dim3(256), 0, st, p);
   } else {
-    if (hasDepth) k_raster<SH, 1, true, true><<<grid, 256, 0, st>>>(p);
-    else k_raster<SH, 1, true, false><<<grid, 256, 0, st>>>(p);
+    if (hasDepth) launchChained(k_raster<SH, 1, true, true>, dim3(grid), dim3(256), 0, st, p);
+    else launchChained(k_raster<SH, 1, true, false>, dim3(grid), dim3(256), 0, st, p);
   }
   (void) hasColor;
 }
@@ -689,6 +702,7 @@ struct CovSlot {
 
 template<int S, bool HAS_DEPTH>
 __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid_constant__ DrawParams p) {
+  chainEnter();
   __shared__ CovSlot covSlots[8][32];
   __shared__ unsigned candMasks[8][32];
   __shared__ int covQueue[8][64];
@@ -744,6 +758,51 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
   CovSlot *slots = covSlots[warp];
   int *queue = covQueue[warp];
   int qn = 0;
+  // the depth functions whose depth write keeps a running minimum or maximum (or no depth write)
+  // take the scanned depth path of pass 2; EQUAL, NOTEQUAL, ALWAYS and NEVER with depth writes run
+  // each pixel's pairs in order on its owner lane
+  const bool testDepth = p.depthTest && HAS_DEPTH;
+  const int df = p.depthFunc;
+  const bool scanDepth = !testDepth || !p.depthMask || df == DEPTH_LESS || df == DEPTH_LEQUAL ||
+                         df == DEPTH_GREATER || df == DEPTH_GEQUAL;
+  const float keepId = (df == DEPTH_LESS || df == DEPTH_LEQUAL) ? __int_as_float(0x7f800000) : __int_as_float(0xff800000);
+  // appends one record per lane with a non-zero sample mask, in lane order, to this warp's list
+  auto appendRecords = [&](uint32_t mask, uint32_t meta, int prim, uint32_t pixw, float b0, float b1, float b2) {
+    const unsigned want = __ballot_sync(0xffffffffu, mask != 0);
+    if (!want || dead) return;
+    const int n = __popc(want);
+    if (head < 0) {
+      ch = head = allocChunk(p, lane);
+      cnt = 0;
+      if (ch < 0) {
+        dead = true;
+        return;
+      }
+    }
+    int nch = -1;
+    if (cnt + n > kChunk) nch = allocChunk(p, lane);
+    if (mask) {
+      const int ei = cnt + __popc(want & lt);
+      const int c2 = ei < kChunk ? ch : nch;
+      if (c2 >= 0) {
+        const size_t r = (size_t) c2 * kChunk + (ei < kChunk ? ei : ei - kChunk);
+        p.recA[r] = make_int4(prim, (int) meta, (int) pixw, __float_as_int(b0));
+        p.recB[r] = make_float2(b1, b2);
+      }
+    }
+    total += (unsigned long long) n;
+    if (cnt + n > kChunk) {
+      if (lane == 0) {
+        p.chunkFill[ch] = kChunk;
+        if (nch >= 0) p.chunkNext[ch] = nch;
+      }
+      cnt = cnt + n - kChunk;
+      ch = nch;
+      if (nch < 0) dead = true;
+    } else {
+      cnt += n;
+    }
+  };
   for (int base = start; base < end || qn > 0;) {
     // dense batches: the tile-list primitives whose rectangle touches this warp's pixels, in list
     // order, 32 at a time (most of a tile's list misses any one 8x4 rectangle)
@@ -820,11 +879,58 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
         sl.nq = nq;
         sl.prim = pr;
       }
+      const int s0 = max(off, r0) - r0, s1 = min(off + cnum, r0 + 32) - r0;   // this lane's pixel's pairs
+      const int nOwn = max(0, s1 - s0);
+      if (scanDepth && !__any_sync(0xffffffffu, sl.nq > 1)) {
+        // every pair at once: a pixel's pairs occupy consecutive lanes in candidate order, so the
+        // depth each one is tested against is a segmented scan over the lanes (depthKeep), seeded
+        // with the pixel's depth; the segment's last lane holds the pixel's new depth
+        const bool has = kk < pairs && sl.nq > 0;
+        uint32_t cov = 0u;
+        if (has) cov = S == 4 ? ((sl.cv.mask & 16u) ? (sl.cv.mask & 15u) : 0u) : (sl.cv.mask & 1u);
+        uint32_t pass = cov;
+        if (testDepth) {
+          const int segStart = max(offL, r0) - r0;
+          const bool inDL = __shfl_sync(0xffffffffu, inD, L);
+          const float zs[4] = {sl.cv.z0, sl.cv.z1, sl.cv.z2, sl.cv.z3};
+          const float fbd[4] = {fb.d0, fb.d1, fb.d2, fb.d3};
+          float last[4] = {0.f, 0.f, 0.f, 0.f};
+          pass = 0u;
+#pragma unroll
+          for (int q = 0; q < S; q++) {
+            const float cz = gclamp(zs[q], p.vp.absMin, p.vp.absMax);
+            float cur = __shfl_sync(0xffffffffu, fbd[q], L);
+            if (p.depthMask) {
+              float x = ((cov >> q) & 1u) && cz == cz ? cz : keepId;
+#pragma unroll
+              for (int d = 1; d < 32; d <<= 1) {
+                const float y = __shfl_up_sync(0xffffffffu, x, d);
+                if (lane - d >= segStart) x = depthKeep(y, x, p.depthFunc);
+              }
+              const float ex = __shfl_up_sync(0xffffffffu, x, 1);
+              if (lane > segStart) cur = depthKeep(cur, ex, p.depthFunc);
+              last[q] = __shfl_sync(0xffffffffu, x, nOwn > 0 ? s1 - 1 : lane);
+            }
+            if (((cov >> q) & 1u) && inDL && depthCmp(cz, cur, p.depthFunc)) pass |= 1u << q;
+          }
+          if (p.depthMask && inD && nOwn > 0) {
+            fb.d0 = depthKeep(fb.d0, last[0], p.depthFunc);
+            if (S == 4) {
+              fb.d1 = depthKeep(fb.d1, last[1], p.depthFunc);
+              fb.d2 = depthKeep(fb.d2, last[2], p.depthFunc);
+              fb.d3 = depthKeep(fb.d3, last[3], p.depthFunc);
+            }
+          }
+        }
+        const int lpx = rx0 + (L & 7), lpy = ry0 + (L >> 3);
+        appendRecords(pass, (uint32_t) L | (pass << 5) | ((uint32_t) (lpx - sl.x0) << 9) |
+                                ((uint32_t) (lpy - sl.y0) << 10) | ((uint32_t) view << 11),
+                      sl.prim, (uint32_t) lpx | ((uint32_t) lpy << 16), sl.cv.b0, sl.cv.b1, sl.cv.b2);
+        continue;
+      }
       slots[lane] = sl;
       __syncwarp();
       // owner phase: this lane's pairs of the round, in order
-      const int s0 = max(off, r0) - r0, s1 = min(off + cnum, r0 + 32) - r0;
-      const int nOwn = max(0, s1 - s0);
       const int maxOwn = __reduce_max_sync(0xffffffffu, nOwn);
       for (int q = 0; q < maxOwn; q++) {
         const CovSlot *e = q < nOwn ? &slots[s0 + q] : nullptr;
@@ -838,42 +944,9 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
             qx = (k % e->nx) ? e->x1 : e->x0;
             mask = depthOps<S, HAS_DEPTH>(p, e->cv, inD, fb);
           }
-          unsigned want = __ballot_sync(0xffffffffu, mask != 0);
-          if (!want || dead) continue;
-          const int n = __popc(want);
-          if (head < 0) {
-            ch = head = allocChunk(p, lane);
-            cnt = 0;
-            if (ch < 0) {
-              dead = true;
-              continue;
-            }
-          }
-          int nch = -1;
-          if (cnt + n > kChunk) nch = allocChunk(p, lane);
-          if (mask) {
-            int ei = cnt + __popc(want & lt);
-            int c2 = ei < kChunk ? ch : nch;
-            if (c2 >= 0) {
-              size_t r = (size_t) c2 * kChunk + (ei < kChunk ? ei : ei - kChunk);
-              uint32_t meta = (uint32_t) lane | (mask << 5) | ((uint32_t) (px - qx) << 9) |
-                              ((uint32_t) (py - qy) << 10) | ((uint32_t) view << 11);
-              p.recA[r] = make_int4(e->prim, (int) meta, (int) pixWord, __float_as_int(e->cv.b0));
-              p.recB[r] = make_float2(e->cv.b1, e->cv.b2);
-            }
-          }
-          total += (unsigned long long) n;
-          if (cnt + n > kChunk) {
-            if (lane == 0) {
-              p.chunkFill[ch] = kChunk;
-              if (nch >= 0) p.chunkNext[ch] = nch;
-            }
-            cnt = cnt + n - kChunk;
-            ch = nch;
-            if (nch < 0) dead = true;
-          } else {
-            cnt += n;
-          }
+          appendRecords(mask, (uint32_t) lane | (mask << 5) | ((uint32_t) (px - qx) << 9) |
+                                  ((uint32_t) (py - qy) << 10) | ((uint32_t) view << 11),
+                        e ? e->prim : 0, pixWord, e ? e->cv.b0 : 0.f, e ? e->cv.b1 : 0.f, e ? e->cv.b2 : 0.f);
         }
       }
       __syncwarp();
@@ -925,6 +998,7 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
 // and latency-bound, more warps beat a few spills
 template<int SH, int S>
 __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ DrawParams p) {
+  chainEnter();
   const int n = min(p.counters[kCntDense], p.chunkCap * kChunk);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int r = p.recDense[i];
@@ -942,6 +1016,7 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ DrawPa
 // colour operations in each warp's list order, then colour store and MSAA resolve
 template<int S>
 __global__ void __launch_bounds__(256) k_rop(const __grid_constant__ DrawParams p) {
+  chainEnter();
   __shared__ float4 scol[8][kChunk];
   __shared__ uint32_t smeta[8][kChunk];
   __shared__ uint32_t sown[8][kChunk];
@@ -1024,8 +1099,8 @@ __global__ void __launch_bounds__(256) k_rop(const __grid_constant__ DrawParams 
 template<int SH>
 void launchShadeModel(const DrawParams &p, cudaStream_t st) {
   const int grid = 152 * 16;
-  if (p.samples == 4) k_shade<SH, 4><<<grid, 128, 0, st>>>(p);
-  else k_shade<SH, 1><<<grid, 128, 0, st>>>(p);
+  if (p.samples == 4) launchChained(k_shade<SH, 4>, dim3(grid), dim3(128), 0, st, p);
+  else launchChained(k_shade<SH, 1>, dim3(grid), dim3(128), 0, st, p);
 }
 
 }  // namespace sglc

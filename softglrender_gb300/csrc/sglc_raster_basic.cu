@@ -33,11 +33,11 @@ bool deferredShadingModel(int shading) {
 void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st, cudaEvent_t evCov, cudaEvent_t evShade) {
   const int grid = p.views * p.tilesPerView + 3 * (p.tileOrder ? p.heavySlots : 0);   // see tileJob
   if (p.samples == 4) {
-    if (hasDepth) k_raster_cov<4, true><<<grid, 256, 0, st>>>(p);
-    else k_raster_cov<4, false><<<grid, 256, 0, st>>>(p);
+    if (hasDepth) launchChained(k_raster_cov<4, true>, dim3(grid), dim3(256), 0, st, p);
+    else launchChained(k_raster_cov<4, false>, dim3(grid), dim3(256), 0, st, p);
   } else {
-    if (hasDepth) k_raster_cov<1, true><<<grid, 256, 0, st>>>(p);
-    else k_raster_cov<1, false><<<grid, 256, 0, st>>>(p);
+    if (hasDepth) launchChained(k_raster_cov<1, true>, dim3(grid), dim3(256), 0, st, p);
+    else launchChained(k_raster_cov<1, false>, dim3(grid), dim3(256), 0, st, p);
   }
   if (evCov) cudaEventRecord(evCov, st);
   switch (p.shading) {
@@ -52,16 +52,16 @@ void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st, c
     case SH_FXAA: launchShadeEnvironment(p, st); break;
   }
   if (evShade) cudaEventRecord(evShade, st);
-  if (p.samples == 4) k_rop<4><<<grid, 256, 0, st>>>(p);
-  else k_rop<1><<<grid, 256, 0, st>>>(p);
+  if (p.samples == 4) launchChained(k_rop<4>, dim3(grid), dim3(256), 0, st, p);
+  else launchChained(k_rop<1>, dim3(grid), dim3(256), 0, st, p);
 }
 
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
   int grid = p.views * p.tilesPerView;
   if (!hasColor) {   // depth-only pass: the fragment shader is skipped (RendererSoft.cpp:346-348)
     if (!hasDepth) return;
-    if (p.samples == 4) k_raster<SH_BASE, 4, false, true><<<grid, 256, 0, st>>>(p);
-    else k_raster<SH_BASE, 1, false, true><<<grid, 256, 0, st>>>(p);
+    if (p.samples == 4) launchChained(k_raster<SH_BASE, 4, false, true>, dim3(grid), dim3(256), 0, st, p);
+    else launchChained(k_raster<SH_BASE, 1, false, true>, dim3(grid), dim3(256), 0, st, p);
     return;
   }
   switch (p.shading) {

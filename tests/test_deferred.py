@@ -10,7 +10,7 @@ from softglrender_gb300 import scenes as S
 from softglrender_gb300.batch import BatchConfig, BatchedViews
 from softglrender_gb300.ibl import IBLGenerator, equirect_sky
 
-from helpers import render
+from helpers import assert_outputs_match, render
 
 pytestmark = pytest.mark.gpu
 
@@ -63,6 +63,73 @@ def test_deferred_equals_fused_ibl(cuda_lib):
         r.destroy()
     for x, y in zip(*outs):
         assert np.array_equal(x, y)
+
+
+def _spheres_scene(samples, func, mask, clear_depth, w=160, h=120):
+    """Three overlapping spheres drawn without culling (two to four fragments per pixel), directional
+    Blinn-Phong (a deferred shading model), one depth function and depth-write setting for all."""
+    vert, idx = S.uv_sphere(40, 20)
+    eye = np.array([0.0, 0.0, 3.2])
+    Pm = S.perspective(np.pi / 3.0, w / h, 0.05, False)
+    VP = S.mm4(Pm, S.look_at(eye, [0, 0, 0], [0, 1, 0]))
+    scene_block = S.uniforms_scene([0.15, 0.15, 0.15], eye, S.normalize(np.array([0.4, 0.7, 0.6])), [1, 1, 1])
+    material = S.uniforms_material(True, False, False, 1.0, 0.6, [1, 1, 1, 1])
+    tex = S.TextureSpec("u_albedoMap", A.TextureDesc(64, 64, A.TextureType_2D, A.TextureFormat_RGBA8,
+                                                     A.TextureUsage_Sampler | A.TextureUsage_UploadData, True, False),
+                        A.SamplerDesc(A.Filter_LINEAR_MIPMAP_LINEAR, A.Filter_LINEAR, A.Wrap_REPEAT, A.Wrap_REPEAT,
+                                      A.Wrap_REPEAT), layers=[S.checkerboard(64, 8, 11)])
+    st = A.RenderStates(blend=False, depthTest=True, depthMask=mask, depthFunc=func, cullFace=False)
+    draws = []
+    for t in ([-0.45, 0.0, 0.0], [0.4, 0.15, -0.35], [0.0, -0.25, 0.45]):
+        M = np.eye(4)
+        M[:3, 3] = t
+        blocks = {"UniformsModel": S.uniforms_model(M, S.mm4(VP, M), None, False), "UniformsScene": scene_block,
+                  "UniformsMaterial": material}
+        draws.append(S.DrawSpec(vert, 64, idx, A.Shading_BlinnPhongDir, ("ALBEDO_MAP",), st, blocks, [tex]))
+    clear = A.ClearStates(True, True, (0.05, 0.05, 0.08, 1.0), clear_depth)
+    return S.Scene("spheres", [S.PassSpec(w, h, samples, clear, draws)])
+
+
+@pytest.mark.parametrize("samples", [1, 4])
+@pytest.mark.parametrize("mask", [True, False])
+@pytest.mark.parametrize("func", range(8))
+def test_deferred_depth_functions_equal_fused(func, mask, samples, cuda_lib):
+    """The coverage kernel evaluates a pixel's fragments as a scan for LESS / LEQUAL / GREATER /
+    GEQUAL with depth writes (and for any function without them) and in order on the pixel's lane
+    for the rest; both give the fused kernel's images bit for bit."""
+    far = func in (A.DepthFunc_LESS, A.DepthFunc_LEQUAL, A.DepthFunc_EQUAL)
+    scene = _spheres_scene(samples, func, mask, 1.0 if far else 0.0 if func != A.DepthFunc_NOTEQUAL else 0.5)
+    a = _render_mode(cuda_lib, scene, True)
+    b = _render_mode(cuda_lib, scene, False)
+    for k in a:
+        x, y = a[k], b[k]
+        if x.dtype == np.float32:
+            x, y = x.view(np.uint32), y.view(np.uint32)
+        assert np.array_equal(x, y), k
+
+
+@pytest.mark.parametrize("func", [A.DepthFunc_LESS, A.DepthFunc_LEQUAL, A.DepthFunc_GREATER, A.DepthFunc_GEQUAL])
+def test_deferred_depth_functions_match_oracle(func, cuda_lib, oracle_lib):
+    scene = _spheres_scene(4, func, True, 1.0 if func in (A.DepthFunc_LESS, A.DepthFunc_LEQUAL) else 0.0)
+    gpu, _ = render(cuda_lib, scene)
+    cpu, _ = render(oracle_lib, scene)
+    assert_outputs_match(gpu, cpu, f"spheres depth func {func}")
+
+
+def test_deferred_early_z_off_equals_fused(cuda_lib):
+    scene = _spheres_scene(4, A.DepthFunc_LEQUAL, True, 1.0)
+    outs = []
+    for deferred in (True, False):
+        r = A.Renderer(cuda_lib, 0)
+        r.setDeferredShading(deferred)
+        r.setEnableEarlyZ(False)
+        inst = S.SceneInstance(r, scene)
+        inst.render()
+        r.waitIdle()
+        outs.append(inst.outputs())
+        r.destroy()
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k].view(np.uint8), outs[1][k].view(np.uint8)), k
 
 
 CFG = BatchConfig(views=6, size=96, shadow=256, lon=48, lat=24, tex=64, seed=4300)
