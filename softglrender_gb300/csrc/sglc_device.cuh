@@ -445,6 +445,81 @@ static __device__ __forceinline__ uint32_t textureImpl(const DevSampler &s, int 
   return mixTexel(th, tl, frac, isF);
 }
 
+// RGBA8 lookups with the channels as floats. The reference mixes u8 texels in float and stores each
+// mix back to u8 (glm::mix on u8vec4 truncates), so the bilinear and trilinear stages above pack and
+// unpack between mixes. For weights in [0, 1] every mix lies in [0, 256), where that store equals
+// truncf of the float mix: the float path keeps the channels as integer-valued floats from the texel
+// loads to the shader's /255 and skips the packing. A weight outside [0, 1] (NaN or infinite
+// coordinates, NaN LOD) sends the lookup through textureImpl instead, whose stores define it.
+__device__ __forceinline__ float4 mixF4(float4 X, float4 Y, float a) {
+  const float ia = 1.f - a;
+  return make_float4(truncf(X.x * ia + Y.x * a), truncf(X.y * ia + Y.y * a), truncf(X.z * ia + Y.z * a),
+                     truncf(X.w * ia + Y.w * a));
+}
+
+// bilinearPx as floats; false (nothing written) when a weight lies outside [0, 1]
+__device__ __forceinline__ bool bilinearPxF(const DevTex &t, int face, int level, float ux, float uy, int wrap,
+                                            uint32_t border, float4 &out) {
+  float fx0 = ux - 0.5f, fy0 = uy - 0.5f;
+  float flx = floorf(fx0), fly = floorf(fy0);
+  const float fx = fx0 - flx, fy = fy0 - fly;
+  if (!(fx >= 0.f && fx <= 1.f && fy >= 0.f && fy <= 1.f)) return false;
+  int x = (int) flx, y = (int) fly;
+  const int w = t.w[level], h = t.h[level], tw = t.tilesW[level], layout = t.layout;
+  const uint32_t *lv = t.base + (size_t) face * t.layerStride + t.offset[level];
+  int xa = wrapCoord(x, w, wrap), xb = wrapCoord(x + 1, w, wrap);
+  int ya = wrapCoord(y, h, wrap), yb = wrapCoord(y + 1, h, wrap);
+  bool vxa = (unsigned) xa < (unsigned) w, vxb = (unsigned) xb < (unsigned) w;
+  bool vya = (unsigned) ya < (unsigned) h, vyb = (unsigned) yb < (unsigned) h;
+  uint32_t fill = wrap == WRAP_BORDER ? border : 0u;
+  uint32_t s1 = (vxa && vya) ? __ldg(lv + levelIndex(layout, xa, ya, w, tw)) : fill;
+  uint32_t s2 = (vxb && vya) ? __ldg(lv + levelIndex(layout, xb, ya, w, tw)) : fill;
+  uint32_t s3 = (vxa && vyb) ? __ldg(lv + levelIndex(layout, xa, yb, w, tw)) : fill;
+  uint32_t s4 = (vxb && vyb) ? __ldg(lv + levelIndex(layout, xb, yb, w, tw)) : fill;
+  out = mixF4(mixF4(unpack4(s1), unpack4(s2), fx), mixF4(unpack4(s3), unpack4(s4), fx), fy);
+  return true;
+}
+
+static __device__ __noinline__ float4 textureRGBA8Packed(const DevSampler &s, int face, float u, float v, float lod) {
+  return unpack4(textureImpl(s, face, u, v, lod));
+}
+
+// unpack4(textureImpl(s, face, u, v, lod)) for RGBA8 textures, computed as floats
+static __device__ __forceinline__ float4 textureRGBA8(const DevSampler &s, int face, float u, float v, float lod) {
+  const DevTex &t = s.tex;
+  if (t.levels <= 0) return make_float4(0.f, 0.f, 0.f, 0.f);
+  if (s.isFloat) return textureRGBA8Packed(s, face, u, v, lod);
+  const int f = s.filter;
+  const bool nearest = (f & 1) == 0;
+  const int maxLevel = t.levels - 1;
+  int hi = 0, lo = 0;
+  bool two = false;
+  float frac = 0.f;
+  if (f == FILTER_NN || f == FILTER_LN) {
+    hi = min(max((int) ceilf(lod + 0.5f) - 1, 0), maxLevel);
+  } else if (f >= FILTER_NL) {
+    float fl = floorf(lod);
+    hi = min(max((int) fl, 0), maxLevel);
+    lo = min(max(hi + 1, 0), maxLevel);
+    two = hi != lo;
+    frac = lod - fl;
+  }
+  if (two && !(frac >= 0.f && frac <= 1.f)) return textureRGBA8Packed(s, face, u, v, lod);
+  float4 th, tl;
+  if (nearest) {
+    th = unpack4(nearestSample(t, face, hi, u, v, s.wrap, s.border));
+    if (!two) return th;
+    tl = unpack4(nearestSample(t, face, lo, u, v, s.wrap, s.border));
+  } else {
+    if (!bilinearPxF(t, face, hi, u * (float) t.w[hi], v * (float) t.h[hi], s.wrap, s.border, th))
+      return textureRGBA8Packed(s, face, u, v, lod);
+    if (!two) return th;
+    if (!bilinearPxF(t, face, lo, u * (float) t.w[lo], v * (float) t.h[lo], s.wrap, s.border, tl))
+      return textureRGBA8Packed(s, face, u, v, lod);
+  }
+  return mixF4(th, tl, frac);
+}
+
 // textureLodOffset at LOD 0 (SamplerSoft.h:117-165, 214-238): integer texel offset added to the
 // scaled coordinate (bilinear) or to the floored texel (nearest)
 static __device__ __noinline__ uint32_t textureOffsetImpl(const DevSampler &s, float u, float v, int ox, int oy) {

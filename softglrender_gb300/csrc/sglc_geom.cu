@@ -415,16 +415,21 @@ __global__ void k_tile_ranges(const uint32_t *keys, const int *nPtr, int *tileSt
 
 // Raster CTA order: tiles bucketed by log2 of their list length, longest first, so the tiles that
 // take longest start first and do not form the tail of the launch. One CTA; order within a bucket
-// is arbitrary (tiles are independent).
+// is arbitrary (tiles are independent). Most tiles of a frame fall in a few buckets (the empty one
+// above all), so each warp adds its lanes of one bucket with one shared-memory atomic.
 __global__ void __launch_bounds__(1024) k_tile_order(const int *tileStart, const int *tileEnd, int numTiles,
                                                      int *order) {
   chainEnter();
   __shared__ int cnt[33], off[33];
+  const int lane = threadIdx.x & 31;
   if (threadIdx.x < 33) cnt[threadIdx.x] = 0;
   __syncthreads();
-  for (int t = threadIdx.x; t < numTiles; t += blockDim.x) {
-    int len = tileEnd[t] - tileStart[t];
-    atomicAdd(&cnt[len > 0 ? 32 - __clz(len) : 0], 1);
+  const int span = (numTiles + blockDim.x - 1) / blockDim.x * blockDim.x;   // whole warps every round
+  for (int t = threadIdx.x; t < span; t += blockDim.x) {
+    const int len = t < numTiles ? tileEnd[t] - tileStart[t] : 0;
+    const int b = t < numTiles ? (len > 0 ? 32 - __clz(len) : 0) : 33;
+    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    if (b < 33 && lane == __ffs(peers) - 1) atomicAdd(&cnt[b], __popc(peers));
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -435,10 +440,15 @@ __global__ void __launch_bounds__(1024) k_tile_order(const int *tileStart, const
     }
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < numTiles; t += blockDim.x) {
-    int len = tileEnd[t] - tileStart[t];
-    int pos = atomicAdd(&off[len > 0 ? 32 - __clz(len) : 0], 1);
-    order[pos] = t;
+  for (int t = threadIdx.x; t < span; t += blockDim.x) {
+    const int len = t < numTiles ? tileEnd[t] - tileStart[t] : 0;
+    const int b = t < numTiles ? (len > 0 ? 32 - __clz(len) : 0) : 33;
+    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (b < 33 && lane == leader) base = atomicAdd(&off[b], __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (b < 33) order[base + __popc(peers & ((1u << lane) - 1u))] = t;
   }
 }
 

@@ -108,14 +108,16 @@ __device__ __forceinline__ float4 tex2D(const DrawParams &p, int slot, float u, 
   const DevSampler &s = p.samp[slot];
   float lod = 0.f;
   if (s.lodFromDerivative) lod += lodOf(s, f);
-  return unpackUnit4(textureImpl(s, 0, u, v, lod));
+  const float4 c = textureRGBA8(s, 0, u, v, lod);
+  return make_float4(div255(c.x), div255(c.y), div255(c.z), div255(c.w));
 }
 
 __device__ __forceinline__ float4 texCube(const DrawParams &p, int slot, f3 d, float lod) {
   int face;
   float u, v;
   cubeUV(d, &face, &u, &v);
-  return unpackUnit4(textureImpl(p.samp[slot], face, u, v, lod));
+  const float4 c = textureRGBA8(p.samp[slot], face, u, v, lod);
+  return make_float4(div255(c.x), div255(c.y), div255(c.z), div255(c.w));
 }
 
 __device__ __forceinline__ f3 normalFromMap(const DrawParams &p, const FragIn &f, int nOff, int tOff) {
@@ -444,8 +446,8 @@ __device__ __forceinline__ float fxaaQuality(float q) {
 __device__ __forceinline__ float rgb2luma(f3 c) { return dot3(c, mk3(0.299f, 0.587f, 0.114f)); }
 __device__ __forceinline__ float fxaaClamp01(float x) { return gclamp(x, 0.0f, 1.0f); }
 __device__ __forceinline__ f3 fxaaTex(const DrawParams &p, float u, float v) {
-  float4 c = unpackUnit4(textureImpl(p.samp[0], 0, u, v, 0.f));
-  return mk3(c.x, c.y, c.z);
+  const float4 c = textureRGBA8(p.samp[0], 0, u, v, 0.f);
+  return mk3(div255(c.x), div255(c.y), div255(c.z));
 }
 __device__ __forceinline__ f3 fxaaTexOff(const DrawParams &p, float u, float v, int ox, int oy) {
   float4 c = unpackUnit4(textureOffsetImpl(p.samp[0], u, v, ox, oy));
