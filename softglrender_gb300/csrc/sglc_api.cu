@@ -819,10 +819,10 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     CK(cudaMemsetAsync(p.counters, 0, sizeof(int) * 16, c->stream));
     if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[0], c->stream));
     launchVertexAndClip(p, c->stream);
-    scanExclusive(p.clipExtra, p.clipAppendOff, nullptr, std::max(p.ntri, 1), c->scanScratch.as<int>(), c->stream);
+    scanExclusive2(p.clipExtra, p.clipAppendOff, nullptr, std::max(p.ntri, 1), c->scanScratch.as<int>(), c->stream);
     launchClipAppend(p, c->stream);
     launchSetup(p, p.primCap, c->stream);
-    scanExclusive(p.tileCount, p.pairOff, p.counters + 3, p.primCap, c->scanScratch.as<int>(), c->stream);
+    scanExclusive2(p.tileCount, p.pairOff, p.counters + 3, p.primCap, c->scanScratch.as<int>(), c->stream);
     CK(cudaGetLastError());
     if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[1], c->stream));
     int newVerts = -1, polys = -1, np = p.primCap, nPairs;
@@ -854,7 +854,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       // no read-back: the bin arrays have the set capacity, the sort and ranges read the pair count
       // (clamped to it) from the device
       nPairs = (int) std::max<int64_t>(1, std::min<int64_t>(c->cap.bin_entries, 1 << 30));
-      launchClampCount(p.pairOff + p.primCap, nPairs, p.counters + 4, c->stream);
+      p.binPairTotal = p.pairOff + p.primCap;   // k_bin_emit clamps it into counters[4]
       nPairsDev = p.counters + 4;
     }
     CK(c->keyA.ensure(sizeof(uint32_t) * (size_t) std::max(nPairs, 1)));
@@ -875,13 +875,17 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     p.pairCap = nPairs;
     p.tileStart = c->tileStart.as<int>();
     p.tileEnd = c->tileEnd.as<int>();
-    CK(cudaMemsetAsync(p.tileStart, 0, sizeof(int) * numTiles, c->stream));
-    CK(cudaMemsetAsync(p.tileEnd, 0, sizeof(int) * numTiles, c->stream));
+    if (np > 0) {
+      p.binZeroRanges = 1;   // k_bin_emit clears the tile ranges
+    } else {
+      CK(cudaMemsetAsync(p.tileStart, 0, sizeof(int) * numTiles, c->stream));
+      CK(cudaMemsetAsync(p.tileEnd, 0, sizeof(int) * numTiles, c->stream));
+    }
     launchBinEmit(p, np, c->stream);
     int keyBits = 1;
     while ((1 << keyBits) < numTiles) keyBits++;
     sortPairs(p, nPairs, nPairsDev, keyBits, c->sortHist.as<int>(), c->sortHistScan.as<int>(),
-              c->scanScratch.as<int>(), c->stream);
+              c->scanScratch.as<int>(), c->stream, true);
     launchTileRanges(p, nPairs, nPairsDev, c->stream);
     const bool heavyFirst = !deferred || c->cap.heavy_first;
     if (heavyFirst) {
@@ -927,17 +931,19 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[2], c->stream));
     c->evDeferred = deferShade && c->statsLevel >= 1;
     if (deferShade) {
+      // k_rop, the draw's last kernel, also keeps the peak of the chunks actually used (the pool is
+      // sized from an upper bound; the peak calibrates capacities) and accumulates the overflow flags
+      p.ropPeakChunks = c->peakChunks.as<int>();
+      p.ropSticky = deferred ? c->sticky.as<int>() : nullptr;
       launchRasterDeferred(p, dt != nullptr, c->stream, c->evDeferred ? c->ev[4] : nullptr,
                            c->evDeferred ? c->ev[5] : nullptr);
-      // chunks actually used (the pool is sized from an upper bound): calibrates capacities
-      launchMaxInto(p.counters + kCntChunks, c->peakChunks.as<int>(), c->stream);
     }
     else launchRaster(p, ct != nullptr, dt != nullptr, c->stream);
     if (c->statsLevel >= 1) {
       CK(cudaEventRecord(c->ev[3], c->stream));
       c->evPending = true;
     }
-    if (deferred) launchAccumulateFlags(p.counters + 2, c->sticky.as<int>(), c->stream);
+    if (deferred && !deferShade) launchAccumulateFlags(p.counters + 2, c->sticky.as<int>(), c->stream);
     CK(cudaGetLastError());
     if (ct && ct->desc.multi_sample) ct->resolvedValid = true;
     c->stats.vertices_in = p.nv;
@@ -945,11 +951,13 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     c->stats.clip_vertices = newVerts;
     c->stats.primitives = deferred ? -1 : np;
     c->stats.bin_entries = deferred ? -1 : nPairs;
-    // vertex, clip, 3 scan, append, count, setup, 3 scan | emit, sort, ranges, order, raster
+    // vertex, clip, 2 scan, append, setup, 2 scan | emit, sort (hist, 2 scan, scatter per pass),
+    // ranges, order, raster (deferred shading: coverage, shade, ROP); flag accumulation when the
+    // draw has capacities and no ROP kernel; a redone attempt ran the 8 geometry launches before
     int sortPasses = nPairs > 0 ? (keyBits + 7) / 8 : 0;
-    c->stats.kernel_launches = (p.nv > 0) + (p.ntri > 0) + 3 + 2 + 1 + 3 + (np > 0) + sortPasses * 5 +
-                               (nPairs > 0) + (heavyFirst ? 1 : 0) + 1 + attempt * 10 + (deferred ? 2 : 0) +
-                               (deferShade ? 3 : 0);
+    c->stats.kernel_launches = (p.nv > 0) + (p.ntri > 0) + 2 + 1 + 1 + 2 + (np > 0) + sortPasses * 4 +
+                               (nPairs > 0) + (heavyFirst ? 1 : 0) + 1 + attempt * 8 +
+                               (deferred && !deferShade ? 1 : 0) + (deferShade ? 2 : 0);
     return SGLC_OK;
   }
   return c->fail(SGLC_ERR_OVERFLOW, "draw: clip capacity could not be satisfied");

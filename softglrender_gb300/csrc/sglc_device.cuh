@@ -209,6 +209,11 @@ struct DrawParams {
   // the heaviest tiles (the first heavySlots of the heavy-first order whose list is longer than
   // heavyMin) are split over 4 CTAs, each warp owning one 8-pixel row instead of an 8x4 block
   int heavySlots, heavyMin;
+  // small steps folded into kernels that run anyway (each null / 0: not done there)
+  int binZeroRanges;              // k_bin_emit zeroes tileStart / tileEnd of all tiles
+  const int *binPairTotal;        // k_bin_emit sets counters[4] = min(*binPairTotal, pairCap)
+  int *ropPeakChunks;             // k_rop: *ropPeakChunks = max(itself, counters[kCntChunks])
+  int *ropSticky;                 // k_rop: *ropSticky |= counters[2] (overflow flags of the draw)
 };
 
 constexpr int kChunk = 32;         // fragment records per chunk
@@ -505,6 +510,9 @@ static __device__ __forceinline__ float4 textureRGBA8(const DevSampler &s, int f
     frac = lod - fl;
   }
   if (two && !(frac >= 0.f && frac <= 1.f)) return textureRGBA8Packed(s, face, u, v, lod);
+  // At a whole-number LOD (frac == 0) the level mix is trunc(th * 1 + tl * 0), which is th for the
+  // finite, integer-valued channels of RGBA8 texels: the second level is not fetched.
+  two = two && frac != 0.f;
   float4 th, tl;
   if (nearest) {
     th = unpack4(nearestSample(t, face, hi, u, v, s.wrap, s.border));

@@ -203,14 +203,11 @@ __global__ void __launch_bounds__(128) k_clip(const __grid_constant__ DrawParams
 }
 
 // number of primitives after clipping, kept on the device for the count-driven kernels
-__global__ void k_prim_count(const __grid_constant__ DrawParams p) {
-  chainEnter();
-  p.counters[3] = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
-}
-
 __global__ void k_clip_append(const __grid_constant__ DrawParams p) {
   chainEnter();
   int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  // the draw's primitive count: input triangles plus the appended fan triangles
+  if (slot == 0) p.counters[3] = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
   int n = min(p.counters[CNT_POLY], p.clipPolyCap);
   if (slot >= n) return;
   int t = p.clipPolyTri[slot];
@@ -311,6 +308,11 @@ __global__ void __launch_bounds__(256) k_setup(const __grid_constant__ DrawParam
 __global__ void __launch_bounds__(256) k_bin_emit(const __grid_constant__ DrawParams p) {
   chainEnter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  // set-up the sort and the tile ranges would otherwise take launches of their own: empty tile
+  // ranges (k_tile_ranges fills the non-empty ones) and the bin-entry count clamped to the capacity
+  if (p.binZeroRanges)
+    for (int t = i; t < p.views * p.tilesPerView; t += gridDim.x * blockDim.x) p.tileStart[t] = p.tileEnd[t] = 0;
+  if (p.binPairTotal && i == 0) p.counters[4] = min(*p.binPairTotal, p.pairCap);
   int np = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
   if (i >= np || p.tileCount[i] == 0) return;
   const TriSetup &T = p.tri[i];
@@ -535,6 +537,44 @@ __global__ void k_scan_add(int *out, const int *nPtr, int nMax, const int *block
   (void) n;
 }
 
+// Two-launch exclusive scan (reduce, then apply): the apply kernel sums the tile totals before its
+// own tile itself instead of reading them from a third launch's scan. Tiles of kScanTile elements;
+// at most kScanTile tiles, as for the three-launch form.
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int *in, const int *nPtr, int nMax,
+                                                              int *blockSums) {
+  chainEnter();
+  const int n = nPtr ? min(*nPtr, nMax) : nMax;
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  int s = 0;
+  for (int k = 0; k < kScanItems; k++) s += base + k < n ? in[base + k] : 0;
+  int total;
+  blockExclusiveScan(s, &total);
+  if (threadIdx.x == 0) blockSums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int *in, int *out, const int *nPtr, int nMax,
+                                                             const int *blockSums) {
+  chainEnter();
+  const int n = nPtr ? min(*nPtr, nMax) : nMax;
+  int before = 0;
+  for (int j = threadIdx.x; j < (int) blockIdx.x; j += blockDim.x) before += blockSums[j];
+  int prefix;
+  blockExclusiveScan(before, &prefix);
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  int v[kScanItems], s = 0;
+  for (int k = 0; k < kScanItems; k++) {
+    v[k] = base + k < n ? in[base + k] : 0;
+    s += v[k];
+  }
+  int total;
+  int pre = prefix + blockExclusiveScan(s, &total);
+  for (int k = 0; k < kScanItems; k++) {
+    if (base + k < nMax) out[base + k] = pre;
+    pre += v[k];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[nMax] = prefix + total;
+}
+
 // ------------------------------------------------------------------------------------------------
 // clear, mip generation
 // ------------------------------------------------------------------------------------------------
@@ -586,6 +626,12 @@ void scanExclusive(const int *in, int *out, const int *nPtr, int nMax, int *bloc
 }
 
 int scanScratchInts(int nMax) { return max(1, cdiv(nMax, kScanTile)) + 1; }
+
+void scanExclusive2(const int *in, int *out, const int *nPtr, int nMax, int *blockSums, cudaStream_t st) {
+  int nb = max(1, cdiv(nMax, kScanTile));
+  launchChained(k_scan_reduce, dim3(nb), dim3(kScanThreads), 0, st, in, nPtr, nMax, blockSums);
+  launchChained(k_scan_apply, dim3(nb), dim3(kScanThreads), 0, st, in, out, nPtr, nMax, (const int *) blockSums);
+}
 
 // ------------------------------------------------------------------------------------------------
 // points and lines: assembly, clipping and culling into drawing-order slots
@@ -705,7 +751,6 @@ void launchPointsLinesGeometry(const DrawParams &p, const LineParams &lp, cudaSt
 
 void launchClipAppend(const DrawParams &p, cudaStream_t st) {
   launchChained(k_clip_append, dim3(max(1, cdiv(p.clipPolyCap, 256))), dim3(256), 0, st, p);
-  launchChained(k_prim_count, dim3(1), dim3(1), 0, st, p);
 }
 
 void launchSetup(const DrawParams &p, int primCount, cudaStream_t st) {
@@ -721,7 +766,7 @@ int sortScratchInts(int nPairs) { return 256 * max(1, cdiv(nPairs, kSortTile)) +
 // sorts (keyA,valA) by key, result back in (keyA,valA); hist needs sortScratchInts ints plus a
 // scan scratch of scanScratchInts(256 * blocks)
 void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, int *hist, int *histScan,
-               int *scanScratch, cudaStream_t st) {
+               int *scanScratch, cudaStream_t st, bool twoLaunchScan) {
   if (nPairs <= 0) return;
   int nb = cdiv(nPairs, kSortTile);
   uint32_t *kin = p.keyA, *kout = p.keyB;
@@ -730,7 +775,8 @@ void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, in
   for (int pass = 0; pass < passes; pass++) {
     int shift = pass * 8;
     launchChained(k_radix_hist, dim3(nb), dim3(kSortThreads), 0, st, kin, nPtr, shift, hist, nb);
-    scanExclusive(hist, histScan, nullptr, 256 * nb, scanScratch, st);
+    if (twoLaunchScan) scanExclusive2(hist, histScan, nullptr, 256 * nb, scanScratch, st);
+    else scanExclusive(hist, histScan, nullptr, 256 * nb, scanScratch, st);
     launchChained(k_radix_scatter, dim3(nb), dim3(kSortThreads), 0, st, kin, vin, kout, vout, nPtr, shift, histScan, nb);
     uint32_t *tk = kin; kin = kout; kout = tk;
     int *tv = vin; vin = vout; vout = tv;
@@ -749,21 +795,10 @@ void launchTileOrder(const DrawParams &p, int *order, cudaStream_t st) {
   launchChained(k_tile_order, dim3(1), dim3(1024), 0, st, p.tileStart, p.tileEnd, p.views * p.tilesPerView, order);
 }
 
-__global__ void k_clamp_count(const int *src, int cap, int *dst) {
-  chainEnter();
-  *dst = min(*src, cap);
-}
 __global__ void k_accumulate_flags(const int *flags, int *sticky) {
   chainEnter();
   *sticky |= *flags;
 }
-
-void launchClampCount(const int *src, int cap, int *dst, cudaStream_t st) { launchChained(k_clamp_count, dim3(1), dim3(1), 0, st, src, cap, dst); }
-__global__ void k_max_into(const int *src, int *dst) {
-  chainEnter();
-  *dst = max(*dst, *src);
-}
-void launchMaxInto(const int *src, int *dst, cudaStream_t st) { launchChained(k_max_into, dim3(1), dim3(1), 0, st, src, dst); }
 
 void launchAccumulateFlags(const int *flags, int *sticky, cudaStream_t st) {
   launchChained(k_accumulate_flags, dim3(1), dim3(1), 0, st, flags, sticky);

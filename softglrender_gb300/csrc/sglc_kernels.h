@@ -8,6 +8,7 @@
 namespace sglc {
 
 void scanExclusive(const int *in, int *out, const int *nPtr, int nMax, int *blockSums, cudaStream_t st);
+void scanExclusive2(const int *in, int *out, const int *nPtr, int nMax, int *blockSums, cudaStream_t st);
 int scanScratchInts(int nMax);
 void launchVertexAndClip(const DrawParams &p, cudaStream_t st);
 void launchClipAppend(const DrawParams &p, cudaStream_t st);
@@ -15,7 +16,7 @@ void launchSetup(const DrawParams &p, int primCount, cudaStream_t st);
 void launchBinEmit(const DrawParams &p, int primCount, cudaStream_t st);
 int sortScratchInts(int nPairs);
 void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, int *hist, int *histScan,
-               int *scanScratch, cudaStream_t st);
+               int *scanScratch, cudaStream_t st, bool twoLaunchScan = false);
 void launchTileRanges(const DrawParams &p, int nPairs, const int *nPtr, cudaStream_t st);
 void launchTileOrder(const DrawParams &p, int *order, cudaStream_t st);
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);
@@ -25,12 +26,8 @@ bool deferredShadingModel(int shading);
 void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st, cudaEvent_t evCov = nullptr,
                           cudaEvent_t evShade = nullptr);
 void launchFill32(uint32_t *dst, uint32_t value, size_t n, cudaStream_t st);
-// *dst = min(*src, cap) (device-side pair count of a synchronisation-free draw)
-void launchClampCount(const int *src, int cap, int *dst, cudaStream_t st);
 // *sticky |= *flags
 void launchAccumulateFlags(const int *flags, int *sticky, cudaStream_t st);
-// *dst = max(*dst, *src)
-void launchMaxInto(const int *src, int *dst, cudaStream_t st);
 void launchMipLevel(const DevTex &t, int face, int level, int isFloat, cudaStream_t st);
 void launchSwizzleIn(const DevTex &t, int face, int level, const uint32_t *src, cudaStream_t st);
 void launchSwizzleOut(const DevTex &t, int face, int level, uint32_t *dst, cudaStream_t st);

@@ -1020,6 +1020,10 @@ __global__ void __launch_bounds__(256) k_rop(const __grid_constant__ DrawParams 
   __shared__ float4 scol[8][kChunk];
   __shared__ uint32_t smeta[8][kChunk];
   __shared__ uint32_t sown[8][kChunk];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {   // the draw's last kernel: its peak chunk use and flags
+    if (p.ropPeakChunks) *p.ropPeakChunks = max(*p.ropPeakChunks, p.counters[kCntChunks]);
+    if (p.ropSticky) *p.ropSticky |= p.counters[2];
+  }
   const TileJob job = tileJob(p);
   if (job.skip) return;
   const int tile = job.tile;
