@@ -522,6 +522,44 @@ def main():
         r._call("texture_read_image", ct.handle, 0, 0, 1, out.ctypes.data_as(C.c_void_p), out.nbytes)
     e2e_graph_fps = world * args.steps / max_over_ranks(time.perf_counter() - t0, pg, f"cuda:{local}" if pg and torch.cuda.is_available() else None)
 
+    # two frames in flight: a second renderer (its own stream and its own copy of the scene's
+    # resources) driven by a second host thread; both threads run the loop above (upload, eager
+    # frame, blocking read-back), so one renderer's copies overlap the other's kernels. The
+    # library's calls release the interpreter lock while they wait.
+    import threading
+    r2 = sg.RendererCUDA(local)
+    inst2 = S.SceneInstance(r2, scene)
+    tuned2 = autotune(r2, inst2.render, reps=3)
+    lanes = []
+    for rr, ii in ((r, inst), (r2, inst2)):
+        ub = [b for b in ii.draws[0][0][2].blocks.values() if b.name == "UniformsModel"][0]
+        lanes.append((rr, ii, ii.draws[0][0][0], ub, ii.color_tex[0],
+                      torch.empty(W * H * 4, dtype=torch.uint8, pin_memory=True).numpy()))
+
+    def frame_loop(lane, n):
+        rr, ii, vv, ub, cc, oo = lane
+        for _ in range(n):
+            vv.updateVertexData(pinned_v)
+            ub.setData(model_bytes)
+            ii.render()
+            rr._call("texture_read_image", cc.handle, 0, 0, 1, oo.ctypes.data_as(C.c_void_p), oo.nbytes)
+
+    for lane in lanes:
+        frame_loop(lane, 2)
+    half = [args.steps // 2, args.steps - args.steps // 2]
+    barrier(pg)
+    t0 = time.perf_counter()
+    threads = [threading.Thread(target=frame_loop, args=(lanes[i], half[i])) for i in range(2)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    e2e2_fps = world * args.steps / max_over_ranks(time.perf_counter() - t0, pg, f"cuda:{local}" if pg and torch.cuda.is_available() else None)
+    barrier(pg)
+    two_identical = bool(np.array_equal(lanes[0][5], lanes[1][5]) and np.array_equal(lanes[0][5], out))
+    tuned2.destroy()
+    r2.destroy()
+
     result = {
         "metric": METRIC,
         "value": round(fps, 3),
@@ -544,8 +582,12 @@ def main():
         "stage_ms": {"geometry": round(geo_ms, 4), "binning": round(bin_ms, 4), "raster": round(raster_ms, 4),
                      "raster_coverage": round(parts["coverage"], 4), "raster_shading": round(parts["shading"], 4),
                      "raster_rop": round(parts["rop"], 4)},
-        "e2e": {"value": round(e2e_fps, 3), "unit": "frames/s", "h2d_bytes_per_step": int(pinned_v.nbytes + len(model_bytes)),
-                "d2h_bytes_per_step": int(out.nbytes), "submission": "eager, tuned capacities",
+        "e2e": {"value": round(e2e2_fps, 3), "unit": "frames/s", "h2d_bytes_per_step": int(pinned_v.nbytes + len(model_bytes)),
+                "d2h_bytes_per_step": int(out.nbytes),
+                "submission": "eager, tuned capacities; two renderers on two host threads (two frames in flight), "
+                              "each frame: vertex array + model uniforms uploaded, frame, resolved image read back",
+                "images_identical": two_identical,
+                "one_frame_in_flight_value": round(e2e_fps, 3),
                 "graph_replay_value": round(e2e_graph_fps, 3)},
         "gpu_launches": launches_per_frame * args.steps,
         "roofline": {"bound": "hbm", "kernel": "k_raster_cov<4,depth>", "achieved": round(achieved, 1),
