@@ -257,6 +257,75 @@ def bench_batched_views(r, stream, with_cpu: bool):
     return out
 
 
+def bench_uneven_lanes(r, cfg, u, per_scene, net, lanes: int = 4):
+    """The uneven batch over `lanes` renderers whose submissions run concurrently (scenes
+    assigned longest first by their measured single-scene times); the batch time runs from an
+    event every lane's stream waits on to the last lane's end. Plain shaders, then the neural
+    shader (the trained network copied to every lane) when it is bound."""
+    import torch
+    import softglrender_gb300 as sg
+    from softglrender_gb300.neural import NeuralShader
+    from softglrender_gb300.uneven import UnevenLanes
+    dev = torch.cuda.current_device()
+    rs = [sg.RendererCUDA(dev) for _ in range(lanes)]
+    ul = UnevenLanes(rs, cfg, per_scene)
+    streams = [torch.cuda.ExternalStream(x.stream(), device=dev) for x in rs]
+
+    def batch_ms(n):
+        ms = []
+        for _ in range(n):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(streams[0])
+            for st in streams[1:]:
+                st.wait_event(e0)
+            ul.launch()
+            for st in streams[1:]:
+                e = torch.cuda.Event()
+                e.record(st)
+                streams[0].wait_event(e)
+            e1.record(streams[0])
+            ul.wait()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.median(ms))
+
+    ul.tune(reps=3)
+    ul.launch()
+    ul.wait()
+    plain_ms = batch_ms(5)
+    # spot check: the lanes' images equal the single renderer's (every 8th scene)
+    same = True
+    r.setCapacity(None)
+    u.render()
+    r.waitIdle()
+    for s in range(0, cfg.scenes, 8):
+        a, b = ul.outputs(s), u.outputs(s)
+        same &= all(np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)) for k in a)
+    res = {"lanes": lanes, "scenes_per_lane": [len(g) for g in ul.groups],
+           "plain_ms_per_batch": round(plain_ms, 3), "plain_scenes_per_s": round(cfg.scenes / (plain_ms / 1e3), 1),
+           "images_equal_single_renderer": bool(same)}
+    nets = []
+    if net is not None:
+        params = net.get_params()
+        for x, b in zip(rs, ul.batches):
+            nn = NeuralShader(x)
+            nn.set_params(params)
+            for prog in b.pbr_programs():
+                nn.bind(prog)
+            nets.append(nn)
+        ul.tune(reps=3)
+        ul.launch()
+        ul.wait()
+        n_ms = batch_ms(5)
+        res.update({"neural_ms_per_batch": round(n_ms, 3), "neural_scenes_per_s": round(cfg.scenes / (n_ms / 1e3), 1)})
+    ul.release()
+    for nn in nets:
+        nn.destroy()
+    for x in rs:
+        x.destroy()
+    return res
+
+
 def bench_uneven(r, stream, net, neural_bound: bool, with_cpu: bool):
     """64 independent scenes in one CUDA-graph submission (plain shaders, and with the neural IBL
     shader bound to the PBR scenes when it met its threshold); per-scene frames/s from eager
@@ -309,6 +378,7 @@ def bench_uneven(r, stream, net, neural_bound: bool, with_cpu: bool):
     out["per_scene_fps"] = [round(1e3 / m, 1) for m in per_scene]
     out["per_scene"] = [{"tris": u.triangles[s], "res": u.plan[s]["res"], "pbr_msaa4": bool(u.plan[s]["pbr"]),
                          "ms": round(per_scene[s], 4)} for s in range(cfg.scenes)]
+    out["lanes"] = bench_uneven_lanes(r, cfg, u, per_scene, net if neural_bound else None)
     if with_cpu:
         import oracle
         from softglrender_gb300 import api as A

@@ -304,7 +304,9 @@ typedef struct sglc_graph sglc_graph;
  * of attachments and other synchronising calls are not allowed inside a capture. */
 SGLC_API sglc_status sglc_graph_begin(sglc_context *ctx);
 SGLC_API sglc_status sglc_graph_end(sglc_context *ctx, sglc_graph **out);
-/* Enqueue one replay of the graph on its context's stream. */
+/* Enqueue one replay of the graph on its context's stream. Refused (SGLC_ERR_INVALID_VALUE) once the
+ * context has freed or grown any buffer or resource since the capture; other contexts' frees do
+ * not affect it, so graphs of several contexts can be captured and replayed concurrently. */
 SGLC_API sglc_status sglc_graph_launch(sglc_graph *graph);
 SGLC_API sglc_status sglc_graph_destroy(sglc_graph *graph);
 

@@ -127,22 +127,29 @@ struct Object {
   std::map<int, int> resBlocks, resSamplers;
 };
 
-// Process-wide count of device frees by the renderer: a CUDA graph records device addresses, so a
-// graph captured before any buffer it uses was freed (a working array grown, a resource
-// released) must not be replayed; sglc_graph_launch compares this count with the capture's.
+// Counts of device frees: a CUDA graph records device addresses, so a graph captured before any
+// buffer it uses was freed (a working array grown, a resource released) must not be replayed;
+// sglc_graph_launch compares the counts with the capture's. Each context counts the frees of its
+// own buffers and resources (a graph uses only its context's), so renderers that grow or release
+// memory do not invalidate other renderers' graphs; g_freeEpoch counts frees owned by no context.
 std::atomic<unsigned long long> g_freeEpoch{0};
 
 // grow-only device buffer
 struct DevBuf {
   void *ptr = nullptr;
   size_t bytes = 0;
+  std::atomic<unsigned long long> *epoch = nullptr;   // the owning context's free count
   static thread_local bool capturing;   // a graph capture is in progress on this thread
+  void countFree() {
+    if (epoch) (*epoch)++;
+    else g_freeEpoch++;
+  }
   cudaError_t ensure(size_t need) {
     if (need <= bytes) return cudaSuccess;
     if (capturing) return cudaErrorStreamCaptureUnsupported;   // run the sequence once before capturing
     if (ptr) {
       cudaFree(ptr);
-      g_freeEpoch++;
+      countFree();
     }
     ptr = nullptr;
     bytes = 0;
@@ -155,7 +162,7 @@ struct DevBuf {
   void release() {
     if (ptr) {
       cudaFree(ptr);
-      g_freeEpoch++;
+      countFree();
     }
     ptr = nullptr;
     bytes = 0;
@@ -209,7 +216,19 @@ struct Ctx {
   sglc_capacity peak{};              // largest counts of exactly sized draws since the last query
   DevBuf sticky;                     // overflow flags accumulated over draws
   bool capturing = false;
-  unsigned long long captureEpoch = 0;
+  unsigned long long captureEpoch = 0, captureCtxEpoch = 0;
+  std::atomic<unsigned long long> freeEpoch{0};   // frees of this context's buffers and resources
+  // every working array of the context
+  template<typename F>
+  void forEachBuf(F f) {
+    DevBuf *bufs[] = {&vClip, &vFrag, &vMask, &vVary, &vAttrExtra, &prims, &clipExtra, &clipAppendOff, &clipPoly,
+                      &clipPolyTri, &counters, &tri, &tileCount, &pairOff, &keyA, &keyB, &valA, &valB, &tileStart,
+                      &tileEnd, &tileOrder, &scanScratch, &sortHist, &sortHistScan, &staging, &batchU, &batchTargets,
+                      &sticky, &lpSlot, &lpOrigin, &lpStampCount, &lpStampOff, &lpStampGeo, &lpStampRow,
+                      &lpStampColor, &lpStampVary, &lpFragCount, &lpFragOff, &lpMisc, &recA, &recB, &recColor,
+                      &chunkNext, &chunkFill, &warpHead, &recDense, &peakChunks};
+    for (DevBuf *b : bufs) f(*b);
+  }
   std::vector<void *> captureHostBufs;   // pinned host sources of memcpy nodes in the capture
   // neural IBL shader: training-record capture target
   float *capRecords = nullptr;
@@ -309,8 +328,8 @@ sglc_status allocTexture(Ctx *c, TexObj &t) {
   return SGLC_OK;
 }
 
-void freeTexture(TexObj &t) {
-  if (t.dev || t.resolved) g_freeEpoch++;
+void freeTexture(TexObj &t, std::atomic<unsigned long long> &epoch) {
+  if (t.dev || t.resolved) epoch++;
   if (t.dev) cudaFree(t.dev);
   if (t.resolved) cudaFree(t.resolved);
   t.dev = nullptr;
@@ -980,6 +999,7 @@ void ctxSetCapture(sglc_context *ctx, float *records, unsigned long long *count,
 }
 void ctxDetachNeural(sglc_context *ctx, const sglc_neural *net) {
   Ctx *c = reinterpret_cast<Ctx *>(ctx);
+  c->freeEpoch++;   // the network's buffers are about to be freed: graphs that read them are stale
   for (auto &kv : c->objects)
     if (kv.second.kind == K_PROG && kv.second.prog.neural == net) kv.second.prog.neural = nullptr;
   c->capRecords = nullptr;
@@ -1002,6 +1022,7 @@ sglc_status sglc_create(sglc_context **out, int32_t device) {
   if (cudaSetDevice(device) != cudaSuccess) return SGLC_ERR_DEVICE;
   Ctx *c = new Ctx();
   c->device = device;
+  c->forEachBuf([c](DevBuf &b) { b.epoch = &c->freeEpoch; });
   bool ok = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) == cudaSuccess &&
             cudaMallocHost(&c->hostCounters, 64) == cudaSuccess &&
             cudaMalloc(&c->fragCounter, sizeof(unsigned long long)) == cudaSuccess;
@@ -1020,21 +1041,13 @@ sglc_status sglc_destroy(sglc_context *ctx) {
   cudaStreamSynchronize(c->stream);
   for (auto &kv : c->objects) {
     Object &o = kv.second;
-    if (o.kind == K_TEX) freeTexture(o.tex);
+    if (o.kind == K_TEX) freeTexture(o.tex, c->freeEpoch);
     if (o.kind == K_VAO) {
       cudaFree(o.vao.attr);
       cudaFree(o.vao.idx);
     }
   }
-  DevBuf *bufs[] = {&c->vClip, &c->vFrag, &c->vMask, &c->vVary, &c->vAttrExtra, &c->prims, &c->clipExtra,
-                    &c->clipAppendOff, &c->clipPoly, &c->clipPolyTri, &c->counters, &c->tri, &c->tileCount,
-                    &c->pairOff, &c->keyA, &c->keyB, &c->valA, &c->valB, &c->tileStart, &c->tileEnd, &c->tileOrder,
-                    &c->scanScratch, &c->sortHist, &c->sortHistScan, &c->staging, &c->batchU, &c->batchTargets,
-                    &c->sticky, &c->lpSlot, &c->lpOrigin, &c->lpStampCount, &c->lpStampOff, &c->lpStampGeo,
-                    &c->lpStampRow, &c->lpStampColor, &c->lpStampVary, &c->lpFragCount, &c->lpFragOff, &c->lpMisc,
-                    &c->recA, &c->recB, &c->recColor, &c->chunkNext, &c->chunkFill, &c->warpHead, &c->recDense,
-                    &c->peakChunks};
-  for (DevBuf *b : bufs) b->release();
+  c->forEachBuf([](DevBuf &b) { b.release(); });
   cudaFreeHost(c->hostCounters);
   for (void *h : c->captureHostBufs) cudaFreeHost(h);
   cudaFree(c->fragCounter);
@@ -1055,11 +1068,11 @@ sglc_status sglc_release(sglc_context *ctx, sglc_handle h) {
   auto it = c->objects.find(h);
   if (it == c->objects.end()) return c->fail(SGLC_ERR_INVALID_HANDLE, "release: unknown handle");
   CK(cudaStreamSynchronize(c->stream));
-  if (it->second.kind == K_TEX) freeTexture(it->second.tex);
+  if (it->second.kind == K_TEX) freeTexture(it->second.tex, c->freeEpoch);
   if (it->second.kind == K_VAO) {
     cudaFree(it->second.vao.attr);
     cudaFree(it->second.vao.idx);
-    g_freeEpoch++;
+    c->freeEpoch++;
   }
   c->objects.erase(it);
   return SGLC_OK;
@@ -1722,7 +1735,8 @@ sglc_status sglc_set_tile_size(sglc_context *ctx, int32_t tile) {
 // ------------------------------------------------------------------------------------------------
 struct sglc_graph {
   sglc_context *ctx = nullptr;
-  unsigned long long epoch = 0;   // g_freeEpoch when the capture began
+  unsigned long long epoch = 0;      // g_freeEpoch when the capture began
+  unsigned long long ctxEpoch = 0;   // the context's free count when the capture began
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<void *> hostBufs;
@@ -1738,6 +1752,7 @@ sglc_status sglc_graph_begin(sglc_context *ctx) {
   if (st) return st;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
   c->captureEpoch = g_freeEpoch.load();
+  c->captureCtxEpoch = c->freeEpoch.load();
   c->capturing = true;
   DevBuf::capturing = true;
   return SGLC_OK;
@@ -1771,6 +1786,7 @@ sglc_status sglc_graph_end(sglc_context *ctx, sglc_graph **out) {
   sglc_graph *gr = new sglc_graph();
   gr->ctx = ctx;
   gr->epoch = c->captureEpoch;
+  gr->ctxEpoch = c->captureCtxEpoch;
   gr->graph = g;
   gr->exec = exec;
   gr->hostBufs.swap(bufs);
@@ -1781,7 +1797,7 @@ sglc_status sglc_graph_end(sglc_context *ctx, sglc_graph **out) {
 sglc_status sglc_graph_launch(sglc_graph *g) {
   if (!g || !g->exec) return SGLC_ERR_INVALID_VALUE;
   Ctx *c = reinterpret_cast<Ctx *>(g->ctx);
-  if (g_freeEpoch.load() != g->epoch)
+  if (g_freeEpoch.load() != g->epoch || c->freeEpoch.load() != g->ctxEpoch)
     return c->fail(SGLC_ERR_INVALID_VALUE, "graph_launch: a buffer the graph uses was freed or grown since the capture; "
                                            "capture it again");
   CK(cudaGraphLaunch(g->exec, c->stream));

@@ -7,14 +7,16 @@ IBL maps of the 1080p PBR scene, shared by all PBR scenes), optionally with the 
 bound when it met its PSNR threshold (per material; otherwise the plain shader stays: the
 fallback). `render()` issues the scenes one render pass each; on the GPU the whole sequence is
 captured once in a CUDA graph (softglrender_gb300/graph.py) and replayed with one launch, each
-scene's kernels running in order inside it. Meshes with the same tessellation share their
+scene's kernels running in order inside it. `UnevenLanes` splits the scenes over several renderers
+whose submissions run concurrently. Meshes with the same tessellation share their
 displacement seed (the tessellation is rounded to a multiple of 16 longitude segments), which keeps
 the set-up time of 64 scenes of up to 2M triangles within seconds.
 """
 from __future__ import annotations
 
 from dataclasses import dataclass
-from typing import Dict, List, Optional, Tuple
+from functools import lru_cache
+from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -33,6 +35,28 @@ class UnevenConfig:
     prefilter: int = 512
     irradiance: int = 32
     blinn_tex: int = 512
+
+
+# host-side scene assets, generated once per process and shared by every batch built from them
+# (several renderers of one batch upload the same arrays; the arrays are never written)
+@lru_cache(maxsize=None)
+def _noise_texture(size: int, seed: int, kind: str) -> np.ndarray:
+    return S.noise_texture(size, seed, kind)
+
+
+@lru_cache(maxsize=None)
+def _ibl_maps(seed: int, prefilter: int, irradiance: int):
+    return S.ibl_maps(seed, prefilter, irradiance)
+
+
+@lru_cache(maxsize=None)
+def _checkerboard(size: int, seed: int) -> np.ndarray:
+    return S.checkerboard(size, 8, seed)
+
+
+@lru_cache(maxsize=None)
+def _sphere(lon: int, lat: int, seed: int):
+    return S.uv_sphere(lon, lat, 1.0, displace_seed=seed, amplitude=0.1)
 
 
 def scene_plan(cfg: UnevenConfig) -> List[Dict[str, int]]:
@@ -68,11 +92,11 @@ class UnevenBatch:
                                           ("u_metalRoughnessMap", "metal_rough"))):
             t = r.createTexture(tdesc)
             t.setSamplerDesc(trilinear)
-            t.setImageData([S.noise_texture(cfg.pbr_tex, 3000 + 10 * (k + 1), kind)])
+            t.setImageData([_noise_texture(cfg.pbr_tex, 3000 + 10 * (k + 1), kind)])
             us = r.createUniformSampler(name, tdesc)
             us.setTexture(t)
             pbr_samplers.append(us)
-        pre, irr = S.ibl_maps(3000, cfg.prefilter, cfg.irradiance)
+        pre, irr = _ibl_maps(3000, cfg.prefilter, cfg.irradiance)
         cdesc = A.TextureDesc(cfg.irradiance, cfg.irradiance, A.TextureType_CUBE, A.TextureFormat_RGBA8,
                               A.TextureUsage_Sampler | A.TextureUsage_UploadData, False, False)
         t = r.createTexture(cdesc)
@@ -98,7 +122,7 @@ class UnevenBatch:
                               A.TextureUsage_Sampler | A.TextureUsage_UploadData, True, False)
         bt = r.createTexture(bdesc)
         bt.setSamplerDesc(trilinear)
-        bt.setImageData([S.checkerboard(cfg.blinn_tex, 8, cfg.seed)])
+        bt.setImageData([_checkerboard(cfg.blinn_tex, cfg.seed)])
         blinn_sampler = r.createUniformSampler("u_albedoMap", bdesc)
         blinn_sampler.setTexture(bt)
         self.states = r.createPipelineStates(A.RenderStates(depthTest=True, depthMask=True,
@@ -110,7 +134,7 @@ class UnevenBatch:
                 continue
             key = pl["lon"]
             if key not in meshes:
-                vert, idx = S.uv_sphere(pl["lon"], pl["lat"], 1.0, displace_seed=cfg.seed + key, amplitude=0.1)
+                vert, idx = _sphere(pl["lon"], pl["lat"], cfg.seed + key)
                 meshes[key] = (r.createVertexArrayObject(vert, 64, idx), len(idx) // 3)
             vao, ntri = meshes[key]
             self.triangles.append(ntri)
@@ -178,3 +202,59 @@ class UnevenBatch:
         if it["pbr"]:
             out["resolved"] = it["color"].readImage(resolved=True)
         return out
+
+
+def assign_lanes(cost: Sequence[float], lanes: int) -> List[List[int]]:
+    """Scenes to `lanes` groups: longest first, each to the group with the least cost so far."""
+    groups: List[List[int]] = [[] for _ in range(lanes)]
+    load = [0.0] * lanes
+    for s in sorted(range(len(cost)), key=lambda i: (-cost[i], i)):
+        k = min(range(lanes), key=lambda j: (load[j], j))
+        groups[k].append(s)
+        load[k] += cost[s]
+    return [sorted(g) for g in groups]
+
+
+class UnevenLanes:
+    """The uneven batch over several renderers ("lanes"): each lane has its own stream, working
+    memory and copy of the shared materials, and renders its share of the scenes as one
+    submission (CUDA graph or eager, picked by the autotuner). The lanes' submissions are
+    independent, so the GPU runs them concurrently: scenes too small to fill the GPU (a 128^2
+    target has 64 raster tiles for 152 SMs) overlap instead of running one after another.
+    Every scene's images equal the single-renderer batch's (a scene is drawn the same way on any
+    renderer)."""
+
+    def __init__(self, renderers: Sequence[A.Renderer], cfg: UnevenConfig, cost: Sequence[float]):
+        self.renderers = list(renderers)
+        self.cfg = cfg
+        self.groups = assign_lanes(cost, len(self.renderers))
+        self.batches = [UnevenBatch(r, cfg, only=g) for r, g in zip(self.renderers, self.groups)]
+        self.tuned = []
+
+    def tune(self, reps: int = 3) -> None:
+        """Capacities, tile order and graph-or-eager per lane (softglrender_gb300/autotune.py)."""
+        from .autotune import autotune
+        self.release()
+        for r, b in zip(self.renderers, self.batches):
+            r.setCapacity(None)
+            self.tuned.append(autotune(r, b.render, reps=reps))
+
+    def launch(self) -> None:
+        """Enqueue every lane's submission (each on its own renderer's stream)."""
+        for t in self.tuned:
+            t.run()
+
+    def wait(self) -> None:
+        for r in self.renderers:
+            r.waitIdle()
+
+    def lane_of(self, s: int) -> int:
+        return next(k for k, g in enumerate(self.groups) if s in g)
+
+    def outputs(self, s: int):
+        return self.batches[self.lane_of(s)].outputs(s)
+
+    def release(self) -> None:
+        for t in self.tuned:
+            t.destroy()
+        self.tuned = []

@@ -87,3 +87,32 @@ def test_autotune_picks_a_fitting_configuration(batch):
     t.run()
     _same(_outs(b), exact)
     t.destroy()
+
+
+def test_graph_is_invalidated_by_its_own_renderer_only(batch, cuda_lib):
+    """Frees in another renderer (working arrays grown, resources released) leave a graph
+    replayable; releasing a resource of the graph's own renderer makes it refuse to replay."""
+    b = batch
+    b.render()
+    exact = _outs(b)
+    b.r.setCapacity(A.Capacity(1 << 16, 1 << 14, 1 << 14, 1 << 20, 1))
+    b.render()
+    g = Graph(b.r).capture(b.render)
+    other = A.Renderer(cuda_lib, 0)
+    ob = BatchedViews(other, BatchConfig(views=3, size=160, shadow=512, lon=64, lat=32, tex=64, seed=4300))
+    ob.render()                                    # grows the other renderer's working arrays
+    spare = other.createTexture(A.TextureDesc(64, 64, A.TextureType_2D, A.TextureFormat_RGBA8,
+                                              A.TextureUsage_Sampler, False, False))
+    spare.initImageData()
+    other.release(spare)
+    other.waitIdle()
+    g.launch()
+    _same(_outs(b), exact)
+    own = b.r.createTexture(A.TextureDesc(64, 64, A.TextureType_2D, A.TextureFormat_RGBA8,
+                                          A.TextureUsage_Sampler, False, False))
+    own.initImageData()
+    b.r.release(own)
+    with pytest.raises(A.SoftGLError):
+        g.launch()
+    g.destroy()
+    other.destroy()

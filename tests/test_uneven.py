@@ -1,12 +1,13 @@
 """Uneven batch (scenes of different size, resolution, shading and sample count in one
-submission): every scene matches the CPU oracle, and the CUDA-graph replay of the whole batch
-matches its eager submission."""
+submission): every scene matches the CPU oracle, the CUDA-graph replay of the whole batch
+matches its eager submission, and the batch split over concurrent renderers (lanes) gives the
+same images."""
 import numpy as np
 import pytest
 
 from softglrender_gb300 import api as A
 from softglrender_gb300.autotune import autotune
-from softglrender_gb300.uneven import UnevenBatch, UnevenConfig, scene_plan
+from softglrender_gb300.uneven import UnevenBatch, UnevenConfig, UnevenLanes, assign_lanes, scene_plan
 
 from helpers import assert_outputs_match
 
@@ -58,4 +59,38 @@ def test_uneven_graph_replay_matches_eager(cuda_lib):
         for k in eager[s]:
             assert np.array_equal(o[k].view(np.uint8), eager[s][k].view(np.uint8)), (s, k)
     t.destroy()
+    r.destroy()
+
+
+def test_assign_lanes_covers_and_balances():
+    cost = [float(c) for c in (50, 1, 1, 1, 20, 20, 5, 3, 2, 30)]
+    groups = assign_lanes(cost, 3)
+    assert sorted(sum(groups, [])) == list(range(len(cost)))
+    loads = [sum(cost[s] for s in g) for g in groups]
+    assert max(loads) == 50.0 and min(loads) >= 30.0   # the longest scene alone; the rest spread
+    assert assign_lanes(cost, 3) == groups               # deterministic
+    assert assign_lanes(cost, 1) == [list(range(len(cost)))]
+
+
+@pytest.mark.gpu
+def test_uneven_lanes_match_single_renderer(cuda_lib):
+    r = A.Renderer(cuda_lib, 0)
+    u = UnevenBatch(r, SMALL)
+    u.render()
+    r.waitIdle()
+    single = [u.outputs(s) for s in range(SMALL.scenes)]
+    rs = [A.Renderer(cuda_lib, 0) for _ in range(3)]
+    ul = UnevenLanes(rs, SMALL, [float(t) for t in u.triangles])
+    assert sorted(sum(ul.groups, [])) == list(range(SMALL.scenes))
+    ul.tune(reps=2)
+    for _ in range(2):   # two submissions in a row
+        ul.launch()
+        ul.wait()
+        for s in range(SMALL.scenes):
+            o = ul.outputs(s)
+            for k in single[s]:
+                assert np.array_equal(o[k].view(np.uint8), single[s][k].view(np.uint8)), (s, k)
+    ul.release()
+    for x in rs:
+        x.destroy()
     r.destroy()
