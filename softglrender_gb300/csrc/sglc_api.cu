@@ -815,7 +815,10 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     CK(c->clipAppendOff.ensure(sizeof(int) * (size_t) (p.ntri + 1)));
     CK(c->clipPoly.ensure(sizeof(int4) * 3 * (size_t) polyCap));
     CK(c->clipPolyTri.ensure(sizeof(int) * (size_t) polyCap));
-    CK(c->counters.ensure(sizeof(int) * 16));
+    // 16 counters, then the per-scan-tile totals k_clip and k_setup add up for the two scans
+    const int clipTiles = scanTiles(std::max(p.ntri, 1)), primTiles = scanTiles(p.primCap);
+    const size_t counterInts = 16 + (size_t) clipTiles + (size_t) primTiles;
+    CK(c->counters.ensure(sizeof(int) * counterInts));
     CK(c->tri.ensure(sizeof(TriSetup) * (size_t) p.primCap));
     CK(c->tileCount.ensure(sizeof(int) * (size_t) p.primCap));
     CK(c->pairOff.ensure(sizeof(int) * (size_t) (p.primCap + 1)));
@@ -831,17 +834,19 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     p.clipPoly = c->clipPoly.as<int4>();
     p.clipPolyTri = c->clipPolyTri.as<int>();
     p.counters = c->counters.as<int>();
+    p.clipScanSums = p.counters + 16;
+    p.tileScanSums = p.counters + 16 + clipTiles;
     p.tri = c->tri.as<TriSetup>();
     p.tileCount = c->tileCount.as<int>();
     p.pairOff = c->pairOff.as<int>();
 
-    CK(cudaMemsetAsync(p.counters, 0, sizeof(int) * 16, c->stream));
+    CK(cudaMemsetAsync(p.counters, 0, sizeof(int) * counterInts, c->stream));
     if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[0], c->stream));
     launchVertexAndClip(p, c->stream);
-    scanExclusive2(p.clipExtra, p.clipAppendOff, nullptr, std::max(p.ntri, 1), c->scanScratch.as<int>(), c->stream);
+    scanApply(p.clipExtra, p.clipAppendOff, nullptr, std::max(p.ntri, 1), p.clipScanSums, c->stream);
     launchClipAppend(p, c->stream);
     launchSetup(p, p.primCap, c->stream);
-    scanExclusive2(p.tileCount, p.pairOff, p.counters + 3, p.primCap, c->scanScratch.as<int>(), c->stream);
+    scanApply(p.tileCount, p.pairOff, p.counters + 3, p.primCap, p.tileScanSums, c->stream);
     CK(cudaGetLastError());
     if (c->statsLevel >= 1) CK(cudaEventRecord(c->ev[1], c->stream));
     int newVerts = -1, polys = -1, np = p.primCap, nPairs;
@@ -970,12 +975,12 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     c->stats.clip_vertices = newVerts;
     c->stats.primitives = deferred ? -1 : np;
     c->stats.bin_entries = deferred ? -1 : nPairs;
-    // vertex, clip, 2 scan, append, setup, 2 scan | emit, sort (hist, 2 scan, scatter per pass),
-    // ranges, order, raster (deferred shading: coverage, shade, ROP); flag accumulation when the
-    // draw has capacities and no ROP kernel; a redone attempt ran the 8 geometry launches before
+    // vertex, clip, scan, append, setup, scan | emit, sort (hist, 2 scan, scatter per pass), ranges,
+    // order, raster (deferred shading: coverage, shade, ROP); flag accumulation when the draw has
+    // capacities and no ROP kernel; a redone attempt ran the 6 geometry launches before
     int sortPasses = nPairs > 0 ? (keyBits + 7) / 8 : 0;
-    c->stats.kernel_launches = (p.nv > 0) + (p.ntri > 0) + 2 + 1 + 1 + 2 + (np > 0) + sortPasses * 4 +
-                               (nPairs > 0) + (heavyFirst ? 1 : 0) + 1 + attempt * 8 +
+    c->stats.kernel_launches = (p.nv > 0) + (p.ntri > 0) + 1 + 1 + 1 + 1 + (np > 0) + sortPasses * 4 +
+                               (nPairs > 0) + (heavyFirst ? 1 : 0) + 1 + attempt * 6 +
                                (deferred && !deferShade ? 1 : 0) + (deferShade ? 2 : 0);
     return SGLC_OK;
   }

@@ -214,6 +214,8 @@ struct DrawParams {
   const int *binPairTotal;        // k_bin_emit sets counters[4] = min(*binPairTotal, pairCap)
   int *ropPeakChunks;             // k_rop: *ropPeakChunks = max(itself, counters[kCntChunks])
   int *ropSticky;                 // k_rop: *ropSticky |= counters[2] (overflow flags of the draw)
+  int *clipScanSums;              // k_clip adds each scan tile's clipExtra total here (zeroed)
+  int *tileScanSums;              // k_setup adds each scan tile's tileCount total here (zeroed)
 };
 
 constexpr int kChunk = 32;         // fragment records per chunk

@@ -108,6 +108,11 @@ __device__ int newClipVertex(const DrawParams &p, int view, int i0, int i1, floa
   return idx;
 }
 
+// exclusive scans: tiles of kScanTile elements, kScanThreads threads per tile
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
 template<int SH>
 __global__ void __launch_bounds__(128) k_clip(const __grid_constant__ DrawParams p) {
   chainEnter();
@@ -199,6 +204,8 @@ __global__ void __launch_bounds__(128) k_clip(const __grid_constant__ DrawParams
     dst[2] = make_int4(nin > 7 ? in[7] : 0, nin > 8 ? in[8] : 0, nin > 9 ? in[9] : 0, nin > 10 ? in[10] : 0);
     p.clipPolyTri[slot] = t;
     p.clipExtra[t] = nin - 3;
+    // the reduce step of the scan of clipExtra (scan tile totals); clipped triangles are few
+    if (p.clipScanSums && nin > 3) atomicAdd(&p.clipScanSums[t / kScanTile], nin - 3);
   }
 }
 
@@ -300,6 +307,11 @@ __global__ void __launch_bounds__(256) k_setup(const __grid_constant__ DrawParam
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int np = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
   unsigned long long bound = i < np ? setupPrim(p, i) : 0ull;
+  if (p.tileScanSums) {   // the reduce step of the scan of tileCount: a warp's primitives share a scan tile
+    int cnt = i < np ? p.tileCount[i] : 0;
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&p.tileScanSums[i / kScanTile], cnt);
+  }
   for (int o = 16; o > 0; o >>= 1) bound += __shfl_down_sync(0xffffffffu, bound, o);
   if ((threadIdx.x & 31) == 0 && bound)
     atomicAdd(reinterpret_cast<unsigned long long *>(p.counters + kCntBound), bound);
@@ -415,23 +427,36 @@ __global__ void k_tile_ranges(const uint32_t *keys, const int *nPtr, int *tileSt
   if (i == n - 1 || keys[i + 1] != k) tileEnd[k] = i + 1;
 }
 
+// bucket of tile t in the heavy-first order: log2 of its list length (0: empty), 33: no tile
+__device__ __forceinline__ int orderBucket(const int *tileStart, const int *tileEnd, int numTiles, int t) {
+  if (t >= numTiles) return 33;
+  const int len = tileEnd[t] - tileStart[t];
+  return len > 0 ? 32 - __clz(len) : 0;
+}
+
 // Raster CTA order: tiles bucketed by log2 of their list length, longest first, so the tiles that
 // take longest start first and do not form the tail of the launch. One CTA; order within a bucket
 // is arbitrary (tiles are independent). Most tiles of a frame fall in a few buckets (the empty one
-// above all), so each warp adds its lanes of one bucket with one shared-memory atomic.
+// above all), so each warp adds its lanes of one bucket with one shared-memory atomic; each thread
+// issues the loads of K tiles before it uses them.
 __global__ void __launch_bounds__(1024) k_tile_order(const int *tileStart, const int *tileEnd, int numTiles,
                                                      int *order) {
   chainEnter();
+  constexpr int K = 8;   // tiles per thread and sweep, their loads issued together
   __shared__ int cnt[33], off[33];
   const int lane = threadIdx.x & 31;
   if (threadIdx.x < 33) cnt[threadIdx.x] = 0;
   __syncthreads();
-  const int span = (numTiles + blockDim.x - 1) / blockDim.x * blockDim.x;   // whole warps every round
-  for (int t = threadIdx.x; t < span; t += blockDim.x) {
-    const int len = t < numTiles ? tileEnd[t] - tileStart[t] : 0;
-    const int b = t < numTiles ? (len > 0 ? 32 - __clz(len) : 0) : 33;
-    const unsigned peers = __match_any_sync(0xffffffffu, b);
-    if (b < 33 && lane == __ffs(peers) - 1) atomicAdd(&cnt[b], __popc(peers));
+  const int sweep = K * blockDim.x;
+  for (int base = 0; base < numTiles; base += sweep) {   // uniform bounds: whole warps every round
+    int b[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) b[k] = orderBucket(tileStart, tileEnd, numTiles, base + k * blockDim.x + threadIdx.x);
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const unsigned peers = __match_any_sync(0xffffffffu, b[k]);
+      if (b[k] < 33 && lane == __ffs(peers) - 1) atomicAdd(&cnt[b[k]], __popc(peers));
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -442,24 +467,26 @@ __global__ void __launch_bounds__(1024) k_tile_order(const int *tileStart, const
     }
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < span; t += blockDim.x) {
-    const int len = t < numTiles ? tileEnd[t] - tileStart[t] : 0;
-    const int b = t < numTiles ? (len > 0 ? 32 - __clz(len) : 0) : 33;
-    const unsigned peers = __match_any_sync(0xffffffffu, b);
-    const int leader = __ffs(peers) - 1;
-    int base = 0;
-    if (b < 33 && lane == leader) base = atomicAdd(&off[b], __popc(peers));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (b < 33) order[base + __popc(peers & ((1u << lane) - 1u))] = t;
+  for (int base = 0; base < numTiles; base += sweep) {
+    int b[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) b[k] = orderBucket(tileStart, tileEnd, numTiles, base + k * blockDim.x + threadIdx.x);
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const int t = base + k * blockDim.x + threadIdx.x;
+      const unsigned peers = __match_any_sync(0xffffffffu, b[k]);
+      const int leader = __ffs(peers) - 1;
+      int first = 0;
+      if (b[k] < 33 && lane == leader) first = atomicAdd(&off[b[k]], __popc(peers));
+      first = __shfl_sync(0xffffffffu, first, leader);
+      if (b[k] < 33) order[first + __popc(peers & ((1u << lane) - 1u))] = t;
+    }
   }
 }
 
 // ------------------------------------------------------------------------------------------------
 // exclusive scan (three phases), counts read from device memory
 // ------------------------------------------------------------------------------------------------
-constexpr int kScanThreads = 1024;
-constexpr int kScanItems = 4;
-constexpr int kScanTile = kScanThreads * kScanItems;
 
 __device__ __forceinline__ int blockExclusiveScan(int v, int *total) {
   __shared__ int warpSums[32];
@@ -626,6 +653,13 @@ void scanExclusive(const int *in, int *out, const int *nPtr, int nMax, int *bloc
 }
 
 int scanScratchInts(int nMax) { return max(1, cdiv(nMax, kScanTile)) + 1; }
+
+void scanApply(const int *in, int *out, const int *nPtr, int nMax, const int *blockSums, cudaStream_t st) {
+  int nb = max(1, cdiv(nMax, kScanTile));
+  launchChained(k_scan_apply, dim3(nb), dim3(kScanThreads), 0, st, in, out, nPtr, nMax, blockSums);
+}
+
+int scanTiles(int nMax) { return max(1, cdiv(nMax, kScanTile)); }
 
 void scanExclusive2(const int *in, int *out, const int *nPtr, int nMax, int *blockSums, cudaStream_t st) {
   int nb = max(1, cdiv(nMax, kScanTile));

@@ -9,6 +9,10 @@ namespace sglc {
 
 void scanExclusive(const int *in, int *out, const int *nPtr, int nMax, int *blockSums, cudaStream_t st);
 void scanExclusive2(const int *in, int *out, const int *nPtr, int nMax, int *blockSums, cudaStream_t st);
+// the apply step alone, when the producer of `in` already summed each scan tile into blockSums
+// (zeroed beforehand); scanTiles(nMax) tiles
+void scanApply(const int *in, int *out, const int *nPtr, int nMax, const int *blockSums, cudaStream_t st);
+int scanTiles(int nMax);
 int scanScratchInts(int nMax);
 void launchVertexAndClip(const DrawParams &p, cudaStream_t st);
 void launchClipAppend(const DrawParams &p, cudaStream_t st);
