@@ -320,8 +320,8 @@ __global__ void __launch_bounds__(256) k_setup(const __grid_constant__ DrawParam
 __global__ void __launch_bounds__(256) k_bin_emit(const __grid_constant__ DrawParams p) {
   chainEnter();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  // set-up the sort and the tile ranges would otherwise take launches of their own: empty tile
-  // ranges (k_tile_ranges fills the non-empty ones) and the bin-entry count clamped to the capacity
+  // two set-up steps that would otherwise be launches of their own: clearing the tile ranges
+  // (k_tile_ranges fills the non-empty ones) and the bin-entry count clamped to the capacity
   if (p.binZeroRanges)
     for (int t = i; t < p.views * p.tilesPerView; t += gridDim.x * blockDim.x) p.tileStart[t] = p.tileEnd[t] = 0;
   if (p.binPairTotal && i == 0) p.counters[4] = min(*p.binPairTotal, p.pairCap);

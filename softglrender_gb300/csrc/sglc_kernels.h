@@ -1,4 +1,4 @@
-// Host-side launchers of the draw kernels (sglc_kernels.cu).
+// Host-side launchers of the draw kernels (defined in sglc_geom.cu, sglc_raster_*.cu, sglc_lines*.cu).
 #pragma once
 
 #include <cuda_runtime.h>
