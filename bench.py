@@ -30,13 +30,15 @@ WORKLOAD = "pbr_ibl_1080p_msaa4_200k"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-neural", action="store_true", help="skip training / timing the neural IBL shader")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-views measurement")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch measurement")
+    ap.add_argument("--no-configs12", action="store_true",
+                    help="skip the plain small (Blinn-Phong sphere) and geometry stress (1M-triangle soup) frames")
     return ap.parse_args()
 
 
@@ -186,6 +188,139 @@ def run_cpu(scene, steps: int, threads: int, min_seconds: float = 0.0):
     dt = time.perf_counter() - t0
     r.destroy()
     return n / dt, n
+
+
+def frame_bytes(scene) -> int:
+    """Algorithmic bytes of one frame (the frame-level roofline): every draw's vertex array and
+    indices read once, every bound texture's mip chain read once, per pass every colour and depth
+    sample written once plus the resolved image, and for each later draw of a pass that blends or
+    tests depth the colour / depth samples it reads back."""
+    total = texture_bytes(scene)
+    for p in scene.passes:
+        n = p.width * p.height * p.samples
+        total += n * 8 + (p.width * p.height * 4 if p.samples > 1 else 0)
+        for k, d in enumerate(p.draws):
+            total += d.vertexes.nbytes + 4 * len(d.indices)
+            if k > 0:
+                total += n * 4 * (int(d.states.blend) + int(d.states.depthTest))
+    return total
+
+
+def raster_launch_bytes(w, h, samples, cleared, states, bin_entries, primitives, vary_floats, fragments=0,
+                        deferred=False):
+    """Algorithmic bytes of one raster-stage launch of a draw: colour samples written (and read
+    when the pass was not cleared by this draw and the draw blends), depth samples read when not
+    cleared and written when the mask is on, the resolved image, per bin entry its primitive id and
+    128-B set-up record, per primitive its three vertices' varyings, and for deferred shading a
+    24-B record per fragment."""
+    n = w * h * samples
+    b = n * 4 + (w * h * 4 if samples > 1 else 0)
+    if not cleared and states.blend:
+        b += n * 4
+    if states.depthTest and not cleared:
+        b += n * 4
+    if states.depthMask:
+        b += n * 4
+    b += bin_entries * (4 + 128) + primitives * 3 * vary_floats * 4
+    if deferred:
+        b += fragments * 24
+    return int(b)
+
+
+def bench_frame_config(r, stream, flush, scene, workload, steps, with_cpu, cpu_min_s, peak, peak_kind):
+    """One frame configuration on the GPU through the autotuned submission: frames/s, Mfrag/s,
+    Mtris/s, per-draw stage times, the frame-level roofline (frame_bytes) and the roofline of its
+    dominant raster launch (raster_launch_bytes over the median of 5 instrumented frames); plus
+    the CPU pipeline on the host cores over a bounded sample."""
+    import torch
+    from softglrender_gb300 import api as A
+    from softglrender_gb300 import scenes as S
+    from softglrender_gb300.autotune import autotune
+    inst = S.SceneInstance(r, scene)
+    draw_list = [(pi, di) for pi, p in enumerate(scene.passes) for di in range(len(p.draws))]
+    per_draw = []
+    r.setStatsLevel(2)
+    inst.render(after_draw=lambda pi, di: per_draw.append(r.drawStats()))
+    r.setStatsLevel(1)
+    samples = []
+    for _ in range(5):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        cur = []
+        inst.render(after_draw=lambda pi, di: cur.append(r.drawStats()))
+        samples.append(cur)
+    r.setStatsLevel(0)
+    frags = int(sum(d["fragments_shaded"] for d in per_draw))
+    draws = []
+    for k, (pi, di) in enumerate(draw_list):
+        med = {key: float(np.median([smp[k][key] for smp in samples]))
+               for key in ("geometry_ms", "binning_ms", "raster_ms", "coverage_ms", "shading_ms", "rop_ms")}
+        p = scene.passes[pi]
+        d = p.draws[di]
+        deferred = med["coverage_ms"] > 0
+        vary = 8 if d.shading == A.Shading_VertexColor else 32   # varying row: 8 floats, lit models 32
+        kernel_ms = med["coverage_ms"] if deferred else med["raster_ms"]
+        kb = raster_launch_bytes(p.width, p.height, p.samples, di == 0, d.states, int(per_draw[k]["bin_entries"]),
+                                 int(per_draw[k]["primitives"]), vary, int(per_draw[k]["fragments_shaded"]),
+                                 deferred)
+        draws.append({"pass": pi, "draw": di, "triangles": len(d.indices) // 3,
+                      "primitives": int(per_draw[k]["primitives"]), "clip_vertices": int(per_draw[k]["clip_vertices"]),
+                      "bin_entries": int(per_draw[k]["bin_entries"]),
+                      "fragments": int(per_draw[k]["fragments_shaded"]),
+                      "stage_ms": {k2.replace("_ms", ""): round(v, 4) for k2, v in med.items()},
+                      "raster_kernel": "k_raster_cov" if deferred else "k_raster",
+                      "raster_kernel_bytes": kb, "raster_kernel_ms": round(kernel_ms, 4),
+                      "raster_kernel_gbs": round(kb / (kernel_ms * 1e-3) / 1e9, 1) if kernel_ms > 0 else None})
+    tuned = autotune(r, inst.render, reps=5)
+    for _ in range(3):
+        tuned.run()
+    r.waitIdle()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for i in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            starts[i].record(stream)
+        tuned.run()
+        with torch.cuda.stream(stream):
+            ends[i].record(stream)
+    r.waitIdle()
+    torch.cuda.synchronize()
+    frame_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    overflow = r.getOverflow()
+    sub = tuned.result.describe()
+    tuned.destroy()
+    r.setCapacity(None)
+    fps = steps / (sum(frame_ms) / 1e3)
+    fb = frame_bytes(scene)
+    dom = max(draws, key=lambda d: d["raster_kernel_ms"])
+    out = {
+        "workload": workload, "resolution": [scene.passes[0].width, scene.passes[0].height],
+        "msaa": scene.passes[0].samples, "triangles": scene.triangles, "steps": steps,
+        "frames_per_s": round(fps, 2), "ms_per_frame": round(1e3 / fps, 4),
+        "mfrag_per_s": round(frags * fps / 1e6, 2), "fragments_per_frame": frags,
+        "mtris_per_s": round(scene.triangles * fps / 1e6, 2), "overflow_flags": overflow,
+        "draws": draws,
+        "frame_roofline": {"bound": "hbm", "algorithmic_bytes_per_frame": fb,
+                           "achieved": round(fb * fps / 1e9, 1),
+                           "peak": peak, "unit": "GB/s", "peak_source": peak_kind},
+        "roofline": {"bound": "hbm", "kernel": dom["raster_kernel"], "draw": [dom["pass"], dom["draw"]],
+                     "achieved": dom["raster_kernel_gbs"], "peak": peak, "unit": "GB/s",
+                     "frac": round(dom["raster_kernel_gbs"] / peak, 4) if dom["raster_kernel_gbs"] else None,
+                     "algorithmic_bytes_per_launch": dom["raster_kernel_bytes"], "kernel_ms": dom["raster_kernel_ms"],
+                     "peak_source": peak_kind},
+        "submission": {k: v for k, v in sub.items() if k != "candidates"},
+    }
+    out["frame_roofline"]["frac"] = round(out["frame_roofline"]["achieved"] / peak, 4)
+    if with_cpu:
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        cpu_fps, cpu_frames = run_cpu(scene, 1, threads, min_seconds=cpu_min_s)
+        out["cpu_baseline"] = {"value": round(cpu_fps, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+                               "sample": f"{cpu_frames} full frames of {workload} after 1 warm-up, at least "
+                                         f"{cpu_min_s:.0f} s ({time.perf_counter() - t0:.1f} s with set-up)"}
+    del inst
+    return out
 
 
 def bench_batched_views(r, stream, with_cpu: bool):
@@ -479,6 +614,14 @@ def main():
     barrier(pg)
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
+        # untimed frames of the same submission for at least a second before the timed region, so
+        # the clock sampler (one reading per 200 ms) sees the GPU under this load; then exactly
+        # `steps` timed frames
+        t_pre = time.perf_counter()
+        preroll = 0
+        while time.perf_counter() - t_pre < 1.2:
+            timed_frames(20)
+            preroll += 20
         frame_ms = timed_frames(args.steps)
     barrier(pg)
     total_s = max_over_ranks(sum(frame_ms) / 1e3, pg, f"cuda:{local}" if pg and torch.cuda.is_available() else None)
@@ -538,6 +681,19 @@ def main():
             "train_s": round(rep.train_s, 3), "capture_s": round(rep.capture_s, 3), "final_loss": rep.final_loss,
             "views": {"train": 64, "held_out": 16},
         }
+
+    # ---- the other two frame configurations: the plain small frame (UV sphere, directional
+    # Blinn-Phong, checker mips, 1024x768) and the geometry stress frame (1M-triangle soup, clipping,
+    # reversed Z, opaque then blended pass, 1080p MSAA 4x) ---------------------------------------
+    configs12 = {}
+    if not args.no_configs12:
+        with_cpu = rank == 0 and not args.no_cpu_baseline
+        configs12["plain_small"] = bench_frame_config(r, stream, flush, S.config_plain_small(),
+                                                      "plain_small_1024x768_blinn_4k", args.steps, with_cpu, 10.0,
+                                                      peak, peak_kind)
+        configs12["geometry_stress"] = bench_frame_config(r, stream, flush, S.config_geometry_stress(),
+                                                          "geometry_stress_1080p_msaa4_1M_soup", args.steps, with_cpu,
+                                                          10.0, peak, peak_kind)
 
     # ---- batched views: 256 orbit views of a 50k-triangle sphere at 256x256 after a 2048x2048
     # shadow pass, all views in one pipeline pass, submission chosen by the autotuner -----------
@@ -669,6 +825,9 @@ def main():
         "clocks": clocks.summary(),
         "submission": plain_sub,
     }
+    result["clocks"]["window"] = (f"{preroll} untimed frames (>= 1.2 s) of the same submission, then the "
+                                  f"{args.steps} timed frames")
+    result.update(configs12)
     if neural is not None:
         result["neural"] = neural
     if batched is not None:

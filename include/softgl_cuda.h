@@ -366,9 +366,11 @@ SGLC_API sglc_status sglc_program_set_neural_shader(sglc_context *ctx, sglc_hand
  * linear, 4 interleaved samples per pixel when samples = 4. Everything is enqueued on `stream`
  * (a cudaStream_t, 0 = default stream), which is synchronised once at the end to read the
  * capacity flags (SGLC_ERR_OVERFLOW: the attachments' contents are then unspecified).
- * The first call on a device looks up the array's device address; make it before any stream
- * capture. All calls share the array: calls that overlap on the GPU (different streams or
- * threads) race and must be serialised by the caller. */
+ * The first call on a device (per CUDA context current on it) looks up the array's device
+ * address; make it before any stream capture. The array exists once per context that loads the
+ * library, and a device reset gives a new context whose address is looked up again. All calls in
+ * one context share the array: calls that overlap on the GPU (different streams or threads) race
+ * and must be serialised by the caller. */
 typedef struct sglc_noalloc_draw {
   const void *vertexes;           /* device, vertex_count * stride bytes */
   int32_t vertex_count;

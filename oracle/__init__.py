@@ -20,7 +20,6 @@ from typing import Optional
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_TREE = os.environ.get("SOFTGL_REFERENCE_TREE", "/root/reference")
 ORACLE_SO = os.path.join(HERE, "_build", "libsoftgl_oracle.so")
 
 
@@ -36,10 +35,25 @@ def build(verbose: bool = False) -> str:
         if platform.machine() in ("x86_64", "AMD64"):
             cmd.insert(1, "-mfma")   # hardware fmaf (same results as the libm routine, faster)
         subprocess.run(cmd, check=True, capture_output=not verbose)
-    if os.path.isdir(REFERENCE_TREE) and platform.machine() in ("x86_64", "AMD64"):
-        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"REF={REFERENCE_TREE}",
-                        f"OUT={REF_DIR}", "-j4"], check=True, capture_output=not verbose)
+    if platform.machine() in ("x86_64", "AMD64") and _have_reference_tree():
+        subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), f"OUT={REF_DIR}", "-j4"],
+                       check=True, capture_output=not verbose)
     return ORACLE_SO
+
+
+def _have_reference_tree() -> bool:
+    """Whether the reference sources are present (oracle/ref/Makefile decides where they lie;
+    SOFTGL_REFERENCE_TREE overrides it)."""
+    r = subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "have-ref"], capture_output=True)
+    return r.returncode == 0
+
+
+def reference_tree() -> Optional[str]:
+    """The reference tree's root when its sources are present, else None."""
+    if not _have_reference_tree():
+        return None
+    r = subprocess.run(["make", "-s", "-C", os.path.join(HERE, "ref"), "print-ref"], capture_output=True, text=True)
+    return r.stdout.strip() or None
 
 
 def _lib(path: str, prefix: str):

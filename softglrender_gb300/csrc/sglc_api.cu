@@ -16,6 +16,7 @@
 #include "softgl_cuda.h"
 #include "sglc_device.cuh"
 #include "sglc_kernels.h"
+#include "sglc_host_util.h"
 #include "sglc_nn_host.h"
 
 using namespace sglc;
@@ -247,9 +248,11 @@ struct Ctx {
   }
 };
 
+// every entry point over a context runs with the context's device current (restored on return)
 #define CTX                                    \
   if (!ctx) return SGLC_ERR_INVALID_HANDLE;    \
-  Ctx *c = reinterpret_cast<Ctx *>(ctx)
+  Ctx *c = reinterpret_cast<Ctx *>(ctx);       \
+  sglc::DeviceGuard deviceGuard_(c->device)
 #define GET(var, h, kind)                                                     \
   Object *var = c->get(h, kind);                                              \
   if (!var) return c->fail(SGLC_ERR_INVALID_HANDLE, "invalid handle");
@@ -1024,7 +1027,9 @@ sglc_status sglc_create(sglc_context **out, int32_t device) {
     return SGLC_ERR_NO_DEVICE;
   }
   if (device < 0 || device >= n) return SGLC_ERR_INVALID_VALUE;
-  if (cudaSetDevice(device) != cudaSuccess) return SGLC_ERR_DEVICE;
+  sglc::DeviceGuard deviceGuard(device);
+  int current = -1;
+  if (cudaGetDevice(&current) != cudaSuccess || current != device) return SGLC_ERR_DEVICE;
   Ctx *c = new Ctx();
   c->device = device;
   c->forEachBuf([c](DevBuf &b) { b.epoch = &c->freeEpoch; });
@@ -1042,7 +1047,6 @@ sglc_status sglc_create(sglc_context **out, int32_t device) {
 
 sglc_status sglc_destroy(sglc_context *ctx) {
   CTX;
-  cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   for (auto &kv : c->objects) {
     Object &o = kv.second;
@@ -1802,6 +1806,7 @@ sglc_status sglc_graph_end(sglc_context *ctx, sglc_graph **out) {
 sglc_status sglc_graph_launch(sglc_graph *g) {
   if (!g || !g->exec) return SGLC_ERR_INVALID_VALUE;
   Ctx *c = reinterpret_cast<Ctx *>(g->ctx);
+  sglc::DeviceGuard deviceGuard(c->device);
   if (g_freeEpoch.load() != g->epoch || c->freeEpoch.load() != g->ctxEpoch)
     return c->fail(SGLC_ERR_INVALID_VALUE, "graph_launch: a buffer the graph uses was freed or grown since the capture; "
                                            "capture it again");
@@ -1812,6 +1817,7 @@ sglc_status sglc_graph_launch(sglc_graph *g) {
 sglc_status sglc_graph_destroy(sglc_graph *g) {
   if (!g) return SGLC_ERR_INVALID_VALUE;
   Ctx *c = reinterpret_cast<Ctx *>(g->ctx);
+  sglc::DeviceGuard deviceGuard(c->device);
   cudaStreamSynchronize(c->stream);
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);

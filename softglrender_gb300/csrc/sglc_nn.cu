@@ -23,6 +23,7 @@
 
 #include "softgl_cuda.h"
 #include "sglc_nn.cuh"
+#include "sglc_host_util.h"
 #include "sglc_nn_host.h"
 
 namespace sglc {
@@ -403,8 +404,7 @@ struct sglc_neural {
 
 namespace {
 
-std::once_flag gAttrOnce;
-cudaError_t gAttrErr = cudaSuccess;
+PerDeviceAttr gTileAttr;   // k_nn_tile's dynamic shared-memory limit, per device
 
 sglc_status nnFail(sglc_neural *n, sglc_status s, const std::string &msg) {
   ctxSetError(n ? n->ctx : nullptr, msg.c_str());
@@ -438,10 +438,7 @@ unsigned long long splitmix(unsigned long long &s) {
 
 sglc_status runTiles(sglc_neural *n, int mode, long long first, long long rows, int step, unsigned long long seed,
                      float invBatch, float *out) {
-  std::call_once(gAttrOnce, [] {
-    gAttrErr = cudaFuncSetAttribute(k_nn_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmBytes + 1024);
-  });
-  NCK(gAttrErr);
+  NCK(setDynamicSmemOnce(gTileAttr, k_nn_tile, kSmBytes + 1024));
   long long tiles = (rows + 127) / 128;
   int grid = (int) std::min<long long>(tiles, n->sms);
   if (grid <= 0) return SGLC_OK;
@@ -488,7 +485,7 @@ SGLC_API sglc_status sglc_neural_create(sglc_context *ctx, uint64_t seed, sglc_n
   sglc_neural *n = new sglc_neural();
   n->ctx = ctx;
   n->device = ctxDevice(ctx);
-  cudaSetDevice(n->device);
+  DeviceGuard deviceGuard(n->device);
   cudaDeviceGetAttribute(&n->sms, cudaDevAttrMultiProcessorCount, n->device);
   auto fail = [&](cudaError_t e) {
     sglc_neural_destroy(n);
@@ -525,7 +522,7 @@ SGLC_API sglc_status sglc_neural_create(sglc_context *ctx, uint64_t seed, sglc_n
 
 SGLC_API sglc_status sglc_neural_destroy(sglc_neural *n) {
   if (!n) return SGLC_ERR_INVALID_VALUE;
-  cudaSetDevice(n->device);
+  DeviceGuard deviceGuard(n->device);
   if (n->ctx) {
     cudaStreamSynchronize(ctxStream(n->ctx));
     ctxDetachNeural(n->ctx, n);
@@ -542,7 +539,7 @@ SGLC_API int64_t sglc_neural_param_count(void) { return kParams; }
 SGLC_API sglc_status sglc_neural_set_params(sglc_neural *n, const float *in, int64_t count) {
   if (!n || !in) return SGLC_ERR_INVALID_VALUE;
   if (count != kParams) return nnFail(n, SGLC_ERR_INVALID_VALUE, "neural shader: parameter count mismatch");
-  cudaSetDevice(n->device);
+  DeviceGuard deviceGuard(n->device);
   cudaStream_t st = ctxStream(n->ctx);
   NCK(cudaMemcpyAsync(n->params, in, kParams * sizeof(float), cudaMemcpyHostToDevice, st));
   NCK(cudaMemsetAsync(n->m, 0, kParams * sizeof(float), st));
@@ -557,7 +554,7 @@ SGLC_API sglc_status sglc_neural_set_params(sglc_neural *n, const float *in, int
 SGLC_API sglc_status sglc_neural_get_params(sglc_neural *n, float *out, int64_t count) {
   if (!n || !out) return SGLC_ERR_INVALID_VALUE;
   if (count != kParams) return nnFail(n, SGLC_ERR_INVALID_VALUE, "neural shader: parameter count mismatch");
-  cudaSetDevice(n->device);
+  DeviceGuard deviceGuard(n->device);
   cudaStream_t st = ctxStream(n->ctx);
   NCK(cudaMemcpyAsync(out, n->params, kParams * sizeof(float), cudaMemcpyDeviceToHost, st));
   NCK(cudaStreamSynchronize(st));
@@ -566,7 +563,7 @@ SGLC_API sglc_status sglc_neural_get_params(sglc_neural *n, float *out, int64_t 
 
 SGLC_API sglc_status sglc_neural_set_records(sglc_neural *n, const float *records, int64_t count) {
   if (!n || (count > 0 && !records) || count < 0) return SGLC_ERR_INVALID_VALUE;
-  cudaSetDevice(n->device);
+  DeviceGuard deviceGuard(n->device);
   NCK(ensure(&n->records, &n->recCap, count * kRecordFloats));
   cudaStream_t st = ctxStream(n->ctx);
   if (count > 0)
@@ -581,7 +578,7 @@ SGLC_API sglc_status sglc_neural_set_records(sglc_neural *n, const float *record
 SGLC_API sglc_status sglc_neural_get_records(sglc_neural *n, float *out, int64_t first, int64_t count) {
   if (!n || !out || first < 0 || count < 0) return SGLC_ERR_INVALID_VALUE;
   if (first + count > n->nRec) return nnFail(n, SGLC_ERR_INVALID_VALUE, "neural shader: record range out of bounds");
-  cudaSetDevice(n->device);
+  DeviceGuard deviceGuard(n->device);
   cudaStream_t st = ctxStream(n->ctx);
   if (count > 0)
     NCK(cudaMemcpyAsync(out, n->records + (size_t) first * kRecordFloats, (size_t) count * kRecordFloats * sizeof(float),
@@ -592,7 +589,7 @@ SGLC_API sglc_status sglc_neural_get_records(sglc_neural *n, float *out, int64_t
 
 SGLC_API sglc_status sglc_neural_capture(sglc_context *ctx, sglc_neural *n, int64_t capacity, int32_t stride) {
   if (!ctx || !n || capacity < 0 || stride < 1) return SGLC_ERR_INVALID_VALUE;
-  cudaSetDevice(n->device);
+  DeviceGuard deviceGuard(n->device);
   cudaStream_t st = ctxStream(ctx);
   if (capacity == 0) {
     ctxSetCapture(ctx, nullptr, nullptr, 0, 1);
@@ -609,7 +606,7 @@ SGLC_API sglc_status sglc_neural_capture(sglc_context *ctx, sglc_neural *n, int6
 
 SGLC_API sglc_status sglc_neural_record_count(sglc_neural *n, int64_t *count) {
   if (!n || !count) return SGLC_ERR_INVALID_VALUE;
-  cudaSetDevice(n->device);
+  DeviceGuard deviceGuard(n->device);
   cudaStream_t st = ctxStream(n->ctx);
   if (n->captureCap > 0) {
     unsigned long long c = 0;
@@ -625,7 +622,7 @@ SGLC_API sglc_status sglc_neural_record_count(sglc_neural *n, int64_t *count) {
 SGLC_API sglc_status sglc_neural_train(sglc_neural *n, const sglc_neural_train_params *p, float *loss) {
   if (!n || !p || p->steps < 0 || p->batch <= 0) return SGLC_ERR_INVALID_VALUE;
   if (n->nRec <= 0) return nnFail(n, SGLC_ERR_INVALID_VALUE, "neural shader: no training records");
-  cudaSetDevice(n->device);
+  DeviceGuard deviceGuard(n->device);
   cudaStream_t st = ctxStream(n->ctx);
   n->captureCap = 0;
   NCK(cudaMemsetAsync(n->error, 0, sizeof(int), st));
@@ -653,7 +650,7 @@ SGLC_API sglc_status sglc_neural_train(sglc_neural *n, const sglc_neural_train_p
 SGLC_API sglc_status sglc_neural_gradients(sglc_neural *n, int64_t first, int64_t count, float *grads, float *loss) {
   if (!n || !grads || first < 0 || count <= 0) return SGLC_ERR_INVALID_VALUE;
   if (first + count > n->nRec) return nnFail(n, SGLC_ERR_INVALID_VALUE, "neural shader: record range out of bounds");
-  cudaSetDevice(n->device);
+  DeviceGuard deviceGuard(n->device);
   cudaStream_t st = ctxStream(n->ctx);
   NCK(cudaMemsetAsync(n->error, 0, sizeof(int), st));
   sglc_status r = runTiles(n, MODE_GRAD, first, count, 0, 0, 1.0f / (float) count, nullptr);
@@ -675,7 +672,7 @@ SGLC_API sglc_status sglc_neural_infer(sglc_neural *n, int64_t first, int64_t co
   if (!n || !out || first < 0 || count < 0) return SGLC_ERR_INVALID_VALUE;
   if (first + count > n->nRec) return nnFail(n, SGLC_ERR_INVALID_VALUE, "neural shader: record range out of bounds");
   if (count == 0) return SGLC_OK;
-  cudaSetDevice(n->device);
+  DeviceGuard deviceGuard(n->device);
   cudaStream_t st = ctxStream(n->ctx);
   NCK(ensure(&n->out, &n->outCap, count * 3));
   NCK(cudaMemsetAsync(n->error, 0, sizeof(int), st));

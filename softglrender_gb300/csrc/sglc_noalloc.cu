@@ -17,6 +17,9 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <vector>
+
+#include <cuda.h>
 
 #include "softgl_cuda.h"
 #include "sglc_device.cuh"
@@ -77,10 +80,46 @@ static __device__ __align__(256) unsigned char g_noallocScratch[kScratchBytes];
 // number of bin entries the sort may read: min(total, capacity), kept on the device
 __global__ void k_clamp_pairs(const int *total, int cap, int *out) { *out = min(*total, cap); }
 
-// per-device address of g_noallocScratch, looked up once per device (host code cannot use the
-// symbol itself as a device address)
+// Address of g_noallocScratch as seen from one CUDA context, looked up once per (device, driver
+// context) at set-up: host code cannot use the symbol itself as a device address. The array
+// exists once per driver context that loads the library's module, so a host framework that runs
+// its own driver-API context on a device gets its own copy and its own address. Contexts are told
+// apart by cuCtxGetId, which is unique for the life of the process, so a device reset (a new
+// primary context) is looked up afresh rather than served a stale address.
+struct ScratchAddress {
+  int device;
+  unsigned long long contextId;
+  unsigned char *ptr;
+};
 std::mutex g_lock;
-unsigned char *g_scratch[256] = {nullptr};
+std::vector<ScratchAddress> g_scratch;
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+// the current driver context's unique id; 0 when the driver entry points are unavailable (the
+// cache then falls back to one entry per device)
+unsigned long long currentContextId() {
+  static CtxGetCurrentFn getCurrent = nullptr;
+  static CtxGetIdFn getId = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      getCurrent = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      getId = reinterpret_cast<CtxGetIdFn>(f);
+    cudaGetLastError();
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (getCurrent && getId && getCurrent(&ctx) == CUDA_SUCCESS && ctx && getId(ctx, &id) == CUDA_SUCCESS) return id;
+  return 0;
+}
 
 int fail(char *err, size_t errLen, int status, const char *msg) {
   if (err && errLen) {
@@ -118,20 +157,28 @@ extern "C" SGLC_API sglc_status sglc_draw_vertex_color_noalloc(const sglc_noallo
     return fail(err, errLen, SGLC_ERR_INVALID_VALUE, "noalloc draw: render state enum out of range");
 
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256)
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
+    cudaGetLastError();
     return fail(err, errLen, SGLC_ERR_NO_DEVICE, "noalloc draw: no current CUDA device");
-  unsigned char *scratch;
+  }
+  unsigned char *scratch = nullptr;
   {
     std::lock_guard<std::mutex> g(g_lock);
-    if (!g_scratch[dev]) {
-      // first call on this device: resolve the array's device address (do this before any capture)
+    const unsigned long long ctxId = currentContextId();
+    for (const ScratchAddress &a : g_scratch)
+      if (a.device == dev && a.contextId == ctxId) scratch = a.ptr;
+    if (!scratch) {
+      // first call on this device and context: resolve the array's device address (make this
+      // call before any stream capture)
       void *ptr = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&ptr, g_noallocScratch);
-      if (e != cudaSuccess || !ptr)
+      if (e != cudaSuccess || !ptr) {
+        cudaGetLastError();
         return fail(err, errLen, SGLC_ERR_DEVICE, "noalloc draw: cudaGetSymbolAddress of the scratch array failed");
-      g_scratch[dev] = reinterpret_cast<unsigned char *>(ptr);
+      }
+      scratch = reinterpret_cast<unsigned char *>(ptr);
+      g_scratch.push_back({dev, ctxId, scratch});
     }
-    scratch = g_scratch[dev];
   }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
 

@@ -16,6 +16,7 @@
 // candidate per lane per step, with a CTA-wide vote before each step on whether any queue must be
 // flushed first.
 #include "sglc_raster.cuh"
+#include "sglc_host_util.h"
 #include "sglc_nn.cuh"
 
 namespace sglc {
@@ -483,25 +484,23 @@ __global__ void __launch_bounds__(256, 2) k_shade_neural(const __grid_constant__
   if (warp == 0) tc::tmemFree(*tmemSlot, 256);
 }
 
+// A failed attribute set makes the launch after it fail; the draw reports that launch error.
+template<int S>
+static void launchShadeNeuralS(const DrawParams &p, cudaStream_t st) {
+  static PerDeviceAttr attr;
+  setDynamicSmemOnce(attr, k_shade_neural<S>, kSnBytes);
+  k_shade_neural<S><<<152 * 2, 256, kSnBytes, st>>>(p);
+}
+
 void launchShadeNeural(const DrawParams &p, cudaStream_t st) {
-  static bool attr[2] = {false, false};
-  const int k = p.samples == 4 ? 1 : 0;
-  if (!attr[k]) {
-    if (k) cudaFuncSetAttribute(k_shade_neural<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSnBytes);
-    else cudaFuncSetAttribute(k_shade_neural<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSnBytes);
-    attr[k] = true;
-  }
-  if (k) k_shade_neural<4><<<152 * 2, 256, kSnBytes, st>>>(p);
-  else k_shade_neural<1><<<152 * 2, 256, kSnBytes, st>>>(p);
+  if (p.samples == 4) launchShadeNeuralS<4>(p, st);
+  else launchShadeNeuralS<1>(p, st);
 }
 
 template<int S, bool D>
 static void launchNeural(const DrawParams &p, int grid, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_raster_neural<S, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRnBytes);
-    attr = true;
-  }
+  static PerDeviceAttr attr;
+  setDynamicSmemOnce(attr, k_raster_neural<S, D>, kRnBytes);
   k_raster_neural<S, D><<<grid, 256, kRnBytes, st>>>(p);
 }
 

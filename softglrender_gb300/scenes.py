@@ -541,16 +541,20 @@ class SceneInstance:
                 objs.append((vao, prog, res, ps))
             self.draws.append(objs)
 
-    def render(self) -> None:
-        for p, fbo, objs in zip(self.scene.passes, self.fbos, self.draws):
+    def render(self, after_draw=None) -> None:
+        """The frame's calls; `after_draw(pass_index, draw_index)`, when given, runs after each draw
+        (e.g. to read that draw's statistics)."""
+        for pi, (p, fbo, objs) in enumerate(zip(self.scene.passes, self.fbos, self.draws)):
             self.r.beginRenderPass(fbo, p.clear)
             self.r.setViewPort(0, 0, p.width, p.height)
-            for vao, prog, res, ps in objs:
+            for di, (vao, prog, res, ps) in enumerate(objs):
                 self.r.setVertexArrayObject(vao)
                 self.r.setShaderProgram(prog)
                 self.r.setShaderResources(res)
                 self.r.setPipelineStates(ps)
                 self.r.draw()
+                if after_draw is not None:
+                    after_draw(pi, di)
             self.r.endRenderPass()
 
     def outputs(self, pass_index: int = -1) -> Dict[str, np.ndarray]:

@@ -43,3 +43,27 @@ def test_clock_summary_reports_median_under_load_and_reasons():
     assert s["sm_mhz"] == 2070.0            # the lowest quarter (idle samples) is left out
     assert s["reasons"] == ["sw_power_cap"]
     assert bench.ClockSampler(0).summary()["samples"] == 0
+
+
+def test_frame_bytes_of_the_plain_small_frame():
+    """The frame-level algorithmic bytes of the plain small frame: vertex array (2,145 x 64 B),
+    indices (3,968 triangles), the 256^2 checker's mip chain and 1024x768 colour + depth written
+    once: about 6.8 MB."""
+    from softglrender_gb300 import scenes as S
+    sc = S.config_plain_small()
+    d = sc.passes[0].draws[0]
+    tex = sum(max(1, 256 >> l) ** 2 * 4 for l in range(9))
+    want = d.vertexes.nbytes + 4 * len(d.indices) + tex + 1024 * 768 * 8
+    assert bench.frame_bytes(sc) == want
+    assert 6.6e6 < want < 7.0e6
+
+
+def test_raster_launch_bytes_counts_reads_only_when_not_cleared():
+    from softglrender_gb300 import api as A
+    opaque = A.RenderStates(depthTest=True, depthMask=True)
+    blend = A.RenderStates(blend=True, depthTest=True, depthMask=False)
+    n = 64 * 32 * 4
+    a = bench.raster_launch_bytes(64, 32, 4, True, opaque, 0, 0, 8)
+    assert a == n * 4 + 64 * 32 * 4 + n * 4                       # colour + resolved + depth write
+    b = bench.raster_launch_bytes(64, 32, 4, False, blend, 10, 5, 8)
+    assert b == n * 4 + 64 * 32 * 4 + n * 4 + n * 4 + 10 * 132 + 5 * 3 * 8 * 4   # + colour, depth reads

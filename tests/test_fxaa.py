@@ -8,7 +8,7 @@ from softglrender_gb300 import api as A
 from softglrender_gb300 import scenes as S
 from softglrender_gb300.postfx import fxaa
 
-from helpers import COLOR_MIN_FRACTION, color_stats, render
+from helpers import assert_color_bar, render
 
 
 @pytest.fixture(scope="module")
@@ -32,5 +32,4 @@ def test_restatement_equals_reference(filt, aliased, oracle_lib, reference_lib):
 def test_gpu_matches_restatement(filt, aliased, cuda_lib, oracle_lib):
     g = fxaa(A.Renderer(cuda_lib, 0), aliased, filt)
     c = fxaa(A.Renderer(oracle_lib, 0), aliased, filt)
-    mx, frac, nbad = color_stats(g, c)
-    assert frac >= COLOR_MIN_FRACTION, (mx, frac, nbad)
+    assert_color_bar(g, c, f"fxaa filter {filt}")

@@ -1,8 +1,8 @@
 """Parity of the CUDA renderer with the CPU oracle (a restatement of RendererSoft pinned to the
 reference itself by test_oracle_vs_reference.py), on identical seeded inputs, through the C ABI.
 
-The bar: depth (hence coverage, culling and depth-test outcomes) bit-identical; RGBA8 colour within
-1 LSB per channel on at least 99.9% of channels (tests/helpers.py COLOR_MIN_FRACTION). Shading
+The bar: depth (hence coverage, culling and depth-test outcomes) bit-identical; RGBA8 colour with
+every channel within 1 LSB on at least 99.9% of pixels (tests/helpers.py COLOR_MIN_FRACTION). Shading
 models whose arithmetic has no transcendental functions (vertex colour, base colour) must match
 bit for bit."""
 import numpy as np

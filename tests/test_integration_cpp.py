@@ -14,8 +14,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _build(tmp_path):
-    ref = oracle.REFERENCE_TREE
-    if not os.path.isdir(ref):
+    ref = oracle.reference_tree()
+    if ref is None:
         pytest.skip("reference tree not present")
     lib = B.build()
     exe = str(tmp_path / "drive_renderer")
