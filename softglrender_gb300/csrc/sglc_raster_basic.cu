@@ -17,6 +17,7 @@ void launchShadeNeural(const DrawParams &p, cudaStream_t st);
 
 bool deferredShadingModel(int shading) {
   switch (shading) {
+    case SH_VCOLOR:   // cheap shader, but the coverage kernel's balanced pass 2 pays off on dense soups
     case SH_BLINN:
     case SH_BLINN_DIR:
     case SH_PBR:
@@ -41,6 +42,7 @@ void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st, c
   }
   if (evCov) cudaEventRecord(evCov, st);
   switch (p.shading) {
+    case SH_VCOLOR: launchShadeModel<SH_VCOLOR>(p, st); break;
     case SH_BLINN:
     case SH_BLINN_DIR: launchShadeBlinn(p, st); break;
     case SH_PBR: launchShadePbr(p, st); break;
