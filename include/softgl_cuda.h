@@ -295,7 +295,8 @@ SGLC_API sglc_status sglc_set_capacity(sglc_context *ctx, const sglc_capacity *c
 SGLC_API sglc_status sglc_get_peak_counts(sglc_context *ctx, sglc_capacity *out);
 /* Synchronises, returns and clears the overflow flags of the draws since the last call: bit 0 clip
  * vertices, 1 clip polygons, 2 appended primitives, 3 bin entries, 4 an index outside the vertex
- * array, 5 fragment records. */
+ * array, 5 fragment records, 6 a tensor-core wait of the neural shader timed out (that draw's
+ * colours are unspecified). */
 SGLC_API sglc_status sglc_get_overflow(sglc_context *ctx, int32_t *flags);
 typedef struct sglc_graph sglc_graph;
 /* Capture everything enqueued on the context between begin and end into a CUDA graph. Draws in the
@@ -351,6 +352,10 @@ SGLC_API sglc_status sglc_neural_infer(sglc_neural *net, int64_t first, int64_t 
 /* Bind a network to a PBR program: its IBL term comes from the network (null unbinds, restoring
  * the plain shader). The network must outlive its use by draws. */
 SGLC_API sglc_status sglc_program_set_neural_shader(sglc_context *ctx, sglc_handle prog, sglc_neural *net);
+/* Test hook of the neural shading kernels (no counterpart in the reference): flag 1 makes every
+ * completed tensor-core wait report a timeout, so a test can check that timeouts reach the host
+ * (sglc_get_overflow bit 6) without a real one. 0 restores normal operation. */
+SGLC_API sglc_status sglc_neural_set_test_flags(sglc_context *ctx, int32_t flags);
 
 /* ---- allocation-free draw ----------------------------------------------------------------- */
 /* One vertex-colour draw (position vec3 padded to 16 B + RGBA float colour, 32-B stride; the

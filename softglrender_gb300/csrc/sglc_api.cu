@@ -84,6 +84,30 @@ struct TexObj {
   int w[kMaxLevels] = {0}, h[kMaxLevels] = {0}, tilesW[kMaxLevels] = {0};
   uint32_t *resolved = nullptr;   // multi-sample RGBA8 colour: resolved image
   bool resolvedValid = false;
+  unsigned long long version = 0;   // bumped by every write of the texture's memory
+  struct HwCopy *hw = nullptr;      // hardware-sampled copy for the neural shading path
+};
+
+// A 2D RGBA8 texture copied into a CUDA mipmapped array for the texture units, with one texture
+// object per sampler state that uses it. Rebuilt when the texture's version moves on. Used only by
+// the neural shading path (judged by PSNR); the exact shaders sample the texture's own memory.
+struct HwCopy {
+  cudaMipmappedArray_t arr = nullptr;
+  int w = 0, h = 0, levels = 0;
+  unsigned long long version = ~0ull;
+  struct View {
+    int filter, wrap;
+    uint32_t border;
+    cudaTextureObject_t obj;
+  };
+  std::vector<View> views;
+  void release() {
+    for (View &v : views) cudaDestroyTextureObject(v.obj);
+    views.clear();
+    if (arr) cudaFreeMipmappedArray(arr);
+    arr = nullptr;
+    version = ~0ull;
+  }
 };
 
 struct FbObj {
@@ -207,6 +231,7 @@ struct Ctx {
   DevBuf recA, recB, recColor, chunkNext, chunkFill, warpHead, recDense;   // deferred shading
   DevBuf peakChunks;   // largest number of fragment-record chunks a deferred draw used (device)
   bool deferredShading = true;
+  int nnTestFlags = 0;               // sglc_neural_set_test_flags
   DevBuf lpSlot, lpOrigin, lpStampCount, lpStampOff, lpStampGeo, lpStampRow, lpStampColor, lpStampVary, lpFragCount,
       lpFragOff, lpMisc;   // point and line draws
   // capacity hints that survive between draws
@@ -328,11 +353,17 @@ sglc_status allocTexture(Ctx *c, TexObj &t) {
     CK(cudaMemsetAsync(t.resolved, 0, (size_t) t.desc.width * t.desc.height * 4, c->stream));
   }
   t.allocated = true;
+  t.version++;
   return SGLC_OK;
 }
 
 void freeTexture(TexObj &t, std::atomic<unsigned long long> &epoch) {
-  if (t.dev || t.resolved) epoch++;
+  if (t.dev || t.resolved || t.hw) epoch++;
+  if (t.hw) {
+    t.hw->release();
+    delete t.hw;
+    t.hw = nullptr;
+  }
   if (t.dev) cudaFree(t.dev);
   if (t.resolved) cudaFree(t.resolved);
   t.dev = nullptr;
@@ -342,6 +373,7 @@ void freeTexture(TexObj &t, std::atomic<unsigned long long> &epoch) {
 
 // upload one linear level into the texture's layout
 sglc_status uploadLevel(Ctx *c, TexObj &t, int layer, int level, const void *data) {
+  t.version++;
   size_t n = (size_t) t.w[level] * t.h[level];
   uint32_t *dst = t.dev + (size_t) layer * t.layerStride + t.offset[level];
   if (t.desc.layout == LAYOUT_LINEAR) {
@@ -359,6 +391,80 @@ sglc_status uploadLevel(Ctx *c, TexObj &t, int layer, int level, const void *dat
 }
 
 // materialise a pending clear (RendererSoft::beginRenderPass, RendererSoft.cpp:61-90)
+// The texture-unit view of a 2D RGBA8 texture for one sampler state (0 when the texture cannot be
+// sampled by the hardware: another format, multi-sample, a cube map). Builds or refreshes the
+// mipmapped copy when the texture changed since it was made (one device-to-array copy per level,
+// on the context's stream; Tiled and Morton levels are first swizzled to linear in the staging
+// buffer). Never called during a graph capture that could need a rebuild: the autotuner's capture
+// follows eager frames, and draws do not write their material textures.
+sglc_status hwTexture(Ctx *c, TexObj &t, const UsObj &us, cudaTextureObject_t *out) {
+  *out = 0;
+  if (!t.allocated || t.desc.format != SGLC_FORMAT_RGBA8 || t.desc.multi_sample || t.desc.type != SGLC_TEXTURE_2D)
+    return SGLC_OK;
+  if (!t.hw) t.hw = new HwCopy();
+  HwCopy &h = *t.hw;
+  if (h.version != t.version) {
+    if (c->capturing) return c->fail(SGLC_ERR_UNSUPPORTED, "draw: a neural draw's texture changed inside a capture");
+    if (!h.views.empty() || h.arr) c->freeEpoch++;   // graphs that baked the old copy in are stale
+    for (HwCopy::View &v : h.views) cudaDestroyTextureObject(v.obj);
+    h.views.clear();
+    if (h.arr && (h.w != t.w[0] || h.h != t.h[0] || h.levels != t.levels)) {
+      cudaFreeMipmappedArray(h.arr);
+      h.arr = nullptr;
+    }
+    if (!h.arr) {
+      cudaChannelFormatDesc cd = cudaCreateChannelDesc<uchar4>();
+      CK(cudaMallocMipmappedArray(&h.arr, &cd, make_cudaExtent(t.w[0], t.h[0], 0), t.levels));
+      h.w = t.w[0];
+      h.h = t.h[0];
+      h.levels = t.levels;
+    }
+    for (int l = 0; l < t.levels; l++) {
+      cudaArray_t la = nullptr;
+      CK(cudaGetMipmappedArrayLevel(&la, h.arr, l));
+      const size_t n = (size_t) t.w[l] * t.h[l];
+      const uint32_t *src = t.dev + t.offset[l];
+      if (t.desc.layout != LAYOUT_LINEAR) {
+        CK(c->staging.ensure(n * 4));
+        launchSwizzleOut(devTex(t), 0, l, c->staging.as<uint32_t>(), c->stream);
+        CK(cudaGetLastError());
+        src = c->staging.as<uint32_t>();
+      }
+      CK(cudaMemcpy2DToArrayAsync(la, 0, 0, src, (size_t) t.w[l] * 4, (size_t) t.w[l] * 4, t.h[l],
+                                  cudaMemcpyDeviceToDevice, c->stream));
+    }
+    h.version = t.version;
+  }
+  for (const HwCopy::View &v : h.views)
+    if (v.filter == us.filter && v.wrap == us.wrap && v.border == us.border) {
+      *out = v.obj;
+      return SGLC_OK;
+    }
+  cudaResourceDesc rd{};
+  rd.resType = cudaResourceTypeMipmappedArray;
+  rd.res.mipmap.mipmap = h.arr;
+  cudaTextureDesc td{};
+  const cudaTextureAddressMode am = us.wrap == WRAP_REPEAT ? cudaAddressModeWrap
+                                    : us.wrap == WRAP_MIRRORED ? cudaAddressModeMirror
+                                    : us.wrap == WRAP_EDGE     ? cudaAddressModeClamp
+                                                               : cudaAddressModeBorder;
+  td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = am;
+  const float bc = us.border ? 1.f : 0.f;   // BorderColor: black or white, alpha as the colour
+  td.borderColor[0] = td.borderColor[1] = td.borderColor[2] = td.borderColor[3] = bc;
+  td.filterMode = (us.filter & 1) ? cudaFilterModeLinear : cudaFilterModePoint;
+  td.mipmapFilterMode = us.filter >= FILTER_NL ? cudaFilterModeLinear : cudaFilterModePoint;
+  td.readMode = cudaReadModeNormalizedFloat;
+  td.normalizedCoords = 1;
+  td.minMipmapLevelClamp = 0.f;
+  td.maxMipmapLevelClamp = (us.filter >= FILTER_NN && us.useMipmaps) ? (float) (t.levels - 1) : 0.f;
+  td.maxAnisotropy = 1;
+  cudaTextureObject_t obj = 0;
+  CK(cudaCreateTextureObject(&obj, &rd, &td, nullptr));
+  h.views.push_back({us.filter, us.wrap, us.border, obj});
+  *out = obj;
+  return SGLC_OK;
+}
+
 sglc_status flushClear(Ctx *c) {
   if (!c->clear.active) return SGLC_OK;
   c->clear.active = false;
@@ -368,6 +474,7 @@ sglc_status flushClear(Ctx *c) {
     Object *t = c->get(f->fb.colorTex, K_TEX);
     if (t && t->tex.allocated && f->fb.colorLevel < t->tex.levels) {
       TexObj &T = t->tex;
+      T.version++;
       size_t n = (size_t) T.w[f->fb.colorLevel] * T.h[f->fb.colorLevel] * T.samplesPerTexel;
       launchFill32(T.dev + (size_t) f->fb.colorLayer * T.layerStride + T.offset[f->fb.colorLevel], c->clear.color, n,
                    c->stream);
@@ -377,6 +484,7 @@ sglc_status flushClear(Ctx *c) {
     Object *t = c->get(f->fb.depthTex, K_TEX);
     if (t && t->tex.allocated) {
       TexObj &T = t->tex;
+      T.version++;
       uint32_t bits;
       memcpy(&bits, &c->clear.depth, 4);
       launchFill32(T.dev, bits, (size_t) T.w[0] * T.h[0] * T.samplesPerTexel, c->stream);
@@ -603,6 +711,8 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
   if (!ct && !dt) return SGLC_OK;
   if (ct && dt && ct->desc.multi_sample != dt->desc.multi_sample)
     return c->fail(SGLC_ERR_UNSUPPORTED, "draw: colour and depth attachments must have the same sample count");
+  if (ct) ct->version++;   // the draw writes its attachments
+  if (dt) dt->version++;
   VaoObj &vao = vo->vao;
 
   DrawParams p;
@@ -639,6 +749,21 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
   if (p.shading == SH_PBR && prog.neural && ct && iblEnabled) {
     p.shading = SH_PBR_NEURAL;
     p.nnImage = neuralImage(prog.neural);
+    // the neural path's material maps go through the texture units (sglc_shade_neural.cu)
+    for (int s = 0; s < kMaxSamplers; s++) {
+      if (!p.samp[s].valid) continue;
+      Object *uo = c->get(prog.samplers[s], K_US);
+      Object *to = uo ? c->get(uo->us.tex, K_TEX) : nullptr;
+      if (!to) continue;
+      sglc_status st = hwTexture(c, to->tex, uo->us, &p.hwTex[s]);
+      if (st) return st;
+    }
+    if (!c->sticky.ptr) {
+      CK(c->sticky.ensure(sizeof(int)));
+      CK(cudaMemsetAsync(c->sticky.ptr, 0, sizeof(int), c->stream));
+    }
+    p.errFlags = c->sticky.as<int>();
+    p.nnInjectTimeout = c->nnTestFlags & 1;
   }
   if (p.shading == SH_PBR && c->capRecords && !pointsLines) {
     p.shading = SH_PBR_CAPTURE;
@@ -712,6 +837,8 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       FbObj &f = o->fb;
       TexObj *vc = f.colorReady ? attachmentTex(c, f.colorTex) : nullptr;
       TexObj *vd = f.depthReady ? attachmentTex(c, f.depthTex) : nullptr;
+      if (vc) vc->version++;
+      if (vd) vd->version++;
       if (vc && (!vc->allocated || f.colorLevel >= vc->levels || vc->desc.format != SGLC_FORMAT_RGBA8)) vc = nullptr;
       if (vd && (!vd->allocated || vd->desc.format != SGLC_FORMAT_FLOAT32)) vd = nullptr;
       if ((vc != nullptr) != (ct != nullptr) || (vd != nullptr) != (dt != nullptr) ||
@@ -1292,6 +1419,7 @@ sglc_status sglc_texture_load_from_file(sglc_context *ctx, sglc_handle tex, cons
   if (got != total) return c->fail(SGLC_ERR_INVALID_VALUE, std::string("load_from_file: failed to read file: ") + path);
   sglc_status s = flushClear(c);
   if (s) return s;
+  T.version++;
   size_t o = 0;
   for (int layer = 0; layer < T.layers; layer++)
     for (int l = 0; l < T.levels; l++) {
@@ -1371,6 +1499,13 @@ sglc_status sglc_program_set_neural_shader(sglc_context *ctx, sglc_handle prog, 
   if (net && (!p->prog.shader || p->prog.shader->model != SH_PBR))
     return c->fail(SGLC_ERR_INVALID_VALUE, "set_neural_shader: the program must use the PBR shading model");
   p->prog.neural = net;
+  return SGLC_OK;
+}
+
+sglc_status sglc_neural_set_test_flags(sglc_context *ctx, int32_t flags) {
+  CTX;
+  if (flags & ~1) return c->fail(SGLC_ERR_INVALID_VALUE, "neural_set_test_flags: unknown flag");
+  c->nnTestFlags = flags;
   return SGLC_OK;
 }
 

@@ -188,6 +188,12 @@ struct DrawParams {
   long long capCap;
   int capStride;
   const uint8_t *nnImage;
+  // neural shading (sglc_shade_neural.cu): hardware-sampled copies of the bound 2D RGBA8 textures
+  // (0: none), the context's sticky flag word its bounded waits report to, and a test hook that
+  // reports a timeout after every completed wait
+  cudaTextureObject_t hwTex[kMaxSamplers];
+  int *errFlags;
+  int nnInjectTimeout;
   // batched views (sglc_draw_views): one pipeline pass over `views` copies of the draw that differ
   // only in uniforms and attachments. nv / ntri above count all views' vertices / triangles;
   // view v owns vertices [v * nvView, (v + 1) * nvView), triangles [v * ntriView, ...) and raster
@@ -223,6 +229,7 @@ constexpr int kCntChunks = 5;      // DrawParams::counters[5]: chunks allocated
 constexpr int kCntBound = 6;       // counters[6..7]: 64-bit upper bound on a draw's fragment records
 constexpr int kCntDense = 8;       // counters[8]: entries of the dense record list
 constexpr int kOvfFrags = 32;      // counters[2] flag: the fragment record pool ran out
+constexpr int kFlagNeuralTimeout = 64;   // sticky flag: a tensor-core wait of the neural shader timed out
 
 // Point and line draws (sglc_lines.cu; RendererSoft.cpp:301-321, 409-487, 575-712). Every input
 // primitive owns three slots (a point draw uses one, a line draw one, a triangle drawn as points or

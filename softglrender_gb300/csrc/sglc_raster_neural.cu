@@ -108,8 +108,11 @@ __device__ __forceinline__ void ntHandOff() {
   __syncthreads();
 }
 
-__device__ __forceinline__ void ntWait(NeuralCta &n) {
-  tc::barWait(n.bar, n.phase);   // bounded; a timeout leaves this chunk's colours undefined
+// bounded wait; a timeout (or the injected one of a test) leaves this chunk's colours unspecified
+// and is reported through the draw's device error flag
+__device__ __forceinline__ void ntWait(const DrawParams &p, NeuralCta &n) {
+  const bool ok = tc::barWait(n.bar, n.phase);
+  if ((!ok || p.nnInjectTimeout) && p.errFlags) atomicOr(p.errFlags, kFlagNeuralTimeout);
   n.phase ^= 1u;
   tc::fenceAfter();
 }
@@ -149,7 +152,7 @@ __device__ __forceinline__ void neuralFlush(const DrawParams &p, NeuralCta &n, F
       for (int w = 0; w < 2; w++) issueKMajor(n.tmem + 128 * w, n.sX[w], 80, 0, n.sW1, kK1, 0, 64, 80, false);
       tc::commit(n.bar);
     }
-    ntWait(n);
+    ntWait(p, n);
     // layer 1, features 80-159 (the tile is free again)
     encodeChunks<10, 20>(pre.x, n.xTile, n.row, 80, false);
     ntHandOff();
@@ -158,7 +161,7 @@ __device__ __forceinline__ void neuralFlush(const DrawParams &p, NeuralCta &n, F
       for (int w = 0; w < 2; w++) issueKMajor(n.tmem + 128 * w, n.sX[w], 80, 0, n.sW1, kK1, 80, 64, 80, true);
       tc::commit(n.bar);
     }
-    ntWait(n);
+    ntWait(p, n);
     hiddenEpilogue(n.lanes, n.bias, n.xTile, n.row, 64, 0);
     ntHandOff();
     if (threadIdx.x == 0) {
@@ -166,7 +169,7 @@ __device__ __forceinline__ void neuralFlush(const DrawParams &p, NeuralCta &n, F
       for (int w = 0; w < 2; w++) issueKMajor(n.tmem + 128 * w + 64, n.sX[w], 64, 0, n.sW2, 64, 0, 64, 64, false);
       tc::commit(n.bar);
     }
-    ntWait(n);
+    ntWait(p, n);
     hiddenEpilogue(n.lanes + 64, n.bias + 64, n.xTile, n.row, 64, 0);
     ntHandOff();
     if (threadIdx.x == 0) {
@@ -174,7 +177,7 @@ __device__ __forceinline__ void neuralFlush(const DrawParams &p, NeuralCta &n, F
       for (int w = 0; w < 2; w++) issueKMajor(n.tmem + 128 * w, n.sX[w], 64, 0, n.sW3, 64, 0, 16, 64, false);
       tc::commit(n.bar);
     }
-    ntWait(n);
+    ntWait(p, n);
     float y[16];
     tc::ld16(n.lanes, y);
     tc::ldWait();
@@ -360,143 +363,7 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
   if (warp == 0) tc::tmemFree(n.tmem, 256);
 }
 
-// ------------------------------------------------------------------------------------------------
-// Deferred neural shading: the network over the fragment records of k_raster_cov (sglc_raster.cuh),
-// 256 records (two M = 128 tiles) per step, persistent CTAs; nothing couples it to coverage, so
-// every step is a full tile. Colour goes to the records' colour slots for k_rop.
-// ------------------------------------------------------------------------------------------------
-constexpr int kSnX = 0;                               // 2 x [128][80] BF16 input / hidden tiles
-constexpr int kSnImg = kSnX + 2 * 128 * 80 * 2;
-constexpr int kSnBar = kSnImg + kImgBytes;        // one mbarrier per warpgroup
-constexpr int kSnTmem = kSnBar + 16;
-// at least 80 KB so that no more than two CTAs (2 x 256 TMEM columns) share an SM
-constexpr int kSnBytes = (kSnTmem + 4 + 1024) > 80 * 1024 ? (kSnTmem + 4 + 1024) : 80 * 1024;
-static_assert(kSnBytes * 3 > 227 * 1024 && kSnBytes * 2 <= 227 * 1024, "exactly two CTAs per SM");
-
-// barrier among the 128 threads of warpgroup wg (ids 1 and 2; 0 is __syncthreads)
-__device__ __forceinline__ void wgSync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory"); }
-
-// the warpgroup's smem writes become visible to its MMAs, then its issuing thread may go
-__device__ __forceinline__ void wgHandOff(int wg) {
-  tc::fenceProxyAsync();
-  tc::fenceBefore();
-  wgSync(wg);
-}
-
-// Each warpgroup runs its own tile sequence (its own mbarrier, issuing thread and named barrier), so
-// one warpgroup's tensor-core round trips overlap the other's feature and colour work.
-template<int S>
-__global__ void __launch_bounds__(256, 2) k_shade_neural(const __grid_constant__ DrawParams p) {
-  extern __shared__ __align__(1024) uint8_t smraw[];
-  uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t) 1023);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wg = warp >> 2, wgThread = threadIdx.x & 127;
-  uint8_t *xTile = sm + kSnX + wg * 128 * 80 * 2;
-  const uint32_t sX = tc::smemAddr(xTile);
-  uint8_t *img = sm + kSnImg;
-  const uint32_t sW1 = tc::smemAddr(img + kImgW1), sW2 = tc::smemAddr(img + kImgW2), sW3 = tc::smemAddr(img + kImgW3);
-  const float *bias = reinterpret_cast<const float *>(img + kImgBias);
-  uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kSnBar) + wg;
-  uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(sm + kSnTmem);
-  const int row = (warp & 3) * 32 + lane;
-  for (int i = threadIdx.x; i < kImgBytes / 16; i += 256)
-    reinterpret_cast<uint4 *>(img)[i] = __ldg(reinterpret_cast<const uint4 *>(p.nnImage) + i);
-  if (wgThread == 0) tc::barInit(bar, 1);
-  if (warp == 0) tc::tmemAlloc(tmemSlot, 256);
-  tc::fenceBefore();
-  __syncthreads();
-  tc::fenceAfter();
-  const uint32_t tmem = *tmemSlot + 128u * (uint32_t) wg;               // this warpgroup's 128 columns
-  const uint32_t lanes = tmem + ((uint32_t) ((warp & 3) * 32) << 16);   // this thread's TMEM lane
-  uint32_t phase = 0;
-  auto wait = [&]() {
-    tc::barWait(bar, phase);   // bounded; a timeout leaves this tile's colours undefined
-    phase ^= 1u;
-    tc::fenceAfter();
-  };
-
-  const int nRec = min(p.counters[kCntDense], p.chunkCap * kChunk);
-  for (int t0 = (blockIdx.x * 2 + wg) * 128; t0 < nRec; t0 += gridDim.x * 256) {
-    const int di = t0 + wgThread;
-    const int r = di < nRec ? p.recDense[di] : -1;
-    const bool valid = r >= 0;
-    NeuralPre pre;
-    if (valid) {
-      const int4 a = p.recA[r];
-      const float2 b = p.recB[r];
-      const uint32_t meta = (uint32_t) a.y;
-      const int px = a.z & 0xffff, py = (int) ((uint32_t) a.z >> 16);
-      const int qx = px - (int) ((meta >> 9) & 1u), qy = py - (int) ((meta >> 10) & 1u);
-      pre = neuralPre<S>(p, viewUniforms(p, (int) (meta >> 11)), a.x, qx, qy, px, py, __int_as_float(a.w), b.x, b.y);
-    } else {
-#pragma unroll
-      for (int i = 0; i < kIn; i++) pre.x[i] = 0.f;
-      pre.lo0 = pre.lo1 = pre.lo2 = pre.alpha = pre.ao = pre.e0 = pre.e1 = pre.e2 = 0.f;
-    }
-    // layer 1, features 0-79
-    encodeChunks<0, 10>(pre.x, xTile, row, 80, false);
-    wgHandOff(wg);
-    if (wgThread == 0) {
-      tc::fenceAfter();
-      issueKMajor(tmem, sX, 80, 0, sW1, kK1, 0, 64, 80, false);
-      tc::commit(bar);
-    }
-    wait();
-    // layer 1, features 80-159 (the tile is free again)
-    encodeChunks<10, 20>(pre.x, xTile, row, 80, false);
-    wgHandOff(wg);
-    if (wgThread == 0) {
-      tc::fenceAfter();
-      issueKMajor(tmem, sX, 80, 0, sW1, kK1, 80, 64, 80, true);
-      tc::commit(bar);
-    }
-    wait();
-    hiddenEpilogue(lanes, bias, xTile, row, 64, 0);
-    wgHandOff(wg);
-    if (wgThread == 0) {
-      tc::fenceAfter();
-      issueKMajor(tmem + 64, sX, 64, 0, sW2, 64, 0, 64, 64, false);
-      tc::commit(bar);
-    }
-    wait();
-    hiddenEpilogue(lanes + 64, bias + 64, xTile, row, 64, 0);
-    wgHandOff(wg);
-    if (wgThread == 0) {
-      tc::fenceAfter();
-      issueKMajor(tmem, sX, 64, 0, sW3, 64, 0, 16, 64, false);
-      tc::commit(bar);
-    }
-    wait();
-    float y[16];
-    tc::ld16(lanes, y);
-    tc::ldWait();
-    tc::fenceBefore();
-    if (valid) {
-      float a0 = gmax(y[0] + bias[128], 0.f), a1 = gmax(y[1] + bias[129], 0.f), a2 = gmax(y[2] + bias[130], 0.f);
-      f3 ambient = mk3(a0 * a0, a1 * a1, a2 * a2) * pre.ao;
-      p.recColor[r] = pbrFinish(p, ambient, mk3(pre.lo0, pre.lo1, pre.lo2), mk3(pre.e0, pre.e1, pre.e2), pre.alpha);
-    }
-    wgSync(wg);   // every thread has read its TMEM lane before the next tile's layer 1 overwrites it
-  }
-  tc::fenceBefore();
-  __syncthreads();
-  tc::fenceAfter();
-  if (warp == 0) tc::tmemFree(*tmemSlot, 256);
-}
-
 // A failed attribute set makes the launch after it fail; the draw reports that launch error.
-template<int S>
-static void launchShadeNeuralS(const DrawParams &p, cudaStream_t st) {
-  static PerDeviceAttr attr;
-  setDynamicSmemOnce(attr, k_shade_neural<S>, kSnBytes);
-  k_shade_neural<S><<<152 * 2, 256, kSnBytes, st>>>(p);
-}
-
-void launchShadeNeural(const DrawParams &p, cudaStream_t st) {
-  if (p.samples == 4) launchShadeNeuralS<4>(p, st);
-  else launchShadeNeuralS<1>(p, st);
-}
-
 template<int S, bool D>
 static void launchNeural(const DrawParams &p, int grid, cudaStream_t st) {
   static PerDeviceAttr attr;

@@ -1,0 +1,310 @@
+// Deferred neural PBR shading: the fragment records of k_raster_cov (sglc_raster.cuh) shaded by the
+// PBR fragment shader (PbrSoft.h:225-322) with its image-based-lighting term (PbrSoft.h:291-309:
+// irradiance fetch, prefiltered-cube fetch at a roughness LOD, FresnelSchlickRoughness,
+// EnvBRDFApprox) evaluated by the MLP of sglc_nn.cuh on the tensor cores.
+//
+// This path is judged by PSNR against the exact shader, not bit for bit, so its surface terms take
+// the GPU's own fast paths where the exact shader has to reproduce the reference's arithmetic:
+//   * the material maps (albedo, normal, metal-roughness, ao, emissive) are sampled by the texture
+//     units from a hardware copy of each texture (same level contents, same filter / wrap / mip
+//     mode, trilinear filtering in fixed-function hardware), sglc_api.cu keeps the copies current;
+//   * the texture-coordinate derivatives for the LOD come from the triangle's screen-space
+//     barycentric gradients at the shading sample (analytic), instead of re-evaluating the 2x2
+//     quad's neighbours (ShaderSoft.h:117-133);
+//   * pow, reciprocal and normalisation use the fast intrinsics.
+//
+// Kernel layout: one persistent CTA per SM with four warpgroups (512 threads). Each warpgroup
+// walks its own sequence of 128-record tiles: every thread evaluates one record's surface terms
+// and writes the network's 160 input features into its row of the warpgroup's [128][160] BF16
+// tile; one elected thread issues the three layers' tcgen05.mma chains (layer 1 over K = 160 in
+// one chain, then 64 -> 64 and 64 -> 3), each completed through the warpgroup's mbarrier; the
+// epilogues read the FP32 accumulators back from the warpgroup's 128 TMEM columns (bias, ReLU and
+// the BF16 conversion in packed f32x2 / bf16x2 instructions) into the same tile. The four
+// warpgroups' tensor-core round trips overlap each other's surface and feature work.
+// A wait that runs out of polls sets the draw's device error flag (kFlagNeuralTimeout in the
+// context's sticky flags, read by sglc_get_overflow); that tile's colours are then unspecified.
+#include "sglc_raster.cuh"
+#include "sglc_host_util.h"
+#include "sglc_nn.cuh"
+
+namespace sglc {
+
+using namespace nn;
+
+namespace {
+
+constexpr int kWG = 4;                                      // warpgroups per CTA (one CTA per SM)
+constexpr int kThreads = 128 * kWG;
+constexpr int kXBytes = 128 * kK1 * 2;                      // [128][160] BF16 tile of one warpgroup
+constexpr int kSnX = 0;
+constexpr int kSnImg = kSnX + kWG * kXBytes;                // weight image (sglc_nn.cuh)
+constexpr int kSnBar = kSnImg + kImgBytes;                  // one mbarrier per warpgroup
+constexpr int kSnTmem = kSnBar + kWG * 8;
+constexpr int kSnBytes = kSnTmem + 16 + 1024;               // + slack for the 1024-B alignment
+static_assert(kSnImg % 1024 == 0 && kSnBar % 8 == 0, "tile and barrier alignment");
+static_assert(kSnBytes <= 227 * 1024, "fits one CTA per SM");
+
+// barrier among the 128 threads of warpgroup wg (ids 1..4; 0 is __syncthreads)
+__device__ __forceinline__ void wgSync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory"); }
+
+// the warpgroup's shared-memory writes become visible to the tensor core, then its issuer may go
+__device__ __forceinline__ void wgHandOff(int wg) {
+  tc::fenceProxyAsync();
+  tc::fenceBefore();
+  wgSync(wg);
+}
+
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+
+// (a0 + b0, a1 + b1) in one packed FP32 instruction, then ReLU and round to BF16 pairs
+__device__ __forceinline__ uint32_t biasReluBf16(float a0, float a1, float b0, float b1) {
+  unsigned long long s;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(s) : "l"(pack2(a0, a1)), "l"(pack2(b0, b1)));
+  float s0, s1;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(s0), "=f"(s1) : "l"(s));
+  uint32_t r;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(s1), "f"(s0));
+  return r;
+}
+
+// hidden-layer epilogue of one row: 64 accumulator columns + bias, ReLU, BF16 into row `row` of a
+// 64-column tile (same values as hiddenEpilogue in sglc_nn.cuh, in packed instructions)
+__device__ __forceinline__ void hiddenRow(uint32_t taddr, const float *bias, uint8_t *out, int row) {
+#pragma unroll
+  for (int h = 0; h < 4; h++) {
+    float a[16];
+    tc::ld16(taddr + 16 * h, a);
+    tc::ldWait();
+    uint32_t w[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) w[j] = biasReluBf16(a[2 * j], a[2 * j + 1], bias[16 * h + 2 * j], bias[16 * h + 2 * j + 1]);
+    *reinterpret_cast<uint4 *>(out + tc::tileOffset(row, 16 * h, 64)) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4 *>(out + tc::tileOffset(row, 16 * h + 8, 64)) = make_uint4(w[4], w[5], w[6], w[7]);
+  }
+}
+
+// a material map through the texture units: derivative LOD where the reference installs its LOD
+// callback on the sampler (PbrSoft.h:138-151), else level 0
+__device__ __forceinline__ float4 hwSample(const DrawParams &p, int slot, float u, float v, float dudx, float dvdx,
+                                           float dudy, float dvdy) {
+  const cudaTextureObject_t t = p.hwTex[slot];
+  if (!t) return make_float4(0.f, 0.f, 0.f, 0.f);   // no 2D RGBA8 texture bound: as the exact sampler
+  if (p.samp[slot].lodFromDerivative)
+    return tex2DGrad<float4>(t, u, v, make_float2(dudx, dvdx), make_float2(dudy, dvdy));
+  return tex2DLod<float4>(t, u, v, 0.f);
+}
+
+__device__ __forceinline__ f3 fastNormalize(f3 v) { return v * rsqrtf(dot3(v, v)); }
+
+// surface terms and network inputs of one fragment record
+struct Surface {
+  float x[kIn];
+  f3 Lo, emissive;
+  float ao, alpha;
+};
+
+__device__ __forceinline__ Surface surface(const DrawParams &p, int4 a, float2 b) {
+  const int tri = a.x;
+  const uint32_t meta = (uint32_t) a.y;
+  const float b0 = __int_as_float(a.w), b1 = b.x, b2 = b.y;
+  const uint8_t *U = viewUniforms(p, (int) (meta >> 11));
+  const Tri t = loadTri(p.tri + tri);
+  const float *r0 = p.vVary + (size_t) t.vid0 * p.varyStride;
+  const float *r1 = p.vVary + (size_t) t.vid1 * p.varyStride;
+  const float *r2 = p.vVary + (size_t) t.vid2 * p.varyStride;
+  const Vary vy{r0, r1, r2, b0, b1, b2};
+  const float u = vy[0], v = vy[1];
+  float dudx = 0.f, dvdx = 0.f, dudy = 0.f, dvdy = 0.f;
+  if (p.needDeriv) {
+    // screen-space gradients of the linear barycentrics (the reference's barycentric(),
+    // RendererSoft.cpp:1021-1056, differentiated), then of the perspective-correct ones
+    // b_i = l_i w_i / D, D = sum l_j w_j, 1 / D = sum b_j / w_j
+    const float a0 = t.f0x - t.v0x, a1 = t.f0y - t.v0x, c0 = t.f1x - t.v0y, c1 = t.f1y - t.v0y;
+    const float iuz = __fdividef(1.f, a0 * c1 - a1 * c0);
+    const float l1x = -c0 * iuz, l1y = a0 * iuz, l2x = c1 * iuz, l2y = -a1 * iuz;
+    const float l0x = -(l1x + l2x), l0y = -(l1y + l2y);
+    const float invD = __fdividef(b0, t.w0) + __fdividef(b1, t.w1) + __fdividef(b2, t.w2);
+    const float dDx = t.w0 * l0x + t.w1 * l1x + t.w2 * l2x, dDy = t.w0 * l0y + t.w1 * l1y + t.w2 * l2y;
+    const float g0x = (t.w0 * l0x - b0 * dDx) * invD, g0y = (t.w0 * l0y - b0 * dDy) * invD;
+    const float g1x = (t.w1 * l1x - b1 * dDx) * invD, g1y = (t.w1 * l1y - b1 * dDy) * invD;
+    const float g2x = (t.w2 * l2x - b2 * dDx) * invD, g2y = (t.w2 * l2y - b2 * dDy) * invD;
+    const float u0 = __ldg(r0), u1 = __ldg(r1), u2 = __ldg(r2);
+    const float v0 = __ldg(r0 + 1), v1 = __ldg(r1 + 1), v2 = __ldg(r2 + 1);
+    dudx = u0 * g0x + u1 * g1x + u2 * g2x;
+    dudy = u0 * g0y + u1 * g1y + u2 * g2y;
+    dvdx = v0 * g0x + v1 * g1x + v2 * g2x;
+    dvdy = v0 * g0y + v1 * g1y + v2 * g2y;
+  }
+  Surface s;
+  const float4 arg = p.def[0] ? hwSample(p, 0, u, v, dudx, dvdx, dudy, dvdy) : uV4(U, 352);
+  const f3 albedo = mk3(__powf(arg.x, 2.2f), __powf(arg.y, 2.2f), __powf(arg.z, 2.2f));
+  float metallic = 0.f, roughness = 1.f;
+  if (p.def[4]) {
+    const float4 mr = hwSample(p, 4, u, v, dudx, dvdx, dudy, dvdy);
+    metallic = mr.z;
+    roughness = mr.y;
+  }
+  s.ao = p.def[3] ? hwSample(p, 3, u, v, dudx, dvdx, dudy, dvdy).x : 1.f;
+  f3 N;
+  if (p.def[1]) {
+    const f3 Nv = fastNormalize(vy.v3(20));
+    f3 T = fastNormalize(vy.v3(24));
+    T = fastNormalize(T - dot3(T, Nv) * Nv);
+    const f3 B = cross3(T, Nv);
+    const float4 tn4 = hwSample(p, 1, u, v, dudx, dvdx, dudy, dvdy);
+    const f3 tn = mk3(tn4.x * 2.f - 1.f, tn4.y * 2.f - 1.f, tn4.z * 2.f - 1.f);
+    N = fastNormalize(mk3(T.x * tn.x + B.x * tn.y + Nv.x * tn.z, T.y * tn.x + B.y * tn.y + Nv.y * tn.z,
+                          T.z * tn.x + B.z * tn.y + Nv.z * tn.z));
+  } else {
+    N = fastNormalize(vy.v3(4));
+  }
+  const f3 V = fastNormalize(vy.v3(12));
+  const float NdotV = gmax(dot3(N, V), 0.f);
+  f3 Lo = mk3(0.f, 0.f, 0.f);
+  if (uI32(U, 320)) {   // the point light's GGX term (PbrSoft.h:258-290), fast arithmetic
+    const float PI = 3.14159265359f;
+    const f3 ldir = vy.v3(16);
+    const f3 L = fastNormalize(ldir);
+    const f3 H = fastNormalize(V + L);
+    const f3 lDir = ldir * 0.2f;
+    const float att = gclamp(1.f - dot3(lDir, lDir), 0.f, 1.f);
+    const f3 radiance = ld3(U + 304) * att;
+    const float al = roughness * roughness, a2 = al * al;
+    const float NdotH = gmax(dot3(N, H), 0.f);
+    const float den = NdotH * NdotH * (a2 - 1.f) + 1.f;
+    const float NDF = __fdividef(a2, PI * den * den);
+    const float NdotL = gmax(dot3(N, L), 0.f);
+    const float r1 = roughness + 1.f, k = r1 * r1 * 0.125f;
+    const float G = __fdividef(NdotL, NdotL * (1.f - k) + k) * __fdividef(NdotV, NdotV * (1.f - k) + k);
+    const float ct = gmax(dot3(H, V), 0.f);
+    const float om = gclamp(1.f - ct, 0.f, 1.f), om2 = om * om, p5 = om2 * om2 * om;
+    const f3 F0 = mk3(0.04f, 0.04f, 0.04f) * (1.f - metallic) + albedo * metallic;
+    const f3 F = F0 + (1.f - F0) * p5;
+    const float spec = __fdividef(NDF * G, 4.f * NdotV * NdotL + 0.0001f);
+    const f3 kD = (1.f - F) * (1.f - metallic);
+    Lo = (kD * albedo * (1.f / PI) + F * spec) * radiance * NdotL;
+  }
+  s.Lo = Lo;
+  s.emissive = mk3(0.f, 0.f, 0.f);
+  if (p.def[2]) {
+    const float4 e = hwSample(p, 2, u, v, dudx, dvdx, dudy, dvdy);
+    s.emissive = mk3(e.x, e.y, e.z);
+  }
+  s.alpha = arg.w;
+  s.x[0] = N.x; s.x[1] = N.y; s.x[2] = N.z;
+  s.x[3] = V.x; s.x[4] = V.y; s.x[5] = V.z;
+  s.x[6] = roughness; s.x[7] = metallic;
+  s.x[8] = arg.x; s.x[9] = arg.y; s.x[10] = arg.z;
+  s.x[11] = NdotV;
+  return s;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_constant__ DrawParams p) {
+  extern __shared__ __align__(1024) uint8_t smraw[];
+  uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t) 1023);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wg = warp >> 2, wgThread = threadIdx.x & 127;
+  uint8_t *xTile = sm + kSnX + wg * kXBytes;
+  const uint32_t sX = tc::smemAddr(xTile);
+  uint8_t *img = sm + kSnImg;
+  const uint32_t sW1 = tc::smemAddr(img + kImgW1), sW2 = tc::smemAddr(img + kImgW2), sW3 = tc::smemAddr(img + kImgW3);
+  const float *bias = reinterpret_cast<const float *>(img + kImgBias);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kSnBar) + wg;
+  uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(sm + kSnTmem);
+  const int row = (warp & 3) * 32 + lane;
+  for (int i = threadIdx.x; i < kImgBytes / 16; i += kThreads)
+    reinterpret_cast<uint4 *>(img)[i] = __ldg(reinterpret_cast<const uint4 *>(p.nnImage) + i);
+  if (wgThread == 0) tc::barInit(bar, 1);
+  if (warp == 0) tc::tmemAlloc(tmemSlot, 128 * kWG);
+  tc::fenceBefore();
+  __syncthreads();
+  tc::fenceAfter();
+  const uint32_t tmem = *tmemSlot + 128u * (uint32_t) wg;               // this warpgroup's 128 columns
+  const uint32_t lanes = tmem + ((uint32_t) ((warp & 3) * 32) << 16);   // this thread's TMEM lane
+  uint32_t phase = 0;
+  bool timedOut = false;
+  // bounded wait on the warpgroup's mbarrier; a timeout is recorded once and reported to the host
+  auto wait = [&]() {
+    const bool ok = tc::barWait(bar, phase);
+    if (!ok || p.nnInjectTimeout) timedOut = true;
+    phase ^= 1u;
+    tc::fenceAfter();
+  };
+
+  const int nRec = min(p.counters[kCntDense], p.chunkCap * kChunk);
+  for (int t0 = (blockIdx.x * kWG + wg) * 128; t0 < nRec; t0 += gridDim.x * kThreads) {
+    const int di = t0 + wgThread;
+    const int r = di < nRec ? p.recDense[di] : -1;
+    const bool valid = r >= 0;
+    Surface s;
+    if (valid) {
+      s = surface(p, p.recA[r], p.recB[r]);
+    } else {
+#pragma unroll
+      for (int i = 0; i < kIn; i++) s.x[i] = 0.f;
+      s.Lo = s.emissive = mk3(0.f, 0.f, 0.f);
+      s.ao = s.alpha = 0.f;
+    }
+    encodeRow(s.x, xTile, row, false);
+    wgHandOff(wg);
+    if (wgThread == 0) {   // layer 1: [128 x 160] x [160 x 64]
+      tc::fenceAfter();
+      issueKMajor(tmem, sX, kK1, 0, sW1, kK1, 0, kHid, kK1, false);
+      tc::commit(bar);
+    }
+    wait();
+    hiddenRow(lanes, bias, xTile, row);
+    wgHandOff(wg);
+    if (wgThread == 0) {   // layer 2: [128 x 64] x [64 x 64]
+      tc::fenceAfter();
+      issueKMajor(tmem + 64, sX, kHid, 0, sW2, kHid, 0, kHid, kHid, false);
+      tc::commit(bar);
+    }
+    wait();
+    hiddenRow(lanes + 64, bias + 64, xTile, row);
+    wgHandOff(wg);
+    if (wgThread == 0) {   // layer 3: [128 x 64] x [64 x 16] (3 outputs used)
+      tc::fenceAfter();
+      issueKMajor(tmem, sX, kHid, 0, sW3, kHid, 0, kOutPad, kHid, false);
+      tc::commit(bar);
+    }
+    wait();
+    float y[16];
+    tc::ld16(lanes, y);
+    tc::ldWait();
+    tc::fenceBefore();
+    if (valid) {
+      // ambient = max(y, 0)^2 * ao; colour = (ambient + Lo)^(1/2.2) + emissive (PbrSoft.h:311-321)
+      const float a0 = gmax(y[0] + bias[128], 0.f), a1 = gmax(y[1] + bias[129], 0.f), a2 = gmax(y[2] + bias[130], 0.f);
+      const f3 c = mk3(a0 * a0, a1 * a1, a2 * a2) * s.ao + s.Lo;
+      f3 col = mk3(__powf(c.x, 1.f / 2.2f), __powf(c.y, 1.f / 2.2f), __powf(c.z, 1.f / 2.2f));
+      if (p.def[2]) col = col + s.emissive;
+      p.recColor[r] = make_float4(col.x, col.y, col.z, s.alpha);
+    }
+    // every thread has read its TMEM lane and its tile row before the next tile overwrites them
+    wgSync(wg);
+  }
+  if (timedOut && p.errFlags) atomicOr(p.errFlags, kFlagNeuralTimeout);
+  tc::fenceBefore();
+  __syncthreads();
+  tc::fenceAfter();
+  if (warp == 0) tc::tmemFree(*tmemSlot, 128 * kWG);
+}
+
+}  // namespace
+
+// One CTA per SM. A failed attribute set makes the launch after it fail; the draw reports that
+// launch error.
+void launchShadeNeural(const DrawParams &p, cudaStream_t st) {
+  static PerDeviceAttr attr;
+  setDynamicSmemOnce(attr, k_shade_neural, kSnBytes);
+  int sms = 152, dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_shade_neural<<<sms, kThreads, kSnBytes, st>>>(p);
+}
+
+}  // namespace sglc

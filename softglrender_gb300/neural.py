@@ -44,6 +44,7 @@ NEURAL_SIGS = {
     "neural_gradients": ([_P, C.c_int64, C.c_int64, _P, C.POINTER(C.c_float)], C.c_int32),
     "neural_infer": ([_P, C.c_int64, C.c_int64, _P], C.c_int32),
     "program_set_neural_shader": ([_P, C.c_int32, _P], C.c_int32),
+    "neural_set_test_flags": ([_P, C.c_int32], C.c_int32),
 }
 NEURAL_FUNCTIONS = tuple(NEURAL_SIGS)
 
@@ -146,6 +147,14 @@ class NeuralShader:
     def bind(self, program: A.ShaderProgram) -> None:
         self._check(self.fn["program_set_neural_shader"](self.r.ctx, program.handle, self.h),
                     "program_set_neural_shader")
+
+    @staticmethod
+    def set_test_flags(renderer: A.Renderer, flags: int) -> None:
+        """Test hook: flag 1 makes every completed tensor-core wait of the neural shading kernels
+        report a timeout (sticky flag bit 6, Renderer.getOverflow)."""
+        st = _bind(renderer.lib.cdll)["neural_set_test_flags"](renderer.ctx, flags)
+        if st != 0:
+            raise A.SoftGLError(st, "sglc_neural_set_test_flags", "invalid flags")
 
     @staticmethod
     def unbind(renderer: A.Renderer, program: A.ShaderProgram) -> None:

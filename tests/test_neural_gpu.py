@@ -173,3 +173,28 @@ def test_neural_pipeline_gains_over_the_method_without_it(cuda_lib):
     assert rep.bound == (rep.psnr_mean >= 40.0)
     net.destroy()
     r.destroy()
+
+
+@pytest.mark.parametrize("deferred", [True, False])
+def test_neural_wait_timeouts_reach_the_host(cuda_lib, deferred):
+    """A tensor-core wait that times out is reported through the sticky flags (bit 6). The test hook
+    reports a timeout after each wait has completed normally (nothing is abandoned in flight);
+    without it a frame reports nothing."""
+    r = A.Renderer(cuda_lib, 0)
+    r.setDeferredShading(deferred)
+    net = NeuralShader(r, seed=4)
+    inst = S.SceneInstance(r, _small_pbr(view=1))
+    for prog in pbr_programs(inst):
+        net.bind(prog)
+    inst.render()
+    assert r.getOverflow() == 0
+    NeuralShader.set_test_flags(r, 1)
+    inst.render()
+    assert r.getOverflow() & 64
+    NeuralShader.set_test_flags(r, 0)
+    inst.render()
+    assert r.getOverflow() == 0
+    with pytest.raises(A.SoftGLError):
+        NeuralShader.set_test_flags(r, 2)
+    net.destroy()
+    r.destroy()
