@@ -150,6 +150,31 @@ def profiled_traffic(name="k_raster_cov_pbr_ibl_1080p_msaa4.md"):
     return None
 
 
+def profiled_value(name, key):
+    """A `key: <int>` line of a committed ncu summary under profiles/, or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", name)) as f:
+            for line in f:
+                if line.startswith(key + ":"):
+                    return int(line.split(":")[1])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def issue_roofline(warp_instructions, kernel_ms, sm_mhz, sms=152):
+    """The issue-rate bound of a kernel: its warp instructions per launch (ncu
+    smsp__inst_executed.sum) against the SMs' peak issue rate (4 schedulers per SM, one warp
+    instruction per scheduler per clock) over the kernel's CUDA-event time."""
+    if not warp_instructions or not kernel_ms or not sm_mhz:
+        return None
+    peak = sms * 4 * sm_mhz * 1e6
+    achieved = warp_instructions / (kernel_ms * 1e-3)
+    return {"warp_instructions_per_launch": int(warp_instructions), "sm_mhz": sm_mhz,
+            "peak_warp_inst_per_s": peak, "achieved_warp_inst_per_s": round(achieved, 1),
+            "frac": round(achieved / peak, 4)}
+
+
 def build_scene():
     from softglrender_gb300 import scenes as S
     return S.config_pbr()
@@ -825,6 +850,11 @@ def main():
         "clocks": clocks.summary(),
         "submission": plain_sub,
     }
+    # the coverage kernel is issue- and latency-bound (its frame stays in L2): its issue-rate
+    # fraction beside the HBM one, from the committed profile's instruction count
+    result["roofline"]["issue"] = issue_roofline(
+        profiled_value("k_raster_cov_pbr_ibl_1080p_msaa4.md", "warp_instructions_per_launch"), cov_ms,
+        result["clocks"].get("sm_mhz") or 2070.0)
     result["clocks"]["window"] = (f"{preroll} untimed frames (>= 1.2 s) of the same submission, then the "
                                   f"{args.steps} timed frames")
     result.update(configs12)

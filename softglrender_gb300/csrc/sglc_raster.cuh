@@ -233,6 +233,55 @@ struct Samples4 {
   float d0, d1, d2, d3;
 };
 
+// Hierarchical depth rejection for the four ordered depth functions. A sample's depth is the
+// interpolation (b0 z0 + b1 z1) + b2 z2 with barycentrics in [0, 1] summing to 1 within rounding,
+// so every covered sample of a triangle lies in [min z_i, max z_i] up to a few ulps; clamping to the
+// depth range keeps that order. If the triangle's whole range fails the test against the most
+// permissive depth stored in a set of samples (the minimum for GREATER / GEQUAL, the maximum for
+// LESS / LEQUAL), none of its samples there can pass, now or later in the draw (with depth writes
+// the stored depth only moves further in the test's direction), so the triangle is skipped for
+// them. kHizMargin covers the rounding of the interpolation.
+enum { HIZ_NONE = 0, HIZ_GREATER, HIZ_GEQUAL, HIZ_LESS, HIZ_LEQUAL };
+constexpr float kHizMargin = 1e-6f;
+
+__device__ __forceinline__ int hizMode(const DrawParams &p, bool hasDepth) {
+  if (!(p.depthTest && hasDepth)) return HIZ_NONE;
+  switch (p.depthFunc) {
+    case DEPTH_GREATER: return HIZ_GREATER;
+    case DEPTH_GEQUAL: return HIZ_GEQUAL;
+    case DEPTH_LESS: return HIZ_LESS;
+    case DEPTH_LEQUAL: return HIZ_LEQUAL;
+  }
+  return HIZ_NONE;
+}
+
+// the most permissive stored depth of one pixel's samples for the mode (NaN samples pass nothing
+// under an ordered test: they are left out)
+template<int S>
+__device__ __forceinline__ float hizPixelBound(int mode, const Samples4 &fb, bool inD) {
+  const float inf = __int_as_float(0x7f800000);
+  const bool lower = mode == HIZ_GREATER || mode == HIZ_GEQUAL;
+  float b = lower ? inf : -inf;
+  if (!inD || mode == HIZ_NONE) return b;
+  const float d[4] = {fb.d0, fb.d1, fb.d2, fb.d3};
+#pragma unroll
+  for (int q = 0; q < S; q++)
+    if (d[q] == d[q]) b = lower ? fminf(b, d[q]) : fmaxf(b, d[q]);
+  return b;
+}
+
+// true: a triangle whose depths lie in [zmin, zmax] passes the test at no sample with stored depth
+// bound `bound` (hizPixelBound, or its minimum / maximum over several pixels)
+__device__ __forceinline__ bool hizReject(int mode, float zmin, float zmax, float bound) {
+  switch (mode) {
+    case HIZ_GREATER: return zmax + kHizMargin * (fabsf(zmax) + 1.f) <= bound;
+    case HIZ_GEQUAL: return zmax + kHizMargin * (fabsf(zmax) + 1.f) < bound;
+    case HIZ_LESS: return zmin - kHizMargin * (fabsf(zmin) + 1.f) >= bound;
+    case HIZ_LEQUAL: return zmin - kHizMargin * (fabsf(zmin) + 1.f) > bound;
+  }
+  return false;
+}
+
 // per-warp fragment queue in shared memory (phase A appends, phase B shades, phase C applies)
 constexpr int kQueue = 64;
 struct FragQueue {
@@ -396,7 +445,8 @@ __device__ __forceinline__ uint32_t depthOps(const DrawParams &p, const Cover &c
 // (bit = batch index); `prim` = this lane's primitive id.
 template<int S>
 __device__ __forceinline__ unsigned pass1Prim(const DrawParams &p, int prim, int lane, int rx0, int ry0, float lo, float hi,
-                                              float vpExtent, unsigned *candS, int rh = 4) {
+                                              float vpExtent, unsigned *candS, int rh = 4, int hiz = HIZ_NONE,
+                                              float hizBound = 0.f) {
   bool hit = false;
   int4 r = make_int4(0, -1, 0, -1);
   float ea[3] = {0.f, 0.f, 0.f}, eb[3] = {0.f, 0.f, 0.f}, ek[3] = {0.f, 0.f, 0.f}, et[3] = {0.f, 0.f, 0.f};
@@ -415,6 +465,10 @@ __device__ __forceinline__ unsigned pass1Prim(const DrawParams &p, int prim, int
       // |uz| is below FLT_EPSILON covers nothing (RendererSoft.cpp:1035-1037)
       uz = (q0.z - q0.x) * (q1.z - q0.y) - (q0.w - q0.x) * (q1.y - q0.y);
       if (fabsf(uz) < 1.19209290e-07f) hit = false;
+    }
+    if (hit && hiz != HIZ_NONE) {   // the whole triangle fails the depth test at every warp pixel
+      const float4 q2 = __ldg(reinterpret_cast<const float4 *>(tp) + 2);   // z0 z1 z2 w0
+      if (hizReject(hiz, fminf(q2.x, fminf(q2.y, q2.z)), fmaxf(q2.x, fmaxf(q2.y, q2.z)), hizBound)) hit = false;
     }
     if (hit) {
       float X[3] = {q0.x, q0.w, q0.z}, Y[3] = {q0.y, q1.z, q1.y};     // v0, v1, v2
@@ -766,6 +820,7 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
   const bool scanDepth = !testDepth || !p.depthMask || df == DEPTH_LESS || df == DEPTH_LEQUAL ||
                          df == DEPTH_GREATER || df == DEPTH_GEQUAL;
   const float keepId = (df == DEPTH_LESS || df == DEPTH_LEQUAL) ? __int_as_float(0x7f800000) : __int_as_float(0xff800000);
+  const int hiz = hizMode(p, HAS_DEPTH);
   // appends one record per lane with a non-zero sample mask, in lane order, to this warp's list
   auto appendRecords = [&](uint32_t mask, uint32_t meta, int prim, uint32_t pixw, float b0, float b1, float b2) {
     const unsigned want = __ballot_sync(0xffffffffu, mask != 0);
@@ -824,7 +879,18 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
     if (lane < rest) queue[lane] = keep;
     qn = rest;
     __syncwarp();
-    unsigned cand = pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent, candMasks[warp], rh);
+    // depth bounds of this lane's pixel and of the warp's pixels at the start of the batch
+    const float pixBound = hizPixelBound<S>(hiz, fb, inD);
+    float warpBound = pixBound;
+    if (hiz != HIZ_NONE) {
+      const bool lower = hiz == HIZ_GREATER || hiz == HIZ_GEQUAL;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        const float v = __shfl_xor_sync(0xffffffffu, warpBound, o);
+        warpBound = lower ? fminf(warpBound, v) : fmaxf(warpBound, v);
+      }
+    }
+    unsigned cand = pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent, candMasks[warp], rh, hiz, warpBound);
     if (!inPix) cand = 0;
     // pass 2, load-balanced: the (pixel, candidate) pairs of the batch, pixel-major in candidate
     // order, are evaluated 32 at a time by all lanes (coverage does not depend on the depth buffer);
@@ -862,13 +928,19 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
         }
       }
       const int pr = __shfl_sync(0xffffffffu, prim, pos & 31);
+      const float boundL = __shfl_sync(0xffffffffu, pixBound, L);
       CovSlot sl;
       sl.nq = 0;
       if (kk < pairs) {
         const int lpx = rx0 + (L & 7), lpy = ry0 + (L >> 3);
         const TriSetup *tp = p.tri + pr;
         int x0 = 0, x1 = 0, y0 = 0, y1 = 0, nx = 0;
-        int nq = quadsOf(tp, lpx, lpy, x0, x1, y0, y1, nx);
+        bool culled = false;
+        if (hiz != HIZ_NONE) {   // the triangle fails the depth test at every sample of pixel L
+          const float4 q2 = __ldg(reinterpret_cast<const float4 *>(tp) + 2);
+          culled = hizReject(hiz, fminf(q2.x, fminf(q2.y, q2.z)), fmaxf(q2.x, fmaxf(q2.y, q2.z)), boundL);
+        }
+        int nq = culled ? 0 : quadsOf(tp, lpx, lpy, x0, x1, y0, y1, nx);
         Cover cv;
         cv.mask = 0u;
         if (nq) cv = coverSamples<S>(p, loadTriCov(tp), lpx, lpy);

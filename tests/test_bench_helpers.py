@@ -67,3 +67,12 @@ def test_raster_launch_bytes_counts_reads_only_when_not_cleared():
     assert a == n * 4 + 64 * 32 * 4 + n * 4                       # colour + resolved + depth write
     b = bench.raster_launch_bytes(64, 32, 4, False, blend, 10, 5, 8)
     assert b == n * 4 + 64 * 32 * 4 + n * 4 + n * 4 + 10 * 132 + 5 * 3 * 8 * 4   # + colour, depth reads
+
+
+def test_issue_roofline_from_the_committed_profile():
+    w = bench.profiled_value("k_raster_cov_pbr_ibl_1080p_msaa4.md", "warp_instructions_per_launch")
+    assert isinstance(w, int) and w > 1_000_000
+    r = bench.issue_roofline(w, 0.2, 2000.0)
+    assert r["peak_warp_inst_per_s"] == 152 * 4 * 2000e6
+    assert abs(r["frac"] - w / 0.2e-3 / (152 * 4 * 2000e6)) < 1e-3
+    assert bench.issue_roofline(None, 0.2, 2000.0) is None
