@@ -417,7 +417,7 @@ def bench_batched_views(r, stream, with_cpu: bool):
     return out
 
 
-def bench_uneven_lanes(r, cfg, u, per_scene, net, lanes: int = 4):
+def bench_uneven_lanes(r, cfg, u, per_scene, net, materials, lanes: int = 4):
     """The uneven batch over `lanes` renderers whose submissions run concurrently (scenes
     assigned longest first by their measured single-scene times); the batch time runs from an
     event every lane's stream waits on to the last lane's end. Plain shaders, then the neural
@@ -470,8 +470,10 @@ def bench_uneven_lanes(r, cfg, u, per_scene, net, lanes: int = 4):
         for x, b in zip(rs, ul.batches):
             nn = NeuralShader(x)
             nn.set_params(params)
-            for prog in b.pbr_programs():
-                nn.bind(prog)
+            for m, keep in materials.items():
+                for prog in b.pbr_programs(m):
+                    if keep:
+                        nn.bind(prog)
             nets.append(nn)
         ul.tune(reps=3)
         ul.launch()
@@ -486,10 +488,11 @@ def bench_uneven_lanes(r, cfg, u, per_scene, net, lanes: int = 4):
     return res
 
 
-def bench_uneven(r, stream, net, neural_bound: bool, with_cpu: bool):
+def bench_uneven(r, stream, net, materials, with_cpu: bool):
     """64 independent scenes in one CUDA-graph submission (plain shaders, and with the neural IBL
-    shader bound to the PBR scenes when it met its threshold); per-scene frames/s from eager
-    submissions; the CPU pipeline on a sample of the scenes."""
+    shader bound to the PBR scenes of every material that met its threshold, `materials`: material
+    index -> bind); per-scene frames/s from eager submissions; the CPU pipeline on a sample of the
+    scenes."""
     import torch
     from softglrender_gb300.autotune import autotune
     from softglrender_gb300.neural import NeuralShader
@@ -522,23 +525,28 @@ def bench_uneven(r, stream, net, neural_bound: bool, with_cpu: bool):
                     "autotune": {k: v for k, v in tuned.result.describe().items() if k != "candidates"}}
     tuned.destroy()
     r.setCapacity(None)
-    if net is not None and neural_bound:
-        for prog in u.pbr_programs():
-            net.bind(prog)
+    neural_bound = net is not None and any(materials.values())
+    if neural_bound:
+        for m, keep in materials.items():
+            for prog in u.pbr_programs(m):
+                if keep:
+                    net.bind(prog)
         tuned = autotune(r, u.render, reps=3)
         n_ms = time_ms(tuned.run, 5)
         out["neural"] = {"ms_per_batch": round(n_ms, 3), "scenes_per_s": round(cfg.scenes / (n_ms / 1e3), 1),
-                         "pbr_scenes_use_network": True}
+                         "materials_using_network": sorted(m for m, k in materials.items() if k),
+                         "materials_falling_back": sorted(m for m, k in materials.items() if not k),
+                         "pbr_scenes_using_network": sum(len(u.pbr_programs(m)) for m, k in materials.items() if k)}
         tuned.destroy()
         r.setCapacity(None)
         for prog in u.pbr_programs():
             NeuralShader.unbind(r, prog)
     else:
-        out["neural"] = {"pbr_scenes_use_network": False, "reason": "network below its PSNR threshold (fallback)"}
+        out["neural"] = {"pbr_scenes_using_network": 0, "reason": "every material below its PSNR threshold (fallback)"}
     out["per_scene_fps"] = [round(1e3 / m, 1) for m in per_scene]
     out["per_scene"] = [{"tris": u.triangles[s], "res": u.plan[s]["res"], "pbr_msaa4": bool(u.plan[s]["pbr"]),
                          "ms": round(per_scene[s], 4)} for s in range(cfg.scenes)]
-    out["lanes"] = bench_uneven_lanes(r, cfg, u, per_scene, net if neural_bound else None)
+    out["lanes"] = bench_uneven_lanes(r, cfg, u, per_scene, net if neural_bound else None, materials)
     if with_cpu:
         import oracle
         from softglrender_gb300 import api as A
@@ -694,6 +702,10 @@ def main():
         for prog in progs:   # the rest of the bench (end to end) runs the plain shader
             NN.NeuralShader.unbind(r, prog)
         n_fps = args.steps / (sum(n_ms) / 1e3)
+        # per-material decision for the uneven batch's two PBR materials (its environments): the
+        # trained material by its 16 held-out views above, the other on 4 held-out views
+        other = NN.evaluate_material(r, net, "env1", {"ibl_variant": 1}, views=range(64, 68))
+        material_bind = {0: bool(rep.bound), 1: bool(other.bound)}
         neural = {
             "frames_per_s": round(n_fps, 3), "mfrag_per_s": round(frags * n_fps / 1e6, 2),
             "raster_ms": round(n_raster, 4), "speedup_vs_plain_frames": round(n_fps / (args.steps / (sum(frame_ms) / 1e3)), 3),
@@ -705,6 +717,10 @@ def main():
             "records": rep.records, "capture_stride": rep.capture_stride, "train_steps": rep.train_steps,
             "train_s": round(rep.train_s, 3), "capture_s": round(rep.capture_s, 3), "final_loss": rep.final_loss,
             "views": {"train": 64, "held_out": 16},
+            "materials": {"env0": {"psnr_db_min": round(min(rep.psnr_views), 2), "bound": bool(rep.bound),
+                                   "held_out_views": 16},
+                          "env1": {"psnr_db_min": round(other.psnr_min, 2), "bound": bool(other.bound),
+                                   "held_out_views": 4, "trained_on": False}},
         }
 
     # ---- the other two frame configurations: the plain small frame (UV sphere, directional
@@ -731,7 +747,7 @@ def main():
     uneven = None
     if not args.no_uneven:
         uneven = bench_uneven(r, stream, net if neural is not None else None,
-                              bool(neural and neural["bound"]), rank == 0 and not args.no_cpu_baseline)
+                              material_bind if neural is not None else {}, rank == 0 and not args.no_cpu_baseline)
     if neural is not None:
         net.destroy()
 

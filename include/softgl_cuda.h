@@ -271,6 +271,10 @@ SGLC_API sglc_status sglc_set_tile_size(sglc_context *ctx, int32_t tile);
  * rasterise in three kernels: coverage and depth, then the fragment shader over every fragment, then
  * the colour operations in each pixel's order. 0: one fused raster kernel. Same images either way. */
 SGLC_API sglc_status sglc_set_deferred_shading(sglc_context *ctx, int32_t enable);
+/* 1 (default): the deferred raster kernels write each whole 16x16 tile's colour, resolved colour
+ * and depth back from shared memory with TMA bulk tensor stores (single-view draws on attachments
+ * whose rows are a multiple of 16 bytes); 0: every thread stores its own pixel. Same images. */
+SGLC_API sglc_status sglc_set_tma_store(sglc_context *ctx, int32_t enable);
 
 /* ---- synchronisation-free draws and CUDA graphs (no reference counterpart) ------------------- */
 /* Working-array capacities of a draw (a batched draw counts all its views together). */

@@ -577,6 +577,12 @@ sglc_status sglr_set_deferred_shading(sglc_context *ctx, int32_t enable) {
   return SGLC_OK;
 }
 
+sglc_status sglr_set_tma_store(sglc_context *ctx, int32_t enable) {
+  (void) ctx;
+  (void) enable;
+  return SGLC_OK;
+}
+
 sglc_status sglr_set_tile_size(sglc_context *ctx, int32_t tile) {
   (void) ctx;
   (void) tile;

@@ -2175,6 +2175,7 @@ sglc_status sglo_get_stream(sglc_context *, void **stream) {
 }
 sglc_status sglo_set_tile_size(sglc_context *, int32_t) { return SGLC_OK; }
 sglc_status sglo_set_deferred_shading(sglc_context *, int32_t) { return SGLC_OK; }   // one raster path
+sglc_status sglo_set_tma_store(sglc_context *, int32_t) { return SGLC_OK; }   // no tile write-back
 sglc_status sglo_set_stats_level(sglc_context *, int32_t) { return SGLC_OK; }
 
 }  // extern "C"

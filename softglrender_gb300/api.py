@@ -217,6 +217,7 @@ _SIGS = {
     "get_peak_counts": [C.c_void_p, C.c_void_p],
     "set_tile_size": [C.c_void_p, C.c_int32],
     "set_deferred_shading": [C.c_void_p, C.c_int32],
+    "set_tma_store": [C.c_void_p, C.c_int32],
 }
 
 ABI_FUNCTIONS = tuple(_SIGS) + ("last_error",)
@@ -568,3 +569,8 @@ class Renderer:
         """Extension: rasterise heavy shading models in coverage / shade / ROP kernels (default) or
         in one fused kernel; the images are the same."""
         self._call("set_deferred_shading", int(enable))
+
+    def setTmaStore(self, enable: bool) -> None:
+        """Extension: write whole raster tiles back with TMA bulk stores (default) or per-thread
+        stores; the images are the same."""
+        self._call("set_tma_store", int(enable))

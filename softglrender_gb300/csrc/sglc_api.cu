@@ -231,6 +231,7 @@ struct Ctx {
   DevBuf recA, recB, recColor, chunkNext, chunkFill, warpHead, recDense;   // deferred shading
   DevBuf peakChunks;   // largest number of fragment-record chunks a deferred draw used (device)
   bool deferredShading = true;
+  bool tmaStore = true;              // sglc_set_tma_store
   int nnTestFlags = 0;               // sglc_neural_set_test_flags
   DevBuf lpSlot, lpOrigin, lpStampCount, lpStampOff, lpStampGeo, lpStampRow, lpStampColor, lpStampVary, lpFragCount,
       lpFragOff, lpMisc;   // point and line draws
@@ -463,6 +464,41 @@ sglc_status hwTexture(Ctx *c, TexObj &t, const UsObj &us, cudaTextureObject_t *o
   h.views.push_back({us.filter, us.wrap, us.border, obj});
   *out = obj;
   return SGLC_OK;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against the driver)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encodeTiledFn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+// A linear attachment of h rows of w pixels with spp 32-bit samples each, as a 2D tensor map
+// (inner dimension w * spp) with a 16x16-pixel box. False where TMA cannot address it: a base
+// that is not 16-byte aligned or a row that is not a multiple of 16 bytes (then the kernels store
+// per thread).
+bool encodeAttachment(CUtensorMap *m, void *base, int w, int h, int spp) {
+  EncodeTiledFn fn = encodeTiledFn();
+  if (!fn || !base || ((uintptr_t) base & 15) || ((size_t) w * spp * 4) % 16 || w <= 0 || h <= 0) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t) w * spp, (cuuint64_t) h};
+  const cuuint64_t strides[1] = {(cuuint64_t) w * spp * 4};
+  const cuuint32_t box[2] = {(cuuint32_t) (16 * spp), 16};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 sglc_status flushClear(Ctx *c) {
@@ -828,6 +864,13 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     p.dms = dt->desc.multi_sample;
   }
   p.samples = ct ? (ct->desc.multi_sample ? 4 : 1) : (dt->desc.multi_sample ? 4 : 1);
+  // TMA write-back of whole tiles by the deferred raster kernels (single-view draws)
+  if (!bv && c->tmaStore && c->tile == 16) {
+    if (ct && encodeAttachment(&p.tmColor, p.color, p.cw, p.ch, p.samples) &&
+        (p.samples == 1 || encodeAttachment(&p.tmResolved, p.resolved, p.cw, p.ch, 1)))
+      p.tmaStore |= 1;
+    if (dt && encodeAttachment(&p.tmDepth, p.depth, p.dw, p.dh, p.samples)) p.tmaStore |= 2;
+  }
   std::vector<ViewTarget> targets;
   if (bv) {
     // every view's attachments must match view 0's (size, format, samples, presence)
@@ -1862,6 +1905,12 @@ sglc_status sglc_get_stream(sglc_context *ctx, void **stream) {
 sglc_status sglc_set_deferred_shading(sglc_context *ctx, int32_t enable) {
   CTX;
   c->deferredShading = enable != 0;
+  return SGLC_OK;
+}
+
+sglc_status sglc_set_tma_store(sglc_context *ctx, int32_t enable) {
+  CTX;
+  c->tmaStore = enable != 0;
   return SGLC_OK;
 }
 

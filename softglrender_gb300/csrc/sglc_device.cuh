@@ -10,6 +10,7 @@
 
 #include <cstdint>
 #include <utility>
+#include <cuda.h>   // CUtensorMap (the TMA write-back's tensor maps)
 #include <cuda_runtime.h>
 
 namespace sglc {
@@ -194,6 +195,13 @@ struct DrawParams {
   cudaTextureObject_t hwTex[kMaxSamplers];
   int *errFlags;
   int nnInjectTimeout;
+  // TMA write-back of whole 16x16 tiles (single-view draws): tensor maps over this GPU's colour
+  // (samples interleaved), resolved and depth attachments; tmaStore bit 0: colour and resolved by
+  // k_rop, bit 1: depth by k_raster_cov; 0: per-thread stores
+  alignas(64) CUtensorMap tmColor;
+  alignas(64) CUtensorMap tmResolved;
+  alignas(64) CUtensorMap tmDepth;
+  int tmaStore;
   // batched views (sglc_draw_views): one pipeline pass over `views` copies of the draw that differ
   // only in uniforms and attachments. nv / ntri above count all views' vertices / triangles;
   // view v owns vertices [v * nvView, (v + 1) * nvView), triangles [v * ntriView, ...) and raster
@@ -263,6 +271,23 @@ __device__ __forceinline__ int truncI(float f) {
   if (!(f > -2147483904.f && f < 2147483648.f)) return (int) 0x80000000u;
   return (int) f;
 }
+
+// TMA store of a 2D box from shared memory at element coordinates (x, y) of the tensor map (a
+// __grid_constant__ parameter); x * 4 bytes is a multiple of 16 for every use here
+__device__ __forceinline__ void tmaStore2d(const CUtensorMap *map, const void *smem, int x, int y) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"((uint32_t) __cvta_generic_to_shared(smem)), "r"(x), "r"(y)
+               : "memory");
+}
+// commit the thread's bulk stores and wait until they are complete (writes done, not only the
+// shared memory read), so the kernel's completion covers them
+__device__ __forceinline__ void tmaCommitWait() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+// this thread's shared-memory writes become visible to the async (TMA) proxy
+__device__ __forceinline__ void fenceAsyncShared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // uniforms of view v
 __device__ __forceinline__ const uint8_t *viewUniforms(const DrawParams &p, int view) {

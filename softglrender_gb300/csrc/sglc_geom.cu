@@ -240,6 +240,38 @@ __global__ void k_clip_append(const __grid_constant__ DrawParams p) {
 __device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }   // std::min
 __device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }   // std::max
 
+// A triangle that can cover no sample point is not binned (its fragments and depth writes are
+// none either way):
+// * |uz| below FLT_EPSILON: the reference's barycentric() rejects it at every point
+//   (RendererSoft.cpp:1035-1037; uz as it computes it, from the vertices' differences);
+// * a small, well-shaped triangle (bounding-box extent L in [1/256, 1] pixel, |uz| >= 0.01 L^2)
+//   whose bounding box grown by m = 1/32 pixel holds none of the draw's sample points (the pixel
+//   centre, or the four 4x MSAA positions). A point outside the box by m has a barycentric at most
+//   -m / (2 L) (the negative ones sum to at least m / L), while the rounding of the reference's
+//   edge functions there (exact vertex differences, products of magnitude <= 3 px^2) moves a
+//   barycentric by at most ~6e-7 / |uz| + 3e-5 |b|, far less for these triangles: the test cannot
+//   accept the point. Dense meshes at low resolution are mostly such sub-pixel triangles.
+__device__ __forceinline__ bool coversNoSample(const DrawParams &p, float4 a, float4 b, float4 c) {
+  const float a0 = c.x - a.x, a1 = b.x - a.x, c0 = c.y - a.y, c1 = b.y - a.y;   // v2 - v0, v1 - v0
+  const float uz = a0 * c1 - a1 * c0;
+  if (fabsf(uz) < 1.19209290e-07f) return true;
+  const float x0 = smin(smin(a.x, b.x), c.x), x1 = smax(smax(a.x, b.x), c.x);
+  const float y0 = smin(smin(a.y, b.y), c.y), y1 = smax(smax(a.y, b.y), c.y);
+  const float L = smax(x1 - x0, y1 - y0);
+  if (!(L >= 1.f / 256.f && L <= 1.f && fabsf(uz) >= 0.01f * L * L)) return false;
+  const float m = 1.f / 32.f;
+  const int n = p.samples == 4 ? 4 : 1;
+  // 4x MSAA sample positions inside a pixel (RendererInternal.h), else the pixel centre
+  const float sx4[4] = {0.375f, 0.875f, 0.125f, 0.625f}, sy4[4] = {0.875f, 0.625f, 0.375f, 0.125f};
+  for (int i = 0; i < n; i++) {
+    const float ox = n == 4 ? sx4[i] : 0.5f, oy = n == 4 ? sy4[i] : 0.5f;
+    // the smallest sample coordinate k + o >= lo, for both axes; a sample lies in the box if both fit
+    const float sx = ceilf(x0 - m - ox) + ox, sy = ceilf(y0 - m - oy) + oy;
+    if (sx <= x1 + m && sy <= y1 + m) return false;
+  }
+  return true;
+}
+
 // one primitive's setup; returns its upper bound on emitted fragments
 __device__ __forceinline__ unsigned long long setupPrim(const DrawParams &p, int i) {
   int4 pr = p.prims[i];
@@ -267,6 +299,7 @@ __device__ __forceinline__ unsigned long long setupPrim(const DrawParams &p, int
     minX -= 1.f;
     minY -= 1.f;
     if (!(isfinite(minX) && isfinite(minY) && isfinite(maxX) && isfinite(maxY))) discard = true;
+    if (!discard && coversNoSample(p, a, b, c)) discard = true;
     if (!discard) {
       int bcx = (int) (((maxX - minX) + (float) kBlock - 1.f) / (float) kBlock);
       int bcy = (int) (((maxY - minY) + (float) kBlock - 1.f) / (float) kBlock);

@@ -1055,6 +1055,24 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
     d += f;
     c = c == ch ? -1 : p.chunkNext[c];
   }
+  if ((p.tmaStore & 2) && rh == 4) {
+    // whole tile: its depth samples through shared memory and one TMA bulk store
+    __shared__ alignas(128) float sDep[16 * 16 * S];
+    const int li = (py - ty * 16) * 16 + (px - tx * 16);
+    sDep[li * S] = fb.d0;
+    if (S == 4) {
+      sDep[li * 4 + 1] = fb.d1;
+      sDep[li * 4 + 2] = fb.d2;
+      sDep[li * 4 + 3] = fb.d3;
+    }
+    fenceAsyncShared();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tmaStore2d(&p.tmDepth, sDep, tx * 16 * S, ty * 16);
+      tmaCommitWait();
+    }
+    return;
+  }
   if (inD) {
     size_t pix = (size_t) py * p.dw + px;
     if (S == 4) {
@@ -1153,17 +1171,42 @@ __global__ void __launch_bounds__(256) k_rop(const __grid_constant__ DrawParams 
     __syncwarp();
     ch = next;
   }
+  // multiSampleResolve (RendererSoft.cpp:880-912): mean of four u8 samples, truncated
+  uint32_t rsv = 0;
+  if (S == 4) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      uint32_t sum = ((fb.c0 >> (8 * k)) & 255u) + ((fb.c1 >> (8 * k)) & 255u) + ((fb.c2 >> (8 * k)) & 255u) +
+                     ((fb.c3 >> (8 * k)) & 255u);
+      rsv |= ((sum >> 2) & 255u) << (8 * k);
+    }
+  }
+  if ((p.tmaStore & 1) && job.rows == 4) {
+    // whole tile: stage its colour samples and resolved pixels in shared memory in the
+    // attachments' own order and write each with one TMA bulk store (pixels outside the
+    // attachment are clipped by the copy)
+    __shared__ alignas(128) uint32_t sCol[16 * 16 * S];
+    __shared__ alignas(128) uint32_t sRes[S == 4 ? 256 : 1];
+    const int li = (py - ty * 16) * 16 + (px - tx * 16);
+    sCol[li * S] = fb.c0;
+    if (S == 4) {
+      sCol[li * 4 + 1] = fb.c1;
+      sCol[li * 4 + 2] = fb.c2;
+      sCol[li * 4 + 3] = fb.c3;
+      sRes[li] = rsv;
+    }
+    fenceAsyncShared();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tmaStore2d(&p.tmColor, sCol, tx * 16 * S, ty * 16);
+      if (S == 4) tmaStore2d(&p.tmResolved, sRes, tx * 16, ty * 16);
+      tmaCommitWait();
+    }
+    return;
+  }
   if (inC) {
     if (S == 4) {
       *reinterpret_cast<uint4 *>(colorBuf + pix * 4) = make_uint4(fb.c0, fb.c1, fb.c2, fb.c3);
-      // multiSampleResolve (RendererSoft.cpp:880-912): mean of four u8 samples, truncated
-      uint32_t rsv = 0;
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        uint32_t sum = ((fb.c0 >> (8 * k)) & 255u) + ((fb.c1 >> (8 * k)) & 255u) + ((fb.c2 >> (8 * k)) & 255u) +
-                       ((fb.c3 >> (8 * k)) & 255u);
-        rsv |= ((sum >> 2) & 255u) << (8 * k);
-      }
       resolvedBuf[pix] = rsv;
     } else {
       colorBuf[pix] = fb.c0;

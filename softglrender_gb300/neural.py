@@ -14,7 +14,7 @@ from __future__ import annotations
 import ctypes as C
 import time
 from dataclasses import dataclass, field
-from typing import Dict, List, Optional
+from typing import Dict, List, Optional, Sequence
 
 import numpy as np
 
@@ -211,7 +211,7 @@ def train_neural_ibl(renderer: A.Renderer, scene_kwargs: Optional[dict] = None, 
                      inst: Optional[S.SceneInstance] = None, net: Optional[NeuralShader] = None):
     """Capture fragments of `train_views` orbit views of the PBR scene rendered by the plain shader,
     train the network, compare on `test_views` held-out views, and bind it to the scene's PBR
-    program if the mean held-out PSNR reaches `threshold_db` (else the plain shader stays bound).
+    program if the lowest held-out PSNR reaches `threshold_db` (else the plain shader stays bound).
     Returns (instance, network, report)."""
     kw = dict(scene_kwargs or {})
     seed_scene = kw.get("seed", 3000)
@@ -279,7 +279,7 @@ def train_neural_ibl(renderer: A.Renderer, scene_kwargs: Optional[dict] = None, 
             inst.render()
             rep.psnr_untrained.append(psnr(_resolved(inst)[..., :3], plain[..., :3]))
             net.set_params(trained)
-    rep.bound = rep.psnr_mean >= threshold_db
+    rep.bound = min(rep.psnr_views) >= threshold_db
     set_view(inst, views(0))
     for prog in progs:
         if rep.bound:
@@ -287,6 +287,69 @@ def train_neural_ibl(renderer: A.Renderer, scene_kwargs: Optional[dict] = None, 
         else:
             NeuralShader.unbind(renderer, prog)
     return inst, net, rep
+
+
+@dataclass
+class MaterialDecision:
+    """Whether one material keeps the network: its held-out views, plain against neural."""
+    name: str
+    psnr_views: List[float]
+    maxabs_views: List[int]
+    threshold_db: float
+
+    @property
+    def psnr_min(self) -> float:
+        return float(min(self.psnr_views))
+
+    @property
+    def bound(self) -> bool:
+        return self.psnr_min >= self.threshold_db
+
+
+def evaluate_material(renderer: A.Renderer, net: NeuralShader, name: str, scene_kwargs: dict,
+                      views: Sequence[int], threshold_db: float = 40.0) -> MaterialDecision:
+    """Held-out views of one material (the textures and IBL maps of `S.config_pbr(**scene_kwargs)`,
+    e.g. another environment variant) drawn by the plain shader and with the network bound. The
+    viewer maps a shader and its resources per material (Viewer.cpp:628, setupMaterial); the network
+    is kept for a material only if its lowest PSNR over the views reaches `threshold_db`."""
+    kw = dict(scene_kwargs)
+    inst = S.SceneInstance(renderer, S.config_pbr(**kw))
+    progs = pbr_programs(inst)
+    seed = kw.get("seed", 3000)
+    w, h = kw.get("width", 1920), kw.get("height", 1080)
+    ps, mx = [], []
+    for v in views:
+        set_view(inst, S.pbr_view_blocks(seed, v, w, h))
+        for prog in progs:
+            NeuralShader.unbind(renderer, prog)
+        inst.render()
+        plain = _resolved(inst)
+        for prog in progs:
+            net.bind(prog)
+        inst.render()
+        neural = _resolved(inst)
+        ps.append(psnr(neural[..., :3], plain[..., :3]))
+        mx.append(int(np.max(np.abs(neural[..., :3].astype(np.int32) - plain[..., :3]))))
+    for prog in progs:
+        NeuralShader.unbind(renderer, prog)
+    renderer.waitIdle()
+    return MaterialDecision(name, ps, mx, threshold_db)
+
+
+def bind_per_material(net: NeuralShader, programs_by_material: Dict[str, Sequence[A.ShaderProgram]],
+                      decisions: Dict[str, MaterialDecision]) -> Dict[str, bool]:
+    """Bind the network to the programs of every material that keeps it; the others keep (or get
+    back) the plain shader. Returns material -> network bound."""
+    out = {}
+    for name, progs in programs_by_material.items():
+        keep = decisions[name].bound
+        for prog in progs:
+            if keep:
+                net.bind(prog)
+            else:
+                NeuralShader.unbind(net.r, prog)
+        out[name] = keep
+    return out
 
 
 def _without_ibl(material: bytes) -> bytes:

@@ -16,6 +16,7 @@ Layouts follow the reference with GLM aligned types (vec3 = 16 B): View::Vertex 
 """
 from __future__ import annotations
 
+import functools
 import hashlib
 import struct
 from dataclasses import dataclass, field
@@ -333,7 +334,16 @@ def checkerboard(size: int, cells: int, seed: int) -> np.ndarray:
     return img
 
 
+@functools.lru_cache(maxsize=None)
 def noise_texture(size: int, seed: int, kind: str) -> np.ndarray:
+    """Seeded procedural material map (RGBA8). Memoised per process (the 1024^2 maps take seconds to
+    make); the returned array is read-only."""
+    img = _noise_texture(size, seed, kind)
+    img.setflags(write=False)
+    return img
+
+
+def _noise_texture(size: int, seed: int, kind: str) -> np.ndarray:
     y, x = np.mgrid[0:size, 0:size].astype(np.float64)
     u, v = (x + 0.5) / size, (y + 0.5) / size
     # periodic sampling on a torus so REPEAT is seamless
@@ -387,7 +397,27 @@ def sky_radiance(d: np.ndarray, suns: np.ndarray, width: float) -> np.ndarray:
     return col
 
 
-def ibl_maps(seed: int, prefilter_size: int, irradiance_size: int, levels: int = 5):
+@functools.lru_cache(maxsize=None)
+def ibl_maps(seed: int, prefilter_size: int, irradiance_size: int, levels: int = 5, variant: int = 0):
+    """(prefiltered specular chain, irradiance faces) of a seeded environment; memoised per
+    process, read-only arrays. `variant` k > 0 rotates the RGB channels k places (another
+    environment of the same shape: a differently tinted sky)."""
+    pre, irr = _ibl_maps(seed, prefilter_size, irradiance_size, levels)
+    if variant % 3:
+        k = variant % 3
+
+        def rot(img):
+            out = img.copy()
+            out[..., :3] = np.roll(img[..., :3], k, axis=-1)
+            return out
+        pre = [[rot(x) for x in lev] for lev in pre]
+        irr = [rot(x) for x in irr]
+    for img in [x for lev in pre for x in lev] + list(irr):
+        img.setflags(write=False)
+    return pre, irr
+
+
+def _ibl_maps(seed: int, prefilter_size: int, irradiance_size: int, levels: int = 5):
     suns = normalize(np.stack([hash_u01(seed, 300 + k, np.arange(3)) * 2.0 - 1.0 for k in range(3)], axis=-1) +
                      np.array([0.0, 0.6, 0.0]))
 
@@ -659,16 +689,17 @@ def pbr_view_blocks(seed: int, view: int, width: int, height: int) -> Dict[str, 
 
 def config_pbr(seed: int = 3000, width: int = 1920, height: int = 1080, samples: int = 4, lon: int = 448,
                lat: int = 224, tex: int = 1024, prefilter: int = 512, irradiance: int = 32,
-               view: int = 0) -> Scene:
+               view: int = 0, ibl_variant: int = 0) -> Scene:
     """Displaced sphere (value noise, amplitude 0.1) with PBR+IBL: albedo / normal / metal-roughness
-    maps (trilinear), irradiance + 5-level prefiltered specular cube maps, point light, MSAA 4x."""
+    maps (trilinear), irradiance + 5-level prefiltered specular cube maps, point light, MSAA 4x.
+    `ibl_variant` picks the environment (ibl_maps): another variant is another material."""
     vert, idx = uv_sphere(lon, lat, 1.0, displace_seed=seed, amplitude=0.1)
     blocks = pbr_view_blocks(seed, view, width, height)
     trilinear = A.SamplerDesc(A.Filter_LINEAR_MIPMAP_LINEAR, A.Filter_LINEAR, A.Wrap_REPEAT, A.Wrap_REPEAT,
                               A.Wrap_REPEAT)
     tdesc = A.TextureDesc(tex, tex, A.TextureType_2D, A.TextureFormat_RGBA8,
                           A.TextureUsage_Sampler | A.TextureUsage_UploadData, True, False)
-    pre, irr = ibl_maps(seed, prefilter, irradiance)
+    pre, irr = ibl_maps(seed, prefilter, irradiance, variant=ibl_variant)
     cube_pre = TextureSpec("u_prefilterMap",
                            A.TextureDesc(prefilter, prefilter, A.TextureType_CUBE, A.TextureFormat_RGBA8,
                                          A.TextureUsage_Sampler, True, False),

@@ -2,9 +2,10 @@
 
 Each scene is a seeded displaced sphere whose triangle count is drawn log-uniformly from
 [tri_min, tri_max] and whose square resolution is drawn from `resolutions`; even scenes use
-directional Blinn-Phong without MSAA, odd scenes PBR+IBL with 4x MSAA (the material, textures and
-IBL maps of the 1080p PBR scene, shared by all PBR scenes), optionally with the neural IBL shader
-bound when it met its PSNR threshold (per material; otherwise the plain shader stays: the
+directional Blinn-Phong without MSAA, odd scenes PBR+IBL with 4x MSAA: the material maps of the
+1080p PBR scene under one of `pbr_materials` environments (material 0 is the 1080p scene's own IBL
+maps, the others channel-rotated variants of them), optionally with the neural IBL shader bound per
+material where it met its PSNR threshold (otherwise that material keeps the plain shader: the
 fallback). `render()` issues the scenes one render pass each; on the GPU the whole sequence is
 captured once in a CUDA graph (softglrender_gb300/graph.py) and replayed with one launch, each
 scene's kernels running in order inside it. `UnevenLanes` splits the scenes over several renderers
@@ -35,6 +36,7 @@ class UnevenConfig:
     prefilter: int = 512
     irradiance: int = 32
     blinn_tex: int = 512
+    pbr_materials: int = 2   # PBR materials (environments) the PBR scenes alternate between
 
 
 # host-side scene assets, generated once per process and shared by every batch built from them
@@ -45,8 +47,8 @@ def _noise_texture(size: int, seed: int, kind: str) -> np.ndarray:
 
 
 @lru_cache(maxsize=None)
-def _ibl_maps(seed: int, prefilter: int, irradiance: int):
-    return S.ibl_maps(seed, prefilter, irradiance)
+def _ibl_maps(seed: int, prefilter: int, irradiance: int, variant: int = 0):
+    return S.ibl_maps(seed, prefilter, irradiance, variant=variant)
 
 
 @lru_cache(maxsize=None)
@@ -57,6 +59,11 @@ def _checkerboard(size: int, seed: int) -> np.ndarray:
 @lru_cache(maxsize=None)
 def _sphere(lon: int, lat: int, seed: int):
     return S.uv_sphere(lon, lat, 1.0, displace_seed=seed, amplitude=0.1)
+
+
+def material_of(cfg: UnevenConfig, s: int) -> int:
+    """PBR material of scene s (the odd scenes alternate between the materials)."""
+    return (s // 2) % max(1, cfg.pbr_materials)
 
 
 def scene_plan(cfg: UnevenConfig) -> List[Dict[str, int]]:
@@ -87,7 +94,7 @@ class UnevenBatch:
                               A.TextureUsage_Sampler | A.TextureUsage_UploadData, True, False)
         trilinear = A.SamplerDesc(A.Filter_LINEAR_MIPMAP_LINEAR, A.Filter_LINEAR, A.Wrap_REPEAT, A.Wrap_REPEAT,
                                   A.Wrap_REPEAT)
-        pbr_samplers = []
+        material_maps = []
         for k, (name, kind) in enumerate((("u_albedoMap", "albedo"), ("u_normalMap", "normal"),
                                           ("u_metalRoughnessMap", "metal_rough"))):
             t = r.createTexture(tdesc)
@@ -95,29 +102,32 @@ class UnevenBatch:
             t.setImageData([_noise_texture(cfg.pbr_tex, 3000 + 10 * (k + 1), kind)])
             us = r.createUniformSampler(name, tdesc)
             us.setTexture(t)
-            pbr_samplers.append(us)
-        pre, irr = _ibl_maps(3000, cfg.prefilter, cfg.irradiance)
-        cdesc = A.TextureDesc(cfg.irradiance, cfg.irradiance, A.TextureType_CUBE, A.TextureFormat_RGBA8,
-                              A.TextureUsage_Sampler | A.TextureUsage_UploadData, False, False)
-        t = r.createTexture(cdesc)
-        t.setSamplerDesc(A.SamplerDesc(A.Filter_LINEAR, A.Filter_LINEAR, A.Wrap_CLAMP_TO_EDGE, A.Wrap_CLAMP_TO_EDGE,
-                                       A.Wrap_CLAMP_TO_EDGE))
-        t.setImageData(irr)
-        us = r.createUniformSampler("u_irradianceMap", cdesc)
-        us.setTexture(t)
-        pbr_samplers.append(us)
-        pdesc = A.TextureDesc(cfg.prefilter, cfg.prefilter, A.TextureType_CUBE, A.TextureFormat_RGBA8,
-                              A.TextureUsage_Sampler, True, False)
-        t = r.createTexture(pdesc)
-        t.setSamplerDesc(A.SamplerDesc(A.Filter_LINEAR_MIPMAP_LINEAR, A.Filter_LINEAR, A.Wrap_CLAMP_TO_EDGE,
-                                       A.Wrap_CLAMP_TO_EDGE, A.Wrap_CLAMP_TO_EDGE))
-        t.initImageData()
-        for lev, imgs in enumerate(pre):
-            for layer, img in enumerate(imgs):
-                t.setLevelData(layer, lev, img)
-        us = r.createUniformSampler("u_prefilterMap", pdesc)
-        us.setTexture(t)
-        pbr_samplers.append(us)
+            material_maps.append(us)
+        # PBR material m: the shared material maps under environment m (the 1080p PBR scene's IBL
+        # maps, variant m: material 0 is that scene's own environment)
+        self.pbr_samplers = []
+        for m in range(max(1, cfg.pbr_materials)):
+            pre, irr = _ibl_maps(3000, cfg.prefilter, cfg.irradiance, m)
+            cdesc = A.TextureDesc(cfg.irradiance, cfg.irradiance, A.TextureType_CUBE, A.TextureFormat_RGBA8,
+                                  A.TextureUsage_Sampler | A.TextureUsage_UploadData, False, False)
+            t = r.createTexture(cdesc)
+            t.setSamplerDesc(A.SamplerDesc(A.Filter_LINEAR, A.Filter_LINEAR, A.Wrap_CLAMP_TO_EDGE,
+                                           A.Wrap_CLAMP_TO_EDGE, A.Wrap_CLAMP_TO_EDGE))
+            t.setImageData(irr)
+            irr_us = r.createUniformSampler("u_irradianceMap", cdesc)
+            irr_us.setTexture(t)
+            pdesc = A.TextureDesc(cfg.prefilter, cfg.prefilter, A.TextureType_CUBE, A.TextureFormat_RGBA8,
+                                  A.TextureUsage_Sampler, True, False)
+            t = r.createTexture(pdesc)
+            t.setSamplerDesc(A.SamplerDesc(A.Filter_LINEAR_MIPMAP_LINEAR, A.Filter_LINEAR, A.Wrap_CLAMP_TO_EDGE,
+                                           A.Wrap_CLAMP_TO_EDGE, A.Wrap_CLAMP_TO_EDGE))
+            t.initImageData()
+            for lev, imgs in enumerate(pre):
+                for layer, img in enumerate(imgs):
+                    t.setLevelData(layer, lev, img)
+            pre_us = r.createUniformSampler("u_prefilterMap", pdesc)
+            pre_us.setTexture(t)
+            self.pbr_samplers.append(material_maps + [irr_us, pre_us])
         bdesc = A.TextureDesc(cfg.blinn_tex, cfg.blinn_tex, A.TextureType_2D, A.TextureFormat_RGBA8,
                               A.TextureUsage_Sampler | A.TextureUsage_UploadData, True, False)
         bt = r.createTexture(bdesc)
@@ -145,7 +155,7 @@ class UnevenBatch:
                 prog.addDefines(("ALBEDO_MAP", "NORMAL_MAP", "METALROUGHNESS_MAP"))
                 prog.SetShaders(A.Shading_PBR)
                 blocks = S.pbr_view_blocks(cfg.seed + 1, s, res, res)
-                for k, us in enumerate(pbr_samplers):
+                for k, us in enumerate(self.pbr_samplers[material_of(cfg, s)]):
                     resources.setSampler(k, us)
             else:
                 prog.addDefines(("ALBEDO_MAP",))
@@ -175,11 +185,13 @@ class UnevenBatch:
             fbo.setColorAttachment(ct, 0)
             fbo.setDepthAttachment(dt)
             self.items[s] = {"vao": vao, "prog": prog, "res": resources, "fbo": fbo, "color": ct, "depth": dt,
-                             "size": res, "pbr": bool(pl["pbr"])}
+                             "size": res, "pbr": bool(pl["pbr"]),
+                             "material": material_of(cfg, s) if pl["pbr"] else -1}
         self.clear = A.ClearStates(True, True, (0.02, 0.02, 0.03, 1.0), 1.0)
 
-    def pbr_programs(self) -> List[A.ShaderProgram]:
-        return [it["prog"] for it in self.items.values() if it["pbr"]]
+    def pbr_programs(self, material: Optional[int] = None) -> List[A.ShaderProgram]:
+        """Programs of the PBR scenes (of one material when given)."""
+        return [it["prog"] for it in self.items.values() if it["pbr"] and material in (None, it["material"])]
 
     def render_scene(self, s: int) -> None:
         r, it = self.r, self.items[s]

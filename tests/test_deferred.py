@@ -166,3 +166,37 @@ def test_fragment_capacity_overflow_is_reported(cuda_lib):
     out, flags = _batch_outputs(cuda_lib, True, A.Capacity(1 << 16, 1 << 14, 1 << 14, 1 << 20, 1, 64))
     assert flags & 32                    # fragment records
     assert len(out) == CFG.views         # the context stayed usable and the draw completed
+
+
+def _render_tma(lib, scene, tma):
+    r = A.Renderer(lib, 0)
+    r.setTmaStore(tma)
+    inst = S.SceneInstance(r, scene)
+    inst.render()
+    r.waitIdle()
+    out = [inst.outputs(i) for i in range(len(scene.passes))]
+    r.destroy()
+    return out
+
+
+TMA_SCENES = {
+    "pbr_msaa4_320x180": lambda: S.config_pbr(width=320, height=180, lon=96, lat=48, tex=128, prefilter=64,
+                                              irradiance=8),
+    "blinn_1x_300x200": lambda: S.config_plain_small(width=300, height=200, lon=48, lat=24, tex=64),
+    # rows of 257 pixels are not a multiple of 16 bytes: per-thread stores stay in use
+    "soup_1x_257x131": lambda: S.config_geometry_stress(n_tris=4000, width=257, height=131, samples=1),
+    "soup_msaa4_250x150": lambda: S.config_geometry_stress(n_tris=6000, width=250, height=150, samples=4),
+}
+
+
+@pytest.mark.parametrize("name", sorted(TMA_SCENES))
+def test_tma_tile_write_back_equals_per_thread_stores(name, cuda_lib, oracle_lib):
+    """Whole tiles written back from shared memory by TMA bulk tensor stores (colour, resolved and
+    depth; edge tiles clipped by the copy) give the images of per-thread stores, and the oracle's."""
+    scene = TMA_SCENES[name]()
+    a = _render_tma(cuda_lib, scene, True)
+    b = _render_tma(cuda_lib, scene, False)
+    for pa, pb in zip(a, b):
+        for k in pb:
+            assert np.array_equal(pa[k].view(np.uint8), pb[k].view(np.uint8)), k
+    assert_outputs_match(a, render(oracle_lib, scene)[0], name, exact_color=name.startswith("soup"))

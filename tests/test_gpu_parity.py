@@ -11,6 +11,7 @@ import pytest
 from softglrender_gb300 import api as A
 from softglrender_gb300 import scenes as S
 
+from golden.cases import soup
 from helpers import assert_outputs_match, render
 
 pytestmark = pytest.mark.gpu
@@ -24,6 +25,15 @@ CASES = {
     "pbr_small": lambda: S.config_pbr(width=320, height=180, lon=96, lat=48, tex=128, prefilter=64, irradiance=16),
     "pbr_view3": lambda: S.config_pbr(width=480, height=270, lon=128, lat=64, tex=256, prefilter=128, irradiance=16,
                                       view=3),
+    # sub-pixel triangles (most cover no sample point and are not binned) and a dense sphere at a
+    # low resolution, opaque (LESS) and with reversed Z
+    "tiny_soup_msaa4": lambda: soup(40000, 160, 120, 4, [A.RenderStates(depthTest=True, depthMask=True,
+                                                                        depthFunc=A.DepthFunc_LESS)],
+                                    seed=31, median_px=0.15),
+    "tiny_soup_1x_reversed": lambda: soup(40000, 160, 120, 1, [A.RenderStates(depthTest=True, depthMask=True,
+                                                                              depthFunc=A.DepthFunc_GREATER)],
+                                          seed=32, clear_depth=0.0, reverse=True, median_px=0.3),
+    "dense_sphere_96px": lambda: S.config_plain_small(width=96, height=72, lon=512, lat=256, tex=64),
 }
 
 

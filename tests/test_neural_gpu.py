@@ -198,3 +198,44 @@ def test_neural_wait_timeouts_reach_the_host(cuda_lib, deferred):
         NeuralShader.set_test_flags(r, 2)
     net.destroy()
     r.destroy()
+
+
+def test_per_material_fallback_in_one_submission(cuda_lib):
+    """Two PBR materials (the same material maps under two environments, the second a differently
+    tinted sky) in one uneven batch: the network is trained on material 0 only, each material keeps
+    it only if its lowest held-out PSNR reaches the threshold, and in the same submission the
+    material that fell back renders exactly as the plain shader while the other one uses the
+    network."""
+    from softglrender_gb300.neural import bind_per_material, evaluate_material
+    from softglrender_gb300.uneven import UnevenBatch, UnevenConfig
+    r = A.Renderer(cuda_lib, 0)
+    kw = dict(width=320, height=180, lon=96, lat=48, tex=128, prefilter=64, irradiance=16)
+    inst, net, rep = train_neural_ibl(r, kw, train_views=8, test_views=2, records=1 << 18, steps=3000,
+                                      batch=1 << 14, lr=3e-3, seed=3, baselines=False)
+    d0 = evaluate_material(r, net, "env0", dict(kw, ibl_variant=0), views=[20, 21])
+    d1 = evaluate_material(r, net, "env1", dict(kw, ibl_variant=1), views=[20, 21])
+    print("material PSNR min:", round(d0.psnr_min, 2), round(d1.psnr_min, 2))
+    assert d0.psnr_min > d1.psnr_min + 6.0     # the network only knows environment 0
+    threshold = 0.5 * (d0.psnr_min + d1.psnr_min)
+    d0.threshold_db = d1.threshold_db = threshold
+    cfg = UnevenConfig(scenes=6, tri_min=2000, tri_max=20000, resolutions=(64, 128), seed=5100, pbr_tex=128,
+                       prefilter=64, irradiance=16, blinn_tex=64, pbr_materials=2)
+    u = UnevenBatch(r, cfg)
+    u.render()
+    r.waitIdle()
+    plain = {s: u.outputs(s) for s in u.items}
+    bound = bind_per_material(net, {"env0": u.pbr_programs(0), "env1": u.pbr_programs(1)},
+                              {"env0": d0, "env1": d1})
+    assert bound == {"env0": True, "env1": False}
+    u.render()
+    r.waitIdle()
+    for s, it in u.items.items():
+        o = u.outputs(s)
+        if not it["pbr"] or it["material"] == 1:   # plain shader: bit for bit
+            for k in plain[s]:
+                assert np.array_equal(o[k].view(np.uint8), plain[s][k].view(np.uint8)), (s, k)
+        else:                                      # the network: same coverage and depth, colour changed
+            assert np.array_equal(o["depth"].view(np.uint32), plain[s]["depth"].view(np.uint32))
+            assert not np.array_equal(o["resolved"], plain[s]["resolved"])
+    net.destroy()
+    r.destroy()
