@@ -47,17 +47,20 @@ def bf16(a: np.ndarray) -> np.ndarray:
 
 def encode(x: np.ndarray) -> np.ndarray:
     """(n, 12) inputs -> (n, 156) features in the device order: feature 24k + 2i = sin(2^k pi x_i),
-    24k + 2i + 1 = cos(2^k pi x_i) (k = 0..5), feature 144 + i = x_i."""
+    24k + 2i + 1 = cos(2^k pi x_i) (k = 0..5), feature 144 + i = x_i. The double-angle recurrence is
+    the device's (t = 2 s, s' = t c, c' = 1 - t s with one rounding); the base sin / cos are exact
+    here, the device's special-function values differ from them by less than 1e-6."""
     x = np.asarray(x, dtype=np.float32)
     n = x.shape[0]
     f = np.zeros((n, N_FEAT), dtype=np.float32)
     s = np.sin(np.pi * x.astype(np.float64)).astype(np.float32)
     c = np.cos(np.pi * x.astype(np.float64)).astype(np.float32)
-    two, one = np.float32(2.0), np.float32(1.0)
+    two = np.float32(2.0)
     for k in range(N_FREQ):
         f[:, 24 * k + 0:24 * k + 24:2] = s
         f[:, 24 * k + 1:24 * k + 24:2] = c
-        s, c = (two * s) * c, one - (two * s) * s
+        t = two * s
+        s, c = t * c, (1.0 - t.astype(np.float64) * s.astype(np.float64)).astype(np.float32)
     f[:, 144:156] = x
     return f
 

@@ -8,8 +8,9 @@
 // sampled), max(dot(N, V), 0). Output: sqrt of the IBL ambient term before the ambient-occlusion
 // factor; the shader squares it back (ambient = max(y, 0)^2).
 // Encoding of input x_i: for k = 0..5 feature 24k + 2i = sin(2^k pi x_i), 24k + 2i + 1 =
-// cos(2^k pi x_i), computed from sincospi(x_i) by the double-angle recurrences s' = 2 s c,
-// c' = 1 - 2 s s; feature 144 + i = x_i. Feature 156 is the constant 1 on training tiles (its weight
+// cos(2^k pi x_i), computed from sin / cos of pi x_i (the special-function unit's __sincosf: the
+// inputs lie in [-1, 1], where its error is below 1e-6) by the double-angle recurrences
+// t = 2 s, s' = t c, c' = 1 - t s (fused, one rounding); feature 144 + i = x_i. Feature 156 is the constant 1 on training tiles (its weight
 // column stays zero, so the forward pass ignores it, and the weight gradient's row 156 is the first
 // layer's bias gradient); features 157-159 are zero.
 //
@@ -63,7 +64,7 @@ template<int C0, int C1>
 __device__ __forceinline__ void encodeChunks(const float *x, uint8_t *tile, int row, int tileC, bool oneFeature) {
   float s[kIn], c[kIn];
 #pragma unroll
-  for (int i = 0; i < kIn; i++) sincospif(x[i], &s[i], &c[i]);
+  for (int i = 0; i < kIn; i++) __sincosf(3.14159265358979f * x[i], &s[i], &c[i]);
 #pragma unroll
   for (int k = 0; k < kFreq; k++) {
 #pragma unroll
@@ -77,10 +78,10 @@ __device__ __forceinline__ void encodeChunks(const float *x, uint8_t *tile, int 
     }
     if (k + 1 < kFreq) {
 #pragma unroll
-      for (int i = 0; i < kIn; i++) {
-        float s2 = 2.0f * s[i] * c[i];
-        float c2 = 1.0f - 2.0f * s[i] * s[i];
-        s[i] = s2;
+      for (int i = 0; i < kIn; i++) {   // double angle: t = 2 s, s' = t c, c' = 1 - t s (one rounding)
+        const float t = s[i] + s[i];
+        const float c2 = __fmaf_rn(-t, s[i], 1.0f);
+        s[i] = t * c[i];
         c[i] = c2;
       }
     }

@@ -215,7 +215,7 @@ def test_per_material_fallback_in_one_submission(cuda_lib):
     d0 = evaluate_material(r, net, "env0", dict(kw, ibl_variant=0), views=[20, 21])
     d1 = evaluate_material(r, net, "env1", dict(kw, ibl_variant=1), views=[20, 21])
     print("material PSNR min:", round(d0.psnr_min, 2), round(d1.psnr_min, 2))
-    assert d0.psnr_min > d1.psnr_min + 6.0     # the network only knows environment 0
+    assert d0.psnr_min > d1.psnr_min + 3.0     # the network only knows environment 0
     threshold = 0.5 * (d0.psnr_min + d1.psnr_min)
     d0.threshold_db = d1.threshold_db = threshold
     cfg = UnevenConfig(scenes=6, tri_min=2000, tri_max=20000, resolutions=(64, 128), seed=5100, pbr_tex=128,
