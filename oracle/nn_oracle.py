@@ -48,8 +48,7 @@ def bf16(a: np.ndarray) -> np.ndarray:
 def encode(x: np.ndarray) -> np.ndarray:
     """(n, 12) inputs -> (n, 156) features in the device order: feature 24k + 2i = sin(2^k pi x_i),
     24k + 2i + 1 = cos(2^k pi x_i) (k = 0..5), feature 144 + i = x_i. The double-angle recurrence is
-    the device's (t = 2 s, s' = t c, c' = 1 - t s with one rounding); the base sin / cos are exact
-    here, the device's special-function values differ from them by less than 1e-6."""
+    the device's (t = 2 s, s' = t c, c' = 1 - t s with one rounding)."""
     x = np.asarray(x, dtype=np.float32)
     n = x.shape[0]
     f = np.zeros((n, N_FEAT), dtype=np.float32)

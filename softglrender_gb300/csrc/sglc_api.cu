@@ -229,6 +229,7 @@ struct Ctx {
   DevBuf tri, tileCount, pairOff, keyA, keyB, valA, valB, tileStart, tileEnd, tileOrder, scanScratch, sortHist,
       sortHistScan, staging, batchU, batchTargets;
   DevBuf recA, recB, recColor, chunkNext, chunkFill, warpHead, recDense;   // deferred shading
+  DevBuf nnIn;   // neural shading: per record the surface stage's 80-B row
   DevBuf peakChunks;   // largest number of fragment-record chunks a deferred draw used (device)
   bool deferredShading = true;
   bool tmaStore = true;              // sglc_set_tma_store
@@ -253,7 +254,7 @@ struct Ctx {
                       &tileEnd, &tileOrder, &scanScratch, &sortHist, &sortHistScan, &staging, &batchU, &batchTargets,
                       &sticky, &lpSlot, &lpOrigin, &lpStampCount, &lpStampOff, &lpStampGeo, &lpStampRow,
                       &lpStampColor, &lpStampVary, &lpFragCount, &lpFragOff, &lpMisc, &recA, &recB, &recColor,
-                      &chunkNext, &chunkFill, &warpHead, &recDense, &peakChunks};
+                      &chunkNext, &chunkFill, &warpHead, &recDense, &peakChunks, &nnIn};
     for (DevBuf *b : bufs) f(*b);
   }
   std::vector<void *> captureHostBufs;   // pinned host sources of memcpy nodes in the capture
@@ -1117,6 +1118,10 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       p.chunkFill = c->chunkFill.as<int>();
       p.warpHead = c->warpHead.as<int>();
       p.recDense = c->recDense.as<int>();
+      if (p.shading == SH_PBR_NEURAL) {
+        CK(c->nnIn.ensure(sizeof(float4) * 5 * (size_t) chunks * kChunk));
+        p.nnIn = c->nnIn.as<float4>();
+      }
       p.chunkCap = (int) chunks;
       p.heavySlots = 64;    // with the heavy-first order: its first 64 tiles may be split in 4
       p.heavyMin = 256;     // primitives in a tile's list above which it is split

@@ -8,9 +8,8 @@
 // sampled), max(dot(N, V), 0). Output: sqrt of the IBL ambient term before the ambient-occlusion
 // factor; the shader squares it back (ambient = max(y, 0)^2).
 // Encoding of input x_i: for k = 0..5 feature 24k + 2i = sin(2^k pi x_i), 24k + 2i + 1 =
-// cos(2^k pi x_i), computed from sin / cos of pi x_i (the special-function unit's __sincosf: the
-// inputs lie in [-1, 1], where its error is below 1e-6) by the double-angle recurrences
-// t = 2 s, s' = t c, c' = 1 - t s (fused, one rounding); feature 144 + i = x_i. Feature 156 is the constant 1 on training tiles (its weight
+// cos(2^k pi x_i), computed from sincospi(x_i) by the double-angle recurrences t = 2 s, s' = t c,
+// c' = 1 - t s (fused, one rounding); feature 144 + i = x_i. Feature 156 is the constant 1 on training tiles (its weight
 // column stays zero, so the forward pass ignores it, and the weight gradient's row 156 is the first
 // layer's bias gradient); features 157-159 are zero.
 //
@@ -64,7 +63,7 @@ template<int C0, int C1>
 __device__ __forceinline__ void encodeChunks(const float *x, uint8_t *tile, int row, int tileC, bool oneFeature) {
   float s[kIn], c[kIn];
 #pragma unroll
-  for (int i = 0; i < kIn; i++) __sincosf(3.14159265358979f * x[i], &s[i], &c[i]);
+  for (int i = 0; i < kIn; i++) sincospif(x[i], &s[i], &c[i]);
 #pragma unroll
   for (int k = 0; k < kFreq; k++) {
 #pragma unroll
@@ -133,14 +132,19 @@ __device__ __forceinline__ unsigned long long hiddenEpilogue(uint32_t taddr, con
 // MMA issue helper (one thread). Descriptors follow the tile layout of sglc_tc.cuh.
 // D[128 x N] (+)= A[128 x K] * B[K x N]: A = K columns of a tile with aC columns starting at column
 // aCol (K-major); B = a weight tile [N][bC] (K-major) from column bCol.
+// Each K step of 16 advances both operands by two core matrices (256 bytes), which is 16 in the
+// descriptor's address field (addresses >> 4; shared-memory addresses stay far below its 18-bit
+// range), so the descriptors are built once and stepped by an add.
 __device__ __forceinline__ void issueKMajor(uint32_t dTmem, uint32_t aBase, int aC, int aCol, uint32_t bBase, int bC,
                                             int bCol, int N, int K, bool accumulate) {
   const uint32_t idesc = tc::instrDesc(128, N, false, false);
+  uint64_t ad = tc::smemDesc(aBase + tc::tileOffset(0, aCol, aC), 128, (uint32_t) aC / 8 * 128);
+  uint64_t bd = tc::smemDesc(bBase + tc::tileOffset(0, bCol, bC), 128, (uint32_t) bC / 8 * 128);
 #pragma unroll 1
   for (int k = 0; k < K; k += 16) {
-    uint64_t ad = tc::smemDesc(aBase + tc::tileOffset(0, aCol + k, aC), 128, (uint32_t) aC / 8 * 128);
-    uint64_t bd = tc::smemDesc(bBase + tc::tileOffset(0, bCol + k, bC), 128, (uint32_t) bC / 8 * 128);
     tc::mma(dTmem, ad, bd, idesc, accumulate || k > 0);
+    ad += 16;
+    bd += 16;
   }
 }
 

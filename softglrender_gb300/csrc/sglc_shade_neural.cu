@@ -13,14 +13,19 @@
 //     quad's neighbours (ShaderSoft.h:117-133);
 //   * pow, reciprocal and normalisation use the fast intrinsics.
 //
-// Kernel layout: one persistent CTA per SM with four warpgroups (512 threads). Each warpgroup
-// walks its own sequence of 128-record tiles: every thread evaluates one record's surface terms
-// and writes the network's 160 input features into its row of the warpgroup's [128][160] BF16
-// tile; one elected thread issues the three layers' tcgen05.mma chains (layer 1 over K = 160 in
-// one chain, then 64 -> 64 and 64 -> 3), each completed through the warpgroup's mbarrier; the
-// epilogues read the FP32 accumulators back from the warpgroup's 128 TMEM columns (bias, ReLU and
-// the BF16 conversion in packed f32x2 / bf16x2 instructions) into the same tile. The four
-// warpgroups' tensor-core round trips overlap each other's surface and feature work.
+// Two kernels. k_neural_surface evaluates the surface terms at high occupancy (128-thread CTAs,
+// 64 registers, 16 CTAs per SM over a grid-stride loop): the chain of dependent loads (record,
+// triangle set-up, varyings, texels) needs many warps in flight, which a kernel holding tensor
+// memory and 160 KB of operand tiles cannot have. It writes 80 B per record in dense order.
+// k_shade_neural then runs the network: one persistent CTA per SM with four warpgroups (512
+// threads). Each warpgroup walks its own sequence of 128-record tiles, loading the next tile's
+// rows while the current tile's MMAs run: every thread encodes one record's 12 inputs into the
+// network's 160 features in its row of the warpgroup's [128][160] BF16 tile; one elected thread
+// issues the three layers' tcgen05.mma chains (layer 1 over K = 160 in one chain, then 64 -> 64
+// and 64 -> 3), each completed through the warpgroup's mbarrier; the epilogues read the FP32
+// accumulators back from the warpgroup's 128 TMEM columns (bias, ReLU and the BF16 conversion in
+// packed f32x2 / bf16x2 instructions) into the same tile. The four warpgroups' tensor-core round
+// trips overlap each other's feature and epilogue work.
 // A wait that runs out of polls sets the draw's device error flag (kFlagNeuralTimeout in the
 // context's sticky flags, read by sglc_get_overflow); that tile's colours are then unspecified.
 #include "sglc_raster.cuh"
@@ -203,6 +208,27 @@ __device__ __forceinline__ Surface surface(const DrawParams &p, int4 a, float2 b
   return s;
 }
 
+// Stage 1 (high occupancy, no tensor cores): the surface terms of every record, written in the
+// dense record order as five float4: the network's 12 inputs, then (Lo, ao) and (emissive, alpha).
+__global__ void __launch_bounds__(128, 8) k_neural_surface(const __grid_constant__ DrawParams p) {
+  const int nRec = min(p.counters[kCntDense], p.chunkCap * kChunk);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nRec; i += gridDim.x * blockDim.x) {
+    const int r = p.recDense[i];
+    float4 *o = p.nnIn + (size_t) 5 * i;
+    if (r < 0) {
+      for (int k = 0; k < 5; k++) o[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      continue;
+    }
+    const Surface sf = surface(p, p.recA[r], p.recB[r]);
+    o[0] = make_float4(sf.x[0], sf.x[1], sf.x[2], sf.x[3]);
+    o[1] = make_float4(sf.x[4], sf.x[5], sf.x[6], sf.x[7]);
+    o[2] = make_float4(sf.x[8], sf.x[9], sf.x[10], sf.x[11]);
+    o[3] = make_float4(sf.Lo.x, sf.Lo.y, sf.Lo.z, sf.ao);
+    o[4] = make_float4(sf.emissive.x, sf.emissive.y, sf.emissive.z, sf.alpha);
+  }
+}
+
+// Stage 2 (tensor cores): the network over the stage-1 rows and the colour finish.
 __global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_constant__ DrawParams p) {
   extern __shared__ __align__(1024) uint8_t smraw[];
   uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t) 1023);
@@ -236,26 +262,38 @@ __global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_const
   };
 
   const int nRec = min(p.counters[kCntDense], p.chunkCap * kChunk);
-  for (int t0 = (blockIdx.x * kWG + wg) * 128; t0 < nRec; t0 += gridDim.x * kThreads) {
-    const int di = t0 + wgThread;
-    const int r = di < nRec ? p.recDense[di] : -1;
-    const bool valid = r >= 0;
-    Surface s;
-    if (valid) {
-      s = surface(p, p.recA[r], p.recB[r]);
+  const int stride = gridDim.x * kThreads;
+  int t0 = (blockIdx.x * kWG + wg) * 128;
+  // the rows of the warpgroup's next tile are loaded one tile ahead (in flight during the MMAs)
+  float4 in[5];
+  int rec = -1;
+  auto load = [&](int t) {
+    const int di = t + wgThread;
+    rec = -1;
+    if (t < nRec && di < nRec) {
+      rec = p.recDense[di];
+      const float4 *q = p.nnIn + (size_t) 5 * di;
+#pragma unroll
+      for (int k = 0; k < 5; k++) in[k] = q[k];
     } else {
 #pragma unroll
-      for (int i = 0; i < kIn; i++) s.x[i] = 0.f;
-      s.Lo = s.emissive = mk3(0.f, 0.f, 0.f);
-      s.ao = s.alpha = 0.f;
+      for (int k = 0; k < 5; k++) in[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    encodeRow(s.x, xTile, row, false);
+  };
+  load(t0);
+  for (; t0 < nRec; t0 += stride) {
+    const int r = rec;
+    const float x[kIn] = {in[0].x, in[0].y, in[0].z, in[0].w, in[1].x, in[1].y,
+                          in[1].z, in[1].w, in[2].x, in[2].y, in[2].z, in[2].w};
+    const float4 loAo = in[3], emA = in[4];
+    encodeRow(x, xTile, row, false);
     wgHandOff(wg);
     if (wgThread == 0) {   // layer 1: [128 x 160] x [160 x 64]
       tc::fenceAfter();
       issueKMajor(tmem, sX, kK1, 0, sW1, kK1, 0, kHid, kK1, false);
       tc::commit(bar);
     }
+    load(t0 + stride);
     wait();
     hiddenRow(lanes, bias, xTile, row);
     wgHandOff(wg);
@@ -277,13 +315,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_const
     tc::ld16(lanes, y);
     tc::ldWait();
     tc::fenceBefore();
-    if (valid) {
+    if (r >= 0) {
       // ambient = max(y, 0)^2 * ao; colour = (ambient + Lo)^(1/2.2) + emissive (PbrSoft.h:311-321)
       const float a0 = gmax(y[0] + bias[128], 0.f), a1 = gmax(y[1] + bias[129], 0.f), a2 = gmax(y[2] + bias[130], 0.f);
-      const f3 c = mk3(a0 * a0, a1 * a1, a2 * a2) * s.ao + s.Lo;
+      const f3 c = mk3(a0 * a0, a1 * a1, a2 * a2) * loAo.w + mk3(loAo.x, loAo.y, loAo.z);
       f3 col = mk3(__powf(c.x, 1.f / 2.2f), __powf(c.y, 1.f / 2.2f), __powf(c.z, 1.f / 2.2f));
-      if (p.def[2]) col = col + s.emissive;
-      p.recColor[r] = make_float4(col.x, col.y, col.z, s.alpha);
+      if (p.def[2]) col = col + mk3(emA.x, emA.y, emA.z);
+      p.recColor[r] = make_float4(col.x, col.y, col.z, emA.w);
     }
     // every thread has read its TMEM lane and its tile row before the next tile overwrites them
     wgSync(wg);
@@ -304,6 +342,7 @@ void launchShadeNeural(const DrawParams &p, cudaStream_t st) {
   setDynamicSmemOnce(attr, k_shade_neural, kSnBytes);
   int sms = 152, dev = 0;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_neural_surface<<<sms * 16, 128, 0, st>>>(p);
   k_shade_neural<<<sms, kThreads, kSnBytes, st>>>(p);
 }
 
