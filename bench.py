@@ -37,6 +37,11 @@ def parse():
     ap.add_argument("--no-neural", action="store_true", help="skip training / timing the neural IBL shader")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-views measurement")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch measurement")
+    ap.add_argument("--profile-scene", default=None,
+                    help="render one workload for --frames frames (after one warm-up frame) and exit, for a "
+                         "profiler: plain_small, geometry_stress[:TRIANGLES], pbr, pbr_neural[:TRAIN_STEPS], "
+                         "pbr_per_thread_stores")
+    ap.add_argument("--frames", type=int, default=3)
     ap.add_argument("--no-configs12", action="store_true",
                     help="skip the plain small (Blinn-Phong sphere) and geometry stress (1M-triangle soup) frames")
     return ap.parse_args()
@@ -567,8 +572,41 @@ def bench_uneven(r, stream, net, materials, with_cpu: bool):
     return out
 
 
+def profile_scene(args):
+    """Render one workload a few frames on cuda:0 (no timing, no JSON line): the command the
+    committed ncu summaries under profiles/ were captured from."""
+    import softglrender_gb300 as sg
+    from softglrender_gb300 import scenes as S
+    name, _, arg = args.profile_scene.partition(":")
+    r = sg.RendererCUDA(0)
+    if name == "plain_small":
+        scene = S.config_plain_small()
+    elif name == "geometry_stress":
+        scene = S.config_geometry_stress(n_tris=int(arg or 1_000_000))
+    elif name in ("pbr", "pbr_neural", "pbr_per_thread_stores"):
+        scene = S.config_pbr()
+    else:
+        raise SystemExit(f"unknown --profile-scene {name}")
+    if name == "pbr_per_thread_stores":
+        r.setTmaStore(False)
+    inst = S.SceneInstance(r, scene)
+    if name == "pbr_neural":
+        from softglrender_gb300 import neural as NN
+        _, net, _ = NN.train_neural_ibl(r, {}, inst=inst, steps=int(arg or 600), test_views=2, baselines=False)
+        for prog in NN.pbr_programs(inst):
+            net.bind(prog)
+    inst.render()
+    r.waitIdle()
+    for _ in range(args.frames):
+        inst.render()
+    r.waitIdle()
+    print(f"profile scene {args.profile_scene}: {args.frames} frames after a warm-up frame")
+
+
 def main():
     args = parse()
+    if args.profile_scene:
+        return profile_scene(args)
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":
         return main_reference(args, world, rank, pg)

@@ -281,11 +281,11 @@ __device__ __forceinline__ void tmaStore2d(const CUtensorMap *map, const void *s
                "r"((uint32_t) __cvta_generic_to_shared(smem)), "r"(x), "r"(y)
                : "memory");
 }
-// commit the thread's bulk stores and wait until they are complete (writes done, not only the
-// shared memory read), so the kernel's completion covers them
+// commit the thread's bulk stores and wait until they have read shared memory (the CTA may then
+// retire; the grid's completion, which the next chained kernel waits for, covers the writes)
 __device__ __forceinline__ void tmaCommitWait() {
   asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 // this thread's shared-memory writes become visible to the async (TMA) proxy
 __device__ __forceinline__ void fenceAsyncShared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }

@@ -59,11 +59,18 @@ constexpr int kRecordFloats = 16;
 // Encode one fragment's 12 inputs into row `row` of a core-matrix tile (BF16), one 16-byte store per
 // 8 features: the 8-feature chunks [C0, C1) go to tile columns 8 * (chunk - C0) of a tile with
 // `tileC` columns (the whole row: C0 = 0, C1 = 20, tileC = 160).
-template<int C0, int C1>
+// FAST (the shading kernels, judged by PSNR): sin / cos of pi x from the special-function unit
+// (__sincosf; the inputs lie in [-1, 1], where its error is below 1e-6, which can move a feature
+// across a BF16 rounding boundary, one BF16 ulp); otherwise sincospi (training and the inference
+// entry point, which the oracle checks).
+template<int C0, int C1, bool FAST = false>
 __device__ __forceinline__ void encodeChunks(const float *x, uint8_t *tile, int row, int tileC, bool oneFeature) {
   float s[kIn], c[kIn];
 #pragma unroll
-  for (int i = 0; i < kIn; i++) sincospif(x[i], &s[i], &c[i]);
+  for (int i = 0; i < kIn; i++) {
+    if (FAST) __sincosf(3.14159265358979f * x[i], &s[i], &c[i]);
+    else sincospif(x[i], &s[i], &c[i]);
+  }
 #pragma unroll
   for (int k = 0; k < kFreq; k++) {
 #pragma unroll
@@ -97,8 +104,9 @@ __device__ __forceinline__ void encodeChunks(const float *x, uint8_t *tile, int 
   }
 }
 
+template<bool FAST = false>
 __device__ __forceinline__ void encodeRow(const float *x, uint8_t *tile, int row, bool oneFeature) {
-  encodeChunks<0, 20>(x, tile, row, kK1, oneFeature);
+  encodeChunks<0, 20, FAST>(x, tile, row, kK1, oneFeature);
 }
 
 // Epilogue of a hidden layer for one row: 64 accumulator columns from TMEM (this thread's lane),

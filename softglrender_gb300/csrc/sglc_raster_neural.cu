@@ -145,7 +145,7 @@ __device__ __forceinline__ void neuralFlush(const DrawParams &p, NeuralCta &n, F
       pre.lo0 = pre.lo1 = pre.lo2 = pre.alpha = pre.ao = pre.e0 = pre.e1 = pre.e2 = 0.f;
     }
     // layer 1, features 0-79
-    encodeChunks<0, 10>(pre.x, n.xTile, n.row, 80, false);
+    encodeChunks<0, 10, true>(pre.x, n.xTile, n.row, 80, false);
     ntHandOff();
     if (threadIdx.x == 0) {
       tc::fenceAfter();
@@ -154,7 +154,7 @@ __device__ __forceinline__ void neuralFlush(const DrawParams &p, NeuralCta &n, F
     }
     ntWait(p, n);
     // layer 1, features 80-159 (the tile is free again)
-    encodeChunks<10, 20>(pre.x, n.xTile, n.row, 80, false);
+    encodeChunks<10, 20, true>(pre.x, n.xTile, n.row, 80, false);
     ntHandOff();
     if (threadIdx.x == 0) {
       tc::fenceAfter();

@@ -80,15 +80,21 @@ __device__ __forceinline__ uint32_t biasReluBf16(float a0, float a1, float b0, f
 // 64-column tile (same values as hiddenEpilogue in sglc_nn.cuh, in packed instructions)
 __device__ __forceinline__ void hiddenRow(uint32_t taddr, const float *bias, uint8_t *out, int row) {
 #pragma unroll
-  for (int h = 0; h < 4; h++) {
-    float a[16];
-    tc::ld16(taddr + 16 * h, a);
+  for (int h = 0; h < 2; h++) {   // 32 columns per TMEM load, one wait each
+    float a[32];
+    tc::ld32(taddr + 32 * h, a);
     tc::ldWait();
-    uint32_t w[8];
+    const float2 *b2 = reinterpret_cast<const float2 *>(bias + 32 * h);
+    uint32_t w[16];
 #pragma unroll
-    for (int j = 0; j < 8; j++) w[j] = biasReluBf16(a[2 * j], a[2 * j + 1], bias[16 * h + 2 * j], bias[16 * h + 2 * j + 1]);
-    *reinterpret_cast<uint4 *>(out + tc::tileOffset(row, 16 * h, 64)) = make_uint4(w[0], w[1], w[2], w[3]);
-    *reinterpret_cast<uint4 *>(out + tc::tileOffset(row, 16 * h + 8, 64)) = make_uint4(w[4], w[5], w[6], w[7]);
+    for (int j = 0; j < 16; j++) {
+      const float2 b = b2[j];
+      w[j] = biasReluBf16(a[2 * j], a[2 * j + 1], b.x, b.y);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      *reinterpret_cast<uint4 *>(out + tc::tileOffset(row, 32 * h + 8 * q, 64)) =
+          make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
   }
 }
 
@@ -286,7 +292,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_const
     const float x[kIn] = {in[0].x, in[0].y, in[0].z, in[0].w, in[1].x, in[1].y,
                           in[1].z, in[1].w, in[2].x, in[2].y, in[2].z, in[2].w};
     const float4 loAo = in[3], emA = in[4];
-    encodeRow(x, xTile, row, false);
+    encodeRow<true>(x, xTile, row, false);
     wgHandOff(wg);
     if (wgThread == 0) {   // layer 1: [128 x 160] x [160 x 64]
       tc::fenceAfter();
