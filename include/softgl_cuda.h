@@ -265,7 +265,9 @@ SGLC_API sglc_status sglc_get_draw_stats(sglc_context *ctx, sglc_draw_stats *out
 SGLC_API sglc_status sglc_set_stats_level(sglc_context *ctx, int32_t level);
 /* The CUDA stream the context enqueues on (as an opaque pointer, cudaStream_t). */
 SGLC_API sglc_status sglc_get_stream(sglc_context *ctx, void **stream);
-/* Raster tile edge in pixels (8, 16 or 32); picked by the autotuner, default 16. */
+/* Height of the raster tiles that heavy shading models' deferred kernels work on: 16 (16x16
+ * pixels, 256 threads per tile, the default) or 8 (16x8 pixels, 128 threads); other draws use
+ * 16x16. Picked by the autotuner (softglrender_gb300/autotune.py). */
 SGLC_API sglc_status sglc_set_tile_size(sglc_context *ctx, int32_t tile);
 /* 1 (default): shading models with a heavy fragment shader (Blinn-Phong, PBR, skybox / IBL, FXAA)
  * rasterise in three kernels: coverage and depth, then the fragment shader over every fragment, then

@@ -1,15 +1,15 @@
-"""Autotuner for synchronisation-free frames: picks working-array capacities, the raster tile order
-and eager-versus-graph submission for a given frame by measuring them.
+"""Autotuner for synchronisation-free frames: picks working-array capacities, the raster tile shape,
+the raster tile order and eager-versus-graph submission for a given frame by measuring them.
 
 1. Calibration: the frame runs once with exact sizing (one count read-back per draw); the peak
    counts over its draws (clip vertices and polygons, appended primitives, bin entries) times a
    headroom give the capacities, doubled until the frame runs without overflow (sglc_get_overflow);
    all candidates then share them.
-2. Candidates: raster tiles longest-list-first or in index order; the frame enqueued call by call
-   or captured once in a CUDA graph and replayed. Each runs `reps` times after warm-up, timed with
-   CUDA events on the renderer's stream; the fastest wins.
-The raster tile is 16 x 16 pixels with 256 threads in this build (the only tile size compiled), so
-tile size is reported, not searched.
+2. Candidates: the deferred raster's tile shape (16x16 pixels with 256 threads, or 16x8 with 128;
+   capacities calibrated for each, the reference's counterpart is its raster block size,
+   RendererSoft.h:128), raster tiles longest-list-first or in index order, and the frame enqueued
+   call by call or captured once in a CUDA graph and replayed. Each runs `reps` times after
+   warm-up, timed with CUDA events on the renderer's stream; the fastest wins.
 """
 from __future__ import annotations
 
@@ -53,6 +53,7 @@ class Tuned:
         if self.graph is not None:
             self.graph.launch()
         else:
+            self.r.setTileSize(self.result.tile)
             self.frame()
 
     def destroy(self) -> None:
@@ -79,9 +80,9 @@ def _timer(r: A.Renderer):
     return time_ms
 
 
-def autotune(r: A.Renderer, frame: Callable[[], None], headroom: float = 1.25, reps: int = 5,
-             heavy_first=(1, 0), graph=(False, True)) -> Tuned:
-    time_ms = _timer(r)
+def _calibrate(r: A.Renderer, frame: Callable[[], None], headroom: float) -> A.Capacity:
+    """Capacities from the peak counts of an exactly sized run, times a headroom, doubled until the
+    frame runs without overflow."""
     r.setCapacity(None)
     r.getPeakCounts()   # reset
     frame()
@@ -92,47 +93,60 @@ def autotune(r: A.Renderer, frame: Callable[[], None], headroom: float = 1.25, r
                      max(1024, int(pk.appended_primitives * headroom) + 1024),
                      max(4096, int(pk.bin_entries * headroom) + 4096), 1,
                      int(pk.fragments * headroom) + 4096 if pk.fragments else 0)
-    # fit the capacities once (eager); every candidate then uses them unchanged, so no working array
-    # grows (and no captured graph loses its buffers) after the first capture
     for _ in range(8):
         r.setCapacity(cap)
         frame()
         if r.getOverflow() == 0:
-            break
+            return cap
         cap = A.Capacity(cap.clip_vertices * 2, cap.clip_polygons * 2, cap.appended_primitives * 2,
                          cap.bin_entries * 2, 1, cap.fragments * 2)
-    else:
-        r.setCapacity(None)
-        raise RuntimeError("autotune: the frame does not fit its capacities")
-    table, best, best_graph = [], None, None
-    for hf in heavy_first:
-        for use_graph in graph:
-            cap.heavy_first = hf
-            r.setCapacity(cap)
-            g = None
-            if use_graph:
-                frame()   # the uncaptured run that sizes every working array
-                r.waitIdle()
-                g = Graph(r).capture(frame)
-                run = g.launch
-            else:
-                run = frame
-            for _ in range(2):
-                run()
-            ms = time_ms(run, reps)
-            ok = r.getOverflow() == 0
-            table.append({"heavy_first": hf, "graph": use_graph, "ms": round(ms, 4), "fits": ok})
-            if ok and (best is None or ms < best.ms):
-                if best_graph is not None:
-                    best_graph.destroy()
-                best = TuneResult(A.Capacity(cap.clip_vertices, cap.clip_polygons, cap.appended_primitives,
-                                             cap.bin_entries, hf, cap.fragments), hf, use_graph, ms)
-                best_graph = g
-            elif g is not None:
-                g.destroy()
+    r.setCapacity(None)
+    raise RuntimeError("autotune: the frame does not fit its capacities")
+
+
+def autotune(r: A.Renderer, frame: Callable[[], None], headroom: float = 1.25, reps: int = 5,
+             heavy_first=(1, 0), graph=(False, True), tiles=(16, 8)) -> Tuned:
+    """Search tile height (16x16 or 16x8 raster tiles of the deferred kernels, sglc_set_tile_size)
+    x tile order x eager-or-graph submission; capacities are calibrated per tile height. The winner's
+    settings stay on the renderer (and its graph, when it won, is captured afresh under them)."""
+    time_ms = _timer(r)
+    table, best, best_cap = [], None, None
+    for tile in tiles:
+        r.setTileSize(tile)
+        cap = _calibrate(r, frame, headroom)
+        for hf in heavy_first:
+            for use_graph in graph:
+                cap.heavy_first = hf
+                r.setCapacity(cap)
+                g = None
+                if use_graph:
+                    frame()   # the uncaptured run that sizes every working array
+                    r.waitIdle()
+                    g = Graph(r).capture(frame)
+                    run = g.launch
+                else:
+                    run = frame
+                for _ in range(2):
+                    run()
+                ms = time_ms(run, reps)
+                ok = r.getOverflow() == 0
+                table.append({"tile": tile, "threads_per_tile": 16 * tile, "heavy_first": hf, "graph": use_graph,
+                              "ms": round(ms, 4), "fits": ok})
+                if g is not None:
+                    g.destroy()
+                if ok and (best is None or ms < best.ms):
+                    best = TuneResult(A.Capacity(cap.clip_vertices, cap.clip_polygons, cap.appended_primitives,
+                                                 cap.bin_entries, hf, cap.fragments), hf, use_graph, ms,
+                                      tile=tile, threads_per_tile=16 * tile)
     if best is None:
         r.setCapacity(None)
         raise RuntimeError("autotune: no candidate fitted its capacities")
     best.table = table
+    r.setTileSize(best.tile)
     r.setCapacity(best.capacity)
-    return Tuned(r, frame, best, best_graph)
+    g = None
+    if best.graph:
+        frame()   # sizes the arrays for the winner's settings, then the graph is captured under them
+        r.waitIdle()
+        g = Graph(r).capture(frame)
+    return Tuned(r, frame, best, g)

@@ -214,6 +214,7 @@ struct Ctx {
   std::string err;
   bool earlyZ = true;
   int tile = 16;
+  int tileH = 16;                    // sglc_set_tile_size: height of the deferred raster's tiles
   Viewport vp{};
   int fb = 0, vao = 0, prog = 0, states = 0;
   PendingClear clear;
@@ -487,15 +488,15 @@ EncodeTiledFn encodeTiledFn() {
 }
 
 // A linear attachment of h rows of w pixels with spp 32-bit samples each, as a 2D tensor map
-// (inner dimension w * spp) with a 16x16-pixel box. False where TMA cannot address it: a base
+// (inner dimension w * spp) with a box of one raster tile (16 x boxH pixels). False where TMA cannot address it: a base
 // that is not 16-byte aligned or a row that is not a multiple of 16 bytes (then the kernels store
 // per thread).
-bool encodeAttachment(CUtensorMap *m, void *base, int w, int h, int spp) {
+bool encodeAttachment(CUtensorMap *m, void *base, int w, int h, int spp, int boxH) {
   EncodeTiledFn fn = encodeTiledFn();
   if (!fn || !base || ((uintptr_t) base & 15) || ((size_t) w * spp * 4) % 16 || w <= 0 || h <= 0) return false;
   const cuuint64_t dims[2] = {(cuuint64_t) w * spp, (cuuint64_t) h};
   const cuuint64_t strides[1] = {(cuuint64_t) w * spp * 4};
-  const cuuint32_t box[2] = {(cuuint32_t) (16 * spp), 16};
+  const cuuint32_t box[2] = {(cuuint32_t) (16 * spp), (cuuint32_t) boxH};
   const cuuint32_t estr[2] = {1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
@@ -865,12 +866,16 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     p.dms = dt->desc.multi_sample;
   }
   p.samples = ct ? (ct->desc.multi_sample ? 4 : 1) : (dt->desc.multi_sample ? 4 : 1);
+  // raster tile: 16 pixels wide; 16 high, or the context's 8 for draws the deferred kernels raster
+  // (the fused raster kernel has one shape)
+  p.tile = c->tile;
+  p.tileH = c->deferredShading && ct && deferredShadingModel(p.shading) && !pointsLines ? c->tileH : 16;
   // TMA write-back of whole tiles by the deferred raster kernels (single-view draws)
-  if (!bv && c->tmaStore && c->tile == 16) {
-    if (ct && encodeAttachment(&p.tmColor, p.color, p.cw, p.ch, p.samples) &&
-        (p.samples == 1 || encodeAttachment(&p.tmResolved, p.resolved, p.cw, p.ch, 1)))
+  if (!bv && c->tmaStore) {
+    if (ct && encodeAttachment(&p.tmColor, p.color, p.cw, p.ch, p.samples, p.tileH) &&
+        (p.samples == 1 || encodeAttachment(&p.tmResolved, p.resolved, p.cw, p.ch, 1, p.tileH)))
       p.tmaStore |= 1;
-    if (dt && encodeAttachment(&p.tmDepth, p.depth, p.dw, p.dh, p.samples)) p.tmaStore |= 2;
+    if (dt && encodeAttachment(&p.tmDepth, p.depth, p.dw, p.dh, p.samples, p.tileH)) p.tmaStore |= 2;
   }
   std::vector<ViewTarget> targets;
   if (bv) {
@@ -927,10 +932,9 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
   p.nv = (int) vao.nv;
   p.indices = vao.idx;
   p.ntri = (int) (vao.nidx / 3);
-  p.tile = c->tile;
   int fw = std::max(p.cw, p.dw), fh = std::max(p.ch, p.dh);
   p.tilesX = (fw + p.tile - 1) / p.tile;
-  p.tilesY = (fh + p.tile - 1) / p.tile;
+  p.tilesY = (fh + p.tileH - 1) / p.tileH;
   int numTiles = p.tilesX * p.tilesY;
   p.views = 1;
   p.nvView = p.nv;
@@ -1098,10 +1102,12 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     bool deferShade = c->deferredShading && ct && deferredShadingModel(p.shading);
     long long chunks = 0;
     if (deferShade) {
-      const long long warps = ((long long) numTiles + 3 * 64) * 8;   // split tiles have 4 x 8 warps
+      const long long warps = ((long long) numTiles + 3 * 64) * (p.tileH / 2);   // split tiles: 4 CTAs
       chunks = deferred ? (c->cap.fragments + kChunk - 1) / kChunk
                         : (long long) (fragBound / kChunk) + warps + 1;
       if (chunks < 1 || chunks * kChunk > (1ll << 28)) deferShade = false;   // single kernel instead
+      if (!deferShade && p.tileH != 16)
+        return c->fail(SGLC_ERR_OVERFLOW, "draw: more than 2^28 fragment records need 16x16 tiles (sglc_set_tile_size)");
     }
     if (deferShade) {
       CK(c->recA.ensure(sizeof(int4) * (size_t) chunks * kChunk));
@@ -1109,7 +1115,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       CK(c->recColor.ensure(sizeof(float4) * (size_t) chunks * kChunk));
       CK(c->chunkNext.ensure(sizeof(int) * (size_t) chunks));
       CK(c->chunkFill.ensure(sizeof(int) * (size_t) chunks));
-      CK(c->warpHead.ensure(sizeof(int) * (size_t) numTiles * 32));
+      CK(c->warpHead.ensure(sizeof(int) * (size_t) numTiles * 4 * (p.tileH / 2)));
       CK(c->recDense.ensure(sizeof(int) * (size_t) chunks * kChunk));
       p.recA = c->recA.as<int4>();
       p.recB = c->recB.as<float2>();
@@ -1921,8 +1927,9 @@ sglc_status sglc_set_tma_store(sglc_context *ctx, int32_t enable) {
 
 sglc_status sglc_set_tile_size(sglc_context *ctx, int32_t tile) {
   CTX;
-  if (tile != 16) return c->fail(SGLC_ERR_UNSUPPORTED, "set_tile_size: this build rasterises 16x16 tiles");
-  c->tile = tile;
+  if (tile != 16 && tile != 8)
+    return c->fail(SGLC_ERR_UNSUPPORTED, "set_tile_size: raster tiles are 16 (16x16 pixels) or 8 (16x8) high");
+  c->tileH = tile;
   return SGLC_OK;
 }
 

@@ -177,7 +177,8 @@ struct DrawParams {
   int *valA, *valB;               // primitive ids
   int pairCap;
   int *tileStart, *tileEnd;
-  int tile;                       // tile edge in pixels (8, 16 or 32)
+  int tile;                       // raster tile width in pixels (16)
+  int tileH;                      // raster tile height in pixels: 16, or 8 (deferred raster only)
   int tilesX, tilesY;
   unsigned long long *fragCounter;   // FS invocations (instrumented runs only), else null
   int needDeriv;                  // the FS reads texcoord derivatives (a bound 2D sampler with a LOD callback)
@@ -199,9 +200,9 @@ struct DrawParams {
   // TMA write-back of whole 16x16 tiles (single-view draws): tensor maps over this GPU's colour
   // (samples interleaved), resolved and depth attachments; tmaStore bit 0: colour and resolved by
   // k_rop, bit 1: depth by k_raster_cov; 0: per-thread stores
-  alignas(64) CUtensorMap tmColor;
-  alignas(64) CUtensorMap tmResolved;
-  alignas(64) CUtensorMap tmDepth;
+  CUtensorMap tmColor;
+  CUtensorMap tmResolved;
+  CUtensorMap tmDepth;
   int tmaStore;
   // batched views (sglc_draw_views): one pipeline pass over `views` copies of the draw that differ
   // only in uniforms and attachments. nv / ntri above count all views' vertices / triangles;

@@ -322,7 +322,7 @@ __device__ __forceinline__ unsigned long long setupPrim(const DrawParams &p, int
         T.rx1 = min(min((int) floorf(maxX) + 1, bsxL + kBlock), fw - 1);
         T.ry1 = min(min((int) floorf(maxY) + 1, bsyL + kBlock), fh - 1);
         if (T.rx1 >= T.rx0 && T.ry1 >= T.ry0) {
-          int tx0 = T.rx0 / p.tile, tx1 = T.rx1 / p.tile, ty0 = T.ry0 / p.tile, ty1 = T.ry1 / p.tile;
+          int tx0 = T.rx0 / p.tile, tx1 = T.rx1 / p.tile, ty0 = T.ry0 / p.tileH, ty1 = T.ry1 / p.tileH;
           cnt = (tx1 - tx0 + 1) * (ty1 - ty0 + 1);
         }
       }
@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(256) k_bin_emit(const __grid_constant__ DrawPa
   const TriSetup &T = p.tri[i];
   int off = p.pairOff[i];
   const uint32_t viewBase = (uint32_t) T.view * (uint32_t) p.tilesPerView;
-  int tx0 = T.rx0 / p.tile, tx1 = T.rx1 / p.tile, ty0 = T.ry0 / p.tile, ty1 = T.ry1 / p.tile;
+  int tx0 = T.rx0 / p.tile, tx1 = T.rx1 / p.tile, ty0 = T.ry0 / p.tileH, ty1 = T.ry1 / p.tileH;
   for (int ty = ty0; ty <= ty1; ty++)
     for (int tx = tx0; tx <= tx1; tx++) {
       if (off >= p.pairCap) {

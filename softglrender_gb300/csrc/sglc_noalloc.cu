@@ -264,6 +264,7 @@ extern "C" SGLC_API sglc_status sglc_draw_vertex_color_noalloc(const sglc_noallo
   p.tileStart = reinterpret_cast<int *>(scratch + oTileStart);
   p.tileEnd = reinterpret_cast<int *>(scratch + oTileEnd);
   p.tile = kTile;
+  p.tileH = kTile;
   p.tilesX = (d->width + kTile - 1) / kTile;
   p.tilesY = (d->height + kTile - 1) / kTile;
   int numTiles = p.tilesX * p.tilesY;

@@ -754,12 +754,13 @@ struct CovSlot {
   int prim;
 };
 
-template<int S, bool HAS_DEPTH>
-__global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid_constant__ DrawParams p) {
+template<int S, bool HAS_DEPTH, int W>
+__global__ void __launch_bounds__(32 * W, (S == 4 ? 2 : 4) * 8 / W) k_raster_cov(const __grid_constant__ DrawParams p) {
+  constexpr int TH = 2 * W;   // tile height in pixels (width 16): W warps of 8x4 pixels, two per row
   chainEnter();
-  __shared__ CovSlot covSlots[8][32];
-  __shared__ unsigned candMasks[8][32];
-  __shared__ int covQueue[8][64];
+  __shared__ CovSlot covSlots[W][32];
+  __shared__ unsigned candMasks[W][32];
+  __shared__ int covQueue[W][64];
   const TileJob job = tileJob(p);
   if (job.skip) return;
   const int tile = job.tile, rh = job.rows;
@@ -767,7 +768,7 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
   const int vtile = tile - view * p.tilesPerView;
   const int tx = vtile % p.tilesX, ty = vtile / p.tilesX;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4 + job.part;
+  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * TH + (warp >> 1) * 4 + job.part;
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
   const bool own = (lane >> 3) < rh;   // this lane has a pixel (all 32 in a whole tile, 8 in a split one)
   const bool inD = HAS_DEPTH && own && px < p.dw && py < p.dh;
@@ -778,7 +779,7 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
     // an empty list (most tiles of a frame): no records, so no part in the dense list (the whole
     // CTA leaves here); only the warps' empty record lists and, on a pass's first draw, the
     // cleared depth
-    if (lane == 0) p.warpHead[(tile * 4 + job.part) * 8 + warp] = -1;
+    if (lane == 0) p.warpHead[(tile * 4 + job.part) * W + warp] = -1;
     if (inD && p.pendingClear && p.clearDepthFlag) {
       const size_t pix = (size_t) py * p.dw + px;
       if (S == 4) {
@@ -1025,14 +1026,14 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
     }
   }
   if (lane == 0) {
-    p.warpHead[(tile * 4 + job.part) * 8 + warp] = head;
+    p.warpHead[(tile * 4 + job.part) * W + warp] = head;
     if (ch >= 0) p.chunkFill[ch] = cnt;
     if (p.fragCounter && total) atomicAdd(p.fragCounter, total);
   }
   // the dense record list: one contiguous run per CTA (one atomic), each warp's records in its
   // list order inside it, so the shading kernel reads no unfilled chunk slots and keeps each warp's
   // records together
-  __shared__ int wRecs[8], ctaBase;
+  __shared__ int wRecs[W], ctaBase;
   int recs = 0;
   for (int c = head; c >= 0;) {   // this warp's chunks: every one full but the last
     const int f = c == ch ? cnt : kChunk;
@@ -1043,7 +1044,7 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
   __syncthreads();
   if (threadIdx.x == 0) {
     int sum = 0;
-    for (int w = 0; w < 8; w++) sum += wRecs[w];
+    for (int w = 0; w < W; w++) sum += wRecs[w];
     ctaBase = sum ? atomicAdd(&p.counters[kCntDense], sum) : 0;
   }
   __syncthreads();
@@ -1057,8 +1058,8 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
   }
   if ((p.tmaStore & 2) && rh == 4) {
     // whole tile: its depth samples through shared memory and one TMA bulk store
-    __shared__ alignas(128) float sDep[16 * 16 * S];
-    const int li = (py - ty * 16) * 16 + (px - tx * 16);
+    __shared__ alignas(128) float sDep[16 * TH * S];
+    const int li = (py - ty * TH) * 16 + (px - tx * 16);
     sDep[li * S] = fb.d0;
     if (S == 4) {
       sDep[li * 4 + 1] = fb.d1;
@@ -1068,7 +1069,7 @@ __global__ void __launch_bounds__(256, S == 4 ? 2 : 4) k_raster_cov(const __grid
     fenceAsyncShared();
     __syncthreads();
     if (threadIdx.x == 0) {
-      tmaStore2d(&p.tmDepth, sDep, tx * 16 * S, ty * 16);
+      tmaStore2d(&p.tmDepth, sDep, tx * 16 * S, ty * TH);
       tmaCommitWait();
     }
     return;
@@ -1104,12 +1105,13 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ DrawPa
 }
 
 // colour operations in each warp's list order, then colour store and MSAA resolve
-template<int S>
-__global__ void __launch_bounds__(256) k_rop(const __grid_constant__ DrawParams p) {
+template<int S, int W>
+__global__ void __launch_bounds__(32 * W) k_rop(const __grid_constant__ DrawParams p) {
+  constexpr int TH = 2 * W;   // tile height in pixels (width 16)
   chainEnter();
-  __shared__ float4 scol[8][kChunk];
-  __shared__ uint32_t smeta[8][kChunk];
-  __shared__ uint32_t sown[8][kChunk];
+  __shared__ float4 scol[W][kChunk];
+  __shared__ uint32_t smeta[W][kChunk];
+  __shared__ uint32_t sown[W][kChunk];
   if (blockIdx.x == 0 && threadIdx.x == 0) {   // the draw's last kernel: its peak chunk use and flags
     if (p.ropPeakChunks) *p.ropPeakChunks = max(*p.ropPeakChunks, p.counters[kCntChunks]);
     if (p.ropSticky) *p.ropSticky |= p.counters[2];
@@ -1121,7 +1123,7 @@ __global__ void __launch_bounds__(256) k_rop(const __grid_constant__ DrawParams 
   const int vtile = tile - view * p.tilesPerView;
   const int tx = vtile % p.tilesX, ty = vtile / p.tilesX;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4 + job.part;
+  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * TH + (warp >> 1) * 4 + job.part;
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
   const bool inC = (lane >> 3) < job.rows && px < p.cw && py < p.ch;
   uint32_t *colorBuf = p.viewTarget ? p.viewTarget[view].color : p.color;
@@ -1138,7 +1140,7 @@ __global__ void __launch_bounds__(256) k_rop(const __grid_constant__ DrawParams 
       fb.c0 = colorBuf[pix];
     }
   }
-  int ch = p.warpHead[(tile * 4 + job.part) * 8 + warp];
+  int ch = p.warpHead[(tile * 4 + job.part) * W + warp];
   while (ch >= 0) {
     const int fill = p.chunkFill[ch];
     const size_t r = (size_t) ch * kChunk + lane;
@@ -1185,9 +1187,9 @@ __global__ void __launch_bounds__(256) k_rop(const __grid_constant__ DrawParams 
     // whole tile: stage its colour samples and resolved pixels in shared memory in the
     // attachments' own order and write each with one TMA bulk store (pixels outside the
     // attachment are clipped by the copy)
-    __shared__ alignas(128) uint32_t sCol[16 * 16 * S];
-    __shared__ alignas(128) uint32_t sRes[S == 4 ? 256 : 1];
-    const int li = (py - ty * 16) * 16 + (px - tx * 16);
+    __shared__ alignas(128) uint32_t sCol[16 * TH * S];
+    __shared__ alignas(128) uint32_t sRes[S == 4 ? 16 * TH : 1];
+    const int li = (py - ty * TH) * 16 + (px - tx * 16);
     sCol[li * S] = fb.c0;
     if (S == 4) {
       sCol[li * 4 + 1] = fb.c1;
@@ -1198,8 +1200,8 @@ __global__ void __launch_bounds__(256) k_rop(const __grid_constant__ DrawParams 
     fenceAsyncShared();
     __syncthreads();
     if (threadIdx.x == 0) {
-      tmaStore2d(&p.tmColor, sCol, tx * 16 * S, ty * 16);
-      if (S == 4) tmaStore2d(&p.tmResolved, sRes, tx * 16, ty * 16);
+      tmaStore2d(&p.tmColor, sCol, tx * 16 * S, ty * TH);
+      if (S == 4) tmaStore2d(&p.tmResolved, sRes, tx * 16, ty * TH);
       tmaCommitWait();
     }
     return;

@@ -31,15 +31,28 @@ bool deferredShadingModel(int shading) {
   return false;   // base / vertex colour: the shader is a load
 }
 
+// the coverage kernel for the tile shape: 16 x 16 pixels (8 warps) or 16 x 8 (4 warps)
+template<int W>
+static void launchCoverage(const DrawParams &p, bool hasDepth, int grid, cudaStream_t st) {
+  if (p.samples == 4) {
+    if (hasDepth) launchChained(k_raster_cov<4, true, W>, dim3(grid), dim3(32 * W), 0, st, p);
+    else launchChained(k_raster_cov<4, false, W>, dim3(grid), dim3(32 * W), 0, st, p);
+  } else {
+    if (hasDepth) launchChained(k_raster_cov<1, true, W>, dim3(grid), dim3(32 * W), 0, st, p);
+    else launchChained(k_raster_cov<1, false, W>, dim3(grid), dim3(32 * W), 0, st, p);
+  }
+}
+
+template<int W>
+static void launchRop(const DrawParams &p, int grid, cudaStream_t st) {
+  if (p.samples == 4) launchChained(k_rop<4, W>, dim3(grid), dim3(32 * W), 0, st, p);
+  else launchChained(k_rop<1, W>, dim3(grid), dim3(32 * W), 0, st, p);
+}
+
 void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st, cudaEvent_t evCov, cudaEvent_t evShade) {
   const int grid = p.views * p.tilesPerView + 3 * (p.tileOrder ? p.heavySlots : 0);   // see tileJob
-  if (p.samples == 4) {
-    if (hasDepth) launchChained(k_raster_cov<4, true>, dim3(grid), dim3(256), 0, st, p);
-    else launchChained(k_raster_cov<4, false>, dim3(grid), dim3(256), 0, st, p);
-  } else {
-    if (hasDepth) launchChained(k_raster_cov<1, true>, dim3(grid), dim3(256), 0, st, p);
-    else launchChained(k_raster_cov<1, false>, dim3(grid), dim3(256), 0, st, p);
-  }
+  if (p.tileH == 8) launchCoverage<4>(p, hasDepth, grid, st);
+  else launchCoverage<8>(p, hasDepth, grid, st);
   if (evCov) cudaEventRecord(evCov, st);
   switch (p.shading) {
     case SH_VCOLOR: launchShadeModel<SH_VCOLOR>(p, st); break;
@@ -54,8 +67,8 @@ void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st, c
     case SH_FXAA: launchShadeEnvironment(p, st); break;
   }
   if (evShade) cudaEventRecord(evShade, st);
-  if (p.samples == 4) launchChained(k_rop<4>, dim3(grid), dim3(256), 0, st, p);
-  else launchChained(k_rop<1>, dim3(grid), dim3(256), 0, st, p);
+  if (p.tileH == 8) launchRop<4>(p, grid, st);
+  else launchRop<8>(p, grid, st);
 }
 
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {

@@ -200,3 +200,44 @@ def test_tma_tile_write_back_equals_per_thread_stores(name, cuda_lib, oracle_lib
         for k in pb:
             assert np.array_equal(pa[k].view(np.uint8), pb[k].view(np.uint8)), k
     assert_outputs_match(a, render(oracle_lib, scene)[0], name, exact_color=name.startswith("soup"))
+
+
+def _render_tile(lib, scene, tile):
+    r = A.Renderer(lib, 0)
+    r.setTileSize(tile)
+    inst = S.SceneInstance(r, scene)
+    inst.render()
+    r.waitIdle()
+    out = [inst.outputs(i) for i in range(len(scene.passes))]
+    r.destroy()
+    return out
+
+
+TILE_SCENES = {
+    "pbr_msaa4": lambda: S.config_pbr(width=320, height=180, lon=96, lat=48, tex=128, prefilter=64, irradiance=8),
+    "blinn_1x_odd": lambda: S.config_plain_small(width=301, height=203, lon=48, lat=24, tex=64),
+    # dense enough that the heaviest tiles are split over four CTAs
+    "dense_pbr_msaa4": lambda: S.config_pbr(width=160, height=96, lon=512, lat=256, tex=64, prefilter=32,
+                                            irradiance=8),
+    "soup_msaa4_two_passes": lambda: S.config_geometry_stress(n_tris=20000, width=250, height=150, samples=4),
+}
+
+
+@pytest.mark.parametrize("name", sorted(TILE_SCENES))
+def test_16x8_tiles_equal_16x16_tiles(name, cuda_lib, oracle_lib):
+    """The deferred raster on 16x8 tiles (4 warps per CTA) gives the images of 16x16 tiles (8 warps)
+    and the oracle's: a pixel still belongs to one warp, whose list keeps the primitive order."""
+    scene = TILE_SCENES[name]()
+    a = _render_tile(cuda_lib, scene, 8)
+    b = _render_tile(cuda_lib, scene, 16)
+    for pa, pb in zip(a, b):
+        for k in pb:
+            assert np.array_equal(pa[k].view(np.uint8), pb[k].view(np.uint8)), k
+    assert_outputs_match(a, render(oracle_lib, scene)[0], name, exact_color=name.startswith("soup"))
+
+
+def test_tile_size_rejects_other_shapes(cuda_lib):
+    r = A.Renderer(cuda_lib, 0)
+    with pytest.raises(A.SoftGLError):
+        r.setTileSize(32)
+    r.destroy()
