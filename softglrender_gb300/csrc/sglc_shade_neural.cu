@@ -14,7 +14,7 @@
 //   * pow, reciprocal and normalisation use the fast intrinsics.
 //
 // Two kernels. k_neural_surface evaluates the surface terms at high occupancy (128-thread CTAs,
-// 64 registers, 16 CTAs per SM over a grid-stride loop): the chain of dependent loads (record,
+// up to 10 per SM, over a grid-stride loop): the chain of dependent loads (record,
 // triangle set-up, varyings, texels) needs many warps in flight, which a kernel holding tensor
 // memory and 160 KB of operand tiles cannot have. It writes 80 B per record in dense order.
 // k_shade_neural then runs the network: one persistent CTA per SM with four warpgroups (512
@@ -23,8 +23,8 @@
 // network's 160 features in its row of the warpgroup's [128][160] BF16 tile; one elected thread
 // issues the three layers' tcgen05.mma chains (layer 1 over K = 160 in one chain, then 64 -> 64
 // and 64 -> 3), each completed through the warpgroup's mbarrier; the epilogues read the FP32
-// accumulators back from the warpgroup's 128 TMEM columns (bias, ReLU and the BF16 conversion in
-// packed f32x2 / bf16x2 instructions) into the same tile. The four warpgroups' tensor-core round
+// accumulators back from the warpgroup's 128 TMEM columns (bias add, then ReLU and the BF16
+// conversion in one bf16x2 instruction) into the same tile. The four warpgroups' tensor-core round
 // trips overlap each other's feature and epilogue work.
 // A wait that runs out of polls sets the draw's device error flag (kFlagNeuralTimeout in the
 // context's sticky flags, read by sglc_get_overflow); that tile's colours are then unspecified.
@@ -59,25 +59,15 @@ __device__ __forceinline__ void wgHandOff(int wg) {
   wgSync(wg);
 }
 
-__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
-  unsigned long long r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-
-// (a0 + b0, a1 + b1) in one packed FP32 instruction, then ReLU and round to BF16 pairs
+// a0 + b0, a1 + b1, then ReLU and rounding to a BF16 pair in one conversion
 __device__ __forceinline__ uint32_t biasReluBf16(float a0, float a1, float b0, float b1) {
-  unsigned long long s;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(s) : "l"(pack2(a0, a1)), "l"(pack2(b0, b1)));
-  float s0, s1;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(s0), "=f"(s1) : "l"(s));
   uint32_t r;
-  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(s1), "f"(s0));
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(a1 + b1), "f"(a0 + b0));
   return r;
 }
 
 // hidden-layer epilogue of one row: 64 accumulator columns + bias, ReLU, BF16 into row `row` of a
-// 64-column tile (same values as hiddenEpilogue in sglc_nn.cuh, in packed instructions)
+// 64-column tile (same values as hiddenEpilogue in sglc_nn.cuh, fewer instructions)
 __device__ __forceinline__ void hiddenRow(uint32_t taddr, const float *bias, uint8_t *out, int row) {
 #pragma unroll
   for (int h = 0; h < 2; h++) {   // 32 columns per TMEM load, one wait each
@@ -127,8 +117,22 @@ __device__ __forceinline__ Surface surface(const DrawParams &p, int4 a, float2 b
   const float *r0 = p.vVary + (size_t) t.vid0 * p.varyStride;
   const float *r1 = p.vVary + (size_t) t.vid1 * p.varyStride;
   const float *r2 = p.vVary + (size_t) t.vid2 * p.varyStride;
-  const Vary vy{r0, r1, r2, b0, b1, b2};
-  const float u = vy[0], v = vy[1];
+  // the varyings this path reads, one 16-byte load per group of four floats of each vertex row
+  // (rows are 32-byte aligned), interpolated at the use: u v, normal, view and light direction, N, T
+  auto group = [&](int g, float4 &q0, float4 &q1, float4 &q2) {
+    q0 = __ldg(reinterpret_cast<const float4 *>(r0) + g);
+    q1 = __ldg(reinterpret_cast<const float4 *>(r1) + g);
+    q2 = __ldg(reinterpret_cast<const float4 *>(r2) + g);
+  };
+  auto lerp = [&](float a0, float a1, float a2) { return __fmaf_rn(a2, b2, __fmaf_rn(a1, b1, a0 * b0)); };
+  auto at3 = [&](int i) {   // i = 4 g (+ 0): components i, i + 1, i + 2
+    float4 q0, q1, q2;
+    group(i >> 2, q0, q1, q2);
+    return mk3(lerp(q0.x, q1.x, q2.x), lerp(q0.y, q1.y, q2.y), lerp(q0.z, q1.z, q2.z));
+  };
+  float4 g00, g01, g02;
+  group(0, g00, g01, g02);
+  const float u = lerp(g00.x, g01.x, g02.x), v = lerp(g00.y, g01.y, g02.y);
   float dudx = 0.f, dvdx = 0.f, dudy = 0.f, dvdy = 0.f;
   if (p.needDeriv) {
     // screen-space gradients of the linear barycentrics (the reference's barycentric(),
@@ -143,8 +147,8 @@ __device__ __forceinline__ Surface surface(const DrawParams &p, int4 a, float2 b
     const float g0x = (t.w0 * l0x - b0 * dDx) * invD, g0y = (t.w0 * l0y - b0 * dDy) * invD;
     const float g1x = (t.w1 * l1x - b1 * dDx) * invD, g1y = (t.w1 * l1y - b1 * dDy) * invD;
     const float g2x = (t.w2 * l2x - b2 * dDx) * invD, g2y = (t.w2 * l2y - b2 * dDy) * invD;
-    const float u0 = __ldg(r0), u1 = __ldg(r1), u2 = __ldg(r2);
-    const float v0 = __ldg(r0 + 1), v1 = __ldg(r1 + 1), v2 = __ldg(r2 + 1);
+    const float u0 = g00.x, u1 = g01.x, u2 = g02.x;
+    const float v0 = g00.y, v1 = g01.y, v2 = g02.y;
     dudx = u0 * g0x + u1 * g1x + u2 * g2x;
     dudy = u0 * g0y + u1 * g1y + u2 * g2y;
     dvdx = v0 * g0x + v1 * g1x + v2 * g2x;
@@ -162,8 +166,8 @@ __device__ __forceinline__ Surface surface(const DrawParams &p, int4 a, float2 b
   s.ao = p.def[3] ? hwSample(p, 3, u, v, dudx, dvdx, dudy, dvdy).x : 1.f;
   f3 N;
   if (p.def[1]) {
-    const f3 Nv = fastNormalize(vy.v3(20));
-    f3 T = fastNormalize(vy.v3(24));
+    const f3 Nv = fastNormalize(at3(20));
+    f3 T = fastNormalize(at3(24));
     T = fastNormalize(T - dot3(T, Nv) * Nv);
     const f3 B = cross3(T, Nv);
     const float4 tn4 = hwSample(p, 1, u, v, dudx, dvdx, dudy, dvdy);
@@ -171,14 +175,14 @@ __device__ __forceinline__ Surface surface(const DrawParams &p, int4 a, float2 b
     N = fastNormalize(mk3(T.x * tn.x + B.x * tn.y + Nv.x * tn.z, T.y * tn.x + B.y * tn.y + Nv.y * tn.z,
                           T.z * tn.x + B.z * tn.y + Nv.z * tn.z));
   } else {
-    N = fastNormalize(vy.v3(4));
+    N = fastNormalize(at3(4));
   }
-  const f3 V = fastNormalize(vy.v3(12));
+  const f3 V = fastNormalize(at3(12));
   const float NdotV = gmax(dot3(N, V), 0.f);
   f3 Lo = mk3(0.f, 0.f, 0.f);
   if (uI32(U, 320)) {   // the point light's GGX term (PbrSoft.h:258-290), fast arithmetic
     const float PI = 3.14159265359f;
-    const f3 ldir = vy.v3(16);
+    const f3 ldir = at3(16);
     const f3 L = fastNormalize(ldir);
     const f3 H = fastNormalize(V + L);
     const f3 lDir = ldir * 0.2f;
@@ -216,7 +220,7 @@ __device__ __forceinline__ Surface surface(const DrawParams &p, int4 a, float2 b
 
 // Stage 1 (high occupancy, no tensor cores): the surface terms of every record, written in the
 // dense record order as five float4: the network's 12 inputs, then (Lo, ao) and (emissive, alpha).
-__global__ void __launch_bounds__(128, 8) k_neural_surface(const __grid_constant__ DrawParams p) {
+__global__ void __launch_bounds__(128, 10) k_neural_surface(const __grid_constant__ DrawParams p) {
   const int nRec = min(p.counters[kCntDense], p.chunkCap * kChunk);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nRec; i += gridDim.x * blockDim.x) {
     const int r = p.recDense[i];
@@ -348,7 +352,7 @@ void launchShadeNeural(const DrawParams &p, cudaStream_t st) {
   setDynamicSmemOnce(attr, k_shade_neural, kSnBytes);
   int sms = 152, dev = 0;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  k_neural_surface<<<sms * 16, 128, 0, st>>>(p);
+  k_neural_surface<<<sms * 10, 128, 0, st>>>(p);
   k_shade_neural<<<sms, kThreads, kSnBytes, st>>>(p);
 }
 
