@@ -17,15 +17,15 @@
 // up to 10 per SM, over a grid-stride loop): the chain of dependent loads (record,
 // triangle set-up, varyings, texels) needs many warps in flight, which a kernel holding tensor
 // memory and 160 KB of operand tiles cannot have. It writes 80 B per record in dense order.
-// k_shade_neural then runs the network: one persistent CTA per SM with four warpgroups (512
-// threads). Each warpgroup walks its own sequence of 128-record tiles, loading the next tile's
-// rows while the current tile's MMAs run: every thread encodes one record's 12 inputs into the
-// network's 160 features in its row of the warpgroup's [128][160] BF16 tile; one elected thread
-// issues the three layers' tcgen05.mma chains (layer 1 over K = 160 in one chain, then 64 -> 64
-// and 64 -> 3), each completed through the warpgroup's mbarrier; the epilogues read the FP32
-// accumulators back from the warpgroup's 128 TMEM columns (bias add, then ReLU and the BF16
-// conversion in one bf16x2 instruction) into the same tile. The four warpgroups' tensor-core round
-// trips overlap each other's feature and epilogue work.
+// k_shade_neural then runs the network: one persistent CTA per SM with eight warpgroups (1,024
+// threads, 64 registers each: enough warps in flight to cover the tensor-core round trips and the
+// TMEM loads). Each warpgroup walks its own sequence of 128-record tiles: every thread encodes one
+// record's 12 inputs into the network's features in its row of the warpgroup's [128][80] BF16 tile,
+// 80 features at a time; one elected thread issues the tcgen05.mma chains (layer 1 in two K halves
+// of 80 accumulating into the same TMEM columns, then 64 -> 64 and 64 -> 3), each completed through
+// the warpgroup's mbarrier; the epilogues read the FP32 accumulators back from the warpgroup's 64
+// TMEM columns (bias add, then ReLU and the BF16 conversion in one bf16x2 instruction) into the same
+// tile. The eight warpgroups' round trips overlap each other's feature and epilogue work.
 // A wait that runs out of polls sets the draw's device error flag (kFlagNeuralTimeout in the
 // context's sticky flags, read by sglc_get_overflow); that tile's colours are then unspecified.
 #include "sglc_raster.cuh"
@@ -38,15 +38,17 @@ using namespace nn;
 
 namespace {
 
-constexpr int kWG = 4;                                      // warpgroups per CTA (one CTA per SM)
-constexpr int kThreads = 128 * kWG;
-constexpr int kXBytes = 128 * kK1 * 2;                      // [128][160] BF16 tile of one warpgroup
+constexpr int kWG = 8;                                      // warpgroups per CTA (one CTA per SM)
+constexpr int kThreads = 128 * kWG;                         // 1024 threads, 64 registers each
+constexpr int kXCols = kK1 / 2;                             // layer 1 runs in two K halves of 80
+constexpr int kXBytes = 128 * kXCols * 2;                   // [128][80] BF16 tile of one warpgroup
 constexpr int kSnX = 0;
 constexpr int kSnImg = kSnX + kWG * kXBytes;                // weight image (sglc_nn.cuh)
 constexpr int kSnBar = kSnImg + kImgBytes;                  // one mbarrier per warpgroup
 constexpr int kSnTmem = kSnBar + kWG * 8;
 constexpr int kSnBytes = kSnTmem + 16 + 1024;               // + slack for the 1024-B alignment
 static_assert(kSnImg % 1024 == 0 && kSnBar % 8 == 0, "tile and barrier alignment");
+static_assert(kXBytes >= 128 * kHid * 2, "the hidden tiles reuse the input tile");
 static_assert(kSnBytes <= 227 * 1024, "fits one CTA per SM");
 
 // barrier among the 128 threads of warpgroup wg (ids 1..4; 0 is __syncthreads)
@@ -70,21 +72,19 @@ __device__ __forceinline__ uint32_t biasReluBf16(float a0, float a1, float b0, f
 // 64-column tile (same values as hiddenEpilogue in sglc_nn.cuh, fewer instructions)
 __device__ __forceinline__ void hiddenRow(uint32_t taddr, const float *bias, uint8_t *out, int row) {
 #pragma unroll
-  for (int h = 0; h < 2; h++) {   // 32 columns per TMEM load, one wait each
-    float a[32];
-    tc::ld32(taddr + 32 * h, a);
+  for (int h = 0; h < 4; h++) {
+    float a[16];
+    tc::ld16(taddr + 16 * h, a);
     tc::ldWait();
-    const float2 *b2 = reinterpret_cast<const float2 *>(bias + 32 * h);
-    uint32_t w[16];
+    const float2 *b2 = reinterpret_cast<const float2 *>(bias + 16 * h);
+    uint32_t w[8];
 #pragma unroll
-    for (int j = 0; j < 16; j++) {
+    for (int j = 0; j < 8; j++) {
       const float2 b = b2[j];
       w[j] = biasReluBf16(a[2 * j], a[2 * j + 1], b.x, b.y);
     }
-#pragma unroll
-    for (int q = 0; q < 4; q++)
-      *reinterpret_cast<uint4 *>(out + tc::tileOffset(row, 32 * h + 8 * q, 64)) =
-          make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+    *reinterpret_cast<uint4 *>(out + tc::tileOffset(row, 16 * h, 64)) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4 *>(out + tc::tileOffset(row, 16 * h + 8, 64)) = make_uint4(w[4], w[5], w[6], w[7]);
   }
 }
 
@@ -255,11 +255,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_const
   for (int i = threadIdx.x; i < kImgBytes / 16; i += kThreads)
     reinterpret_cast<uint4 *>(img)[i] = __ldg(reinterpret_cast<const uint4 *>(p.nnImage) + i);
   if (wgThread == 0) tc::barInit(bar, 1);
-  if (warp == 0) tc::tmemAlloc(tmemSlot, 128 * kWG);
+  if (warp == 0) tc::tmemAlloc(tmemSlot, 64 * kWG);
   tc::fenceBefore();
   __syncthreads();
   tc::fenceAfter();
-  const uint32_t tmem = *tmemSlot + 128u * (uint32_t) wg;               // this warpgroup's 128 columns
+  // this warpgroup's 64 TMEM columns: layer 1's accumulator, then layer 2's, then layer 3's
+  const uint32_t tmem = *tmemSlot + 64u * (uint32_t) wg;
   const uint32_t lanes = tmem + ((uint32_t) ((warp & 3) * 32) << 16);   // this thread's TMEM lane
   uint32_t phase = 0;
   bool timedOut = false;
@@ -270,63 +271,47 @@ __global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_const
     phase ^= 1u;
     tc::fenceAfter();
   };
+  auto issue = [&](uint32_t aC, uint32_t bBase, int bC, int bCol, int N, int K, bool acc) {
+    wgHandOff(wg);
+    if (wgThread == 0) {
+      tc::fenceAfter();
+      issueKMajor(tmem, sX, aC, 0, bBase, bC, bCol, N, K, acc);
+      tc::commit(bar);
+    }
+    wait();
+  };
 
   const int nRec = min(p.counters[kCntDense], p.chunkCap * kChunk);
-  const int stride = gridDim.x * kThreads;
-  int t0 = (blockIdx.x * kWG + wg) * 128;
-  // the rows of the warpgroup's next tile are loaded one tile ahead (in flight during the MMAs)
-  float4 in[5];
-  int rec = -1;
-  auto load = [&](int t) {
-    const int di = t + wgThread;
-    rec = -1;
-    if (t < nRec && di < nRec) {
-      rec = p.recDense[di];
+  for (int t0 = (blockIdx.x * kWG + wg) * 128; t0 < nRec; t0 += gridDim.x * kThreads) {
+    const int di = t0 + wgThread;
+    int r = -1;
+    float4 in[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) in[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (di < nRec) {
+      r = p.recDense[di];
       const float4 *q = p.nnIn + (size_t) 5 * di;
 #pragma unroll
       for (int k = 0; k < 5; k++) in[k] = q[k];
-    } else {
-#pragma unroll
-      for (int k = 0; k < 5; k++) in[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-  };
-  load(t0);
-  for (; t0 < nRec; t0 += stride) {
-    const int r = rec;
     const float x[kIn] = {in[0].x, in[0].y, in[0].z, in[0].w, in[1].x, in[1].y,
                           in[1].z, in[1].w, in[2].x, in[2].y, in[2].z, in[2].w};
-    const float4 loAo = in[3], emA = in[4];
-    encodeRow<true>(x, xTile, row, false);
-    wgHandOff(wg);
-    if (wgThread == 0) {   // layer 1: [128 x 160] x [160 x 64]
-      tc::fenceAfter();
-      issueKMajor(tmem, sX, kK1, 0, sW1, kK1, 0, kHid, kK1, false);
-      tc::commit(bar);
-    }
-    load(t0 + stride);
-    wait();
+    // layer 1 over features 0-79, then 80-159 (the tile is free again once the first half is done)
+    encodeChunks<0, 10, true>(x, xTile, row, kXCols, false);
+    issue(kXCols, sW1, kK1, 0, kHid, kXCols, false);
+    encodeChunks<10, 20, true>(x, xTile, row, kXCols, false);
+    issue(kXCols, sW1, kK1, kXCols, kHid, kXCols, true);
     hiddenRow(lanes, bias, xTile, row);
-    wgHandOff(wg);
-    if (wgThread == 0) {   // layer 2: [128 x 64] x [64 x 64]
-      tc::fenceAfter();
-      issueKMajor(tmem + 64, sX, kHid, 0, sW2, kHid, 0, kHid, kHid, false);
-      tc::commit(bar);
-    }
-    wait();
-    hiddenRow(lanes + 64, bias + 64, xTile, row);
-    wgHandOff(wg);
-    if (wgThread == 0) {   // layer 3: [128 x 64] x [64 x 16] (3 outputs used)
-      tc::fenceAfter();
-      issueKMajor(tmem, sX, kHid, 0, sW3, kHid, 0, kOutPad, kHid, false);
-      tc::commit(bar);
-    }
-    wait();
+    issue(kHid, sW2, kHid, 0, kHid, kHid, false);          // layer 2: [128 x 64] x [64 x 64]
+    hiddenRow(lanes, bias + 64, xTile, row);
+    issue(kHid, sW3, kHid, 0, kOutPad, kHid, false);       // layer 3: [128 x 64] x [64 x 16], 3 used
     float y[16];
     tc::ld16(lanes, y);
     tc::ldWait();
     tc::fenceBefore();
     if (r >= 0) {
       // ambient = max(y, 0)^2 * ao; colour = (ambient + Lo)^(1/2.2) + emissive (PbrSoft.h:311-321)
+      const float4 loAo = in[3], emA = in[4];
       const float a0 = gmax(y[0] + bias[128], 0.f), a1 = gmax(y[1] + bias[129], 0.f), a2 = gmax(y[2] + bias[130], 0.f);
       const f3 c = mk3(a0 * a0, a1 * a1, a2 * a2) * loAo.w + mk3(loAo.x, loAo.y, loAo.z);
       f3 col = mk3(__powf(c.x, 1.f / 2.2f), __powf(c.y, 1.f / 2.2f), __powf(c.z, 1.f / 2.2f));
@@ -340,7 +325,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_const
   tc::fenceBefore();
   __syncthreads();
   tc::fenceAfter();
-  if (warp == 0) tc::tmemFree(*tmemSlot, 128 * kWG);
+  if (warp == 0) tc::tmemFree(*tmemSlot, 64 * kWG);
 }
 
 }  // namespace
