@@ -206,7 +206,8 @@ SGLC_API sglc_status sglc_texture_read_image(sglc_context *ctx, sglc_handle tex,
 SGLC_API sglc_status sglc_texture_store_to_file(sglc_context *ctx, sglc_handle tex, const char *path);
 SGLC_API sglc_status sglc_texture_load_from_file(sglc_context *ctx, sglc_handle tex, const char *path);
 
-/* ---- vertex array (Renderer::createVertexArrayObject, Renderer.h:37; VertexSoft.h:16-31) ---- */
+/* ---- vertex array (Renderer::createVertexArrayObject, Renderer.h:37; VertexSoft.h:16-31) ----
+ * Lengths are in bytes, as VertexArray::vertexesBufferLength / indexBufferLength (Vertex.h:33-36). */
 SGLC_API sglc_status sglc_create_vertex_array(sglc_context *ctx, const void *vertexes, size_t vertexes_len,
                                               size_t stride, const int32_t *indices, size_t indices_len,
                                               sglc_handle *out);

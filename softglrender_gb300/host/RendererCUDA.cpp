@@ -107,6 +107,18 @@ void TextureCUDA::storeToFile(const char *path) {
   renderer->check(sglc_texture_store_to_file(renderer->ctx(), handle, path), "storeToFile");
 }
 
+bool TextureCUDA::setLevelData(uint32_t layer, uint32_t level, const void *data, size_t bytes) {
+  return renderer->check(sglc_texture_set_level_data(renderer->ctx(), handle, (int32_t) layer, (int32_t) level, data,
+                                                     bytes),
+                         "setLevelData");
+}
+
+bool TextureCUDA::readImage(void *out, size_t bytes, uint32_t layer, uint32_t level, bool resolved) {
+  return renderer->check(sglc_texture_read_image(renderer->ctx(), handle, (int32_t) layer, (int32_t) level,
+                                                 resolved ? 1 : 0, out, bytes),
+                         "readImage");
+}
+
 bool FrameBufferCUDA::isValid() {
   int32_t v = 0;
   renderer->check(sglc_framebuffer_is_valid(renderer->ctx(), handle, &v), "isValid");

@@ -30,6 +30,13 @@ class TextureCUDA : public Texture {
   // TextureSoft::loadFromFile / storeToFile (TextureSoft.h:166-215): the IBL cache format
   bool loadFromFile(const char *path);
   void storeToFile(const char *path);
+  // One level of one layer from host memory (the reference fills prefiltered IBL levels by
+  // rendering into a level attachment, Environment.cpp:152-195; a cached chain uploads directly)
+  bool setLevelData(uint32_t layer, uint32_t level, const void *data, size_t bytes);
+  // The pixels dumpImage writes, copied to host memory in linear row order (the software back-end's
+  // callers read TextureSoft's buffers directly): RGBA8 4 B, FLOAT32 4 B per sample; a multi-sample
+  // texture gives its 4 interleaved samples per pixel, or with `resolved` its resolved RGBA8 image
+  bool readImage(void *out, size_t bytes, uint32_t layer, uint32_t level, bool resolved);
 
   RendererCUDA *renderer;
   sglc_handle handle;
