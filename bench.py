@@ -734,7 +734,8 @@ def main():
             tuned_n.run()
         torch.cuda.synchronize()
         n_ms = timed_frames(args.steps, tuned_n.run)
-        n_raster, _, _ = raster_ms_median()
+        n_parts = {}
+        n_raster, _, _ = raster_ms_median(parts=n_parts)
         tuned_n.destroy()
         r.setCapacity(None)
         for prog in progs:   # the rest of the bench (end to end) runs the plain shader
@@ -748,6 +749,10 @@ def main():
             "frames_per_s": round(n_fps, 3), "mfrag_per_s": round(frags * n_fps / 1e6, 2),
             "raster_ms": round(n_raster, 4), "speedup_vs_plain_frames": round(n_fps / (args.steps / (sum(frame_ms) / 1e3)), 3),
             "speedup_vs_plain_raster": round(raster_ms / n_raster, 3),
+            # the fragment shader's own throughput: the same records shaded by the plain PBR+IBL
+            # kernel against the neural kernels (surface terms + network), CUDA events around them
+            "shading_ms": round(n_parts["shading"], 4), "plain_shading_ms": round(parts["shading"], 4),
+            "speedup_vs_plain_shading": round(parts["shading"] / n_parts["shading"], 3),
             "psnr_db_mean": round(rep.psnr_mean, 2), "psnr_db_min": round(min(rep.psnr_views), 2),
             "max_abs_lsb": int(max(rep.maxabs_views)), "threshold_db": 40.0, "bound": bool(rep.bound),
             "psnr_db_without_network": round(float(np.mean(rep.psnr_without)), 2),

@@ -320,7 +320,28 @@ __global__ void __launch_bounds__(128, 1) k_nn_tile(const TileArgs a) {
   if (warp == 0) tc::tmemFree(tmem, kTmCols);
 }
 
+// the inference image's copy of parameter i (layout in sglc_nn.cuh); a bias goes in as two BF16
+// values whose sum carries 16 significant bits
+__device__ __forceinline__ void writeInferImage(uint8_t *img, int i, float w) {
+  uint8_t *im = img + kInferOffset;
+  auto put = [&](int base, int r, int c, int C, float v) {
+    *reinterpret_cast<__nv_bfloat16 *>(im + base + tc::tileOffset(r, c, C)) = __float2bfloat16_rn(v);
+  };
+  auto putBias = [&](int base, int r, int c, int C) {
+    const float hi = __bfloat162float(__float2bfloat16_rn(w));
+    put(base, r, c, C, w);
+    put(base, r, c + 1, C, w - hi);
+  };
+  if (i < kB1) put(kIW1, i / kFeat, inferColumn(i % kFeat), kK1, w);
+  else if (i < kW2) putBias(kIW1, i - kB1, 158, kK1);
+  else if (i < kB2) put(kIW2, (i - kW2) / 64, (i - kW2) % 64, 80, w);
+  else if (i < kW3) putBias(kIW2, i - kB2, 64, 80);
+  else if (i < kB3) put(kIW3, (i - kW3) / 64, (i - kW3) % 64, 80, w);
+  else if (i < kParams) putBias(kIW3, i - kB3, 64, 80);
+}
+
 __device__ __forceinline__ void writeImage(uint8_t *img, int i, float w) {
+  writeInferImage(img, i, w);
   if (i < kB1) {
     *reinterpret_cast<__nv_bfloat16 *>(img + kImgW1 + tc::tileOffset(i / kFeat, i % kFeat, kK1)) = __float2bfloat16_rn(w);
   } else if (i < kW2) {
@@ -496,12 +517,12 @@ SGLC_API sglc_status sglc_neural_create(sglc_context *ctx, uint64_t seed, sglc_n
   if ((e = cudaMalloc(&n->params, kParams * sizeof(float))) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&n->m, kParams * sizeof(float))) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&n->v, kParams * sizeof(float))) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc(&n->image, kImgBytes)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&n->image, kImageAllocBytes)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&n->capCount, sizeof(unsigned long long))) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&n->scratch, kPartialStride * sizeof(float))) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&n->error, sizeof(int))) != cudaSuccess) return fail(e);
   cudaStream_t st = ctxStream(ctx);
-  cudaMemsetAsync(n->image, 0, kImgBytes, st);
+  cudaMemsetAsync(n->image, 0, kImageAllocBytes, st);
   cudaMemsetAsync(n->error, 0, sizeof(int), st);
   cudaMemsetAsync(n->capCount, 0, sizeof(unsigned long long), st);
   // He-uniform initialisation from the seed (biases zero)

@@ -53,6 +53,28 @@ constexpr int kImgBias = kImgW3 + kOutPad * kHid * 2;    // 30720
 constexpr int kImgBytes = kImgBias + (64 + 64 + 4) * 4;  // 31248
 static_assert(kImgBytes % 16 == 0, "image copies in 16-byte pieces");
 
+// Inference image (follows the training image in the same allocation, at kInferOffset): the same
+// network laid out for the deferred shading kernel, which encodes a fragment in two halves of 80
+// features (inputs 0-5, then inputs 6-11) and folds every bias into its layer's MMA:
+//   W1 [64][160]: half H (columns 80H..80H+79) holds inputs 6H+j, j = 0..5: column 80H + 12k + 2j
+//                 = sin(2^k pi x), + 1 = cos, k = 0..5; column 80H + 72 + j = x; columns 158 and
+//                 159 hold b1 split into a BF16 high part and the BF16 rounding of its remainder
+//                 (the encoder puts 1 in both input columns), 78 and 79 stay zero;
+//   W2 [64][80], W3 [16][80]: columns 0-63 the weights, 64 and 65 the bias split the same way
+//                 (the hidden tiles carry ones there), the rest zero.
+constexpr int kIW1 = 0;
+constexpr int kIW2 = kIW1 + kHid * kK1 * 2;               // 20480
+constexpr int kIW3 = kIW2 + kHid * 80 * 2;                // 30720
+constexpr int kInferBytes = kIW3 + kOutPad * 80 * 2;      // 33280
+constexpr int kInferOffset = kImgBytes;                   // 16-byte aligned
+constexpr int kImageAllocBytes = kInferOffset + kInferBytes;
+
+// inference-image column of canonical first-layer feature f (0..155)
+__host__ __device__ constexpr int inferColumn(int f) {
+  return f < 144 ? 80 * (((f % 24) / 2) / 6) + 12 * (f / 24) + 2 * (((f % 24) / 2) % 6) + (f & 1)
+                 : 80 * ((f - 144) / 6) + 72 + (f - 144) % 6;
+}
+
 // training record: 12 inputs, 3 targets (sqrt of the ambient term), 1 pad
 constexpr int kRecordFloats = 16;
 

@@ -19,13 +19,17 @@
 // memory and 160 KB of operand tiles cannot have. It writes 80 B per record in dense order.
 // k_shade_neural then runs the network: one persistent CTA per SM with eight warpgroups (1,024
 // threads, 64 registers each: enough warps in flight to cover the tensor-core round trips and the
-// TMEM loads). Each warpgroup walks its own sequence of 128-record tiles: every thread encodes one
-// record's 12 inputs into the network's features in its row of the warpgroup's [128][80] BF16 tile,
-// 80 features at a time; one elected thread issues the tcgen05.mma chains (layer 1 in two K halves
-// of 80 accumulating into the same TMEM columns, then 64 -> 64 and 64 -> 3), each completed through
-// the warpgroup's mbarrier; the epilogues read the FP32 accumulators back from the warpgroup's 64
-// TMEM columns (bias add, then ReLU and the BF16 conversion in one bf16x2 instruction) into the same
-// tile. The eight warpgroups' round trips overlap each other's feature and epilogue work.
+// TMEM loads). Each warpgroup walks its own sequence of 128-record tiles with its own [128][80] BF16
+// tile, mbarrier and 64 TMEM columns, over the inference image of the weights (sglc_nn.cuh):
+//   * every thread encodes its record's inputs 0-5 into its tile row (80 features: sin / cos at six
+//     frequencies from one special-function sin / cos and packed FP32x2 double-angle recurrences,
+//     the inputs themselves), one elected thread issues layer 1's first K half; then inputs 6-11 and
+//     two ones (the bias columns) for the second half, accumulating into the same TMEM columns;
+//   * the epilogues only read the FP32 accumulators (bias included) and apply ReLU with the BF16
+//     rounding in one bf16x2 conversion per pair, into the same tile, whose columns 64-65 hold ones
+//     for the next layer's bias (64 -> 64, then 64 -> 3 with N = 16);
+//   * each of the record's three 32-byte row parts is loaded just before the wait that hides it.
+// The eight warpgroups' round trips overlap each other's feature and epilogue work.
 // A wait that runs out of polls sets the draw's device error flag (kFlagNeuralTimeout in the
 // context's sticky flags, read by sglc_get_overflow); that tile's colours are then unspecified.
 #include "sglc_raster.cuh"
@@ -43,12 +47,12 @@ constexpr int kThreads = 128 * kWG;                         // 1024 threads, 64 
 constexpr int kXCols = kK1 / 2;                             // layer 1 runs in two K halves of 80
 constexpr int kXBytes = 128 * kXCols * 2;                   // [128][80] BF16 tile of one warpgroup
 constexpr int kSnX = 0;
-constexpr int kSnImg = kSnX + kWG * kXBytes;                // weight image (sglc_nn.cuh)
-constexpr int kSnBar = kSnImg + kImgBytes;                  // one mbarrier per warpgroup
+constexpr int kSnImg = kSnX + kWG * kXBytes;                // inference image (sglc_nn.cuh)
+constexpr int kSnBar = kSnImg + kInferBytes;                // one mbarrier per warpgroup
 constexpr int kSnTmem = kSnBar + kWG * 8;
 constexpr int kSnBytes = kSnTmem + 16 + 1024;               // + slack for the 1024-B alignment
 static_assert(kSnImg % 1024 == 0 && kSnBar % 8 == 0, "tile and barrier alignment");
-static_assert(kXBytes >= 128 * kHid * 2, "the hidden tiles reuse the input tile");
+static_assert(kXCols == 80 && kInferBytes % 16 == 0, "the hidden tiles (64 + 16 columns) reuse the input tile");
 static_assert(kSnBytes <= 227 * 1024, "fits one CTA per SM");
 
 // barrier among the 128 threads of warpgroup wg (ids 1..4; 0 is __syncthreads)
@@ -61,30 +65,95 @@ __device__ __forceinline__ void wgHandOff(int wg) {
   wgSync(wg);
 }
 
-// a0 + b0, a1 + b1, then ReLU and rounding to a BF16 pair in one conversion
-__device__ __forceinline__ uint32_t biasReluBf16(float a0, float a1, float b0, float b1) {
+// ReLU and rounding to a BF16 pair in one conversion (a0 in the low half)
+__device__ __forceinline__ uint32_t reluBf16(float a0, float a1) {
   uint32_t r;
-  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(a1 + b1), "f"(a0 + b0));
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(a1), "f"(a0));
+  return r;
+}
+__device__ __forceinline__ uint32_t bf16Pair(float a0, float a1) {
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(a1), "f"(a0));
   return r;
 }
 
-// hidden-layer epilogue of one row: 64 accumulator columns + bias, ReLU, BF16 into row `row` of a
-// 64-column tile (same values as hiddenEpilogue in sglc_nn.cuh, fewer instructions)
-__device__ __forceinline__ void hiddenRow(uint32_t taddr, const float *bias, uint8_t *out, int row) {
+// packed FP32x2 arithmetic (two lanes per instruction)
+__device__ __forceinline__ uint64_t f2(float a, float b) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void unf2(uint64_t v, float &a, float &b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// One half of a fragment's first-layer features (inference image column order, sglc_nn.cuh) into
+// row `row` of an 80-column tile: inputs x[0..5] are network inputs 6H..6H+5. Word 6k + j of the
+// row holds (sin, cos)(2^k pi x_j); the recurrence t = 2 s, s' = t c, c' = 1 - t s (one rounding)
+// runs on input pairs in packed FP32x2 instructions.
+template<int H>
+__device__ __forceinline__ void encodeHalf(const float *x, uint8_t *tile, int row) {
+  float s[6], c[6];
+#pragma unroll
+  for (int j = 0; j < 6; j++) __sincosf(3.14159265358979f * x[j], &s[j], &c[j]);
+  uint32_t w[40];
+  const uint64_t one2 = f2(1.f, 1.f);
+#pragma unroll
+  for (int k = 0; k < kFreq; k++) {
+#pragma unroll
+    for (int j = 0; j < 6; j++) w[6 * k + j] = bf16Pair(s[j], c[j]);
+#pragma unroll
+    for (int q = 0; q < 10; q++)   // chunks complete after this frequency go out now
+      if (4 * q + 3 < 6 * (k + 1) && 4 * q + 3 >= 6 * k)
+        *reinterpret_cast<uint4 *>(tile + tc::tileOffset(row, 8 * q, 80)) =
+            make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+    if (k + 1 < kFreq) {
+#pragma unroll
+      for (int j = 0; j < 6; j += 2) {
+        const uint64_t sv = f2(s[j], s[j + 1]), cv = f2(c[j], c[j + 1]);
+        const uint64_t t = add2(sv, sv);
+        const uint64_t sn = mul2(t, cv);
+        const uint64_t cn = fma2(t ^ 0x8000000080000000ull, sv, one2);
+        unf2(sn, s[j], s[j + 1]);
+        unf2(cn, c[j], c[j + 1]);
+      }
+    }
+  }
+  w[36] = bf16Pair(x[0], x[1]);
+  w[37] = bf16Pair(x[2], x[3]);
+  w[38] = bf16Pair(x[4], x[5]);
+  w[39] = H == 1 ? 0x3F803F80u : 0u;   // the two bias inputs of the second half
+  *reinterpret_cast<uint4 *>(tile + tc::tileOffset(row, 72, 80)) = make_uint4(w[36], w[37], w[38], w[39]);
+}
+
+// hidden-layer epilogue of one row: 64 accumulator columns (bias included), ReLU, BF16 into
+// columns 0-63 of row `row` of the 80-column tile
+__device__ __forceinline__ void reluRow(uint32_t taddr, uint8_t *tile, int row) {
 #pragma unroll
   for (int h = 0; h < 4; h++) {
     float a[16];
     tc::ld16(taddr + 16 * h, a);
     tc::ldWait();
-    const float2 *b2 = reinterpret_cast<const float2 *>(bias + 16 * h);
-    uint32_t w[8];
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const float2 b = b2[j];
-      w[j] = biasReluBf16(a[2 * j], a[2 * j + 1], b.x, b.y);
-    }
-    *reinterpret_cast<uint4 *>(out + tc::tileOffset(row, 16 * h, 64)) = make_uint4(w[0], w[1], w[2], w[3]);
-    *reinterpret_cast<uint4 *>(out + tc::tileOffset(row, 16 * h + 8, 64)) = make_uint4(w[4], w[5], w[6], w[7]);
+    for (int q = 0; q < 2; q++)
+      *reinterpret_cast<uint4 *>(tile + tc::tileOffset(row, 16 * h + 8 * q, 80)) =
+          make_uint4(reluBf16(a[8 * q], a[8 * q + 1]), reluBf16(a[8 * q + 2], a[8 * q + 3]),
+                     reluBf16(a[8 * q + 4], a[8 * q + 5]), reluBf16(a[8 * q + 6], a[8 * q + 7]));
   }
 }
 
@@ -118,7 +187,7 @@ __device__ __forceinline__ Surface surface(const DrawParams &p, int4 a, float2 b
   const float *r1 = p.vVary + (size_t) t.vid1 * p.varyStride;
   const float *r2 = p.vVary + (size_t) t.vid2 * p.varyStride;
   // the varyings this path reads, one 16-byte load per group of four floats of each vertex row
-  // (rows are 32-byte aligned), interpolated at the use: u v, normal, view and light direction, N, T
+  // (rows are 32-byte aligned), interpolated at the use: u v, normal, world position, N, T
   auto group = [&](int g, float4 &q0, float4 &q1, float4 &q2) {
     q0 = __ldg(reinterpret_cast<const float4 *>(r0) + g);
     q1 = __ldg(reinterpret_cast<const float4 *>(r1) + g);
@@ -177,12 +246,16 @@ __device__ __forceinline__ Surface surface(const DrawParams &p, int4 a, float2 b
   } else {
     N = fastNormalize(at3(4));
   }
-  const f3 V = fastNormalize(at3(12));
+  // the camera and light directions are affine in the world position (PbrSoft.h VS: u_cameraPosition
+  // - worldPos, u_pointLightPosition - worldPos), so they are taken from the interpolated position:
+  // one varying group instead of two
+  const f3 world = at3(8);
+  const f3 V = fastNormalize(ld3(U + 272) - world);
   const float NdotV = gmax(dot3(N, V), 0.f);
   f3 Lo = mk3(0.f, 0.f, 0.f);
   if (uI32(U, 320)) {   // the point light's GGX term (PbrSoft.h:258-290), fast arithmetic
     const float PI = 3.14159265359f;
-    const f3 ldir = at3(16);
+    const f3 ldir = ld3(U + 288) - world;
     const f3 L = fastNormalize(ldir);
     const f3 H = fastNormalize(V + L);
     const f3 lDir = ldir * 0.2f;
@@ -247,13 +320,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_const
   uint8_t *xTile = sm + kSnX + wg * kXBytes;
   const uint32_t sX = tc::smemAddr(xTile);
   uint8_t *img = sm + kSnImg;
-  const uint32_t sW1 = tc::smemAddr(img + kImgW1), sW2 = tc::smemAddr(img + kImgW2), sW3 = tc::smemAddr(img + kImgW3);
-  const float *bias = reinterpret_cast<const float *>(img + kImgBias);
+  const uint32_t sW1 = tc::smemAddr(img + kIW1), sW2 = tc::smemAddr(img + kIW2), sW3 = tc::smemAddr(img + kIW3);
   uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kSnBar) + wg;
   uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(sm + kSnTmem);
   const int row = (warp & 3) * 32 + lane;
-  for (int i = threadIdx.x; i < kImgBytes / 16; i += kThreads)
-    reinterpret_cast<uint4 *>(img)[i] = __ldg(reinterpret_cast<const uint4 *>(p.nnImage) + i);
+  const uint4 *src = reinterpret_cast<const uint4 *>(p.nnImage + kInferOffset);
+  for (int i = threadIdx.x; i < kInferBytes / 16; i += kThreads) reinterpret_cast<uint4 *>(img)[i] = __ldg(src + i);
   if (wgThread == 0) tc::barInit(bar, 1);
   if (warp == 0) tc::tmemAlloc(tmemSlot, 64 * kWG);
   tc::fenceBefore();
@@ -271,48 +343,59 @@ __global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_const
     phase ^= 1u;
     tc::fenceAfter();
   };
-  auto issue = [&](uint32_t aC, uint32_t bBase, int bC, int bCol, int N, int K, bool acc) {
+  // the tile's shared-memory writes -> one MMA chain D[128 x N] (+)= tile[128 x 80] * B[80 x N]
+  auto issue = [&](uint32_t bBase, int bC, int bCol, int N, bool acc) {
     wgHandOff(wg);
     if (wgThread == 0) {
       tc::fenceAfter();
-      issueKMajor(tmem, sX, aC, 0, bBase, bC, bCol, N, K, acc);
+      issueKMajor(tmem, sX, kXCols, 0, bBase, bC, bCol, N, kXCols, acc);
       tc::commit(bar);
     }
-    wait();
   };
 
   const int nRec = min(p.counters[kCntDense], p.chunkCap * kChunk);
   for (int t0 = (blockIdx.x * kWG + wg) * 128; t0 < nRec; t0 += gridDim.x * kThreads) {
     const int di = t0 + wgThread;
-    int r = -1;
-    float4 in[5];
-#pragma unroll
-    for (int k = 0; k < 5; k++) in[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (di < nRec) {
-      r = p.recDense[di];
-      const float4 *q = p.nnIn + (size_t) 5 * di;
-#pragma unroll
-      for (int k = 0; k < 5; k++) in[k] = q[k];
+    const bool live = di < nRec;
+    const float4 *q = p.nnIn + (size_t) 5 * di;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 q0 = live ? q[0] : z4, q1 = live ? q[1] : z4;
+    // layer 1: inputs 0-5 (N, V), then inputs 6-11 (roughness, metallic, albedo, N.V) and the bias
+    {
+      const float x[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
+      encodeHalf<0>(x, xTile, row);
     }
-    const float x[kIn] = {in[0].x, in[0].y, in[0].z, in[0].w, in[1].x, in[1].y,
-                          in[1].z, in[1].w, in[2].x, in[2].y, in[2].z, in[2].w};
-    // layer 1 over features 0-79, then 80-159 (the tile is free again once the first half is done)
-    encodeChunks<0, 10, true>(x, xTile, row, kXCols, false);
-    issue(kXCols, sW1, kK1, 0, kHid, kXCols, false);
-    encodeChunks<10, 20, true>(x, xTile, row, kXCols, false);
-    issue(kXCols, sW1, kK1, kXCols, kHid, kXCols, true);
-    hiddenRow(lanes, bias, xTile, row);
-    issue(kHid, sW2, kHid, 0, kHid, kHid, false);          // layer 2: [128 x 64] x [64 x 64]
-    hiddenRow(lanes, bias + 64, xTile, row);
-    issue(kHid, sW3, kHid, 0, kOutPad, kHid, false);       // layer 3: [128 x 64] x [64 x 16], 3 used
+    issue(sW1, kK1, 0, kHid, false);
+    const float4 q2 = live ? q[2] : z4;
+    wait();
+    {
+      const float x[6] = {q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+      encodeHalf<1>(x, xTile, row);
+    }
+    issue(sW1, kK1, kXCols, kHid, true);
+    wait();
+    reluRow(lanes, xTile, row);
+    *reinterpret_cast<uint4 *>(xTile + tc::tileOffset(row, 64, 80)) = make_uint4(0x3F803F80u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4 *>(xTile + tc::tileOffset(row, 72, 80)) = make_uint4(0u, 0u, 0u, 0u);
+    issue(sW2, 80, 0, kHid, false);                       // layer 2: [128 x 80] x [80 x 64]
+    wait();
+    reluRow(lanes, xTile, row);
+    issue(sW3, 80, 0, kOutPad, false);                    // layer 3: [128 x 80] x [80 x 16], 3 used
+    int r = -1;
+    float4 loAo = z4, emA = z4;
+    if (live) {
+      r = p.recDense[di];
+      loAo = q[3];
+      emA = q[4];
+    }
+    wait();
     float y[16];
     tc::ld16(lanes, y);
     tc::ldWait();
     tc::fenceBefore();
     if (r >= 0) {
       // ambient = max(y, 0)^2 * ao; colour = (ambient + Lo)^(1/2.2) + emissive (PbrSoft.h:311-321)
-      const float4 loAo = in[3], emA = in[4];
-      const float a0 = gmax(y[0] + bias[128], 0.f), a1 = gmax(y[1] + bias[129], 0.f), a2 = gmax(y[2] + bias[130], 0.f);
+      const float a0 = gmax(y[0], 0.f), a1 = gmax(y[1], 0.f), a2 = gmax(y[2], 0.f);
       const f3 c = mk3(a0 * a0, a1 * a1, a2 * a2) * loAo.w + mk3(loAo.x, loAo.y, loAo.z);
       f3 col = mk3(__powf(c.x, 1.f / 2.2f), __powf(c.y, 1.f / 2.2f), __powf(c.z, 1.f / 2.2f));
       if (p.def[2]) col = col + mk3(emA.x, emA.y, emA.z);
