@@ -199,15 +199,18 @@ def texture_bytes(scene) -> int:
     return total
 
 
-def run_cpu(scene, steps: int, threads: int, min_seconds: float = 0.0):
-    """The CPU pipeline (oracle restatement, all host threads) on `steps` frames of the workload,
-    continuing until at least `min_seconds` have elapsed. Returns (frames/s, frames timed)."""
+def run_cpu(scene, steps: int, threads: int, min_seconds: float = 0.0, lib=None):
+    """The CPU pipeline on `steps` frames of the workload, continuing until at least `min_seconds`
+    have elapsed: the oracle restatement with `threads` host threads, or `lib` (the reference's own
+    multi-threaded build, which sizes its thread pool itself). Returns (frames/s, frames timed)."""
     import oracle
     from softglrender_gb300 import api as A
     from softglrender_gb300 import scenes as S
-    lib = oracle.restatement()
+    port = lib is None
+    lib = oracle.restatement() if port else lib
     r = A.Renderer(lib, 0)
-    lib.cdll.sglo_set_threads(r.ctx, threads)
+    if port:
+        lib.cdll.sglo_set_threads(r.ctx, threads)
     inst = S.SceneInstance(r, scene)
     inst.render()   # warm-up
     t0 = time.perf_counter()
@@ -493,6 +496,26 @@ def bench_uneven_lanes(r, cfg, u, per_scene, net, materials, lanes: int = 4):
     return res
 
 
+def tuned_launches(r, submit) -> int:
+    """Kernel launches of one eager submission (the sum of every draw's count in the draw stats)."""
+    total = [0]
+    orig_draw, orig_scenes = r.draw, r.drawScenes
+
+    def count(fn):
+        def wrapped(*a, **k):
+            fn(*a, **k)
+            total[0] += r.drawStats()["kernel_launches"]
+        return wrapped
+    r.draw, r.drawScenes = count(orig_draw), count(orig_scenes)
+    try:
+        r.setCapacity(None)
+        submit()
+        r.waitIdle()
+    finally:
+        r.draw, r.drawScenes = orig_draw, orig_scenes
+    return total[0]
+
+
 def bench_uneven(r, stream, net, materials, with_cpu: bool):
     """64 independent scenes in one CUDA-graph submission (plain shaders, and with the neural IBL
     shader bound to the PBR scenes of every material that met its threshold, `materials`: material
@@ -524,9 +547,26 @@ def bench_uneven(r, stream, net, materials, with_cpu: bool):
     per_scene = [time_ms(lambda s=s: u.render_scene(s), 3) for s in range(cfg.scenes)]
     out = {"workload": "uneven_64_scenes_1k_2M_tris_128_2048", "scenes": cfg.scenes,
            "triangles_total": int(sum(u.triangles)), "setup_s": round(setup_s, 2)}
+    classes = u.classes()
+    # the batch as one multi-scene draw per class (one pipeline pass each: every stage one launch
+    # over all of the class's scenes, the raster stage one heaviest-first (scene, tile) queue),
+    # and as per-scene render passes, each captured in one graph
+    tuned = autotune(r, u.render_batched, reps=3)
+    batched_ms = time_ms(tuned.run, 5)
+    batched_launches = tuned_launches(r, u.render_batched)
+    out["batched"] = {"ms_per_batch": round(batched_ms, 3), "scenes_per_s": round(cfg.scenes / (batched_ms / 1e3), 1),
+                      "draws": len(classes), "classes": {f"{'pbr' if k[0] else 'blinn_phong'}"
+                                                         f"{'_material%d' % k[1] if k[0] else ''}": len(v)
+                                                         for k, v in classes.items()},
+                      "kernel_launches": batched_launches,
+                      "autotune": {k: v for k, v in tuned.result.describe().items() if k != "candidates"}}
+    tuned.destroy()
+    r.setCapacity(None)
     tuned = autotune(r, u.render, reps=3)
     plain_ms = time_ms(tuned.run, 5)
     out["plain"] = {"ms_per_batch": round(plain_ms, 3), "scenes_per_s": round(cfg.scenes / (plain_ms / 1e3), 1),
+                    "submission": "one render pass per scene, one graph",
+                    "kernel_launches": tuned_launches(r, u.render),
                     "autotune": {k: v for k, v in tuned.result.describe().items() if k != "candidates"}}
     tuned.destroy()
     r.setCapacity(None)
@@ -536,9 +576,16 @@ def bench_uneven(r, stream, net, materials, with_cpu: bool):
             for prog in u.pbr_programs(m):
                 if keep:
                     net.bind(prog)
+        tuned = autotune(r, u.render_batched, reps=3)
+        nb_ms = time_ms(tuned.run, 5)
+        tuned.destroy()
+        r.setCapacity(None)
+        out["batched"].update({"neural_ms_per_batch": round(nb_ms, 3),
+                               "neural_scenes_per_s": round(cfg.scenes / (nb_ms / 1e3), 1)})
         tuned = autotune(r, u.render, reps=3)
         n_ms = time_ms(tuned.run, 5)
         out["neural"] = {"ms_per_batch": round(n_ms, 3), "scenes_per_s": round(cfg.scenes / (n_ms / 1e3), 1),
+                         "submission": "one render pass per scene, one graph",
                          "materials_using_network": sorted(m for m, k in materials.items() if k),
                          "materials_falling_back": sorted(m for m, k in materials.items() if not k),
                          "pbr_scenes_using_network": sum(len(u.pbr_programs(m)) for m, k in materials.items() if k)}
@@ -939,10 +986,12 @@ def main():
 
 
 def main_reference(args, world, rank, pg):
-    """The reference's CPU pipeline on the host cores: the reference itself cannot run on this
-    machine (its raster is x86 SSE/AVX2 code and its sources are not shipped here), so the
-    C++ restatement of it (oracle/softgl_oracle.cpp, bit-identical to the reference where the
-    reference builds) runs with all host threads."""
+    """The reference's CPU pipeline on the host cores: the reference's own multi-threaded build
+    (oracle/_ref, RendererSoft with its ThreadPool, compiled from the reference sources) where it
+    was built (an x86-64 host with the reference tree); elsewhere (the Arm GPU host: the reference's
+    raster is x86 SSE/AVX2 code and its sources are not shipped) the C++ restatement of it
+    (oracle/softgl_oracle.cpp, bit-identical to the reference where the reference builds) with all
+    host threads."""
     if rank != 0:
         if pg is not None:
             pg.destroy_process_group()
@@ -952,8 +1001,10 @@ def main_reference(args, world, rank, pg):
     scene = build_scene()
     threads = os.cpu_count() or 1
     steps = max(1, min(args.steps, 3))
+    ref = oracle.reference("mt")
+    kind = "reference" if ref is not None else "port"
     t0 = time.perf_counter()
-    fps, steps = run_cpu(scene, steps, threads, min_seconds=10.0)
+    fps, steps = run_cpu(scene, steps, threads, min_seconds=10.0, lib=ref)
     dt = time.perf_counter() - t0
     result = {
         "metric": METRIC, "value": round(fps, 4), "unit": "frames/s", "n_gpus": world, "steps": steps,
@@ -961,7 +1012,7 @@ def main_reference(args, world, rank, pg):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
         "config": {"workload": WORKLOAD, "resolution": [1920, 1080], "msaa": 4, "triangles": scene.triangles},
         "impl": "reference",
-        "cpu_baseline": {"value": round(fps, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": round(fps, 4), "unit": "frames/s", "cores": threads, "kind": kind,
                          "sample": f"{steps} full frames after 1 warm-up, at least 10 s ({dt:.1f} s with set-up)"},
         "e2e": {"value": round(fps, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

@@ -260,6 +260,21 @@ SGLC_API sglc_status sglc_set_enable_early_z(sglc_context *ctx, int32_t enable);
  * (view, triangle) and (view, tile) work items). */
 SGLC_API sglc_status sglc_draw_views(sglc_context *ctx, const sglc_handle *framebuffers, const sglc_handle *resources,
                                      int32_t count, const sglc_clear_states *clear);
+/* Multi-scene draw: independent scenes that share the bound program, pipeline states and samplers
+ * but not geometry or frame size, scene s drawn from vertex_arrays[s] into framebuffers[s] with
+ * the uniform blocks of resources[s]. The result is identical to, for each scene in order:
+ * beginRenderPass(framebuffers[s], clear); setViewPort(0, 0, W, H) with the scene's attachment size;
+ * setVertexArrayObject(vertex_arrays[s]); setShaderResources(resources[s]); draw(); endRenderPass().
+ * Attachments may differ in size between scenes, not in presence or sample count; vertex arrays
+ * must share their stride; every scene's resources must bind the textures and sampler states that
+ * resources[0] binds (SGLC_ERR_INVALID_VALUE otherwise). The GPU runs all scenes in one pipeline
+ * pass: one launch per stage over every (scene, vertex), (scene, triangle) and (scene, tile) work
+ * item, the raster stage taking tiles from one heaviest-first queue across the scenes. It replaces
+ * the per-scene loop over Renderer calls that RendererSoft runs one block task queue for at a time
+ * (RendererSoft.cpp:731-737 feeding ThreadPool.h:100-110). */
+SGLC_API sglc_status sglc_draw_scenes(sglc_context *ctx, const sglc_handle *vertex_arrays,
+                                      const sglc_handle *framebuffers, const sglc_handle *resources, int32_t count,
+                                      const sglc_clear_states *clear);
 /* Counters of the last draw (synchronises). */
 SGLC_API sglc_status sglc_get_draw_stats(sglc_context *ctx, sglc_draw_stats *out);
 /* 0: no instrumentation; 1: per-stage device timings of each draw; 2: also count fragments. */

@@ -534,6 +534,32 @@ sglc_status sglr_draw_views(sglc_context *ctx, const sglc_handle *fbs, const sgl
   return SGLC_OK;
 }
 
+// The multi-scene draw on the reference: each scene in its own render pass, viewport over its whole
+// frame (the larger of its attachments), its own vertex array.
+sglc_status sglr_draw_scenes(sglc_context *ctx, const sglc_handle *vaos, const sglc_handle *fbs, const sglc_handle *res,
+                             int32_t count, const sglc_clear_states *clear) {
+  auto *c = reinterpret_cast<Ctx *>(ctx);
+  sglc_clear_states none{0, 0, {0.f, 0.f, 0.f, 0.f}, 1.f};
+  for (int v = 0; v < count; v++) {
+    Object *f = c->get(fbs[v]);
+    CTX_CHECK(f && f->fb);
+    int w = 0, h = 0;
+    for (const FrameBufferAttachment *a : {&f->fb->getColorAttachment(), &f->fb->getDepthAttachment()})
+      if (a->tex) {
+        w = std::max(w, (int) a->tex->getLevelWidth(a->level));
+        h = std::max(h, (int) a->tex->getLevelHeight(a->level));
+      }
+    sglc_status s = sglr_begin_render_pass(ctx, fbs[v], clear ? clear : &none);
+    if (!s) s = sglr_set_viewport(ctx, 0, 0, w, h);
+    if (!s) s = sglr_set_vertex_array(ctx, vaos[v]);
+    if (!s) s = sglr_set_shader_resources(ctx, res[v]);
+    if (!s) s = sglr_draw(ctx);
+    if (!s) s = sglr_end_render_pass(ctx);
+    if (s) return s;
+  }
+  return SGLC_OK;
+}
+
 // Capacities only change how the GPU back-end sizes its working arrays; RendererSoft has none.
 sglc_status sglr_set_capacity(sglc_context *, const sglc_capacity *) { return SGLC_OK; }
 sglc_status sglr_get_peak_counts(sglc_context *, sglc_capacity *out) {

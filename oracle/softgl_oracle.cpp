@@ -2147,6 +2147,27 @@ sglc_status sglo_draw_views(sglc_context *ctx, const sglc_handle *fbs, const sgl
   }
   return SGLC_OK;
 }
+// The multi-scene draw restated as what it stands for: each scene in its own render pass with the
+// viewport over its whole frame (the larger of its attachments) and its own vertex array.
+sglc_status sglo_draw_scenes(sglc_context *ctx, const sglc_handle *vaos, const sglc_handle *fbs, const sglc_handle *res,
+                             int32_t count, const sglc_clear_states *clear) {
+  CTX;
+  sglc_clear_states none{0, 0, {0.f, 0.f, 0.f, 0.f}, 1.f};
+  for (int v = 0; v < count; v++) {
+    GET(f, fbs[v], 1);
+    Level *col = f->fb.colorReady ? attachmentLevel(c, f->fb.colorTex, f->fb.colorLayer, f->fb.colorLevel) : nullptr;
+    Level *dep = f->fb.depthReady ? attachmentLevel(c, f->fb.depthTex, 0, 0) : nullptr;
+    const int w = std::max(col ? col->w : 0, dep ? dep->w : 0), h = std::max(col ? col->h : 0, dep ? dep->h : 0);
+    sglc_status s = sglo_begin_render_pass(ctx, fbs[v], clear ? clear : &none);
+    if (!s) s = sglo_set_viewport(ctx, 0, 0, w, h);
+    if (!s) s = sglo_set_vertex_array(ctx, vaos[v]);
+    if (!s) s = sglo_set_shader_resources(ctx, res[v]);
+    if (!s) s = sglo_draw(ctx);
+    if (!s) s = sglo_end_render_pass(ctx);
+    if (s) return s;
+  }
+  return SGLC_OK;
+}
 sglc_status sglo_wait_idle(sglc_context *) { return SGLC_OK; }
 // Capacities only change how the GPU back-end sizes its working arrays; the CPU pipeline has no
 // capacities and never overflows.

@@ -212,6 +212,8 @@ _SIGS = {
     "get_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
     "set_stats_level": [C.c_void_p, C.c_int32],
     "draw_views": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32, C.c_void_p],
+    "draw_scenes": [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32,
+                    C.c_void_p],
     "set_capacity": [C.c_void_p, C.c_void_p],
     "get_overflow": [C.c_void_p, C.POINTER(C.c_int32)],
     "get_peak_counts": [C.c_void_p, C.c_void_p],
@@ -541,6 +543,22 @@ class Renderer:
             cs = _ClearStates(int(clear.depthFlag), int(clear.colorFlag), (C.c_float * 4)(*clear.clearColor),
                               clear.clearDepth)
         self._call("draw_views", fbs, res, n, C.byref(cs) if cs is not None else None)
+
+    def drawScenes(self, vaos: Sequence["VertexArrayObject"], framebuffers: Sequence[FrameBuffer],
+                   resources: Sequence[ShaderResources], clear: Optional[ClearStates] = None) -> None:
+        """Multi-scene draw (extension): independent scenes (own vertex array, framebuffer of any
+        size, uniform blocks) sharing the bound program, states and samplers, in one pipeline pass;
+        equal to one render pass per scene with the viewport over the scene's whole frame."""
+        n = len(framebuffers)
+        assert len(resources) == n and len(vaos) == n
+        vas = (C.c_int32 * n)(*[v.handle for v in vaos])
+        fbs = (C.c_int32 * n)(*[f.handle for f in framebuffers])
+        res = (C.c_int32 * n)(*[r.handle for r in resources])
+        cs = None
+        if clear is not None:
+            cs = _ClearStates(int(clear.depthFlag), int(clear.colorFlag), (C.c_float * 4)(*clear.clearColor),
+                              clear.clearDepth)
+        self._call("draw_scenes", vas, fbs, res, n, C.byref(cs) if cs is not None else None)
 
     def waitIdle(self) -> None:
         self._call("wait_idle")

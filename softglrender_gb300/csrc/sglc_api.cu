@@ -228,7 +228,7 @@ struct Ctx {
   // scratch
   DevBuf vClip, vFrag, vMask, vVary, vAttrExtra, prims, clipExtra, clipAppendOff, clipPoly, clipPolyTri, counters;
   DevBuf tri, tileCount, pairOff, keyA, keyB, valA, valB, tileStart, tileEnd, tileOrder, scanScratch, sortHist,
-      sortHistScan, staging, batchU, batchTargets;
+      sortHistScan, staging, batchU, batchTargets, batchScenes;
   DevBuf recA, recB, recColor, chunkNext, chunkFill, warpHead, recDense;   // deferred shading
   DevBuf nnIn;   // neural shading: per record the surface stage's 80-B row
   DevBuf peakChunks;   // largest number of fragment-record chunks a deferred draw used (device)
@@ -252,7 +252,7 @@ struct Ctx {
   void forEachBuf(F f) {
     DevBuf *bufs[] = {&vClip, &vFrag, &vMask, &vVary, &vAttrExtra, &prims, &clipExtra, &clipAppendOff, &clipPoly,
                       &clipPolyTri, &counters, &tri, &tileCount, &pairOff, &keyA, &keyB, &valA, &valB, &tileStart,
-                      &tileEnd, &tileOrder, &scanScratch, &sortHist, &sortHistScan, &staging, &batchU, &batchTargets,
+                      &tileEnd, &tileOrder, &scanScratch, &sortHist, &sortHistScan, &staging, &batchU, &batchTargets, &batchScenes,
                       &sticky, &lpSlot, &lpOrigin, &lpStampCount, &lpStampOff, &lpStampGeo, &lpStampRow,
                       &lpStampColor, &lpStampVary, &lpFragCount, &lpFragOff, &lpMisc, &recA, &recB, &recColor,
                       &chunkNext, &chunkFill, &warpHead, &recDense, &peakChunks, &nnIn};
@@ -540,6 +540,7 @@ TexObj *attachmentTex(Ctx *c, int h) {
 // A batched draw (sglc_draw_views): per-view framebuffers and uniform bytes, one clear for all.
 struct BatchViews {
   int count = 0;
+  const sglc_handle *vaos = nullptr;   // non-null: a multi-scene draw (sglc_draw_scenes), one per view
   const sglc_handle *fbs = nullptr;
   std::vector<uint8_t> uniforms;   // count x kUniformBytes
   const sglc_clear_states *clear = nullptr;
@@ -630,7 +631,7 @@ sglc_status drawPointsLines(Ctx *c, DrawParams &p, const sglc_render_states &rs,
     CK(c->sortHistScan.ensure(sizeof(int) * (size_t) sortInts));
     CK(c->scanScratch.ensure(sizeof(int) * (size_t) scanScratchInts(std::max(n + 1, sortInts)) * 2));
     sortPairs(p, n, nDev, keyBits, c->sortHist.as<int>(), c->sortHistScan.as<int>(), c->scanScratch.as<int>(), st);
-    launches += 5 * ((keyBits + 7) / 8);
+    launches += 5 * sortPassCount(keyBits);
     return SGLC_OK;
   };
   auto bitsFor = [](long long n) {
@@ -727,8 +728,34 @@ sglc_status drawPointsLines(Ctx *c, DrawParams &p, const sglc_render_states &rs,
   return SGLC_OK;
 }
 
+// RendererSoft::setViewPort (RendererSoft.cpp:92-113): the viewport transform with depth range [0, 1]
+Viewport makeViewport(int x, int y, int w, int h) {
+  Viewport v;
+  v.x = (float) x;
+  v.y = (float) y;
+  v.w = (float) w;
+  v.h = (float) h;
+  float minD = 0.f, maxD = 1.f;
+  v.absMin = std::min(minD, maxD);
+  v.absMax = std::max(minD, maxD);
+  v.oX = v.x + v.w / 2.f;
+  v.oY = v.y + v.h / 2.f;
+  v.oZ = minD;
+  v.oW = 0.f;
+  v.pX = v.w / 2.f;
+  v.pY = v.h / 2.f;
+  v.pZ = maxD - minD;
+  v.pW = 1.f;
+  return v;
+}
+
+// the viewport a multi-scene draw gives each scene: its whole frame
+Viewport fullViewport(int w, int h) { return makeViewport(0, 0, w, h); }
+
 sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
-  Object *fo = c->get(bv ? bv->fbs[0] : c->fb, K_FB), *vo = c->get(c->vao, K_VAO), *po = c->get(c->prog, K_PROG);
+  const bool scenes = bv && bv->vaos;
+  Object *fo = c->get(bv ? bv->fbs[0] : c->fb, K_FB), *vo = c->get(scenes ? bv->vaos[0] : c->vao, K_VAO),
+         *po = c->get(c->prog, K_PROG);
   if (!fo || !vo || !po) return SGLC_OK;   // RendererSoft::draw is a silent no-op (RendererSoft.cpp:137-139)
   Object *so = c->get(c->states, K_STATES);
   if (!so) return c->fail(SGLC_ERR_INVALID_VALUE, "draw: no pipeline states bound");
@@ -878,6 +905,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     if (dt && encodeAttachment(&p.tmDepth, p.depth, p.dw, p.dh, p.samples, p.tileH)) p.tmaStore |= 2;
   }
   std::vector<ViewTarget> targets;
+  std::vector<SceneRec> sceneRecs;
   if (bv) {
     // every view's attachments must match view 0's (size, format, samples, presence)
     for (int v = 0; v < bv->count; v++) {
@@ -890,10 +918,21 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       if (vd) vd->version++;
       if (vc && (!vc->allocated || f.colorLevel >= vc->levels || vc->desc.format != SGLC_FORMAT_RGBA8)) vc = nullptr;
       if (vd && (!vd->allocated || vd->desc.format != SGLC_FORMAT_FLOAT32)) vd = nullptr;
+      // (a multi-scene draw: sizes may differ, presence and sample count may not)
       if ((vc != nullptr) != (ct != nullptr) || (vd != nullptr) != (dt != nullptr) ||
-          (vc && (vc->w[f.colorLevel] != p.cw || vc->h[f.colorLevel] != p.ch || vc->desc.multi_sample != p.cms)) ||
-          (vd && (vd->w[0] != p.dw || vd->h[0] != p.dh || vd->desc.multi_sample != p.dms)))
+          (vc && vc->desc.multi_sample != p.cms) || (vd && vd->desc.multi_sample != p.dms) ||
+          (!scenes && vc && (vc->w[f.colorLevel] != p.cw || vc->h[f.colorLevel] != p.ch)) ||
+          (!scenes && vd && (vd->w[0] != p.dw || vd->h[0] != p.dh)))
         return c->fail(SGLC_ERR_INVALID_VALUE, "draw_views: every view needs attachments like view 0's");
+      if (scenes) {   // this scene's frame: its attachment sizes and a viewport over them
+        SceneRec sr{};
+        sr.cw = vc ? vc->w[f.colorLevel] : 0;
+        sr.ch = vc ? vc->h[f.colorLevel] : 0;
+        sr.dw = vd ? vd->w[0] : 0;
+        sr.dh = vd ? vd->h[0] : 0;
+        sr.vp = fullViewport(std::max(sr.cw, sr.dw), std::max(sr.ch, sr.dh));
+        sceneRecs.push_back(sr);
+      }
       ViewTarget t{};
       if (vc) {
         t.color = vc->dev + (size_t) f.colorLayer * vc->layerStride + vc->offset[f.colorLevel];
@@ -940,7 +979,43 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
   p.nvView = p.nv;
   p.ntriView = p.ntri;
   p.tilesPerView = numTiles;
-  if (bv) {
+  std::vector<int> sceneBases;   // multi-scene draws: first vertex, triangle and tile of every scene
+  if (scenes) {
+    // every scene's vertex array, its ranges of the pass's vertices, triangles and tiles
+    long long nv = 0, nt = 0, tiles = 0;
+    sceneBases.resize(3 * ((size_t) bv->count + 1));
+    int *vBase = sceneBases.data(), *tBase = vBase + bv->count + 1, *tileBase = tBase + bv->count + 1;
+    for (int v = 0; v < bv->count; v++) {
+      Object *so2 = c->get(bv->vaos[v], K_VAO);
+      if (!so2) return c->fail(SGLC_ERR_INVALID_HANDLE, "draw_scenes: invalid vertex array handle");
+      const VaoObj &sv = so2->vao;
+      if (sv.stride != vao.stride) return c->fail(SGLC_ERR_INVALID_VALUE, "draw_scenes: vertex strides differ");
+      SceneRec &sr = sceneRecs[v];
+      sr.attr = sv.attr;
+      sr.indices = sv.idx;
+      sr.nv = (int) sv.nv;
+      sr.ntri = (int) (sv.nidx / 3);
+      sr.tilesX = (std::max(sr.cw, sr.dw) + p.tile - 1) / p.tile;
+      sr.tilesY = (std::max(sr.ch, sr.dh) + p.tileH - 1) / p.tileH;
+      vBase[v] = (int) nv;
+      tBase[v] = (int) nt;
+      tileBase[v] = (int) tiles;
+      nv += sr.nv;
+      nt += sr.ntri;
+      tiles += (long long) sr.tilesX * sr.tilesY;
+      if (nt * 3 > (1ll << 30) || nv > (1ll << 30) || tiles > (1ll << 30))
+        return c->fail(SGLC_ERR_INVALID_VALUE, "draw_scenes: batch too large");
+    }
+    vBase[bv->count] = (int) nv;
+    tBase[bv->count] = (int) nt;
+    tileBase[bv->count] = (int) tiles;
+    p.views = bv->count;
+    p.nv = (int) nv;
+    p.ntri = (int) nt;
+    p.nvView = p.ntriView = p.tilesPerView = 0;   // per scene instead
+    numTiles = (int) tiles;
+    p.vp = sceneRecs[0].vp;
+  } else if (bv) {
     if ((long long) p.ntri * bv->count * 3 > (1ll << 30) || (long long) p.nv * bv->count > (1ll << 30) ||
         (long long) numTiles * bv->count > (1ll << 30))
       return c->fail(SGLC_ERR_INVALID_VALUE, "draw_views: batch too large");
@@ -948,6 +1023,9 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     p.nv *= bv->count;
     p.ntri *= bv->count;
     numTiles *= bv->count;
+  }
+  p.numTiles = numTiles;
+  if (bv) {
     CK(c->batchU.ensure(bv->uniforms.size()));
     CK(c->batchTargets.ensure(sizeof(ViewTarget) * targets.size()));
     const void *srcU = bv->uniforms.data(), *srcT = targets.data();
@@ -967,6 +1045,27 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
                        c->stream));
     p.viewU = c->batchU.as<uint8_t>();
     p.viewTarget = c->batchTargets.as<ViewTarget>();
+    if (scenes) {   // the scene records, then the three base arrays
+      const size_t recBytes = sizeof(SceneRec) * sceneRecs.size(), baseBytes = sizeof(int) * sceneBases.size();
+      std::vector<uint8_t> blob(recBytes + baseBytes);
+      memcpy(blob.data(), sceneRecs.data(), recBytes);
+      memcpy(blob.data() + recBytes, sceneBases.data(), baseBytes);
+      CK(c->batchScenes.ensure(blob.size()));
+      const void *srcS = blob.data();
+      if (c->capturing) {
+        void *hs = nullptr;
+        CK(cudaMallocHost(&hs, blob.size()));
+        c->captureHostBufs.push_back(hs);
+        memcpy(hs, blob.data(), blob.size());
+        srcS = hs;
+      }
+      CK(cudaMemcpyAsync(c->batchScenes.ptr, srcS, blob.size(), cudaMemcpyHostToDevice, c->stream));
+      p.scenes = c->batchScenes.as<SceneRec>();
+      const int *bases = reinterpret_cast<const int *>(c->batchScenes.as<uint8_t>() + recBytes);
+      p.sceneVBase = bases;
+      p.sceneTBase = bases + bv->count + 1;
+      p.sceneTileBase = bases + 2 * (bv->count + 1);
+    }
     if (p.shading == SH_PBR_CAPTURE) p.shading = SH_PBR;   // no training capture in batched draws
   }
 
@@ -1162,7 +1261,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     // vertex, clip, scan, append, setup, scan | emit, sort (hist, 2 scan, scatter per pass), ranges,
     // order, raster (deferred shading: coverage, shade, ROP); flag accumulation when the draw has
     // capacities and no ROP kernel; a redone attempt ran the 6 geometry launches before
-    int sortPasses = nPairs > 0 ? (keyBits + 7) / 8 : 0;
+    int sortPasses = nPairs > 0 ? sortPassCount(keyBits) : 0;
     c->stats.kernel_launches = (p.nv > 0) + (p.ntri > 0) + 1 + 1 + 1 + 1 + (np > 0) + sortPasses * 4 +
                                (nPairs > 0) + (heavyFirst ? 1 : 0) + 1 + attempt * 6 +
                                (deferred && !deferShade ? 1 : 0) + (deferShade ? 2 : 0);
@@ -1695,22 +1794,7 @@ sglc_status sglc_begin_render_pass(sglc_context *ctx, sglc_handle fb, const sglc
 
 sglc_status sglc_set_viewport(sglc_context *ctx, int32_t x, int32_t y, int32_t w, int32_t h) {
   CTX;
-  Viewport &v = c->vp;
-  v.x = (float) x;
-  v.y = (float) y;
-  v.w = (float) w;
-  v.h = (float) h;
-  float minD = 0.f, maxD = 1.f;
-  v.absMin = std::min(minD, maxD);
-  v.absMax = std::max(minD, maxD);
-  v.oX = v.x + v.w / 2.f;
-  v.oY = v.y + v.h / 2.f;
-  v.oZ = minD;
-  v.oW = 0.f;
-  v.pX = v.w / 2.f;
-  v.pY = v.h / 2.f;
-  v.pZ = maxD - minD;
-  v.pW = 1.f;
+  c->vp = makeViewport(x, y, w, h);
   return SGLC_OK;
 }
 
@@ -1767,23 +1851,31 @@ sglc_status sglc_draw(sglc_context *ctx) {
   return drawImpl(c);
 }
 
-sglc_status sglc_draw_views(sglc_context *ctx, const sglc_handle *framebuffers, const sglc_handle *resources,
-                            int32_t count, const sglc_clear_states *clear) {
+}  // extern "C"
+
+namespace {
+
+// sglc_draw_views / sglc_draw_scenes: per-view uniforms and attachments (and, for scenes, vertex
+// arrays), the bound program and states, one pipeline pass
+sglc_status drawBatch(sglc_context *ctx, const sglc_handle *vaos, const sglc_handle *framebuffers,
+                      const sglc_handle *resources, int32_t count, const sglc_clear_states *clear, const char *what) {
   CTX;
+  const std::string w(what);
   if (count <= 0 || !framebuffers || !resources)
-    return c->fail(SGLC_ERR_INVALID_VALUE, "draw_views: need at least one view");
+    return c->fail(SGLC_ERR_INVALID_VALUE, w + ": need at least one view");
   Object *po = c->get(c->prog, K_PROG);
-  if (!po || !po->prog.shader) return c->fail(SGLC_ERR_INVALID_VALUE, "draw_views: no shader program bound");
+  if (!po || !po->prog.shader) return c->fail(SGLC_ERR_INVALID_VALUE, w + ": no shader program bound");
   ProgObj &P = po->prog;
   BatchViews bv;
   bv.count = count;
+  bv.vaos = vaos;
   bv.fbs = framebuffers;
   bv.clear = clear;
   bv.uniforms.resize((size_t) count * kUniformBytes);
   for (int v = 0; v < count; v++) {
     Object *fo = c->get(framebuffers[v], K_FB);
     Object *r = c->get(resources[v], K_RES);
-    if (!fo || !r) return c->fail(SGLC_ERR_INVALID_HANDLE, "draw_views: invalid framebuffer or resources handle");
+    if (!fo || !r) return c->fail(SGLC_ERR_INVALID_HANDLE, w + ": invalid framebuffer or resources handle");
     for (int h : {fo->fb.colorReady ? fo->fb.colorTex : 0, fo->fb.depthReady ? fo->fb.depthTex : 0}) {
       Object *t = c->get(h, K_TEX);
       if (t && !t->tex.allocated) {
@@ -1808,7 +1900,42 @@ sglc_status sglc_draw_views(sglc_context *ctx, const sglc_handle *framebuffers, 
   // samplers are shared by all views: view 0's resources bind them
   sglc_status st = sglc_set_shader_resources(ctx, resources[0]);
   if (st) return st;
+  if (vaos) {   // scenes bring their own resources: each must bind what scene 0 bound
+    for (int v = 1; v < count; v++) {
+      Object *r = c->get(resources[v], K_RES);
+      for (auto &kv : r->resSamplers) {
+        Object *u = c->get(kv.second, K_US);
+        if (!u) continue;
+        for (auto &d : P.shader->uniforms) {
+          if (d.samplerSlot < 0 || u->us.name != d.name) continue;
+          Object *b = c->get(P.samplers[d.samplerSlot], K_US);
+          const UsObj &x = u->us;
+          if (!b || b->us.tex != x.tex || b->us.filter != x.filter || b->us.wrap != x.wrap || b->us.border != x.border)
+            return c->fail(SGLC_ERR_INVALID_VALUE, w + ": every scene must bind the textures and sampler states of "
+                                                       "scene 0");
+        }
+      }
+    }
+  }
   return drawImpl(c, &bv);
+}
+
+}  // namespace
+
+extern "C" {
+
+sglc_status sglc_draw_views(sglc_context *ctx, const sglc_handle *framebuffers, const sglc_handle *resources,
+                            int32_t count, const sglc_clear_states *clear) {
+  return drawBatch(ctx, nullptr, framebuffers, resources, count, clear, "draw_views");
+}
+
+sglc_status sglc_draw_scenes(sglc_context *ctx, const sglc_handle *vertex_arrays, const sglc_handle *framebuffers,
+                             const sglc_handle *resources, int32_t count, const sglc_clear_states *clear) {
+  if (!vertex_arrays) {
+    Ctx *c = reinterpret_cast<Ctx *>(ctx);
+    return c ? c->fail(SGLC_ERR_INVALID_VALUE, "draw_scenes: no vertex arrays") : SGLC_ERR_INVALID_VALUE;
+  }
+  return drawBatch(ctx, vertex_arrays, framebuffers, resources, count, clear, "draw_scenes");
 }
 
 sglc_status sglc_set_capacity(sglc_context *ctx, const sglc_capacity *cap) {

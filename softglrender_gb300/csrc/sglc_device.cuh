@@ -117,6 +117,17 @@ struct ViewTarget {
   float *depth;
 };
 
+// one scene of a multi-scene draw (sglc_draw_scenes): its own vertex array, attachments and
+// viewport; its vertices, triangles and raster tiles are consecutive ranges of the pass's
+struct SceneRec {
+  const float *attr;              // the scene's vertex rows
+  const int *indices;
+  int nv, ntri;                   // the scene's vertices and triangles
+  int tilesX, tilesY;
+  int cw, ch, dw, dh;             // colour / depth attachment sizes
+  Viewport vp;
+};
+
 // everything a draw's kernels read; passed by value as a __grid_constant__ parameter
 struct DrawParams {
   // shader
@@ -213,6 +224,12 @@ struct DrawParams {
   int tilesPerView;
   const uint8_t *viewU;            // views x kUniformBytes, or null: DrawParams::u
   const ViewTarget *viewTarget;    // per-view attachments, or null: color / resolved / depth above
+  // multi-scene draws: per scene its record and (views + 1 entries each) the first vertex, triangle
+  // and raster tile of scene v; null for every other draw. The views then differ in geometry and
+  // frame size, and nvView / ntriView / tilesPerView are unused.
+  const SceneRec *scenes;
+  const int *sceneVBase, *sceneTBase, *sceneTileBase;
+  int numTiles;                    // raster tiles of the pass, all views
   // deferred shading (k_raster_cov -> k_shade -> k_rop in sglc_raster.cuh): fragment records in
   // chunks of kChunk, one linked chunk list per raster warp, in the warp's fragment order
   int4 *recA;                     // triangle, meta, px | py << 16, b0 bits
@@ -294,6 +311,65 @@ __device__ __forceinline__ void fenceAsyncShared() { asm volatile("fence.proxy.a
 // uniforms of view v
 __device__ __forceinline__ const uint8_t *viewUniforms(const DrawParams &p, int view) {
   return p.viewU ? p.viewU + (size_t) view * kUniformBytes : p.u;
+}
+
+// the scene whose range [base[v], base[v + 1]) holds index i (base[0] = 0, n scenes)
+__device__ __forceinline__ int sceneOf(const int *base, int n, int i) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(base + mid) <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// the viewport transform of view v
+__device__ __forceinline__ const Viewport &viewViewport(const DrawParams &p, int view) {
+  return p.scenes ? p.scenes[view].vp : p.vp;
+}
+
+// where raster tile `tile` of a pass lies: its view, tile coordinates, the view's attachment sizes
+// and viewport extent, and its attachments
+struct TileFrame {
+  int view, tx, ty;
+  int cW, cH, dW, dH;
+  float vpW, vpH;
+  uint32_t *color, *resolved;
+  float *depth;
+};
+
+__device__ __forceinline__ TileFrame tileFrame(const DrawParams &p, int tile) {
+  TileFrame f;
+  int vtile, tilesX;
+  if (p.scenes) {
+    f.view = sceneOf(p.sceneTileBase, p.views, tile);
+    const SceneRec &S = p.scenes[f.view];
+    vtile = tile - p.sceneTileBase[f.view];
+    tilesX = S.tilesX;
+    f.cW = S.cw;
+    f.cH = S.ch;
+    f.dW = S.dw;
+    f.dH = S.dh;
+    f.vpW = S.vp.w;
+    f.vpH = S.vp.h;
+  } else {
+    f.view = p.views > 1 ? tile / p.tilesPerView : 0;
+    vtile = tile - f.view * p.tilesPerView;
+    tilesX = p.tilesX;
+    f.cW = p.cw;
+    f.cH = p.ch;
+    f.dW = p.dw;
+    f.dH = p.dh;
+    f.vpW = p.vp.w;
+    f.vpH = p.vp.h;
+  }
+  f.tx = vtile % tilesX;
+  f.ty = vtile / tilesX;
+  f.color = p.viewTarget ? p.viewTarget[f.view].color : p.color;
+  f.resolved = p.viewTarget ? p.viewTarget[f.view].resolved : p.resolved;
+  f.depth = p.viewTarget ? p.viewTarget[f.view].depth : p.depth;
+  return f;
 }
 
 // ------------------------------------------------------------------------------------------------

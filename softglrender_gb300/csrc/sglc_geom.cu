@@ -38,12 +38,12 @@ __device__ __forceinline__ int clipMaskOf(float4 c) {
 }
 
 // perspectiveDivideImpl + viewportTransformImpl (RendererSoft.cpp:981-992)
-__device__ __forceinline__ float4 toScreen(const DrawParams &p, float4 c) {
+__device__ __forceinline__ float4 toScreen(const Viewport &vp, float4 c) {
   float invW = 1.f / c.w;
   float4 f = make_float4(c.x * invW, c.y * invW, c.z * invW, c.w * invW);
   f.w = invW;
-  f = make_float4(f.x * p.vp.pX, f.y * p.vp.pY, f.z * p.vp.pZ, f.w * p.vp.pW);
-  return make_float4(f.x + p.vp.oX, f.y + p.vp.oY, f.z + p.vp.oZ, f.w + p.vp.oW);
+  f = make_float4(f.x * vp.pX, f.y * vp.pY, f.z * vp.pZ, f.w * vp.pW);
+  return make_float4(f.x + vp.oX, f.y + vp.oY, f.z + vp.oZ, f.w + vp.oW);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -58,24 +58,32 @@ __global__ void __launch_bounds__(256) k_vertex(const __grid_constant__ DrawPara
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int q = p.varyStride / 4;
+  const int sf = p.strideF;
+  const int i0 = i - lane;
+  const int rows = min(32, p.nv - i0);
   float v[32];
 #pragma unroll
   for (int k = 0; k < 32; k++) v[k] = 0.f;
   if (i < p.nv) {
-    const int view = p.views > 1 ? i / p.nvView : 0;
-    const float *a = p.attr + (size_t) (i - view * p.nvView) * p.strideF;
+    int view;
+    const float *a;
+    if (p.scenes) {   // a multi-scene draw: the scene's own vertex rows
+      view = sceneOf(p.sceneVBase, p.views, i);
+      a = p.scenes[view].attr + (size_t) (i - p.sceneVBase[view]) * sf;
+    } else {
+      view = p.views > 1 ? i / p.nvView : 0;
+      a = p.attr + (size_t) (i - view * p.nvView) * sf;
+    }
     float4 c = runVS<SH>(p, viewUniforms(p, view), a, v);
     p.vClip[i] = c;
     p.vMask[i] = (uint8_t) clipMaskOf(c);
-    p.vFrag[i] = toScreen(p, c);
+    p.vFrag[i] = toScreen(viewViewport(p, view), c);
   }
   float4 *st = stage[warp];
 #pragma unroll
   for (int k = 0; k < 8; k++)
     if (k < q) st[lane * q + k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
   __syncwarp();
-  const int i0 = i - lane;
-  const int rows = min(32, p.nv - i0);
   if (rows > 0) {
     float4 *dst = reinterpret_cast<float4 *>(p.vVary + (size_t) i0 * p.varyStride);
     for (int e = lane; e < rows * q; e += 32) dst[e] = st[e];
@@ -86,7 +94,12 @@ __global__ void __launch_bounds__(256) k_vertex(const __grid_constant__ DrawPara
 // assembly + clipping
 // ------------------------------------------------------------------------------------------------
 __device__ __forceinline__ const float *attrOf(const DrawParams &p, int idx) {
-  return idx < p.nv ? p.attr + (size_t) (idx % p.nvView) * p.strideF : p.vAttrExtra + (size_t) (idx - p.nv) * p.strideF;
+  if (idx >= p.nv) return p.vAttrExtra + (size_t) (idx - p.nv) * p.strideF;
+  if (p.scenes) {
+    const int v = sceneOf(p.sceneVBase, p.views, idx);
+    return p.scenes[v].attr + (size_t) (idx - p.sceneVBase[v]) * p.strideF;
+  }
+  return p.attr + (size_t) (idx % p.nvView) * p.strideF;
 }
 
 template<int SH>
@@ -104,7 +117,7 @@ __device__ int newClipVertex(const DrawParams &p, int view, int i0, int i1, floa
   float4 c = runVS<SH>(p, viewUniforms(p, view), dst, v);
   p.vClip[idx] = c;
   p.vMask[idx] = (uint8_t) clipMaskOf(c);
-  p.vFrag[idx] = toScreen(p, c);
+  p.vFrag[idx] = toScreen(viewViewport(p, view), c);
   return idx;
 }
 
@@ -118,20 +131,32 @@ __global__ void __launch_bounds__(128) k_clip(const __grid_constant__ DrawParams
   chainEnter();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= p.ntri) return;
-  const int view = p.views > 1 ? t / p.ntriView : 0;
-  const int lt = t - view * p.ntriView;
+  int view, lt, nvView, vBase;
+  const int *indices;
+  if (p.scenes) {   // a multi-scene draw: the scene's own indices into its own vertex rows
+    view = sceneOf(p.sceneTBase, p.views, t);
+    lt = t - p.sceneTBase[view];
+    indices = p.scenes[view].indices;
+    nvView = p.scenes[view].nv;
+    vBase = p.sceneVBase[view];
+  } else {
+    view = p.views > 1 ? t / p.ntriView : 0;
+    lt = t - view * p.ntriView;
+    indices = p.indices;
+    nvView = p.nvView;
+    vBase = view * p.nvView;
+  }
   const int viewBits = view << 8;   // primitive flags: bit 0 discard, bits 8+ view
-  int i0 = p.indices[3 * lt], i1 = p.indices[3 * lt + 1], i2 = p.indices[3 * lt + 2];
+  int i0 = indices[3 * lt], i1 = indices[3 * lt + 1], i2 = indices[3 * lt + 2];
   p.clipExtra[t] = 0;
-  if ((unsigned) i0 >= (unsigned) p.nvView || (unsigned) i1 >= (unsigned) p.nvView ||
-      (unsigned) i2 >= (unsigned) p.nvView) {
+  if ((unsigned) i0 >= (unsigned) nvView || (unsigned) i1 >= (unsigned) nvView || (unsigned) i2 >= (unsigned) nvView) {
     atomicOr(&p.counters[CNT_FLAGS], OVF_BADINDEX);
     p.prims[t] = make_int4(0, 0, 0, 1);
     return;
   }
-  i0 += view * p.nvView;
-  i1 += view * p.nvView;
-  i2 += view * p.nvView;
+  i0 += vBase;
+  i1 += vBase;
+  i2 += vBase;
   int mask = p.vMask[i0] | p.vMask[i1] | p.vMask[i2];
   if (mask == 0) {
     p.prims[t] = make_int4(i0, i1, i2, viewBits);
@@ -223,7 +248,7 @@ __global__ void k_clip_append(const __grid_constant__ DrawParams p) {
   int ids[11] = {a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
   int nin = a.x;
   int base = p.ntri + p.clipAppendOff[t];
-  const int viewBits = (p.views > 1 ? t / p.ntriView : 0) << 8;
+  const int viewBits = (p.scenes ? sceneOf(p.sceneTBase, p.views, t) : (p.views > 1 ? t / p.ntriView : 0)) << 8;
   for (int k = 3; k < nin; k++) {
     int dst = base + k - 3;
     if (dst >= p.primCap) {
@@ -294,8 +319,9 @@ __device__ __forceinline__ unsigned long long setupPrim(const DrawParams &p, int
     float maxX = smax(smax(a.x, b.x), c.x), maxY = smax(smax(a.y, b.y), c.y);
     minX = smax(minX - 0.5f, 0.f);
     minY = smax(minY - 0.5f, 0.f);
-    maxX = smin(maxX + 0.5f, p.vp.w - 1.f);
-    maxY = smin(maxY + 0.5f, p.vp.h - 1.f);
+    const Viewport &vp = viewViewport(p, pr.w >> 8);
+    maxX = smin(maxX + 0.5f, vp.w - 1.f);
+    maxY = smin(maxY + 0.5f, vp.h - 1.f);
     minX -= 1.f;
     minY -= 1.f;
     if (!(isfinite(minX) && isfinite(minY) && isfinite(maxX) && isfinite(maxY))) discard = true;
@@ -317,6 +343,11 @@ __device__ __forceinline__ unsigned long long setupPrim(const DrawParams &p, int
         int bsx0 = (int) (minX + 0.f), bsy0 = (int) (minY + 0.f);
         int bsxL = (int) (minX + (float) ((bcx - 1) * kBlock)), bsyL = (int) (minY + (float) ((bcy - 1) * kBlock));
         int fw = max(p.cw, p.dw), fh = max(p.ch, p.dh);
+        if (p.scenes) {
+          const SceneRec &S = p.scenes[T.view];
+          fw = max(S.cw, S.dw);
+          fh = max(S.ch, S.dh);
+        }
         T.rx0 = max(bsx0 + 1, 0);
         T.ry0 = max(bsy0 + 1, 0);
         T.rx1 = min(min((int) floorf(maxX) + 1, bsxL + kBlock), fw - 1);
@@ -356,13 +387,15 @@ __global__ void __launch_bounds__(256) k_bin_emit(const __grid_constant__ DrawPa
   // two set-up steps that would otherwise be launches of their own: clearing the tile ranges
   // (k_tile_ranges fills the non-empty ones) and the bin-entry count clamped to the capacity
   if (p.binZeroRanges)
-    for (int t = i; t < p.views * p.tilesPerView; t += gridDim.x * blockDim.x) p.tileStart[t] = p.tileEnd[t] = 0;
+    for (int t = i; t < p.numTiles; t += gridDim.x * blockDim.x) p.tileStart[t] = p.tileEnd[t] = 0;
   if (p.binPairTotal && i == 0) p.counters[4] = min(*p.binPairTotal, p.pairCap);
   int np = min(p.ntri + p.clipAppendOff[p.ntri], p.primCap);
   if (i >= np || p.tileCount[i] == 0) return;
   const TriSetup &T = p.tri[i];
   int off = p.pairOff[i];
-  const uint32_t viewBase = (uint32_t) T.view * (uint32_t) p.tilesPerView;
+  const uint32_t viewBase =
+      p.scenes ? (uint32_t) p.sceneTileBase[T.view] : (uint32_t) T.view * (uint32_t) p.tilesPerView;
+  const int tilesX = p.scenes ? p.scenes[T.view].tilesX : p.tilesX;
   int tx0 = T.rx0 / p.tile, tx1 = T.rx1 / p.tile, ty0 = T.ry0 / p.tileH, ty1 = T.ry1 / p.tileH;
   for (int ty = ty0; ty <= ty1; ty++)
     for (int tx = tx0; tx <= tx1; tx++) {
@@ -370,7 +403,7 @@ __global__ void __launch_bounds__(256) k_bin_emit(const __grid_constant__ DrawPa
         atomicOr(&p.counters[CNT_FLAGS], OVF_PAIRS);
         return;
       }
-      p.keyA[off] = viewBase + (uint32_t) (ty * p.tilesX + tx);
+      p.keyA[off] = viewBase + (uint32_t) (ty * tilesX + tx);
       p.valA[off] = i;
       off++;
     }
@@ -384,31 +417,36 @@ constexpr int kSortItems = 8;                       // per thread
 constexpr int kSortTile = kSortThreads * kSortItems; // 2048 items per CTA
 
 __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint32_t *keys, const int *nPtr, int shift,
-                                                             int *hist, int numBlocks) {
+                                                             int bits, int *hist, int numBlocks) {
   chainEnter();
-  __shared__ int h[256];
+  __shared__ int h[1 << kMaxDigitBits];
+  const int buckets = 1 << bits;
+  const uint32_t mask = (uint32_t) buckets - 1u;
   int n = *nPtr;
-  for (int d = threadIdx.x; d < 256; d += blockDim.x) h[d] = 0;
+  for (int d = threadIdx.x; d < buckets; d += blockDim.x) h[d] = 0;
   __syncthreads();
   int base = blockIdx.x * kSortTile;
   for (int k = 0; k < kSortItems; k++) {
     int i = base + k * kSortThreads + threadIdx.x;
-    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1);
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & mask], 1);
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d * numBlocks + blockIdx.x] = h[d];
+  for (int d = threadIdx.x; d < buckets; d += blockDim.x) hist[d * numBlocks + blockIdx.x] = h[d];
 }
 
 // Items of a CTA are split into 8 contiguous warp ranges of 256; each warp ranks its range in
 // order (match.any + popc), then warp prefixes per digit make the scatter stable.
 __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t *keysIn, const int *valsIn,
                                                                 uint32_t *keysOut, int *valsOut, const int *nPtr,
-                                                                int shift, const int *histOff, int numBlocks) {
+                                                                int shift, int bits, const int *histOff,
+                                                                int numBlocks) {
   chainEnter();
-  __shared__ int wcount[8][256];
+  __shared__ int wcount[8][1 << kMaxDigitBits];
+  const int buckets = 1 << bits;
+  const uint32_t mask = (uint32_t) buckets - 1u;
   int n = *nPtr;
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int d = lane; d < 256; d += 32) wcount[warp][d] = 0;
+  for (int d = lane; d < buckets; d += 32) wcount[warp][d] = 0;
   __syncwarp();
   int base = blockIdx.x * kSortTile + warp * (kSortTile / 8);
   uint32_t myKey[kSortItems];
@@ -418,12 +456,12 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t *
     int i = base + k * 32 + lane;
     bool valid = i < n;
     uint32_t key = valid ? keysIn[i] : 0u;
-    int dig = valid ? (int) ((key >> shift) & 255u) : 256;
+    int dig = valid ? (int) ((key >> shift) & mask) : buckets;
     unsigned peers = __match_any_sync(0xffffffffu, dig);
     int rank = __popc(peers & lt);
-    int before = dig < 256 ? wcount[warp][dig] : 0;
+    int before = dig < buckets ? wcount[warp][dig] : 0;
     __syncwarp();
-    if (dig < 256 && rank == 0) wcount[warp][dig] = before + __popc(peers);
+    if (dig < buckets && rank == 0) wcount[warp][dig] = before + __popc(peers);
     __syncwarp();
     myKey[k] = key;
     myVal[k] = valid ? valsIn[i] : 0;
@@ -432,7 +470,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t *
   }
   __syncthreads();
   // exclusive prefix over warps for each digit
-  for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+  for (int d = threadIdx.x; d < buckets; d += blockDim.x) {
     int s = 0;
     for (int w = 0; w < 8; w++) {
       int c = wcount[w][d];
@@ -443,7 +481,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t *
   __syncthreads();
   for (int k = 0; k < kSortItems; k++) {
     int d = myDig[k];
-    if (d >= 256) continue;
+    if (d >= buckets) continue;
     int pos = histOff[d * numBlocks + blockIdx.x] + wcount[warp][d] + myPos[k];
     keysOut[pos] = myKey[k];
     valsOut[pos] = myVal[k];
@@ -828,23 +866,30 @@ void launchBinEmit(const DrawParams &p, int primCount, cudaStream_t st) {
   if (primCount > 0) launchChained(k_bin_emit, dim3(cdiv(primCount, 256)), dim3(256), 0, st, p);
 }
 
-int sortScratchInts(int nPairs) { return 256 * max(1, cdiv(nPairs, kSortTile)) + 1; }
+int sortScratchInts(int nPairs) { return (1 << kMaxDigitBits) * max(1, cdiv(nPairs, kSortTile)) + 1; }
+int sortPassCount(int keyBits, int maxDigitBits) {
+  maxDigitBits = min(max(maxDigitBits, 1), kMaxDigitBits);
+  return max(1, cdiv(max(keyBits, 1), maxDigitBits));
+}
 
 // sorts (keyA,valA) by key, result back in (keyA,valA); hist needs sortScratchInts ints plus a
-// scan scratch of scanScratchInts(256 * blocks)
+// scan scratch of scanScratchInts(2^digit bits * blocks)
 void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, int *hist, int *histScan,
-               int *scanScratch, cudaStream_t st, bool twoLaunchScan) {
+               int *scanScratch, cudaStream_t st, bool twoLaunchScan, int maxDigitBits) {
   if (nPairs <= 0) return;
   int nb = cdiv(nPairs, kSortTile);
   uint32_t *kin = p.keyA, *kout = p.keyB;
   int *vin = p.valA, *vout = p.valB;
-  int passes = keyBits <= 8 ? 1 : (keyBits <= 16 ? 2 : (keyBits <= 24 ? 3 : 4));
+  // as few passes as digits of at most maxDigitBits bits allow, the key bits spread evenly over them
+  const int passes = sortPassCount(keyBits, maxDigitBits);
+  const int bits = cdiv(max(keyBits, 1), passes);
   for (int pass = 0; pass < passes; pass++) {
-    int shift = pass * 8;
-    launchChained(k_radix_hist, dim3(nb), dim3(kSortThreads), 0, st, kin, nPtr, shift, hist, nb);
-    if (twoLaunchScan) scanExclusive2(hist, histScan, nullptr, 256 * nb, scanScratch, st);
-    else scanExclusive(hist, histScan, nullptr, 256 * nb, scanScratch, st);
-    launchChained(k_radix_scatter, dim3(nb), dim3(kSortThreads), 0, st, kin, vin, kout, vout, nPtr, shift, histScan, nb);
+    int shift = pass * bits;
+    launchChained(k_radix_hist, dim3(nb), dim3(kSortThreads), 0, st, kin, nPtr, shift, bits, hist, nb);
+    if (twoLaunchScan) scanExclusive2(hist, histScan, nullptr, (1 << bits) * nb, scanScratch, st);
+    else scanExclusive(hist, histScan, nullptr, (1 << bits) * nb, scanScratch, st);
+    launchChained(k_radix_scatter, dim3(nb), dim3(kSortThreads), 0, st, kin, vin, kout, vout, nPtr, shift, bits,
+                  histScan, nb);
     uint32_t *tk = kin; kin = kout; kout = tk;
     int *tv = vin; vin = vout; vout = tv;
   }
@@ -859,7 +904,7 @@ void launchTileRanges(const DrawParams &p, int nPairs, const int *nPtr, cudaStre
 }
 
 void launchTileOrder(const DrawParams &p, int *order, cudaStream_t st) {
-  launchChained(k_tile_order, dim3(1), dim3(1024), 0, st, p.tileStart, p.tileEnd, p.views * p.tilesPerView, order);
+  launchChained(k_tile_order, dim3(1), dim3(1024), 0, st, p.tileStart, p.tileEnd, p.numTiles, order);
 }
 
 __global__ void k_accumulate_flags(const int *flags, int *sticky) {

@@ -18,9 +18,14 @@ void launchVertexAndClip(const DrawParams &p, cudaStream_t st);
 void launchClipAppend(const DrawParams &p, cudaStream_t st);
 void launchSetup(const DrawParams &p, int primCount, cudaStream_t st);
 void launchBinEmit(const DrawParams &p, int primCount, cudaStream_t st);
+// stable LSD radix sort of (keyA, valA) by the low keyBits bits of the key, in as few passes as
+// digits of at most maxDigitBits (<= kMaxDigitBits) bits allow; hist and histScan hold
+// sortScratchInts(nPairs) ints (2^maxDigitBits buckets per block of 2048 pairs are used)
+constexpr int kMaxDigitBits = 10;
 int sortScratchInts(int nPairs);
+int sortPassCount(int keyBits, int maxDigitBits = kMaxDigitBits);
 void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, int *hist, int *histScan,
-               int *scanScratch, cudaStream_t st, bool twoLaunchScan = false);
+               int *scanScratch, cudaStream_t st, bool twoLaunchScan = false, int maxDigitBits = kMaxDigitBits);
 void launchTileRanges(const DrawParams &p, int nPairs, const int *nPtr, cudaStream_t st);
 void launchTileOrder(const DrawParams &p, int *order, cudaStream_t st);
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st);

@@ -272,6 +272,7 @@ extern "C" SGLC_API sglc_status sglc_draw_vertex_color_noalloc(const sglc_noallo
   p.nvView = p.nv;
   p.ntriView = p.ntri;
   p.tilesPerView = numTiles;
+  p.numTiles = numTiles;
   int *scan = reinterpret_cast<int *>(scratch + oScan);
   int *hist = reinterpret_cast<int *>(scratch + oHist);
   int *histScan = reinterpret_cast<int *>(scratch + oHistScan);
@@ -290,7 +291,7 @@ extern "C" SGLC_API sglc_status sglc_draw_vertex_color_noalloc(const sglc_noallo
   launchBinEmit(p, p.primCap, st);
   int keyBits = 1;
   while ((1 << keyBits) < numTiles) keyBits++;
-  sortPairs(p, kMaxPairs, p.counters + 4, keyBits, hist, histScan, scan, st);
+  sortPairs(p, kMaxPairs, p.counters + 4, keyBits, hist, histScan, scan, st, false, 8);   // 256-bucket digits
   launchTileRanges(p, kMaxPairs, p.counters + 4, st);
   launchTileOrder(p, reinterpret_cast<int *>(scratch + oTileOrder), st);
   p.tileOrder = reinterpret_cast<int *>(scratch + oTileOrder);

@@ -564,25 +564,24 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
   __shared__ FragQueue queues[HAS_COLOR ? 8 : 1];
   __shared__ unsigned candMasks[8][32];
   const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
-  const int view = p.views > 1 ? tile / p.tilesPerView : 0;
-  const int vtile = tile - view * p.tilesPerView;
-  const int tx = vtile % p.tilesX, ty = vtile / p.tilesX;
+  const TileFrame fr = tileFrame(p, tile);
+  const int view = fr.view;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
+  const int rx0 = fr.tx * 16 + (warp & 1) * 8, ry0 = fr.ty * 16 + (warp >> 1) * 4;
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
-  const bool inC = HAS_COLOR && px < p.cw && py < p.ch;
-  const bool inD = HAS_DEPTH && px < p.dw && py < p.dh;
+  const bool inC = HAS_COLOR && px < fr.cW && py < fr.cH;
+  const bool inD = HAS_DEPTH && px < fr.dW && py < fr.dH;
   FragQueue &q = queues[HAS_COLOR ? warp : 0];
   const uint8_t *U = viewUniforms(p, view);
-  uint32_t *colorBuf = p.viewTarget ? p.viewTarget[view].color : p.color;
-  uint32_t *resolvedBuf = p.viewTarget ? p.viewTarget[view].resolved : p.resolved;
-  float *depthBuf = p.viewTarget ? p.viewTarget[view].depth : p.depth;
+  uint32_t *colorBuf = fr.color;
+  uint32_t *resolvedBuf = fr.resolved;
+  float *depthBuf = fr.depth;
   int count = 0;
   unsigned long long mine = 0ull;   // queue entries of this lane's pixel
   const unsigned lt = (1u << lane) - 1u;
   Samples4 fb = {0u, 0u, 0u, 0u, 0.f, 0.f, 0.f, 0.f};
   if (inC) {
-    size_t pix = (size_t) py * p.cw + px;
+    size_t pix = (size_t) py * fr.cW + px;
     if (p.pendingClear && p.clearColorFlag) {
       fb.c0 = fb.c1 = fb.c2 = fb.c3 = p.clearColor;
     } else if (S == 4) {
@@ -593,7 +592,7 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
     }
   }
   if (inD) {
-    size_t pix = (size_t) py * p.dw + px;
+    size_t pix = (size_t) py * fr.dW + px;
     if (p.pendingClear && p.clearDepthFlag) {
       fb.d0 = fb.d1 = fb.d2 = fb.d3 = p.clearDepth;
     } else if (S == 4) {
@@ -606,7 +605,7 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
   const int start = p.tileStart[tile], end = p.tileEnd[tile];
   // sample box offsets inside a pixel: 4x MSAA samples span [1/8, 7/8], one sample sits at 1/2
   const float lo = S == 4 ? 0.125f : 0.5f, hi = S == 4 ? 0.875f : 0.5f;
-  const float vpExtent = fabsf(p.vp.w) + fabsf(p.vp.h) + 2.f * (float) (rx0 + ry0) + 64.f;
+  const float vpExtent = fabsf(fr.vpW) + fabsf(fr.vpH) + 2.f * (float) (rx0 + ry0) + 64.f;
   for (int base = start; base < end; base += 32) {
     int prim;
     unsigned cand = pass1Candidates<S>(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim, candMasks[warp]);
@@ -654,7 +653,7 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
   }
   if (HAS_COLOR && count > 0) flushQueue<SH, S, HAS_DEPTH>(p, U, q, count, mine, lane, rx0, ry0, inC, fb);
   if (inC) {
-    size_t pix = (size_t) py * p.cw + px;
+    size_t pix = (size_t) py * fr.cW + px;
     if (S == 4) {
       *reinterpret_cast<uint4 *>(colorBuf + pix * 4) = make_uint4(fb.c0, fb.c1, fb.c2, fb.c3);
       // multiSampleResolve (RendererSoft.cpp:880-912): mean of four u8 samples, truncated
@@ -671,7 +670,7 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
     }
   }
   if (inD) {
-    size_t pix = (size_t) py * p.dw + px;
+    size_t pix = (size_t) py * fr.dW + px;
     if (S == 4) {
       *reinterpret_cast<float4 *>(depthBuf + pix * 4) = make_float4(fb.d0, fb.d1, fb.d2, fb.d3);
     } else {
@@ -682,7 +681,7 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
 
 template<int SH>
 void launchRasterModel(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
-  int grid = p.views * p.tilesPerView;
+  int grid = p.numTiles;
   if (p.samples == 4) {
     if (hasDepth) launchChained(k_raster<SH, 4, true, true>, dim3(grid), dim3(256), 0, st, p);
     else launchChained(k_raster<SH, 4, true, false>, dim3(grid), dim3(256), 0, st, p);
@@ -734,7 +733,7 @@ struct TileJob {
 
 __device__ __forceinline__ TileJob tileJob(const DrawParams &p) {
   const int H = p.tileOrder ? p.heavySlots : 0;
-  const int nTiles = p.views * p.tilesPerView;
+  const int nTiles = p.numTiles;
   const int b = blockIdx.x;
   if (b < 4 * H) {
     const int slot = b >> 2, part = b & 3;
@@ -764,15 +763,14 @@ __global__ void __launch_bounds__(32 * W, (S == 4 ? 2 : 4) * 8 / W) k_raster_cov
   const TileJob job = tileJob(p);
   if (job.skip) return;
   const int tile = job.tile, rh = job.rows;
-  const int view = p.views > 1 ? tile / p.tilesPerView : 0;
-  const int vtile = tile - view * p.tilesPerView;
-  const int tx = vtile % p.tilesX, ty = vtile / p.tilesX;
+  const TileFrame fr = tileFrame(p, tile);
+  const int view = fr.view, tx = fr.tx, ty = fr.ty;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * TH + (warp >> 1) * 4 + job.part;
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
   const bool own = (lane >> 3) < rh;   // this lane has a pixel (all 32 in a whole tile, 8 in a split one)
-  const bool inD = HAS_DEPTH && own && px < p.dw && py < p.dh;
-  float *depthBuf = p.viewTarget ? p.viewTarget[view].depth : p.depth;
+  const bool inD = HAS_DEPTH && own && px < fr.dW && py < fr.dH;
+  float *depthBuf = fr.depth;
   const unsigned lt = (1u << lane) - 1u;
   const int start = p.tileStart[tile], end = p.tileEnd[tile];
   if (start >= end) {
@@ -781,7 +779,7 @@ __global__ void __launch_bounds__(32 * W, (S == 4 ? 2 : 4) * 8 / W) k_raster_cov
     // cleared depth
     if (lane == 0) p.warpHead[(tile * 4 + job.part) * W + warp] = -1;
     if (inD && p.pendingClear && p.clearDepthFlag) {
-      const size_t pix = (size_t) py * p.dw + px;
+      const size_t pix = (size_t) py * fr.dW + px;
       if (S == 4) {
         *reinterpret_cast<float4 *>(depthBuf + pix * 4) = make_float4(p.clearDepth, p.clearDepth, p.clearDepth,
                                                                       p.clearDepth);
@@ -793,7 +791,7 @@ __global__ void __launch_bounds__(32 * W, (S == 4 ? 2 : 4) * 8 / W) k_raster_cov
   }
   Samples4 fb = {0u, 0u, 0u, 0u, 0.f, 0.f, 0.f, 0.f};
   if (inD) {
-    size_t pix = (size_t) py * p.dw + px;
+    size_t pix = (size_t) py * fr.dW + px;
     if (p.pendingClear && p.clearDepthFlag) {
       fb.d0 = fb.d1 = fb.d2 = fb.d3 = p.clearDepth;
     } else if (S == 4) {
@@ -803,13 +801,13 @@ __global__ void __launch_bounds__(32 * W, (S == 4 ? 2 : 4) * 8 / W) k_raster_cov
       fb.d0 = depthBuf[pix];
     }
   }
-  const bool inPix = (own && px < p.cw && py < p.ch) || inD;
+  const bool inPix = (own && px < fr.cW && py < fr.cH) || inD;
   const uint32_t pixWord = (uint32_t) px | ((uint32_t) py << 16);
   int head = -1, ch = -1, cnt = 0;
   bool dead = false;
   unsigned long long total = 0;
   const float lo = S == 4 ? 0.125f : 0.5f, hi = S == 4 ? 0.875f : 0.5f;
-  const float vpExtent = fabsf(p.vp.w) + fabsf(p.vp.h) + 2.f * (float) (rx0 + ry0) + 64.f;
+  const float vpExtent = fabsf(fr.vpW) + fabsf(fr.vpH) + 2.f * (float) (rx0 + ry0) + 64.f;
   CovSlot *slots = covSlots[warp];
   int *queue = covQueue[warp];
   int qn = 0;
@@ -1075,7 +1073,7 @@ __global__ void __launch_bounds__(32 * W, (S == 4 ? 2 : 4) * 8 / W) k_raster_cov
     return;
   }
   if (inD) {
-    size_t pix = (size_t) py * p.dw + px;
+    size_t pix = (size_t) py * fr.dW + px;
     if (S == 4) {
       *reinterpret_cast<float4 *>(depthBuf + pix * 4) = make_float4(fb.d0, fb.d1, fb.d2, fb.d3);
     } else {
@@ -1119,17 +1117,16 @@ __global__ void __launch_bounds__(32 * W) k_rop(const __grid_constant__ DrawPara
   const TileJob job = tileJob(p);
   if (job.skip) return;
   const int tile = job.tile;
-  const int view = p.views > 1 ? tile / p.tilesPerView : 0;
-  const int vtile = tile - view * p.tilesPerView;
-  const int tx = vtile % p.tilesX, ty = vtile / p.tilesX;
+  const TileFrame fr = tileFrame(p, tile);
+  const int tx = fr.tx, ty = fr.ty;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * TH + (warp >> 1) * 4 + job.part;
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
-  const bool inC = (lane >> 3) < job.rows && px < p.cw && py < p.ch;
-  uint32_t *colorBuf = p.viewTarget ? p.viewTarget[view].color : p.color;
-  uint32_t *resolvedBuf = p.viewTarget ? p.viewTarget[view].resolved : p.resolved;
+  const bool inC = (lane >> 3) < job.rows && px < fr.cW && py < fr.cH;
+  uint32_t *colorBuf = fr.color;
+  uint32_t *resolvedBuf = fr.resolved;
   Samples4 fb = {0u, 0u, 0u, 0u, 0.f, 0.f, 0.f, 0.f};
-  const size_t pix = (size_t) py * p.cw + px;
+  const size_t pix = (size_t) py * fr.cW + px;
   if (inC) {
     if (p.pendingClear && p.clearColorFlag) {
       fb.c0 = fb.c1 = fb.c2 = fb.c3 = p.clearColor;

@@ -50,7 +50,7 @@ static void launchRop(const DrawParams &p, int grid, cudaStream_t st) {
 }
 
 void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st, cudaEvent_t evCov, cudaEvent_t evShade) {
-  const int grid = p.views * p.tilesPerView + 3 * (p.tileOrder ? p.heavySlots : 0);   // see tileJob
+  const int grid = p.numTiles + 3 * (p.tileOrder ? p.heavySlots : 0);   // see tileJob
   if (p.tileH == 8) launchCoverage<4>(p, hasDepth, grid, st);
   else launchCoverage<8>(p, hasDepth, grid, st);
   if (evCov) cudaEventRecord(evCov, st);
@@ -72,7 +72,7 @@ void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st, c
 }
 
 void launchRaster(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
-  int grid = p.views * p.tilesPerView;
+  int grid = p.numTiles;
   if (!hasColor) {   // depth-only pass: the fragment shader is skipped (RendererSoft.cpp:346-348)
     if (!hasDepth) return;
     if (p.samples == 4) launchChained(k_raster<SH_BASE, 4, false, true>, dim3(grid), dim3(256), 0, st, p);

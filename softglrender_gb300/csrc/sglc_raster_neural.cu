@@ -218,17 +218,16 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
   uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t) 1023);
   FragQueueN *queues = reinterpret_cast<FragQueueN *>(sm + kRnQueues);
   const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
-  const int view = p.views > 1 ? tile / p.tilesPerView : 0;
-  const int vtile = tile - view * p.tilesPerView;
-  const int tx = vtile % p.tilesX, ty = vtile / p.tilesX;
-  uint32_t *colorBuf = p.viewTarget ? p.viewTarget[view].color : p.color;
-  uint32_t *resolvedBuf = p.viewTarget ? p.viewTarget[view].resolved : p.resolved;
-  float *depthBuf = p.viewTarget ? p.viewTarget[view].depth : p.depth;
+  const TileFrame fr = tileFrame(p, tile);
+  const int view = fr.view;
+  uint32_t *colorBuf = fr.color;
+  uint32_t *resolvedBuf = fr.resolved;
+  float *depthBuf = fr.depth;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * 16 + (warp >> 1) * 4;
+  const int rx0 = fr.tx * 16 + (warp & 1) * 8, ry0 = fr.ty * 16 + (warp >> 1) * 4;
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
-  const bool inC = px < p.cw && py < p.ch;
-  const bool inD = HAS_DEPTH && px < p.dw && py < p.dh;
+  const bool inC = px < fr.cW && py < fr.cH;
+  const bool inD = HAS_DEPTH && px < fr.dW && py < fr.dH;
   FragQueueN &q = queues[warp];
 
   NeuralCta n;
@@ -264,7 +263,7 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
   const unsigned lt = (1u << lane) - 1u;
   Samples4 fb = {0u, 0u, 0u, 0u, 0.f, 0.f, 0.f, 0.f};
   if (inC) {
-    size_t pix = (size_t) py * p.cw + px;
+    size_t pix = (size_t) py * fr.cW + px;
     if (p.pendingClear && p.clearColorFlag) {
       fb.c0 = fb.c1 = fb.c2 = fb.c3 = p.clearColor;
     } else if (S == 4) {
@@ -275,7 +274,7 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
     }
   }
   if (inD) {
-    size_t pix = (size_t) py * p.dw + px;
+    size_t pix = (size_t) py * fr.dW + px;
     if (p.pendingClear && p.clearDepthFlag) {
       fb.d0 = fb.d1 = fb.d2 = fb.d3 = p.clearDepth;
     } else if (S == 4) {
@@ -287,7 +286,7 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
   }
   const int start = p.tileStart[tile], end = p.tileEnd[tile];
   const float lo = S == 4 ? 0.125f : 0.5f, hi = S == 4 ? 0.875f : 0.5f;
-  const float vpExtent = fabsf(p.vp.w) + fabsf(p.vp.h) + 2.f * (float) (rx0 + ry0) + 64.f;
+  const float vpExtent = fabsf(fr.vpW) + fabsf(fr.vpH) + 2.f * (float) (rx0 + ry0) + 64.f;
   for (int base = start; base < end; base += 32) {
     int prim;
     unsigned cand = pass1Candidates<S>(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim, candMasks[warp]);
@@ -334,7 +333,7 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
   }
   if (__syncthreads_or(count > 0)) neuralFlush<S, HAS_DEPTH>(p, n, q, count, mine0, mine1, lane, rx0, ry0, inC, fb);
   if (inC) {
-    size_t pix = (size_t) py * p.cw + px;
+    size_t pix = (size_t) py * fr.cW + px;
     if (S == 4) {
       *reinterpret_cast<uint4 *>(colorBuf + pix * 4) = make_uint4(fb.c0, fb.c1, fb.c2, fb.c3);
       uint32_t rsv = 0;
@@ -350,7 +349,7 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
     }
   }
   if (inD) {
-    size_t pix = (size_t) py * p.dw + px;
+    size_t pix = (size_t) py * fr.dW + px;
     if (S == 4) {
       *reinterpret_cast<float4 *>(depthBuf + pix * 4) = make_float4(fb.d0, fb.d1, fb.d2, fb.d3);
     } else {
@@ -372,7 +371,7 @@ static void launchNeural(const DrawParams &p, int grid, cudaStream_t st) {
 }
 
 void launchRasterNeural(const DrawParams &p, bool hasColor, bool hasDepth, cudaStream_t st) {
-  int grid = p.views * p.tilesPerView;
+  int grid = p.numTiles;
   (void) hasColor;   // the neural shader writes colour; depth-only draws never select it
   if (p.samples == 4) {
     if (hasDepth) launchNeural<4, true>(p, grid, st);

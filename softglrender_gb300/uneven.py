@@ -6,9 +6,11 @@ directional Blinn-Phong without MSAA, odd scenes PBR+IBL with 4x MSAA: the mater
 1080p PBR scene under one of `pbr_materials` environments (material 0 is the 1080p scene's own IBL
 maps, the others channel-rotated variants of them), optionally with the neural IBL shader bound per
 material where it met its PSNR threshold (otherwise that material keeps the plain shader: the
-fallback). `render()` issues the scenes one render pass each; on the GPU the whole sequence is
-captured once in a CUDA graph (softglrender_gb300/graph.py) and replayed with one launch, each
-scene's kernels running in order inside it. `UnevenLanes` splits the scenes over several renderers
+fallback). `render()` issues the scenes one render pass each; `render_batched()` draws each class
+of scenes (Blinn-Phong; PBR of one material) with one multi-scene draw, a single pipeline pass whose
+raster stage takes the (scene, tile) work items of all its scenes from one heaviest-first queue. On
+the GPU either sequence is captured once in a CUDA graph (softglrender_gb300/graph.py) and replayed
+with one launch. `UnevenLanes` splits the scenes over several renderers
 whose submissions run concurrently. Meshes with the same tessellation share their
 displacement seed (the tessellation is rounded to a multiple of 16 longitude segments), which keeps
 the set-up time of 64 scenes of up to 2M triangles within seconds.
@@ -207,6 +209,28 @@ class UnevenBatch:
     def render(self, scenes: Optional[List[int]] = None) -> None:
         for s in (sorted(self.items) if scenes is None else scenes):
             self.render_scene(s)
+
+    def classes(self) -> Dict[Tuple[int, int], List[int]]:
+        """Scenes that share a program configuration, samplers and sample count: the Blinn-Phong
+        scenes (key (0, -1)) and the PBR scenes of each material (key (1, m))."""
+        out: Dict[Tuple[int, int], List[int]] = {}
+        for s in sorted(self.items):
+            it = self.items[s]
+            out.setdefault((int(it["pbr"]), it["material"]), []).append(s)
+        return out
+
+    def render_batched(self) -> None:
+        """The same frames as render(), each class of scenes in one multi-scene draw
+        (Renderer.drawScenes): one pipeline pass, one launch per stage over all of its scenes'
+        vertices, triangles and raster tiles. The class's first program stands for the class
+        (its uniforms come from each scene's resources; a neural binding is per material)."""
+        r = self.r
+        for scenes in self.classes().values():
+            its = [self.items[s] for s in scenes]
+            r.setShaderProgram(its[0]["prog"])
+            r.setPipelineStates(self.states)
+            r.drawScenes([it["vao"] for it in its], [it["fbo"] for it in its], [it["res"] for it in its],
+                         self.clear)
 
     def outputs(self, s: int):
         it = self.items[s]

@@ -43,6 +43,53 @@ def test_uneven_batch_matches_oracle(cuda_lib, oracle_lib):
         assert_outputs_match([g[s]], [c[s]], f"scene {s}")
 
 
+def _render_both(lib, cfg):
+    """Per-scene render passes and the multi-scene draws of the same batch on one renderer."""
+    r = A.Renderer(lib, 0)
+    u = UnevenBatch(r, cfg)
+    u.render()
+    r.waitIdle()
+    single = [u.outputs(s) for s in range(cfg.scenes)]
+    u.render_batched()
+    r.waitIdle()
+    batched = [u.outputs(s) for s in range(cfg.scenes)]
+    r.destroy()
+    return single, batched
+
+
+def _assert_same(a, b, what):
+    for s in range(len(a)):
+        for k in a[s]:
+            assert np.array_equal(a[s][k].view(np.uint8), b[s][k].view(np.uint8)), (what, s, k)
+
+
+def test_multi_scene_draw_is_per_scene_passes_on_oracle(oracle_lib):
+    single, batched = _render_both(oracle_lib, SMALL)
+    _assert_same(single, batched, "oracle")
+
+
+@pytest.mark.gpu
+def test_multi_scene_draw_matches_per_scene_passes(cuda_lib, oracle_lib):
+    """One pipeline pass per class of scenes gives every scene's images bit for bit as its own
+    render pass does, and within the parity bar of the oracle; also with capacities set (no
+    read-back) and replayed from a CUDA graph, twice."""
+    single, batched = _render_both(cuda_lib, SMALL)
+    _assert_same(single, batched, "cuda")
+    c = _render(oracle_lib, SMALL)
+    for s in range(SMALL.scenes):
+        assert_outputs_match([batched[s]], [c[s]], f"multi-scene draw, scene {s}")
+    r = A.Renderer(cuda_lib, 0)
+    u = UnevenBatch(r, SMALL)
+    t = autotune(r, u.render_batched, reps=2, heavy_first=(1,), graph=(True,))
+    for _ in range(2):
+        t.run()
+        r.waitIdle()
+        _assert_same(single, [u.outputs(s) for s in range(SMALL.scenes)], "graph")
+    assert r.getOverflow() == 0
+    t.destroy()
+    r.destroy()
+
+
 @pytest.mark.gpu
 def test_uneven_graph_replay_matches_eager(cuda_lib):
     r = A.Renderer(cuda_lib, 0)
