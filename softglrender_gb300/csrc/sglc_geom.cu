@@ -52,8 +52,12 @@ __device__ __forceinline__ float4 toScreen(const Viewport &vp, float4 c) {
 template<int SH>
 __global__ void __launch_bounds__(256) k_vertex(const __grid_constant__ DrawParams p) {
   chainEnter();
-  // each warp's 32 varying rows are contiguous in memory: they are staged in shared memory and
-  // written as one contiguous run of 16-byte stores (varyStride <= 32 floats for every model)
+  // The warp's 32 attribute rows (the caller's AoS vertex layout) are contiguous in memory unless
+  // they straddle two views: they are then read with coalesced 16-byte loads into shared memory
+  // (rows at an odd float stride, so the threads' reads of their own rows do not collide) and each
+  // thread runs the vertex shader on its row from there. Each warp's 32 varying rows are contiguous
+  // too: they are staged in the same buffer and written as one contiguous run of 16-byte stores
+  // (varyStride <= 32 floats for every model).
   __shared__ float4 stage[8][32 * 8];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -61,6 +65,38 @@ __global__ void __launch_bounds__(256) k_vertex(const __grid_constant__ DrawPara
   const int sf = p.strideF;
   const int i0 = i - lane;
   const int rows = min(32, p.nv - i0);
+  float *sa = reinterpret_cast<float *>(stage[warp]);
+  bool staged = false;
+  if (rows > 0 && (sf & 3) == 0 && sf <= 28) {   // 32 rows of sf + 1 floats fit the warp's buffer
+    int v0 = 0, v1 = 0;
+    const float *src;
+    if (p.scenes) {
+      v0 = sceneOf(p.sceneVBase, p.views, i0);
+      v1 = sceneOf(p.sceneVBase, p.views, i0 + rows - 1);
+      src = p.scenes[v0].attr + (size_t) (i0 - p.sceneVBase[v0]) * sf;
+    } else if (p.views > 1) {
+      v0 = i0 / p.nvView;
+      v1 = (i0 + rows - 1) / p.nvView;
+      src = p.attr + (size_t) (i0 - v0 * p.nvView) * sf;
+    } else {
+      src = p.attr + (size_t) i0 * sf;
+    }
+    if (v0 == v1) {   // warp-uniform
+      const int q4 = sf >> 2;
+      const float4 *s4 = reinterpret_cast<const float4 *>(src);   // rows are multiples of 16 bytes
+      for (int e = lane; e < rows * q4; e += 32) {
+        const float4 f = __ldg(s4 + e);
+        const int r = e / q4;
+        float *d = sa + r * (sf + 1) + 4 * (e - r * q4);
+        d[0] = f.x;
+        d[1] = f.y;
+        d[2] = f.z;
+        d[3] = f.w;
+      }
+      __syncwarp();
+      staged = true;
+    }
+  }
   float v[32];
 #pragma unroll
   for (int k = 0; k < 32; k++) v[k] = 0.f;
@@ -74,12 +110,14 @@ __global__ void __launch_bounds__(256) k_vertex(const __grid_constant__ DrawPara
       view = p.views > 1 ? i / p.nvView : 0;
       a = p.attr + (size_t) (i - view * p.nvView) * sf;
     }
+    if (staged) a = sa + lane * (sf + 1);
     float4 c = runVS<SH>(p, viewUniforms(p, view), a, v);
     p.vClip[i] = c;
     p.vMask[i] = (uint8_t) clipMaskOf(c);
     p.vFrag[i] = toScreen(viewViewport(p, view), c);
   }
   float4 *st = stage[warp];
+  __syncwarp();   // every lane has read its attribute row from the buffer
 #pragma unroll
   for (int k = 0; k < 8; k++)
     if (k < q) st[lane * q + k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
