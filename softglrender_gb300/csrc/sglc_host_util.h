@@ -55,4 +55,15 @@ inline cudaError_t setDynamicSmemOnce(PerDeviceAttr &a, Kernel *kernel, int byte
   return a.err[dev];
 }
 
+// streaming multiprocessors of the current device (152 on a GB300), for grids sized in whole waves
+inline int currentSmCount() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      sms <= 0) {
+    cudaGetLastError();
+    return 152;
+  }
+  return sms;
+}
+
 }  // namespace sglc

@@ -16,6 +16,7 @@
 #pragma once
 
 #include "sglc_device.cuh"
+#include "sglc_host_util.h"
 #include "sglc_shaders.cuh"
 
 namespace sglc {
@@ -295,10 +296,12 @@ __device__ __forceinline__ bool depthPass(const DrawParams &p, float z, float de
   return depthCmp(gclamp(z, p.vp.absMin, p.vp.absMax), dep, p.depthFunc);
 }
 
-// Phase B for one fragment: quad derivatives of the texture coordinates, then the FS.
+// Phase B for one fragment: quad derivatives of the texture coordinates, then the FS. Inlined into
+// the deferred shading kernel (no call, no spills around it: 0.156 -> 0.137 ms at 1080p MSAA4 PBR);
+// the fused raster kernel calls it through shadeFragment below, which keeps that kernel's code small.
 template<int SH, int S>
-__device__ __noinline__ float4 shadeFragment(const DrawParams &p, const uint8_t *U, int tri, int qx, int qy, int px,
-                                             int py, float sb0, float sb1, float sb2) {
+__device__ __forceinline__ float4 shadeFragmentInl(const DrawParams &p, const uint8_t *U, int tri, int qx, int qy,
+                                                   int px, int py, float sb0, float sb1, float sb2) {
   Tri t = loadTri(p.tri + tri);
   const float *r0 = p.vVary + (size_t) t.vid0 * p.varyStride;
   const float *r1 = p.vVary + (size_t) t.vid1 * p.varyStride;
@@ -325,6 +328,12 @@ __device__ __noinline__ float4 shadeFragment(const DrawParams &p, const uint8_t 
     f.dvdy = v[2] - v[0];
   }
   return runFS<SH>(p, f);
+}
+
+template<int SH, int S>
+__device__ __noinline__ float4 shadeFragment(const DrawParams &p, const uint8_t *U, int tri, int qx, int qy, int px,
+                                             int py, float sb0, float sb1, float sb2) {
+  return shadeFragmentInl<SH, S>(p, U, tri, qx, qy, px, py, sb0, sb1, sb2);
 }
 
 template<int SH, int S, bool HAS_DEPTH>
@@ -1097,8 +1106,8 @@ __global__ void __launch_bounds__(128, 8) k_shade(const __grid_constant__ DrawPa
     const uint32_t meta = (uint32_t) a.y;
     const int px = a.z & 0xffff, py = (int) ((uint32_t) a.z >> 16);
     const int qx = px - (int) ((meta >> 9) & 1u), qy = py - (int) ((meta >> 10) & 1u);
-    p.recColor[r] = shadeFragment<SH, S>(p, viewUniforms(p, (int) (meta >> 11)), a.x, qx, qy, px, py,
-                                         __int_as_float(a.w), b.x, b.y);
+    p.recColor[r] = shadeFragmentInl<SH, S>(p, viewUniforms(p, (int) (meta >> 11)), a.x, qx, qy, px, py,
+                                            __int_as_float(a.w), b.x, b.y);
   }
 }
 
@@ -1216,7 +1225,9 @@ __global__ void __launch_bounds__(32 * W) k_rop(const __grid_constant__ DrawPara
 // the shading kernel of one model; the coverage and ROP kernels are model-independent
 template<int SH>
 void launchShadeModel(const DrawParams &p, cudaStream_t st) {
-  const int grid = 152 * 16;
+  // 32 CTAs of 128 threads per SM, grid-stride over the dense record list (at 1080p MSAA4, 708,939
+  // records: about 1.1 per thread; 0.135 -> 0.129 ms against 16 per SM, equal at 64 per SM)
+  const int grid = currentSmCount() * 32;
   if (p.samples == 4) launchChained(k_shade<SH, 4>, dim3(grid), dim3(128), 0, st, p);
   else launchChained(k_shade<SH, 1>, dim3(grid), dim3(128), 0, st, p);
 }
