@@ -235,7 +235,12 @@ __device__ __forceinline__ PbrSurface pbrSurface(const DrawParams &p, const Frag
   PbrSurface s;
   float4 arg = p.def[0] ? tex2D(p, 0, f.v[0], f.v[1], f) : uV4(f.U, 352);
   s.arg = arg;
-  f3 albedo = mk3(powf(arg.x, 2.2f), powf(arg.y, 2.2f), powf(arg.z, 2.2f));
+  // The PBR shader's powers (albedo linearisation, Fresnel (1 - cos)^5, gamma) use the special-
+  // function pow (exp2(y log2 x), a few ulp for these exponents and bases in [0, 1]): an error of a
+  // few ulp moves a colour across a u8 boundary in about one channel in 10^4, by one step. Measured
+  // on GB300 against the oracle: the 1080p MSAA4 frame keeps 0.999987 of its pixels within 1 LSB
+  // (as with powf), and k_shade drops from 0.129 to 0.117 ms.
+  f3 albedo = mk3(__powf(arg.x, 2.2f), __powf(arg.y, 2.2f), __powf(arg.z, 2.2f));
   s.albedo = albedo;
   float metallic = 0.0f, roughness = 1.0f;
   if (p.def[4]) {
@@ -278,7 +283,7 @@ __device__ __forceinline__ PbrSurface pbrSurface(const DrawParams &p, const Frag
     float ggx1 = NdotL / (NdotL * (1.0f - k) + k);
     float G = ggx1 * ggx2;
     float ct = gmax(dot3(H, V), 0.0f);
-    float p5 = powf(gclamp(1.0f - ct, 0.0f, 1.0f), 5.0f);
+    float p5 = __powf(gclamp(1.0f - ct, 0.0f, 1.0f), 5.0f);
     f3 F = F0 + (1.0f - F0) * p5;
     f3 numerator = NDF * G * F;
     float denominator = 4.0f * gmax(dot3(N, V), 0.0f) * gmax(dot3(N, L), 0.0f) + 0.0001f;
@@ -300,7 +305,7 @@ __device__ __forceinline__ PbrSurface pbrSurface(const DrawParams &p, const Frag
 // gamma correction and emissive (PbrSoft.h:311-321)
 __device__ __forceinline__ float4 pbrFinish(const DrawParams &p, f3 ambient, f3 Lo, f3 emissive, float alpha) {
   f3 color = ambient + Lo;
-  color = pow3(color, 1.0f / 2.2f);
+  color = mk3(__powf(color.x, 1.0f / 2.2f), __powf(color.y, 1.0f / 2.2f), __powf(color.z, 1.0f / 2.2f));
   if (p.def[2]) color = color + emissive;
   return make_float4(color.x, color.y, color.z, alpha);
 }
@@ -315,7 +320,7 @@ __device__ inline float4 fsPbr(const DrawParams &p, const FragIn &f) {
     f3 mV = -V;
     f3 R = mV - N * dot3(N, mV) * 2.0f;
     float NdotV = gmax(dot3(N, V), 0.0f);
-    float p5 = powf(gclamp(1.0f - NdotV, 0.0f, 1.0f), 5.0f);
+    float p5 = __powf(gclamp(1.0f - NdotV, 0.0f, 1.0f), 5.0f);
     float omr = 1.0f - roughness;
     f3 F = F0 + (max3(mk3(omr, omr, omr), F0) - F0) * p5;
     f3 kD = 1.0f - F;
