@@ -230,7 +230,7 @@ struct Ctx {
   DevBuf tri, tileCount, pairOff, keyA, keyB, valA, valB, tileStart, tileEnd, tileOrder, scanScratch, sortHist,
       sortHistScan, staging, batchU, batchTargets, batchScenes;
   DevBuf recA, recB, recColor, chunkNext, chunkFill, warpHead, recDense;   // deferred shading
-  DevBuf nnIn;   // neural shading: per record the surface stage's 80-B row
+  DevBuf nnIn;   // neural shading: per record the surface stage's five float4 (blocks of 32 records)
   DevBuf peakChunks;   // largest number of fragment-record chunks a deferred draw used (device)
   bool deferredShading = true;
   bool tmaStore = true;              // sglc_set_tma_store

@@ -207,7 +207,8 @@ struct DrawParams {
   cudaTextureObject_t hwTex[kMaxSamplers];
   int *errFlags;
   int nnInjectTimeout;
-  float4 *nnIn;                   // per dense record: 12 network inputs, (Lo, ao), (emissive, alpha)
+  float4 *nnIn;                   // per dense record: the surface stage's 4 or 5 float4, in blocks of 32
+                                  // records by float4 (sglc_shade_neural.cu nnRow)
   // TMA write-back of whole 16x16 tiles (single-view draws): tensor maps over this GPU's colour
   // (samples interleaved), resolved and depth attachments; tmaStore bit 0: colour and resolved by
   // k_rop, bit 1: depth by k_raster_cov; 0: per-thread stores

@@ -16,7 +16,9 @@
 // Two kernels. k_neural_surface evaluates the surface terms at high occupancy (128-thread CTAs,
 // up to 10 per SM, over a grid-stride loop): the chain of dependent loads (record,
 // triangle set-up, varyings, texels) needs many warps in flight, which a kernel holding tensor
-// memory and 160 KB of operand tiles cannot have. It writes 80 B per record in dense order.
+// memory and 160 KB of operand tiles cannot have. It writes 64 B per record (80 B with an emissive
+// map) in dense order, in blocks of 32 records by float4 (nnRow: each store and each load of the next
+// kernel is one contiguous run per warp).
 // k_shade_neural then runs the network: one persistent CTA per SM with eight warpgroups (1,024
 // threads, 64 registers each: enough warps in flight to cover the tensor-core round trips and the
 // TMEM loads). Each warpgroup walks its own sequence of 128-record tiles with its own [128][80] BF16
@@ -170,6 +172,11 @@ __device__ __forceinline__ float4 hwSample(const DrawParams &p, int slot, float 
 
 __device__ __forceinline__ f3 fastNormalize(f3 v) { return v * rsqrtf(dot3(v, v)); }
 
+// the surface stage's five float4 of dense record i: records in blocks of 32, each block holding its
+// records' first float4, then their second, ... (a warp's 32 consecutive records store and load each
+// float4 as one contiguous 512-byte run); float4 k of the record is row[32 k]
+__device__ __forceinline__ float4 *nnRow(float4 *base, int i) { return base + (size_t) (i >> 5) * 160 + (i & 31); }
+
 // surface terms and network inputs of one fragment record
 struct Surface {
   float x[kIn];
@@ -292,22 +299,24 @@ __device__ __forceinline__ Surface surface(const DrawParams &p, int4 a, float2 b
 }
 
 // Stage 1 (high occupancy, no tensor cores): the surface terms of every record, written in the
-// dense record order as five float4: the network's 12 inputs, then (Lo, ao) and (emissive, alpha).
+// dense record order as float4 (N, V.x), (V.yz, roughness, metallic), (albedo, alpha), (Lo, ao) and,
+// with an emissive map, (emissive, 0); the network's twelfth input, max(N.V, 0), is recomputed from
+// N and V by the next kernel.
 __global__ void __launch_bounds__(128, 10) k_neural_surface(const __grid_constant__ DrawParams p) {
   const int nRec = min(p.counters[kCntDense], p.chunkCap * kChunk);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nRec; i += gridDim.x * blockDim.x) {
     const int r = p.recDense[i];
-    float4 *o = p.nnIn + (size_t) 5 * i;
+    float4 *o = nnRow(p.nnIn, i);
     if (r < 0) {
-      for (int k = 0; k < 5; k++) o[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int k = 0; k < (p.def[2] ? 5 : 4); k++) o[32 * k] = make_float4(0.f, 0.f, 0.f, 0.f);
       continue;
     }
     const Surface sf = surface(p, p.recA[r], p.recB[r]);
     o[0] = make_float4(sf.x[0], sf.x[1], sf.x[2], sf.x[3]);
-    o[1] = make_float4(sf.x[4], sf.x[5], sf.x[6], sf.x[7]);
-    o[2] = make_float4(sf.x[8], sf.x[9], sf.x[10], sf.x[11]);
-    o[3] = make_float4(sf.Lo.x, sf.Lo.y, sf.Lo.z, sf.ao);
-    o[4] = make_float4(sf.emissive.x, sf.emissive.y, sf.emissive.z, sf.alpha);
+    o[32] = make_float4(sf.x[4], sf.x[5], sf.x[6], sf.x[7]);
+    o[64] = make_float4(sf.x[8], sf.x[9], sf.x[10], sf.alpha);
+    o[96] = make_float4(sf.Lo.x, sf.Lo.y, sf.Lo.z, sf.ao);
+    if (p.def[2]) o[128] = make_float4(sf.emissive.x, sf.emissive.y, sf.emissive.z, 0.f);
   }
 }
 
@@ -357,19 +366,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_const
   for (int t0 = (blockIdx.x * kWG + wg) * 128; t0 < nRec; t0 += gridDim.x * kThreads) {
     const int di = t0 + wgThread;
     const bool live = di < nRec;
-    const float4 *q = p.nnIn + (size_t) 5 * di;
+    const float4 *q = nnRow(p.nnIn, di);
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 q0 = live ? q[0] : z4, q1 = live ? q[1] : z4;
+    const float4 q0 = live ? q[0] : z4, q1 = live ? q[32] : z4;
     // layer 1: inputs 0-5 (N, V), then inputs 6-11 (roughness, metallic, albedo, N.V) and the bias
     {
       const float x[6] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y};
       encodeHalf<0>(x, xTile, row);
     }
     issue(sW1, kK1, 0, kHid, false);
-    const float4 q2 = live ? q[2] : z4;
+    const float4 q2 = live ? q[64] : z4;
     wait();
     {
-      const float x[6] = {q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+      // max(N.V, 0) as the surface stage computes it (the inputs are the same floats)
+      const float ndv = gmax(dot3(mk3(q0.x, q0.y, q0.z), mk3(q0.w, q1.x, q1.y)), 0.f);
+      const float x[6] = {q1.z, q1.w, q2.x, q2.y, q2.z, ndv};
       encodeHalf<1>(x, xTile, row);
     }
     issue(sW1, kK1, kXCols, kHid, true);
@@ -385,8 +396,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_const
     float4 loAo = z4, emA = z4;
     if (live) {
       r = p.recDense[di];
-      loAo = q[3];
-      emA = q[4];
+      loAo = q[96];
+      if (p.def[2]) emA = q[128];
     }
     wait();
     float y[16];
@@ -399,7 +410,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_shade_neural(const __grid_const
       const f3 c = mk3(a0 * a0, a1 * a1, a2 * a2) * loAo.w + mk3(loAo.x, loAo.y, loAo.z);
       f3 col = mk3(__powf(c.x, 1.f / 2.2f), __powf(c.y, 1.f / 2.2f), __powf(c.z, 1.f / 2.2f));
       if (p.def[2]) col = col + mk3(emA.x, emA.y, emA.z);
-      p.recColor[r] = make_float4(col.x, col.y, col.z, emA.w);
+      p.recColor[r] = make_float4(col.x, col.y, col.z, q2.w);
     }
     // every thread has read its TMEM lane and its tile row before the next tile overwrites them
     wgSync(wg);
