@@ -461,6 +461,13 @@ def bench_uneven_lanes(r, cfg, u, per_scene, net, materials, lanes: int = 4):
     ul.launch()
     ul.wait()
     plain_ms = batch_ms(5)
+    # the same lanes, each drawing its scenes as one multi-scene draw per class
+    ul.batched = True
+    ul.tune(reps=3)
+    ul.launch()
+    ul.wait()
+    plain_batched_ms = batch_ms(5)
+    ul.batched = False
     # spot check: the lanes' images equal the single renderer's (every 8th scene)
     same = True
     r.setCapacity(None)
@@ -471,6 +478,7 @@ def bench_uneven_lanes(r, cfg, u, per_scene, net, materials, lanes: int = 4):
         same &= all(np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)) for k in a)
     res = {"lanes": lanes, "scenes_per_lane": [len(g) for g in ul.groups],
            "plain_ms_per_batch": round(plain_ms, 3), "plain_scenes_per_s": round(cfg.scenes / (plain_ms / 1e3), 1),
+           "multi_scene_plain_ms_per_batch": round(plain_batched_ms, 3),
            "images_equal_single_renderer": bool(same)}
     nets = []
     if net is not None:
@@ -487,7 +495,14 @@ def bench_uneven_lanes(r, cfg, u, per_scene, net, materials, lanes: int = 4):
         ul.launch()
         ul.wait()
         n_ms = batch_ms(5)
-        res.update({"neural_ms_per_batch": round(n_ms, 3), "neural_scenes_per_s": round(cfg.scenes / (n_ms / 1e3), 1)})
+        ul.batched = True
+        ul.tune(reps=3)
+        ul.launch()
+        ul.wait()
+        nb_ms = batch_ms(5)
+        ul.batched = False
+        res.update({"neural_ms_per_batch": round(n_ms, 3), "neural_scenes_per_s": round(cfg.scenes / (n_ms / 1e3), 1),
+                    "multi_scene_neural_ms_per_batch": round(nb_ms, 3)})
     ul.release()
     for nn in nets:
         nn.destroy()

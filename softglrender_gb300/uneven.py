@@ -260,9 +260,13 @@ class UnevenLanes:
     Every scene's images equal the single-renderer batch's (a scene is drawn the same way on any
     renderer)."""
 
-    def __init__(self, renderers: Sequence[A.Renderer], cfg: UnevenConfig, cost: Sequence[float]):
+    def __init__(self, renderers: Sequence[A.Renderer], cfg: UnevenConfig, cost: Sequence[float],
+                 batched: bool = False):
+        """`batched`: each lane draws its scenes with one multi-scene draw per class
+        (UnevenBatch.render_batched) instead of one render pass per scene."""
         self.renderers = list(renderers)
         self.cfg = cfg
+        self.batched = batched
         self.groups = assign_lanes(cost, len(self.renderers))
         self.batches = [UnevenBatch(r, cfg, only=g) for r, g in zip(self.renderers, self.groups)]
         self.tuned = []
@@ -273,7 +277,7 @@ class UnevenLanes:
         self.release()
         for r, b in zip(self.renderers, self.batches):
             r.setCapacity(None)
-            self.tuned.append(autotune(r, b.render, reps=reps))
+            self.tuned.append(autotune(r, b.render_batched if self.batched else b.render, reps=reps))
 
     def launch(self) -> None:
         """Enqueue every lane's submission (each on its own renderer's stream)."""

@@ -120,14 +120,15 @@ def test_assign_lanes_covers_and_balances():
 
 
 @pytest.mark.gpu
-def test_uneven_lanes_match_single_renderer(cuda_lib):
+@pytest.mark.parametrize("batched", [False, True])
+def test_uneven_lanes_match_single_renderer(cuda_lib, batched):
     r = A.Renderer(cuda_lib, 0)
     u = UnevenBatch(r, SMALL)
     u.render()
     r.waitIdle()
     single = [u.outputs(s) for s in range(SMALL.scenes)]
     rs = [A.Renderer(cuda_lib, 0) for _ in range(3)]
-    ul = UnevenLanes(rs, SMALL, [float(t) for t in u.triangles])
+    ul = UnevenLanes(rs, SMALL, [float(t) for t in u.triangles], batched=batched)
     assert sorted(sum(ul.groups, [])) == list(range(SMALL.scenes))
     ul.tune(reps=2)
     for _ in range(2):   # two submissions in a row
