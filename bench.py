@@ -894,19 +894,22 @@ def main():
         r._call("texture_read_image", ct.handle, 0, 0, 1, out.ctypes.data_as(C.c_void_p), out.nbytes)
     e2e_graph_fps = world * args.steps / max_over_ranks(time.perf_counter() - t0, pg, f"cuda:{local}" if pg and torch.cuda.is_available() else None)
 
-    # two frames in flight: a second renderer (its own stream and its own copy of the scene's
-    # resources) driven by a second host thread; both threads run the loop above (upload, eager
-    # frame, blocking read-back), so one renderer's copies overlap the other's kernels. The
-    # library's calls release the interpreter lock while they wait.
+    # frames in flight: further renderers (each its own stream and its own copy of the scene's
+    # resources) driven by their own host threads; every thread runs the loop above (upload, eager
+    # frame, blocking read-back), so one renderer's copies and kernels overlap the others'. The
+    # library's calls release the interpreter lock while they wait. Two, three and four renderers
+    # are measured; `e2e.value` is the best.
     import threading
-    r2 = sg.RendererCUDA(local)
-    inst2 = S.SceneInstance(r2, scene)
-    tuned2 = autotune(r2, inst2.render, reps=3)
-    lanes = []
-    for rr, ii in ((r, inst), (r2, inst2)):
+    extra = []
+    lanes = [(r, inst, inst.draws[0][0][0], model_ub, ct, out)]
+    for _ in range(3):
+        rr = sg.RendererCUDA(local)
+        ii = S.SceneInstance(rr, scene)
+        tt = autotune(rr, ii.render, reps=3)
         ub = [b for b in ii.draws[0][0][2].blocks.values() if b.name == "UniformsModel"][0]
         lanes.append((rr, ii, ii.draws[0][0][0], ub, ii.color_tex[0],
                       torch.empty(W * H * 4, dtype=torch.uint8, pin_memory=True).numpy()))
+        extra.append((rr, tt))
 
     def frame_loop(lane, n):
         rr, ii, vv, ub, cc, oo = lane
@@ -918,19 +921,25 @@ def main():
 
     for lane in lanes:
         frame_loop(lane, 2)
-    half = [args.steps // 2, args.steps - args.steps // 2]
-    barrier(pg)
-    t0 = time.perf_counter()
-    threads = [threading.Thread(target=frame_loop, args=(lanes[i], half[i])) for i in range(2)]
-    for th in threads:
-        th.start()
-    for th in threads:
-        th.join()
-    e2e2_fps = world * args.steps / max_over_ranks(time.perf_counter() - t0, pg, f"cuda:{local}" if pg and torch.cuda.is_available() else None)
-    barrier(pg)
-    two_identical = bool(np.array_equal(lanes[0][5], lanes[1][5]) and np.array_equal(lanes[0][5], out))
-    tuned2.destroy()
-    r2.destroy()
+    in_flight = {}
+    for k in (2, 3, 4):
+        share = [args.steps // k + (1 if i < args.steps % k else 0) for i in range(k)]
+        barrier(pg)
+        t0 = time.perf_counter()
+        threads = [threading.Thread(target=frame_loop, args=(lanes[i], share[i])) for i in range(k)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        in_flight[k] = world * args.steps / max_over_ranks(time.perf_counter() - t0, pg,
+                                                            f"cuda:{local}" if pg and torch.cuda.is_available() else None)
+        barrier(pg)
+    best_k = max(in_flight, key=lambda k: in_flight[k])
+    e2e2_fps = in_flight[best_k]
+    two_identical = all(np.array_equal(lanes[i][5], out) for i in range(len(lanes)))
+    for rr, tt in extra:
+        tt.destroy()
+        rr.destroy()
 
     result = {
         "metric": METRIC,
@@ -956,8 +965,10 @@ def main():
                      "raster_rop": round(parts["rop"], 4)},
         "e2e": {"value": round(e2e2_fps, 3), "unit": "frames/s", "h2d_bytes_per_step": int(pinned_v.nbytes + len(model_bytes)),
                 "d2h_bytes_per_step": int(out.nbytes),
-                "submission": "eager, tuned capacities; two renderers on two host threads (two frames in flight), "
-                              "each frame: vertex array + model uniforms uploaded, frame, resolved image read back",
+                "submission": f"eager, tuned capacities; {best_k} renderers on {best_k} host threads ({best_k} frames "
+                              "in flight), each frame: vertex array + model uniforms uploaded, frame, resolved image "
+                              "read back",
+                "frames_in_flight": {str(k): round(v, 3) for k, v in in_flight.items()},
                 "images_identical": two_identical,
                 "one_frame_in_flight_value": round(e2e_fps, 3),
                 "graph_replay_value": round(e2e_graph_fps, 3)},
