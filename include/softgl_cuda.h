@@ -257,7 +257,7 @@ SGLC_API sglc_status sglc_set_enable_early_z(sglc_context *ctx, int32_t enable);
  * beginRenderPass(framebuffers[v], clear) (no clear when `clear` is null); setShaderResources(
  * resources[v]); draw(); endRenderPass(). All views' attachments must have view 0's sizes, formats
  * and sample count. The GPU runs every view in one pipeline pass (one launch per stage over all
- * (view, triangle) and (view, tile) work items). */
+ * (view, triangle) and (view, tile) work items). At most 2^20 views per call. */
 SGLC_API sglc_status sglc_draw_views(sglc_context *ctx, const sglc_handle *framebuffers, const sglc_handle *resources,
                                      int32_t count, const sglc_clear_states *clear);
 /* Multi-scene draw: independent scenes that share the bound program, pipeline states and samplers
@@ -271,7 +271,7 @@ SGLC_API sglc_status sglc_draw_views(sglc_context *ctx, const sglc_handle *frame
  * pass: one launch per stage over every (scene, vertex), (scene, triangle) and (scene, tile) work
  * item, the raster stage taking tiles from one heaviest-first queue across the scenes. It replaces
  * the per-scene loop over Renderer calls that RendererSoft runs one block task queue for at a time
- * (RendererSoft.cpp:731-737 feeding ThreadPool.h:100-110). */
+ * (RendererSoft.cpp:731-737 feeding ThreadPool.h:100-110). At most 2^20 scenes per call. */
 SGLC_API sglc_status sglc_draw_scenes(sglc_context *ctx, const sglc_handle *vertex_arrays,
                                       const sglc_handle *framebuffers, const sglc_handle *resources, int32_t count,
                                       const sglc_clear_states *clear);

@@ -1863,6 +1863,8 @@ sglc_status drawBatch(sglc_context *ctx, const sglc_handle *vaos, const sglc_han
   const std::string w(what);
   if (count <= 0 || !framebuffers || !resources)
     return c->fail(SGLC_ERR_INVALID_VALUE, w + ": need at least one view");
+  if (count > (1 << 20))   // fragment records carry the view in 21 bits of their meta word
+    return c->fail(SGLC_ERR_INVALID_VALUE, w + ": at most 2^20 views in one call");
   Object *po = c->get(c->prog, K_PROG);
   if (!po || !po->prog.shader) return c->fail(SGLC_ERR_INVALID_VALUE, w + ": no shader program bound");
   ProgObj &P = po->prog;

@@ -450,9 +450,6 @@ __global__ void __launch_bounds__(256) k_bin_emit(const __grid_constant__ DrawPa
 // ------------------------------------------------------------------------------------------------
 // stable LSD radix sort of (tile, primitive) pairs by tile, 8-bit digits
 // ------------------------------------------------------------------------------------------------
-constexpr int kSortThreads = 256;
-constexpr int kSortItems = 8;                       // per thread
-constexpr int kSortTile = kSortThreads * kSortItems; // 2048 items per CTA
 
 __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint32_t *keys, const int *nPtr, int shift,
                                                              int bits, int *hist, int numBlocks) {
