@@ -23,8 +23,10 @@ void launchBinEmit(const DrawParams &p, int primCount, cudaStream_t st);
 // sortScratchInts(nPairs) ints (2^maxDigitBits buckets per block of 2048 pairs are used)
 constexpr int kMaxDigitBits = 10;
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 2;                          // per thread (512 items per CTA: 0.047 -> 0.039 ms of binning at 1080p, against 2,048)
-constexpr int kSortTile = kSortThreads * kSortItems;   // items per CTA (a multiple of 256)
+constexpr int kSortItemsSmall = 2, kSortItemsLarge = 8;          // items per thread
+constexpr int kSortTileSmall = kSortThreads * kSortItemsSmall;   // 512 items per CTA
+constexpr int kSortTileLarge = kSortThreads * kSortItemsLarge;   // 2,048 items per CTA
+constexpr int kSortSmallMax = 1 << 20;                           // sorts up to this size use the small blocks
 int sortScratchInts(int nPairs);
 int sortPassCount(int keyBits, int maxDigitBits = kMaxDigitBits);
 void sortPairs(const DrawParams &p, int nPairs, const int *nPtr, int keyBits, int *hist, int *histScan,

@@ -43,8 +43,8 @@ constexpr int kVaryStride = 8;             // vertex colour: 4 varyings, row of 
 constexpr int kAttrFloats = 8;             // position vec3 (padded) + RGBA colour
 constexpr int kVCap = kMaxVertices + kMaxClipVertices;
 constexpr int kPrimCap = kMaxTriangles + kMaxAppended;
-constexpr int kSortBlocks = kMaxPairs / kSortTile;
-static_assert(kMaxPairs % kSortTile == 0, "whole sort blocks");
+constexpr int kSortBlocks = kMaxPairs / kSortTileSmall;   // the sort of up to kMaxPairs uses small blocks
+static_assert(kMaxPairs % kSortTileSmall == 0 && kMaxPairs <= kSortSmallMax, "whole small sort blocks");
 
 constexpr size_t align256(size_t n) { return (n + 255) & ~(size_t) 255; }
 // byte offsets of every working buffer inside the scratch array
