@@ -8,7 +8,8 @@
 - 256 batched views at 256x256 after a 2048x2048 shadow pass (one batched draw against the
   reference viewer's one pass per view);
 - the extremes of the 64-scene uneven batch: 1.9M triangles at 1024x1024 PBR MSAA 4x, 830k at
-  2048x2048 PBR, 889k at 128x128 PBR, 1.7M at 512x512 Blinn-Phong, 960 at 2048x2048 PBR.
+  2048x2048 PBR, 889k at 128x128 PBR, 1.7M at 512x512 Blinn-Phong, 960 at 2048x2048 PBR; and all 64
+  scenes as multi-scene draws against their own render passes.
 
 Depth bit for bit; colour within the colour bar (exactly, for vertex colours)."""
 import os
@@ -101,3 +102,30 @@ def test_uneven_extremes_full(cuda_lib, oracle_lib):
     assert max(tris.values()) > 1_800_000 and min(tris.values()) < 1000
     for s in UNEVEN_EXTREMES:
         assert_outputs_match([g[s]], [c[s]], f"scene {s}")
+
+
+def test_uneven_full_multi_scene_equals_per_scene(cuda_lib):
+    """All 64 scenes of the uneven batch (1k-2M triangles, 128^2-2048^2, Blinn-Phong and PBR MSAA 4x)
+    drawn as one multi-scene draw per class equal their own render passes bit for bit (the per-scene
+    passes are checked against the oracle above), eagerly and replayed from the tuned graph."""
+    r = A.Renderer(cuda_lib, 0)
+    u = UnevenBatch(r, UnevenConfig())
+    u.render()
+    r.waitIdle()
+    single = {s: u.outputs(s) for s in range(u.cfg.scenes)}
+    u.render_batched()
+    r.waitIdle()
+    for s in range(u.cfg.scenes):
+        o = u.outputs(s)
+        for k in single[s]:
+            assert np.array_equal(o[k].view(np.uint8), single[s][k].view(np.uint8)), ("eager", s, k)
+    t = autotune(r, u.render_batched, reps=1, heavy_first=(1,), graph=(True,))
+    t.run()
+    r.waitIdle()
+    assert r.getOverflow() == 0
+    for s in range(u.cfg.scenes):
+        o = u.outputs(s)
+        for k in single[s]:
+            assert np.array_equal(o[k].view(np.uint8), single[s][k].view(np.uint8)), ("graph", s, k)
+    t.destroy()
+    r.destroy()
