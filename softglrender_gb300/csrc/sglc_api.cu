@@ -1201,7 +1201,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
     bool deferShade = c->deferredShading && ct && deferredShadingModel(p.shading);
     long long chunks = 0;
     if (deferShade) {
-      const long long warps = ((long long) numTiles + 3 * 64) * (p.tileH / 2);   // split tiles: 4 CTAs
+      const long long warps = ((long long) numTiles + (kSplitParts - 1) * 64) * (p.tileH / 2);   // split tiles
       chunks = deferred ? (c->cap.fragments + kChunk - 1) / kChunk
                         : (long long) (fragBound / kChunk) + warps + 1;
       if (chunks < 1 || chunks * kChunk > (1ll << 28)) deferShade = false;   // single kernel instead
@@ -1214,7 +1214,7 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
       CK(c->recColor.ensure(sizeof(float4) * (size_t) chunks * kChunk));
       CK(c->chunkNext.ensure(sizeof(int) * (size_t) chunks));
       CK(c->chunkFill.ensure(sizeof(int) * (size_t) chunks));
-      CK(c->warpHead.ensure(sizeof(int) * (size_t) numTiles * 4 * (p.tileH / 2)));
+      CK(c->warpHead.ensure(sizeof(int) * (size_t) numTiles * kSplitParts * (p.tileH / 2)));
       CK(c->recDense.ensure(sizeof(int) * (size_t) chunks * kChunk));
       p.recA = c->recA.as<int4>();
       p.recB = c->recB.as<float2>();
@@ -1228,8 +1228,9 @@ sglc_status drawImpl(Ctx *c, const BatchViews *bv = nullptr) {
         p.nnIn = c->nnIn.as<float4>();
       }
       p.chunkCap = (int) chunks;
-      p.heavySlots = 64;    // with the heavy-first order: its first 64 tiles may be split in 4
-      p.heavyMin = 256;     // primitives in a tile's list above which it is split
+      p.heavySlots = 64;    // with the heavy-first order: its first 64 tiles may be split in kSplitParts
+      p.heavyMin = 256;     // primitives in a tile's list above which it is split in 4 (one row per warp)
+      p.heavyMin8 = 1024;   // ... and in 8 (half a row per warp) above four times that: the sphere's poles at 1080p
       if (!c->peakChunks.ptr) {
         CK(c->peakChunks.ensure(sizeof(int)));
         CK(cudaMemsetAsync(c->peakChunks.ptr, 0, sizeof(int), c->stream));

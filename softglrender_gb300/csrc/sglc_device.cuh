@@ -237,12 +237,13 @@ struct DrawParams {
   float2 *recB;                   // b1, b2
   float4 *recColor;               // fragment shader output
   int *chunkNext, *chunkFill;     // per chunk: successor (-1: none), records in it
-  int *warpHead;                  // per raster warp ((tile * 4 + part) * 8 + warp): first chunk, -1: none
+  int *warpHead;                  // per raster warp ((tile * kSplitParts + part) * warps + warp): first chunk, -1: none
   int *recDense;                  // record ids in append-round order, no gaps (-1: a dropped record)
   int chunkCap;
   // the heaviest tiles (the first heavySlots of the heavy-first order whose list is longer than
-  // heavyMin) are split over 4 CTAs, each warp owning one 8-pixel row instead of an 8x4 block
-  int heavySlots, heavyMin;
+  // heavyMin) are split over 4 CTAs, each warp owning one 8-pixel row instead of an 8x4 block, or,
+  // above heavyMin8, over 8 CTAs, each warp owning half a row
+  int heavySlots, heavyMin, heavyMin8;   // split in 4 above heavyMin primitives, in 8 above heavyMin8
   // small steps folded into kernels that run anyway (each null / 0: not done there)
   int binZeroRanges;              // k_bin_emit zeroes tileStart / tileEnd of all tiles
   const int *binPairTotal;        // k_bin_emit sets counters[4] = min(*binPairTotal, pairCap)
@@ -253,6 +254,7 @@ struct DrawParams {
 };
 
 constexpr int kChunk = 32;         // fragment records per chunk
+constexpr int kSplitParts = 8;     // CTAs per split heavy tile of the deferred raster kernels
 constexpr int kCntChunks = 5;      // DrawParams::counters[5]: chunks allocated
 constexpr int kCntBound = 6;       // counters[6..7]: 64-bit upper bound on a draw's fragment records
 constexpr int kCntDense = 8;       // counters[8]: entries of the dense record list

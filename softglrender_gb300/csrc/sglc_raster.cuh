@@ -738,21 +738,39 @@ __device__ __forceinline__ int allocChunk(const DrawParams &p, int lane) {
 struct TileJob {
   int tile, part, rows;   // rows of each warp's block: 4 (whole tile) or 1 (split)
   bool skip;
+  int halves;             // a split tile: 1 (four parts, a whole row per warp) or 2 (eight, half rows)
 };
+
 
 __device__ __forceinline__ TileJob tileJob(const DrawParams &p) {
   const int H = p.tileOrder ? p.heavySlots : 0;
   const int nTiles = p.numTiles;
   const int b = blockIdx.x;
-  if (b < 4 * H) {
-    const int slot = b >> 2, part = b & 3;
-    if (slot >= nTiles) return {0, 0, 4, true};
+  if (b < kSplitParts * H) {
+    const int slot = b / kSplitParts, part = b % kSplitParts;
+    if (slot >= nTiles) return {0, 0, 4, true, 1};
     const int tile = p.tileOrder[slot];
-    if (p.tileEnd[tile] - p.tileStart[tile] > p.heavyMin) return {tile, part, 1, false};
-    return {tile, 0, 4, part != 0};
+    const int len = p.tileEnd[tile] - p.tileStart[tile];
+    if (len > p.heavyMin8) return {tile, part, 1, false, 2};                 // eight parts
+    if (len > p.heavyMin) return {tile, part & 3, 1, part >= 4, 1};        // four parts
+    return {tile, 0, 4, part != 0, 1};
   }
-  const int k = b - 3 * H;
-  return {p.tileOrder ? p.tileOrder[k] : k, 0, 4, false};
+  const int k = b - (kSplitParts - 1) * H;
+  return {p.tileOrder ? p.tileOrder[k] : k, 0, 4, false, 1};
+}
+
+// Pixels of a job: a whole tile gives each warp its 8x4 block (every lane owns a pixel); part q of a
+// split tile gives each warp row q % 4 of its block, and in eight parts only the half of that row
+// numbered q / 4 (lanes 0-3 or 4-7 own a pixel). The 8-pixel row stays the warp's rectangle for the
+// list compaction and pass 1; lanes that own no pixel take part in the load-balanced pass 2 only.
+__device__ __forceinline__ int jobRow(const TileJob &job) { return job.rows == 4 ? 0 : job.part & 3; }
+__device__ __forceinline__ bool jobOwns(const TileJob &job, int lane) {
+  if (job.rows == 4) return true;
+  return (lane >> 3) == 0 && (job.halves == 1 || ((lane & 7) >> 2) == (job.part >> 2));
+}
+// the record-list head of warp `warp` of a job
+__device__ __forceinline__ int warpSlot(const TileJob &job, int W, int warp) {
+  return (job.tile * kSplitParts + job.part) * W + warp;
 }
 
 // one evaluated (pixel, candidate) pair of the load-balanced pass 2
@@ -775,9 +793,9 @@ __global__ void __launch_bounds__(32 * W, (S == 4 ? 2 : 4) * 8 / W) k_raster_cov
   const TileFrame fr = tileFrame(p, tile);
   const int view = fr.view, tx = fr.tx, ty = fr.ty;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * TH + (warp >> 1) * 4 + job.part;
+  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * TH + (warp >> 1) * 4 + jobRow(job);
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
-  const bool own = (lane >> 3) < rh;   // this lane has a pixel (all 32 in a whole tile, 8 in a split one)
+  const bool own = jobOwns(job, lane);   // this lane has a pixel (all 32 in a whole tile, 4 or 8 in a split one)
   const bool inD = HAS_DEPTH && own && px < fr.dW && py < fr.dH;
   float *depthBuf = fr.depth;
   const unsigned lt = (1u << lane) - 1u;
@@ -786,7 +804,7 @@ __global__ void __launch_bounds__(32 * W, (S == 4 ? 2 : 4) * 8 / W) k_raster_cov
     // an empty list (most tiles of a frame): no records, so no part in the dense list (the whole
     // CTA leaves here); only the warps' empty record lists and, on a pass's first draw, the
     // cleared depth
-    if (lane == 0) p.warpHead[(tile * 4 + job.part) * W + warp] = -1;
+    if (lane == 0) p.warpHead[warpSlot(job, W, warp)] = -1;
     if (inD && p.pendingClear && p.clearDepthFlag) {
       const size_t pix = (size_t) py * fr.dW + px;
       if (S == 4) {
@@ -1033,7 +1051,7 @@ __global__ void __launch_bounds__(32 * W, (S == 4 ? 2 : 4) * 8 / W) k_raster_cov
     }
   }
   if (lane == 0) {
-    p.warpHead[(tile * 4 + job.part) * W + warp] = head;
+    p.warpHead[warpSlot(job, W, warp)] = head;
     if (ch >= 0) p.chunkFill[ch] = cnt;
     if (p.fragCounter && total) atomicAdd(p.fragCounter, total);
   }
@@ -1129,9 +1147,9 @@ __global__ void __launch_bounds__(32 * W) k_rop(const __grid_constant__ DrawPara
   const TileFrame fr = tileFrame(p, tile);
   const int tx = fr.tx, ty = fr.ty;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * TH + (warp >> 1) * 4 + job.part;
+  const int rx0 = tx * 16 + (warp & 1) * 8, ry0 = ty * TH + (warp >> 1) * 4 + jobRow(job);
   const int px = rx0 + (lane & 7), py = ry0 + (lane >> 3);
-  const bool inC = (lane >> 3) < job.rows && px < fr.cW && py < fr.cH;
+  const bool inC = jobOwns(job, lane) && px < fr.cW && py < fr.cH;
   uint32_t *colorBuf = fr.color;
   uint32_t *resolvedBuf = fr.resolved;
   Samples4 fb = {0u, 0u, 0u, 0u, 0.f, 0.f, 0.f, 0.f};
@@ -1146,7 +1164,7 @@ __global__ void __launch_bounds__(32 * W) k_rop(const __grid_constant__ DrawPara
       fb.c0 = colorBuf[pix];
     }
   }
-  int ch = p.warpHead[(tile * 4 + job.part) * W + warp];
+  int ch = p.warpHead[warpSlot(job, W, warp)];
   while (ch >= 0) {
     const int fill = p.chunkFill[ch];
     const size_t r = (size_t) ch * kChunk + lane;

@@ -50,7 +50,7 @@ static void launchRop(const DrawParams &p, int grid, cudaStream_t st) {
 }
 
 void launchRasterDeferred(const DrawParams &p, bool hasDepth, cudaStream_t st, cudaEvent_t evCov, cudaEvent_t evShade) {
-  const int grid = p.numTiles + 3 * (p.tileOrder ? p.heavySlots : 0);   // see tileJob
+  const int grid = p.numTiles + (kSplitParts - 1) * (p.tileOrder ? p.heavySlots : 0);   // see tileJob
   if (p.tileH == 8) launchCoverage<4>(p, hasDepth, grid, st);
   else launchCoverage<8>(p, hasDepth, grid, st);
   if (evCov) cudaEventRecord(evCov, st);
