@@ -1879,6 +1879,7 @@ sglc_status drawBatch(sglc_context *ctx, const sglc_handle *vaos, const sglc_han
     Object *fo = c->get(framebuffers[v], K_FB);
     Object *r = c->get(resources[v], K_RES);
     if (!fo || !r) return c->fail(SGLC_ERR_INVALID_HANDLE, w + ": invalid framebuffer or resources handle");
+    if (vaos && !c->get(vaos[v], K_VAO)) return c->fail(SGLC_ERR_INVALID_HANDLE, w + ": invalid vertex array handle");
     for (int h : {fo->fb.colorReady ? fo->fb.colorTex : 0, fo->fb.depthReady ? fo->fb.depthTex : 0}) {
       Object *t = c->get(h, K_TEX);
       if (t && !t->tex.allocated) {

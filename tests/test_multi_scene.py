@@ -148,6 +148,11 @@ def test_multi_scene_errors(cuda_lib):
     with pytest.raises(A.SoftGLError) as e:
         r.drawScenes([items[0]["vao"], items[1]["vao"]], [items[0]["fb"], items[1]["fb"]], res)
     assert e.value.status == A.SGLC_ERR_INVALID_VALUE and "scene 0" in str(e.value)
+    # an invalid vertex array handle is an error (not the silent no-op of a draw without one)
+    with pytest.raises(A.SoftGLError) as e:
+        r.drawScenes([items[0]["vao"], A.VertexArrayObject(r, 99999)], [items[0]["fb"], items[1]["fb"]],
+                     [items[0]["res"], items[1]["res"]])
+    assert e.value.status == A.SGLC_ERR_INVALID_HANDLE
     # the context still draws correctly afterwards
     r.setShaderProgram(prog)
     single = _per_scene(r, prog, states, items)
