@@ -30,7 +30,8 @@
 //   * the epilogues only read the FP32 accumulators (bias included) and apply ReLU with the BF16
 //     rounding in one bf16x2 conversion per pair, into the same tile, whose columns 64-65 hold ones
 //     for the next layer's bias (64 -> 64, then 64 -> 3 with N = 16);
-//   * each of the record's three 32-byte row parts is loaded just before the wait that hides it.
+//   * the record's float4s are loaded where a wait hides them: the first two at the tile's start,
+//     the third before layer 1's first wait, the rest before layer 3's wait.
 // The eight warpgroups' round trips overlap each other's feature and epilogue work.
 // A wait that runs out of polls sets the draw's device error flag (kFlagNeuralTimeout in the
 // context's sticky flags, read by sglc_get_overflow); that tile's colours are then unspecified.
