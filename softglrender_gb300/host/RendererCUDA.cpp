@@ -251,8 +251,14 @@ void RendererCUDA::setShaderProgram(std::shared_ptr<ShaderProgram> &program) {
 // program now and binds the samplers by reference, as UniformSoft does
 void RendererCUDA::setShaderResources(std::shared_ptr<ShaderResources> &resources) {
   if (!resources) return;
+  const sglc_handle h = resourcesHandle(resources);
+  if (h) check(sglc_set_shader_resources(ctx_, h), "setShaderResources");
+}
+
+sglc_handle RendererCUDA::resourcesHandle(const std::shared_ptr<ShaderResources> &resources) {
+  if (!resources) return 0;
   sglc_handle &h = resources_[resources.get()];
-  if (!h && !check(sglc_create_shader_resources(ctx_, &h), "createShaderResources")) return;
+  if (!h && !check(sglc_create_shader_resources(ctx_, &h), "createShaderResources")) return 0;
   for (auto &kv : resources->blocks) {
     auto *b = dynamic_cast<UniformBlockCUDA *>(kv.second.get());
     if (b) check(sglc_shader_resources_set_block(ctx_, h, kv.first, b->handle), "setShaderResources");
@@ -261,7 +267,7 @@ void RendererCUDA::setShaderResources(std::shared_ptr<ShaderResources> &resource
     auto *s = dynamic_cast<UniformSamplerCUDA *>(kv.second.get());
     if (s) check(sglc_shader_resources_set_sampler(ctx_, h, kv.first, s->handle), "setShaderResources");
   }
-  check(sglc_set_shader_resources(ctx_, h), "setShaderResources");
+  return h;
 }
 
 void RendererCUDA::setPipelineStates(std::shared_ptr<PipelineStates> &states) {

@@ -141,6 +141,9 @@ class RendererCUDA : public Renderer {
   // logs a failed call the way the reference reports errors (LOGE + continue)
   bool check(sglc_status s, const char *what);
   sglc_context *ctx() const { return ctx_; }
+  // the C-ABI handle of a ShaderResources with its current blocks and samplers (0 on failure), for
+  // the batched extensions (sglc_draw_views, sglc_draw_scenes) called with the context above
+  sglc_handle resourcesHandle(const std::shared_ptr<ShaderResources> &resources);
 
  private:
   int device_;
