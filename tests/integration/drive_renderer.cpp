@@ -7,6 +7,11 @@
 //   drive_renderer SCENE OUTPUT    the scene file written by tests/integration/scene_file.py; after
 //                                  the last pass the attachments of every pass (colour, resolved
 //                                  colour where multi-sampled, depth) are read back into OUTPUT
+//   drive_renderer SCENE OUTPUT multi
+//                                  the same resources, every pass's first draw then drawn by one
+//                                  multi-scene call (sglc_draw_scenes with the binding's handles,
+//                                  pass 0's program, states and clear), as a C++ caller batches
+//                                  independent scenes
 //
 // On a host without a GPU, create() must fail cleanly and the program reports it (exit code 3).
 // Level-0 images are handed over in tiled and Morton Buffer<T> layouts, so the binding's
@@ -148,7 +153,7 @@ int triangle(std::shared_ptr<Renderer> &renderer) {
   return 0;
 }
 
-int scene(std::shared_ptr<Renderer> &renderer, const char *scenePath, const char *outPath) {
+int scene(std::shared_ptr<Renderer> &renderer, const char *scenePath, const char *outPath, bool multi) {
   Reader in;
   FILE *f = fopen(scenePath, "rb");
   if (!f) {
@@ -302,18 +307,37 @@ int scene(std::shared_ptr<Renderer> &renderer, const char *scenePath, const char
     return 2;
   }
 
-  // the frame: Viewer::drawFrame / pipelineDraw call order
-  for (auto &p : passes) {
-    renderer->beginRenderPass(p.fbo, p.clear);
-    renderer->setViewPort(0, 0, p.width, p.height);
-    for (auto &d : p.draws) {
-      renderer->setVertexArrayObject(d.vao);
-      renderer->setShaderProgram(d.program);
-      renderer->setShaderResources(d.resources);
-      renderer->setPipelineStates(d.states);
-      renderer->draw();
+  if (multi) {
+    // one multi-scene draw over every pass's first draw (the passes share a shading model)
+    auto cuda = std::dynamic_pointer_cast<RendererCUDA>(renderer);
+    std::vector<sglc_handle> vaos, fbos, res;
+    for (auto &p : passes) {
+      vaos.push_back(p.draws[0].vao->getId());
+      fbos.push_back(p.fbo->getId());
+      res.push_back(cuda->resourcesHandle(p.draws[0].resources));
     }
-    renderer->endRenderPass();
+    renderer->setShaderProgram(passes[0].draws[0].program);
+    renderer->setPipelineStates(passes[0].draws[0].states);
+    const ClearStates &c = passes[0].clear;
+    sglc_clear_states cs{c.depthFlag, c.colorFlag, {c.clearColor.r, c.clearColor.g, c.clearColor.b, c.clearColor.a},
+                         c.clearDepth};
+    if (!cuda->check(sglc_draw_scenes(cuda->ctx(), vaos.data(), fbos.data(), res.data(), (int32_t) passes.size(), &cs),
+                     "drawScenes"))
+      return 1;
+  } else {
+    // the frame: Viewer::drawFrame / pipelineDraw call order
+    for (auto &p : passes) {
+      renderer->beginRenderPass(p.fbo, p.clear);
+      renderer->setViewPort(0, 0, p.width, p.height);
+      for (auto &d : p.draws) {
+        renderer->setVertexArrayObject(d.vao);
+        renderer->setShaderProgram(d.program);
+        renderer->setShaderResources(d.resources);
+        renderer->setPipelineStates(d.states);
+        renderer->draw();
+      }
+      renderer->endRenderPass();
+    }
   }
   renderer->waitIdle();
 
@@ -346,6 +370,6 @@ int main(int argc, char **argv) {
     printf("no device\n");
     return 3;
   }
-  if (argc >= 3) return scene(renderer, argv[1], argv[2]);
+  if (argc >= 3) return scene(renderer, argv[1], argv[2], argc >= 4 && strcmp(argv[3], "multi") == 0);
   return triangle(renderer);
 }

@@ -1,9 +1,11 @@
 // Test infrastructure: a recording implementation of the C ABI of include/softgl_cuda.h (the calls
-// the C++ binding softglrender_gb300/host/RendererCUDA.cpp makes). Linked in place of the CUDA
-// library, it performs nothing: every call is written as one text line to the file named by
-// SGLC_TRACE, "<function> <argument>...", each argument tagged
+// the C++ binding softglrender_gb300/host/RendererCUDA.cpp makes, and the multi-scene extension a
+// C++ caller makes with the binding's handles). Linked in place of the CUDA library, it performs
+// nothing: every call is written as one text line to the file named by SGLC_TRACE,
+// "<function> <argument>...", each argument tagged
 //   i:<int>  an integer        h:<n> a handle created earlier in the trace
 //   o:<n>    a handle created by this call        s:<hex> a string        b:<hex> bytes
+//   H:<n>,<n>,...  an array of handles created earlier
 // Structures travel as their bytes (the same layout on every little-endian host the tests use).
 // tests/trace_replay.py replays such a trace through any library that exports the ABI (the CUDA
 // renderer, the CPU oracle, the reference-backed checker) and returns the images read back.
@@ -38,6 +40,10 @@ void argH(sglc_handle h) { fprintf(out(), " h:%d", (int) h); }
 void argS(const char *s) {
   fprintf(out(), " s:");
   hex(s, strlen(s));
+}
+void argHs(const sglc_handle *h, int n) {
+  fprintf(out(), " H:");
+  for (int k = 0; k < n; k++) fprintf(out(), k ? ",%d" : "%d", (int) h[k]);
 }
 void argB(const void *p, size_t n) {
   fprintf(out(), " b:");
@@ -290,6 +296,16 @@ sglc_status sglc_wait_idle(sglc_context *) {
 sglc_status sglc_set_enable_early_z(sglc_context *, int32_t enable) {
   beginCall("set_enable_early_z");
   argI(enable);
+  return endCall();
+}
+sglc_status sglc_draw_scenes(sglc_context *, const sglc_handle *vaos, const sglc_handle *fbs, const sglc_handle *res,
+                             int32_t count, const sglc_clear_states *clear) {
+  beginCall("draw_scenes");
+  argHs(vaos, count);
+  argHs(fbs, count);
+  argHs(res, count);
+  argI(count);
+  argB(clear, sizeof(*clear));
   return endCall();
 }
 

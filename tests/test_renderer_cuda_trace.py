@@ -3,7 +3,8 @@
 The binding compiles only against the reference's headers, which the GPU host does not have, so the
 committed traces in tests/golden/renderer_cuda_<scene>.trace.gz record the C-ABI calls it makes while
 tests/integration/drive_renderer.cpp renders a scene through SoftGL::Renderer (the viewer's call
-sequence, textures handed over in linear, tiled and Morton Buffer<T> layouts). Replaying a trace
+sequence, textures handed over in linear, tiled and Morton Buffer<T> layouts; "multi": three
+independent scenes drawn by one multi-scene call with the binding's handles). Replaying a trace
 through a library makes exactly those calls:
 
 * on the CPU, the oracle's images from the trace equal its images from the Python harness
@@ -76,4 +77,4 @@ def test_binding_trace_renders_on_gpu(name, cuda_lib, oracle_lib):
     within the per-pixel bar (exact for the vertex-colour scene)."""
     gpu = _outputs(cuda_lib, name)
     cpu = _outputs(oracle_lib, name)
-    assert_outputs_match(gpu, cpu, f"RendererCUDA trace {name}", exact_color=(name == "geometry_stress"))
+    assert_outputs_match(gpu, cpu, f"RendererCUDA trace {name}", exact_color=name in ("geometry_stress", "multi"))

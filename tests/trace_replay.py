@@ -3,7 +3,8 @@ while the C++ binding RendererCUDA ran a scene) through any library that exports
 include/softgl_cuda.h: the CUDA renderer, the oracle restatement or the reference-backed checker.
 
 A trace line is "<function> <argument>...", each argument tagged i:<int>, h:<handle made earlier>,
-o:<handle this call makes>, s:<hex string>, b:<hex bytes>. Handles are renumbered through a map, so
+o:<handle this call makes>, s:<hex string>, b:<hex bytes>, H:<handles, comma-separated>. Handles are
+renumbered through a map, so
 the replay's handles need not equal the recorded ones. `replay` returns the images the trace read
 back, in order, shaped like `Texture.readImage`."""
 from __future__ import annotations
@@ -72,6 +73,14 @@ def replay(lib: A.Library, lines: List[List[str]], device: int = 0) -> List[Read
                 ptrs = (C.c_void_p * n)(*[C.addressof(b) for b in cbufs])
                 keep.append(ptrs)
                 call += [h, n, ptrs, nbytes]
+            elif name == "draw_scenes":
+                arrs = [[handles[int(v)] for v in a[2:].split(",")] for a in args[:3]]
+                n = int(args[3][2:])
+                carr = [(C.c_int32 * n)(*x) for x in arrs]
+                keep.extend(carr)
+                cs = C.create_string_buffer(bytes.fromhex(args[4][2:]))
+                keep.append(cs)
+                call += [*carr, n, C.addressof(cs)]
             elif name == "texture_read_image":
                 h = handles[int(args[0][2:])]
                 layer, level, resolved, nbytes = (int(a[2:]) for a in args[1:5])
