@@ -39,7 +39,7 @@ def parse():
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch measurement")
     ap.add_argument("--profile-scene", default=None,
                     help="render one workload for --frames frames (after one warm-up frame) and exit, for a "
-                         "profiler: plain_small, geometry_stress[:TRIANGLES], pbr, pbr_neural[:TRAIN_STEPS], "
+                         "profiler: plain_small, geometry_stress[:TRIANGLES], pbr[:TILE_HEIGHT], pbr_neural[:TRAIN_STEPS], "
                          "pbr_per_thread_stores")
     ap.add_argument("--frames", type=int, default=3)
     ap.add_argument("--no-configs12", action="store_true",
@@ -651,6 +651,8 @@ def profile_scene(args):
         raise SystemExit(f"unknown --profile-scene {name}")
     if name == "pbr_per_thread_stores":
         r.setTmaStore(False)
+    if name == "pbr" and arg:
+        r.setTileSize(int(arg))   # the raster tile height of the tuned submission (8: 16x8 tiles, 128 threads)
     inst = S.SceneInstance(r, scene)
     if name == "pbr_neural":
         from softglrender_gb300 import neural as NN
