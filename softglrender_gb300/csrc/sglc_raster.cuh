@@ -989,28 +989,43 @@ __global__ void __launch_bounds__(32 * W, (S == 4 ? 2 : 4) * 8 / W) k_raster_cov
         uint32_t pass = cov;
         if (testDepth) {
           const int segStart = max(offL, r0) - r0;
+          // the longest segment of the round: scan steps at or beyond it combine no two lanes of
+          // one segment (lane - d < segStart for every lane of it), so they are skipped
+          const int segMax = __reduce_max_sync(0xffffffffu, nOwn);
           const bool inDL = __shfl_sync(0xffffffffu, inD, L);
           const float zs[4] = {sl.cv.z0, sl.cv.z1, sl.cv.z2, sl.cv.z3};
           const float fbd[4] = {fb.d0, fb.d1, fb.d2, fb.d3};
           float last[4] = {0.f, 0.f, 0.f, 0.f};
-          pass = 0u;
+          float cz[4], cur[4], x[4];
 #pragma unroll
           for (int q = 0; q < S; q++) {
-            const float cz = gclamp(zs[q], p.vp.absMin, p.vp.absMax);
-            float cur = __shfl_sync(0xffffffffu, fbd[q], L);
-            if (p.depthMask) {
-              float x = ((cov >> q) & 1u) && cz == cz ? cz : keepId;
-#pragma unroll
-              for (int d = 1; d < 32; d <<= 1) {
-                const float y = __shfl_up_sync(0xffffffffu, x, d);
-                if (lane - d >= segStart) x = depthKeep(y, x, p.depthFunc);
-              }
-              const float ex = __shfl_up_sync(0xffffffffu, x, 1);
-              if (lane > segStart) cur = depthKeep(cur, ex, p.depthFunc);
-              last[q] = __shfl_sync(0xffffffffu, x, nOwn > 0 ? s1 - 1 : lane);
-            }
-            if (((cov >> q) & 1u) && inDL && depthCmp(cz, cur, p.depthFunc)) pass |= 1u << q;
+            cz[q] = gclamp(zs[q], p.vp.absMin, p.vp.absMax);
+            cur[q] = __shfl_sync(0xffffffffu, fbd[q], L);
+            x[q] = ((cov >> q) & 1u) && cz[q] == cz[q] ? cz[q] : keepId;
           }
+          if (p.depthMask) {
+            // the samples' scans step together (independent chains, one branch per step)
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+              if (d >= segMax) break;
+              const bool take = lane - d >= segStart;
+#pragma unroll
+              for (int q = 0; q < S; q++) {
+                const float y = __shfl_up_sync(0xffffffffu, x[q], d);
+                if (take) x[q] = depthKeep(y, x[q], p.depthFunc);
+              }
+            }
+#pragma unroll
+            for (int q = 0; q < S; q++) {
+              const float ex = __shfl_up_sync(0xffffffffu, x[q], 1);
+              if (lane > segStart) cur[q] = depthKeep(cur[q], ex, p.depthFunc);
+              last[q] = __shfl_sync(0xffffffffu, x[q], nOwn > 0 ? s1 - 1 : lane);
+            }
+          }
+          pass = 0u;
+#pragma unroll
+          for (int q = 0; q < S; q++)
+            if (((cov >> q) & 1u) && inDL && depthCmp(cz[q], cur[q], p.depthFunc)) pass |= 1u << q;
           if (p.depthMask && inD && nOwn > 0) {
             fb.d0 = depthKeep(fb.d0, last[0], p.depthFunc);
             if (S == 4) {
