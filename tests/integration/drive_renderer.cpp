@@ -310,6 +310,15 @@ int scene(std::shared_ptr<Renderer> &renderer, const char *scenePath, const char
   if (multi) {
     // one multi-scene draw over every pass's first draw (the passes share a shading model)
     auto cuda = std::dynamic_pointer_cast<RendererCUDA>(renderer);
+    for (auto &p : passes)
+      if (p.draws.empty()) {
+        printf("multi: a pass without draws\n");
+        return 2;
+      }
+    if (!cuda || passes.empty()) {
+      printf("multi: needs a RendererCUDA and at least one pass\n");
+      return 2;
+    }
     std::vector<sglc_handle> vaos, fbos, res;
     for (auto &p : passes) {
       vaos.push_back(p.draws[0].vao->getId());
