@@ -446,6 +446,20 @@ __device__ __forceinline__ uint32_t depthOps(const DrawParams &p, const Cover &c
   return (i0 ? 1u : 0u) | (i1 ? 2u : 0u) | (i2 ? 4u : 0u) | (i3 ? 8u : 0u);
 }
 
+// Lane r holds row r of a 32x32 bit matrix (bit c = column c); returns column `lane` (bit r = row r).
+// Each step swaps the off-diagonal s x s blocks of every 2s x 2s block, for s = 16, 8, 4, 2, 1.
+__device__ __forceinline__ unsigned transposeBits(unsigned x, int lane) {
+  const unsigned lowCols[5] = {0x0000ffffu, 0x00ff00ffu, 0x0f0f0f0fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+  for (int i = 0; i < 5; i++) {
+    const int s = 16 >> i;
+    const unsigned m = lowCols[i];
+    const unsigned y = __shfl_xor_sync(0xffffffffu, x, s);
+    x = (lane & s) ? ((x & ~m) | ((y & ~m) >> s)) : ((x & m) | ((y & m) << s));
+  }
+  return x;
+}
+
 // Pass 1 of a batch of up to 32 tile primitives (lane = primitive): a conservative edge-function
 // test of each triangle against the sample box of every pixel of the warp's 8x4 rectangle, and for
 // 4x MSAA against each of the four sample points of a pixel whose box passes (a triangle covering
@@ -454,7 +468,7 @@ __device__ __forceinline__ uint32_t depthOps(const DrawParams &p, const Cover &c
 // (bit = batch index); `prim` = this lane's primitive id.
 template<int S>
 __device__ __forceinline__ unsigned pass1Prim(const DrawParams &p, int prim, int lane, int rx0, int ry0, float lo, float hi,
-                                              float vpExtent, unsigned *candS, int rh = 4, int hiz = HIZ_NONE,
+                                              float vpExtent, int rh = 4, int hiz = HIZ_NONE,
                                               float hizBound = 0.f) {
   bool hit = false;
   int4 r = make_int4(0, -1, 0, -1);
@@ -535,30 +549,27 @@ __device__ __forceinline__ unsigned pass1Prim(const DrawParams &p, int prim, int
     return cand;
   }
   // small primitives: each lane (primitive) visits only the pixels of the warp's 8x4 rectangle inside
-  // its own pixel rectangle and sets its bit in those pixels' candidate masks (bit = batch index)
-  candS[lane] = 0u;
-  __syncwarp();
+  // its own pixel rectangle and collects the ones that pass in a row (bit = pixel); transposing the
+  // warp's 32x32 bit matrix gives each lane its pixel's candidate mask (bit = batch index)
+  unsigned row = 0u;
   int cx = x0, cy = y0;
-  for (int k = 0; k < nMax; k++) {
-    if (k < n) {
-      if (test(cx, cy)) atomicOr(&candS[(cy - ry0) * 8 + (cx - rx0)], 1u << lane);
-      if (++cx > x1) {
-        cx = x0;
-        cy++;
-      }
+  for (int k = 0; k < n; k++) {
+    if (test(cx, cy)) row |= 1u << ((cy - ry0) * 8 + (cx - rx0));
+    if (++cx > x1) {
+      cx = x0;
+      cy++;
     }
   }
-  __syncwarp();
-  return candS[lane];
+  return transposeBits(row, lane);
 }
 
 // pass 1 for the batch of tile-list entries [base, base + 32): lane i tests entry base + i
 template<int S>
 __device__ __forceinline__ unsigned pass1Candidates(const DrawParams &p, int base, int end, int lane, int rx0, int ry0,
-                                                    float lo, float hi, float vpExtent, int &prim, unsigned *candS) {
+                                                    float lo, float hi, float vpExtent, int &prim) {
   int i = base + lane;
   prim = i < end ? __ldg(p.valA + i) : -1;
-  return pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent, candS);
+  return pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent);
 }
 
 // does a tile-list primitive's pixel rectangle touch the warp's 8x4 rectangle
@@ -571,7 +582,6 @@ template<int SH, int S, bool HAS_COLOR, bool HAS_DEPTH>
 __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawParams p) {
   chainEnter();
   __shared__ FragQueue queues[HAS_COLOR ? 8 : 1];
-  __shared__ unsigned candMasks[8][32];
   const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
   const TileFrame fr = tileFrame(p, tile);
   const int view = fr.view;
@@ -617,7 +627,7 @@ __global__ void __launch_bounds__(256, 2) k_raster(const __grid_constant__ DrawP
   const float vpExtent = fabsf(fr.vpW) + fabsf(fr.vpH) + 2.f * (float) (rx0 + ry0) + 64.f;
   for (int base = start; base < end; base += 32) {
     int prim;
-    unsigned cand = pass1Candidates<S>(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim, candMasks[warp]);
+    unsigned cand = pass1Candidates<S>(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim);
     if (!(inC || inD)) cand = 0;
     // ---- pass 2 (lane = pixel): exact coverage and depth for each candidate, in primitive order
     int nIter = __reduce_max_sync(0xffffffffu, __popc(cand));
@@ -785,7 +795,6 @@ __global__ void __launch_bounds__(32 * W, (S == 4 ? 2 : 4) * 8 / W) k_raster_cov
   constexpr int TH = 2 * W;   // tile height in pixels (width 16): W warps of 8x4 pixels, two per row
   chainEnter();
   __shared__ CovSlot covSlots[W][32];
-  __shared__ unsigned candMasks[W][32];
   __shared__ int covQueue[W][64];
   const TileJob job = tileJob(p);
   if (job.skip) return;
@@ -916,7 +925,7 @@ __global__ void __launch_bounds__(32 * W, (S == 4 ? 2 : 4) * 8 / W) k_raster_cov
         warpBound = lower ? fminf(warpBound, v) : fmaxf(warpBound, v);
       }
     }
-    unsigned cand = pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent, candMasks[warp], rh, hiz, warpBound);
+    unsigned cand = pass1Prim<S>(p, prim, lane, rx0, ry0, lo, hi, vpExtent, rh, hiz, warpBound);
     if (!inPix) cand = 0;
     // pass 2, load-balanced: the (pixel, candidate) pairs of the batch, pixel-major in candidate
     // order, are evaluated 32 at a time by all lanes (coverage does not depend on the depth buffer);

@@ -214,7 +214,6 @@ __device__ __forceinline__ void neuralFlush(const DrawParams &p, NeuralCta &n, F
 template<int S, bool HAS_DEPTH>
 __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant__ DrawParams p) {
   extern __shared__ __align__(1024) uint8_t smraw[];
-  __shared__ unsigned candMasks[8][32];
   uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~(uintptr_t) 1023);
   FragQueueN *queues = reinterpret_cast<FragQueueN *>(sm + kRnQueues);
   const int tile = p.tileOrder ? p.tileOrder[blockIdx.x] : blockIdx.x;
@@ -289,7 +288,7 @@ __global__ void __launch_bounds__(256, 2) k_raster_neural(const __grid_constant_
   const float vpExtent = fabsf(fr.vpW) + fabsf(fr.vpH) + 2.f * (float) (rx0 + ry0) + 64.f;
   for (int base = start; base < end; base += 32) {
     int prim;
-    unsigned cand = pass1Candidates<S>(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim, candMasks[warp]);
+    unsigned cand = pass1Candidates<S>(p, base, end, lane, rx0, ry0, lo, hi, vpExtent, prim);
     if (!(inC || inD)) cand = 0;
     // pass 2 in CTA-wide steps: one candidate per lane per step (up to 2 quads = 64 queue entries)
     while (__syncthreads_or(cand != 0u)) {
